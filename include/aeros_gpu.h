@@ -1,0 +1,262 @@
+/*
+ * aeros_gpu.h -- C-ABI of the GB300 (sm_103a) spectral dynamics path.
+ *
+ * This is the drop-in boundary for aeros' spectral transform module and its
+ * dry time step.  A Fortran host binds it with iso_c_binding (interfaces are
+ * given in INTEGRATION.md); Python binds it with ctypes (aeros_gb300/_capi.py).
+ *
+ * Conventions (identical to the reference arrays, so a Fortran caller passes
+ * its arrays straight through):
+ *   - spectral arrays are complex(c_double) (nlm[, nbatch]), stored as
+ *     interleaved (re, im) doubles, m-major: 0-based lm = m(2T+1-m)/2 + l
+ *     (src/aeros_spectral.f90:478);
+ *   - grid arrays are real(c_double) (nlon, nlat[, nbatch]), longitude
+ *     contiguous, latitude north -> south (src/aeros_defs.f90:196-204);
+ *   - orthonormal harmonics without the Condon-Shortley phase,
+ *     Y_lm = Pbar_lm(cos theta) e^{i m phi} / sqrt(2 pi)
+ *     (src/aeros_spectral.f90:17-27).
+ * Pointers may be host or device memory; host buffers are staged through the
+ * handle's device workspace, device buffers are used in place.
+ *
+ * Every entry point returns an int status: 0 = success, negative = error
+ * (see AEROS_ERR_*).  Nothing aborts the process; the reference's
+ * `stop 1` / `error stop 1` conditions come back as these codes.
+ * A handle is not thread-safe and owns one CUDA stream.
+ */
+#ifndef AEROS_GPU_H
+#define AEROS_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define AEROS_OK                 0
+#define AEROS_ERR_ARG           -1   /* bad argument / shape              */
+#define AEROS_ERR_CUDA          -2   /* CUDA runtime failure              */
+#define AEROS_ERR_NOMEM         -3   /* device allocation failed          */
+#define AEROS_ERR_SINGULAR      -4   /* singular Helmholtz matrix         */
+#define AEROS_ERR_NONFINITE     -5   /* NaN/Inf detected in the state     */
+#define AEROS_ERR_STATE         -6   /* call out of order                 */
+#define AEROS_ERR_UNSUPPORTED   -7   /* size or mode not built            */
+
+/* ---- precision modes of the Legendre contraction ------------------------ */
+#define AEROS_PREC_FP64   0   /* plain FP64 (DFMA)                          */
+#define AEROS_PREC_SPLIT  1   /* split-precision tensor-core (Ozaki) form   */
+
+/* ---- opaque handles ------------------------------------------------------ */
+typedef struct aeros_sht_s *aeros_sht_t;
+typedef struct aeros_dyn_s *aeros_dyn_t;
+
+/* ======================================================================== */
+/* Spectral transforms: mirrors module aeros_spectral                        */
+/* (src/aeros_spectral.f90:128-143)                                          */
+/* ======================================================================== */
+
+/* Smallest quadratically-unaliased Gaussian grid for truncation T:
+ * nlon = 3T+1 rounded up to an even 2/3/5-smooth number, nlat = nlon/2.
+ * Replaces aeros_sht_grid_size (src/aeros_spectral.f90:399-436). */
+int aeros_sht_grid_size(int trunc, int *nlon, int *nlat);
+
+/* Create a transform for truncation T on an (nlon, nlat) Gaussian grid
+ * (nlon/nlat <= 0 pick the default grid) able to process up to `batch_max`
+ * fields per call.  Replaces aeros_sht_init (src/aeros_spectral.f90:147-279)
+ * and the per-thread pool aeros_sht_pool_init (:305-342): one handle per
+ * stream replaces one SHTns config per OpenMP thread. */
+int aeros_sht_create(aeros_sht_t *h, int trunc, int nlon, int nlat, int batch_max);
+
+/* Release a transform.  Replaces aeros_sht_end (src/aeros_spectral.f90:281-303). */
+int aeros_sht_destroy(aeros_sht_t h);
+
+/* Realized configuration and geometry (host arrays; any pointer may be NULL):
+ * sinlat (nlat) = Gauss nodes cos(colatitude) north->south, gauss_w (nlat)
+ * summing to 2, l_of_lm / m_of_lm (nlm).  Replaces the geometry fields of
+ * aeros_sht_class (src/aeros_spectral.f90:47-85). */
+int aeros_sht_info(aeros_sht_t h, int *trunc, int *nlon, int *nlat, int *nlm,
+                   double *sinlat, double *gauss_w, int *l_of_lm, int *m_of_lm);
+
+/* 1-based index of (l, m), or -1 outside the truncation.
+ * Replaces aeros_sht_lm (src/aeros_spectral.f90:460-482). */
+int aeros_sht_lm(aeros_sht_t h, int l, int m);
+
+/* Select the Legendre contraction precision (AEROS_PREC_*). */
+int aeros_sht_set_precision(aeros_sht_t h, int mode);
+
+/* Bind the handle to a caller's CUDA stream (cudaStream_t); NULL = own. */
+int aeros_sht_set_stream(aeros_sht_t h, void *stream);
+
+/* Scalar synthesis: coeffs (nlm, nbatch) -> field (nlon, nlat, nbatch).
+ * Replaces aeros_sht_synthesis / SH_to_spat (src/aeros_spectral.f90:502-515). */
+int aeros_sht_synthesis(aeros_sht_t h, const double *coeffs, double *field, int nbatch);
+
+/* Scalar analysis: field (nlon, nlat, nbatch) -> coeffs (nlm, nbatch).  The
+ * input is NOT destroyed (the reference's contract allows destruction, so this
+ * is a superset).  Replaces aeros_sht_analysis / spat_to_SH (:486-500). */
+int aeros_sht_analysis(aeros_sht_t h, const double *field, double *coeffs, int nbatch);
+
+/* Vector synthesis: spheroidal/toroidal (slm, tlm) -> (v_theta, v_phi), unit
+ * sphere, v_theta positive southward.  Replaces aeros_sht_synthesis_vec /
+ * SHsphtor_to_spat (src/aeros_spectral.f90:545-558). */
+int aeros_sht_synthesis_vec(aeros_sht_t h, const double *slm, const double *tlm,
+                            double *vth, double *vph, int nbatch);
+
+/* Vector analysis: (v_theta, v_phi) -> (slm, tlm); l = 0 returns zero.
+ * Replaces aeros_sht_analysis_vec / spat_to_SHsphtor (:529-543). */
+int aeros_sht_analysis_vec(aeros_sht_t h, const double *vth, const double *vph,
+                           double *slm, double *tlm, int nbatch);
+
+/* Gradient on the unit sphere: gth = dF/dtheta, gph = (1/sin theta) dF/dphi.
+ * Replaces aeros_sht_gradient / SHsph_to_spat (src/aeros_spectral.f90:560-584). */
+int aeros_sht_gradient(aeros_sht_t h, const double *coeffs, double *gth, double *gph,
+                       int nbatch);
+
+/* In-place Laplacian, x (-l(l+1)/a^2); inverse != 0 divides and zeroes l = 0.
+ * Replaces aeros_sht_laplacian (src/aeros_spectral.f90:588-630). */
+int aeros_sht_laplacian(aeros_sht_t h, double *coeffs, int inverse, int nbatch);
+
+/* Global integral a^2 sum_j w_j (sum_i f_ij) 2pi/nlon for each of nbatch
+ * fields, in FP64.  Replaces aeros_sht_surface_integral (:632-666). */
+int aeros_sht_surface_integral(aeros_sht_t h, const double *field, double *total,
+                               int nbatch);
+
+/* Wind <-> vorticity/divergence, one call for nbatch levels, with the
+ * reference's sign conventions (u = V_phi, v = -V_theta, S = -a D/(l(l+1)),
+ * T = a zeta/(l(l+1)), l = 0 discarded).  Replace aeros_uv_from_vordiv,
+ * aeros_vordiv_from_uv and aeros_gradient (src/dynamics/aeros_vordiv.f90:82-205). */
+int aeros_uv_from_vordiv(aeros_sht_t h, const double *vor, const double *div,
+                         double *u, double *v, int nbatch);
+int aeros_vordiv_from_uv(aeros_sht_t h, const double *u, const double *v,
+                         double *vor, double *div, int nbatch);
+int aeros_gradient(aeros_sht_t h, const double *f, double *dfdx, double *dfdy, int nbatch);
+
+/* ======================================================================== */
+/* Dry dynamics step: mirrors aeros_timestep / aeros facade                  */
+/* ======================================================================== */
+
+/* Configuration.  Field meanings follow aeros_param_class
+ * (src/aeros_defs.f90:114-190), the &aeros_vert group
+ * (src/dynamics/aeros_vertical.f90:95-124) and the Held-Suarez constants
+ * (src/physics/aeros_held_suarez.f90:92-101), which are runtime values here so
+ * that ensemble members can carry perturbed forcing. */
+typedef struct aeros_params {
+    int    trunc;          /* triangular truncation T                        */
+    int    nlon, nlat;     /* <= 0: default grid for T                       */
+    int    nlev;           /* full levels                                    */
+    int    nmember;        /* ensemble members stepped together (>= 1)       */
+    int    precision;      /* AEROS_PREC_*                                   */
+    double dt;             /* time step [s]                                  */
+    double eps_filter;     /* RAW filter nu                                  */
+    double raw_alpha;      /* Williams alpha (1 = Robert-Asselin)            */
+    double si_alpha;       /* semi-implicit decentering weight in [0.5, 1]   */
+    double tau_diff;       /* diffusion e-folding at l = lmax [hours]        */
+    int    ndiff;          /* diffusion order (even)                         */
+    int    semi_implicit;  /* 0 = explicit leapfrog                          */
+    int    held_suarez;    /* Held-Suarez forcing on/off                     */
+    int    mass_fixer;     /* global mass fixer on/off                       */
+    /* vertical grid generator */
+    double stretch_a, stretch_r, sigma_t, p_top, ps_ref, t_ref;
+    /* Held-Suarez constants */
+    double hs_t_equator, hs_t_min, hs_dt_y, hs_dtheta_z, hs_sigma_b, hs_p0;
+    double hs_k_a, hs_k_s, hs_k_f;   /* [s-1] */
+} aeros_params;
+
+/* Fill `p` with the Held-Suarez benchmark configuration of
+ * par/held_suarez.nml (T31 L20, dt 1800 s, RAW 0.06/0.53, del^6 6 h, pure
+ * sigma on [0.01, 1], t_ref 300 K, mass fixer on). */
+int aeros_params_default(aeros_params *p);
+
+/* Build the integrator: vertical grid, semi-implicit operators, diffusion
+ * ratios, Held-Suarez factors, device state for p->nmember members.
+ * a_half/b_half (nlev+1) may be NULL (generated from the stretching
+ * parameters) or an explicit hybrid table.  Replaces aeros_timestep_init
+ * (src/dynamics/aeros_timestep.f90:452-598), aeros_vgrid_init
+ * (src/dynamics/aeros_vertical.f90:126-298) and aeros_semiimp_init
+ * (src/dynamics/aeros_semiimp.f90:171-276). */
+int aeros_dyn_create(aeros_dyn_t *h, const aeros_params *p,
+                     const double *a_half, const double *b_half);
+int aeros_dyn_destroy(aeros_dyn_t h);
+
+/* Geometry and vertical coordinate (host arrays, any may be NULL):
+ * A, B (nlev+1), sigma_full (nlev), sinlat, gauss_w (nlat). */
+int aeros_dyn_info(aeros_dyn_t h, int *nlon, int *nlat, int *nlm, int *nlev,
+                   double *a_half, double *b_half, double *sigma_full,
+                   double *sinlat, double *gauss_w);
+
+/* Per-member Held-Suarez equator-pole contrast dT_y [K] and k_a [s-1]. */
+int aeros_dyn_set_member_forcing(aeros_dyn_t h, int member, double dt_y, double k_a);
+
+/* Install the spectral state X^n of every member and restart the leapfrog
+ * (the next step is the start-up step).  vor/div/temp are (nlm, nlev,
+ * nmember), lnps (nlm, nmember).  Mirrors writing ams%now%spec and
+ * ts%nstep = 0 (src/aeros.f90:130-183). */
+int aeros_dyn_set_state(aeros_dyn_t h, const double *vor, const double *div,
+                        const double *temp, const double *lnps);
+int aeros_dyn_get_state(aeros_dyn_t h, double *vor, double *div, double *temp,
+                        double *lnps);
+/* X^(n-1), for restarts (src/dynamics/aeros_timestep.f90:1303-1633). */
+int aeros_dyn_set_old_state(aeros_dyn_t h, const double *vor, const double *div,
+                            const double *temp, const double *lnps, int nstep);
+int aeros_dyn_get_old_state(aeros_dyn_t h, double *vor, double *div, double *temp,
+                            double *lnps);
+
+/* Resting isothermal state at temp [K] and ps [Pa] (<= 0: reference values),
+ * for all members.  Replaces aeros_set_isothermal (src/aeros.f90:130-183). */
+int aeros_dyn_set_isothermal(aeros_dyn_t h, double temp, double ps);
+
+/* Surface geopotential (nlon, nlat) [m2 s-2], shared by all members.
+ * Replaces aeros_timestep_set_phis (src/dynamics/aeros_timestep.f90:1817-1844). */
+int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis);
+
+/* Advance every member by nsteps dynamics steps.  Replaces nsteps calls of
+ * aeros_timestep_step (src/dynamics/aeros_timestep.f90:776-1137), dry path. */
+int aeros_dyn_step(aeros_dyn_t h, int nsteps);
+
+/* Adiabatic spectral tendencies R(X^n) of the current state, no forcing:
+ * replaces aeros_tendency_calc (src/dynamics/aeros_tendency.f90:338-360). */
+int aeros_dyn_tendency(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp,
+                       double *dlnps);
+
+/* Grid-space fields of the current state: u, v, temp (nlon, nlat, nlev,
+ * nmember), ps (nlon, nlat, nmember).  Replaces aeros_timestep_diagnose
+ * (src/dynamics/aeros_timestep.f90:1873-1919). */
+int aeros_dyn_diagnose(aeros_dyn_t h, double *u, double *v, double *temp, double *ps);
+
+/* FP64 global mass [kg], total energy [J], angular momentum [kg m2 s-1] of
+ * every member (nmember each).  Replaces aeros_budget_calc
+ * (src/aeros_budget.f90:61-142). */
+int aeros_dyn_budget(aeros_dyn_t h, double *mass, double *energy, double *angmom);
+
+/* Mass fixer bookkeeping: steps taken, target mass, last and cumulative log
+ * corrections of member 0 (src/dynamics/aeros_timestep.f90:1225-1301). */
+int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target,
+                       double *lnr_last, double *lnr_cum);
+int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass);
+
+/* Zonal-mean statistics (src/aeros_diagnostics.f90:153-276): accumulate one
+ * sample of the current state; read the running means of member `member`
+ * as 7 arrays (nlat, nlev): u, v, temp, u'v', v'T', eke, T'^2, and 2 arrays
+ * (nlat): ps, u_sfc.  `out` holds 7*nlat*nlev + 2*nlat doubles. */
+int aeros_dyn_diag_accumulate(aeros_dyn_t h);
+int aeros_dyn_diag_read(aeros_dyn_t h, int member, double *out, int *nsample);
+
+/* Fastest linear gravity-wave speed [m/s] of the semi-implicit operator W
+ * (src/dynamics/aeros_semiimp.f90:573-620). */
+int aeros_dyn_gwspeed(aeros_dyn_t h, double *cmax);
+
+/* Bind to a caller's CUDA stream; steps are replayed as CUDA graphs on it. */
+int aeros_dyn_set_stream(aeros_dyn_t h, void *stream);
+
+/* Number of this library's kernel launches issued since creation (a step
+ * replayed from a graph counts each kernel node). */
+int aeros_dyn_launch_count(aeros_dyn_t h, long long *count);
+
+/* Last CUDA error string for diagnostics (static storage). */
+const char *aeros_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AEROS_GPU_H */

@@ -1,0 +1,298 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+legs.  Array conventions match the GPU library's Python mirror:
+spectral fields are complex128 arrays shaped (..., nlm); grid fields are
+float64 arrays shaped (..., nlat, nlon) (= Fortran (nlon, nlat, ...)).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+        L.ora_sht_create.restype = vp
+        L.ora_sht_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.ora_sht_destroy.argtypes = [vp]
+        L.ora_dyn_create.restype = vp
+        L.ora_dyn_create.argtypes = [vp, vp, vp, ctypes.c_int, ip]
+        L.ora_dyn_destroy.argtypes = [vp]
+        for name in ["ora_sht_info", "ora_sht_tables", "ora_sht_synthesis", "ora_sht_analysis",
+                     "ora_sht_synthesis_vec", "ora_sht_analysis_vec", "ora_sht_gradient",
+                     "ora_sht_laplacian", "ora_sht_surface_integral", "ora_uv_from_vordiv",
+                     "ora_vordiv_from_uv", "ora_gradient", "ora_dyn_info", "ora_dyn_set_state",
+                     "ora_dyn_get_state", "ora_dyn_get_old_state", "ora_dyn_set_old_state",
+                     "ora_dyn_set_isothermal", "ora_dyn_set_phis", "ora_dyn_set_forcing",
+                     "ora_dyn_step", "ora_dyn_tendency", "ora_dyn_tendency_forced",
+                     "ora_dyn_grid_rhs", "ora_dyn_diagnose", "ora_dyn_counters",
+                     "ora_dyn_set_mass_target", "ora_dyn_budget", "ora_dyn_diag_accumulate",
+                     "ora_dyn_diag_read", "ora_dyn_gwspeed", "ora_dyn_si_linear"]:
+            getattr(L, name).restype = ctypes.c_int
+        L.ora_dyn_set_isothermal.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.ora_dyn_set_forcing.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.ora_dyn_set_mass_target.argtypes = [vp, ctypes.c_double]
+        L.ora_dyn_step.argtypes = [vp, ctypes.c_int]
+        L.ora_grid_size.argtypes = [ctypes.c_int, ip, ip]
+        L.ora_set_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> int:
+    return lib().ora_set_threads(int(n))
+
+
+def grid_size(trunc):
+    a, b = ctypes.c_int(), ctypes.c_int()
+    lib().ora_grid_size(trunc, ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+class OracleSHT:
+    """CPU restatement of aeros_sht_class + the transforms of aeros_spectral."""
+
+    def __init__(self, trunc, nlon=-1, nlat=-1):
+        L = lib()
+        self.h = L.ora_sht_create(trunc, nlon, nlat)
+        T, n1, n2, nlm = (ctypes.c_int() for _ in range(4))
+        L.ora_sht_info(ctypes.c_void_p(self.h), ctypes.byref(T), ctypes.byref(n1), ctypes.byref(n2),
+                       ctypes.byref(nlm), None, None, None, None)
+        self.trunc, self.nlon, self.nlat, self.nlm = T.value, n1.value, n2.value, nlm.value
+        self.sinlat = np.zeros(self.nlat)
+        self.gauss_w = np.zeros(self.nlat)
+        self.l_of_lm = np.zeros(self.nlm, np.int32)
+        self.m_of_lm = np.zeros(self.nlm, np.int32)
+        L.ora_sht_info(ctypes.c_void_p(self.h), None, None, None, None, _p(self.sinlat),
+                       _p(self.gauss_w), _p(self.l_of_lm), _p(self.m_of_lm))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_sht_destroy(ctypes.c_void_p(self.h))
+            self.h = None
+
+    def lm(self, l, m):
+        """0-based index of (l, m) or -1 (src/aeros_spectral.f90:460-482 is 1-based)."""
+        if m < 0 or m > self.trunc or l < m or l > self.trunc:
+            return -1
+        return (m * (2 * self.trunc + 1 - m)) // 2 + l
+
+    def tables(self):
+        P = np.zeros((self.nlm, self.nlat))
+        dP = np.zeros((self.nlm, self.nlat))
+        lib().ora_sht_tables(ctypes.c_void_p(self.h), _p(P), _p(dP))
+        return P, dP
+
+    def _spec(self, shape):
+        return np.zeros(shape + (self.nlm,), np.complex128)
+
+    def _grid(self, shape):
+        return np.zeros(shape + (self.nlat, self.nlon))
+
+    def synthesis(self, c):
+        c = np.ascontiguousarray(c, np.complex128)
+        f = self._grid(c.shape[:-1])
+        lib().ora_sht_synthesis(ctypes.c_void_p(self.h), _p(c), _p(f), int(c.size // self.nlm))
+        return f
+
+    def analysis(self, f):
+        f = np.ascontiguousarray(f, np.float64)
+        c = self._spec(f.shape[:-2])
+        lib().ora_sht_analysis(ctypes.c_void_p(self.h), _p(f), _p(c), int(c.size // self.nlm))
+        return c
+
+    def synthesis_vec(self, s, t):
+        s = np.ascontiguousarray(s, np.complex128)
+        t = np.ascontiguousarray(t, np.complex128)
+        a, b = self._grid(s.shape[:-1]), self._grid(s.shape[:-1])
+        lib().ora_sht_synthesis_vec(ctypes.c_void_p(self.h), _p(s), _p(t), _p(a), _p(b), int(s.size // self.nlm))
+        return a, b
+
+    def analysis_vec(self, vth, vph):
+        vth = np.ascontiguousarray(vth, np.float64)
+        vph = np.ascontiguousarray(vph, np.float64)
+        s, t = self._spec(vth.shape[:-2]), self._spec(vth.shape[:-2])
+        lib().ora_sht_analysis_vec(ctypes.c_void_p(self.h), _p(vth), _p(vph), _p(s), _p(t), int(s.size // self.nlm))
+        return s, t
+
+    def gradient(self, c):
+        c = np.ascontiguousarray(c, np.complex128)
+        a, b = self._grid(c.shape[:-1]), self._grid(c.shape[:-1])
+        lib().ora_sht_gradient(ctypes.c_void_p(self.h), _p(c), _p(a), _p(b), int(c.size // self.nlm))
+        return a, b
+
+    def laplacian(self, c, inverse=False):
+        c = np.array(c, np.complex128, copy=True, order="C")
+        lib().ora_sht_laplacian(ctypes.c_void_p(self.h), _p(c), int(bool(inverse)), int(c.size // self.nlm))
+        return c
+
+    def surface_integral(self, f):
+        f = np.ascontiguousarray(f, np.float64)
+        nb = int(f.size // (self.nlat * self.nlon))
+        out = np.zeros(nb)
+        lib().ora_sht_surface_integral(ctypes.c_void_p(self.h), _p(f), _p(out), nb)
+        return out.reshape(f.shape[:-2]) if f.ndim > 2 else out[0]
+
+    def uv_from_vordiv(self, vor, div):
+        vor = np.ascontiguousarray(vor, np.complex128)
+        div = np.ascontiguousarray(div, np.complex128)
+        u, v = self._grid(vor.shape[:-1]), self._grid(vor.shape[:-1])
+        lib().ora_uv_from_vordiv(ctypes.c_void_p(self.h), _p(vor), _p(div), _p(u), _p(v), int(vor.size // self.nlm))
+        return u, v
+
+    def vordiv_from_uv(self, u, v):
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        vor, div = self._spec(u.shape[:-2]), self._spec(u.shape[:-2])
+        lib().ora_vordiv_from_uv(ctypes.c_void_p(self.h), _p(u), _p(v), _p(vor), _p(div), int(vor.size // self.nlm))
+        return vor, div
+
+    def grad(self, f):
+        f = np.ascontiguousarray(f, np.complex128)
+        a, b = self._grid(f.shape[:-1]), self._grid(f.shape[:-1])
+        lib().ora_gradient(ctypes.c_void_p(self.h), _p(f), _p(a), _p(b), int(f.size // self.nlm))
+        return a, b
+
+
+class OracleDyn:
+    """CPU restatement of aeros_timestep (dry Held-Suarez path), one member."""
+
+    def __init__(self, params, a_half=None, b_half=None, nthreads=0):
+        L = lib()
+        rc = ctypes.c_int()
+        ah = None if a_half is None else np.ascontiguousarray(a_half, np.float64)
+        bh = None if b_half is None else np.ascontiguousarray(b_half, np.float64)
+        self.params = params
+        self.h = L.ora_dyn_create(ctypes.byref(params), _p(ah), _p(bh), int(nthreads), ctypes.byref(rc))
+        if not self.h:
+            raise ValueError(f"oracle dyn_create failed with status {rc.value}")
+        a, b, c, d = (ctypes.c_int() for _ in range(4))
+        L.ora_dyn_info(ctypes.c_void_p(self.h), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d),
+                       None, None, None)
+        self.nlon, self.nlat, self.nlm, self.nlev = a.value, b.value, c.value, d.value
+        self.A = np.zeros(self.nlev + 1)
+        self.B = np.zeros(self.nlev + 1)
+        self.sigma_full = np.zeros(self.nlev)
+        L.ora_dyn_info(ctypes.c_void_p(self.h), None, None, None, None, _p(self.A), _p(self.B), _p(self.sigma_full))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_dyn_destroy(ctypes.c_void_p(self.h))
+            self.h = None
+
+    @property
+    def _h(self):
+        return ctypes.c_void_p(self.h)
+
+    def _alloc_state(self):
+        return (np.zeros((self.nlev, self.nlm), np.complex128), np.zeros((self.nlev, self.nlm), np.complex128),
+                np.zeros((self.nlev, self.nlm), np.complex128), np.zeros(self.nlm, np.complex128))
+
+    def set_state(self, vor, div, temp, lnps):
+        arrs = [np.ascontiguousarray(a, np.complex128) for a in (vor, div, temp, lnps)]
+        lib().ora_dyn_set_state(self._h, *[_p(a) for a in arrs])
+
+    def get_state(self):
+        s = self._alloc_state()
+        lib().ora_dyn_get_state(self._h, *[_p(a) for a in s])
+        return s
+
+    def get_old_state(self):
+        s = self._alloc_state()
+        lib().ora_dyn_get_old_state(self._h, *[_p(a) for a in s])
+        return s
+
+    def set_old_state(self, vor, div, temp, lnps, nstep):
+        arrs = [np.ascontiguousarray(a, np.complex128) for a in (vor, div, temp, lnps)]
+        lib().ora_dyn_set_old_state(self._h, *[_p(a) for a in arrs], int(nstep))
+
+    def set_isothermal(self, temp=-1.0, ps=-1.0):
+        lib().ora_dyn_set_isothermal(self._h, float(temp), float(ps))
+
+    def set_phis(self, phis):
+        phis = np.ascontiguousarray(phis, np.float64)
+        lib().ora_dyn_set_phis(self._h, _p(phis))
+
+    def set_forcing(self, dt_y, k_a):
+        lib().ora_dyn_set_forcing(self._h, float(dt_y), float(k_a))
+
+    def step(self, n=1):
+        rc = lib().ora_dyn_step(self._h, int(n))
+        if rc:
+            raise RuntimeError(f"oracle step failed: {rc}")
+
+    def tendency(self, forced=False):
+        s = self._alloc_state()
+        fn = lib().ora_dyn_tendency_forced if forced else lib().ora_dyn_tendency
+        fn(self._h, *[_p(a) for a in s])
+        return s
+
+    def grid_rhs(self, forced=False):
+        ng = self.nlon * self.nlat
+        out = np.zeros(4 * ng * self.nlev + ng)
+        lib().ora_dyn_grid_rhs(self._h, int(bool(forced)), _p(out))
+        n3 = ng * self.nlev
+        shp = (self.nlev, self.nlat, self.nlon)
+        return (out[:n3].reshape(shp), out[n3:2 * n3].reshape(shp), out[2 * n3:3 * n3].reshape(shp),
+                out[3 * n3:4 * n3].reshape(shp), out[4 * n3:].reshape(self.nlat, self.nlon))
+
+    def diagnose(self):
+        shp = (self.nlev, self.nlat, self.nlon)
+        u, v, t, ps = np.zeros(shp), np.zeros(shp), np.zeros(shp), np.zeros((self.nlat, self.nlon))
+        lib().ora_dyn_diagnose(self._h, _p(u), _p(v), _p(t), _p(ps))
+        return u, v, t, ps
+
+    def counters(self):
+        n = ctypes.c_int()
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        lib().ora_dyn_counters(self._h, ctypes.byref(n), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return n.value, a.value, b.value, c.value
+
+    def set_mass_target(self, m):
+        lib().ora_dyn_set_mass_target(self._h, float(m))
+
+    def budget(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        lib().ora_dyn_budget(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def diag_accumulate(self):
+        lib().ora_dyn_diag_accumulate(self._h)
+
+    def diag_read(self):
+        nl, n = self.nlat, self.nlev
+        out = np.zeros(7 * nl * n + 2 * nl)
+        ns = ctypes.c_int()
+        lib().ora_dyn_diag_read(self._h, _p(out), ctypes.byref(ns))
+        F = nl * n
+        names = ["u", "v", "temp", "uv", "vt", "eke", "tvar"]
+        d = {nm: out[i * F:(i + 1) * F].reshape(n, nl) for i, nm in enumerate(names)}
+        d["ps"] = out[7 * F:7 * F + nl]
+        d["u_sfc"] = out[7 * F + nl:]
+        d["nsample"] = ns.value
+        return d
+
+    def gwspeed(self):
+        c = ctypes.c_double()
+        lib().ora_dyn_gwspeed(self._h, ctypes.byref(c))
+        return c.value
+
+    def si_linear(self):
+        ld = np.zeros((self.nlev, self.nlm), np.complex128)
+        lt = np.zeros((self.nlev, self.nlm), np.complex128)
+        lp = np.zeros(self.nlm, np.complex128)
+        lib().ora_dyn_si_linear(self._h, _p(ld), _p(lt), _p(lp))
+        return ld, lt, lp
