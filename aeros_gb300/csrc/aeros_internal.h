@@ -1,0 +1,142 @@
+// aeros_internal.h -- shared declarations of the sm_103a spectral dynamics library.
+//
+// Device data layout (all FP64):
+//   spectral   double2 [field][lm], lm m-major (src/aeros_spectral.f90:478)
+//   tables     Legendre tables, hemisphere-folded (north half, nh = nlat/2):
+//                Ps/dPs  [lm][j]    synthesis, Pbar and dPbar/dtheta
+//                PaT/dPaT[m-block][j][l-m]  analysis, w_j-weighted, transposed
+//   Fourier    double2 [j][row][m], m = 0..T   (rows = fields x levels x members)
+//   grid       double  [field][j][i]           (= Fortran (nlon, nlat, field))
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+#include <string>
+#include "../../include/aeros_gpu.h"
+
+namespace aeros {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kOmega = 7.292e-5;    // src/aeros_defs.f90:83
+constexpr double kA = 6.371e6;         // r_earth, :84
+constexpr double kGrav = 9.80665;      // :85
+constexpr double kRd = 287.05;         // :88
+constexpr double kCp = 1004.64;        // :90
+constexpr double kKappa = kRd / kCp;   // :92
+
+void set_error(const std::string &s);
+
+#define AEROS_CUDA(call)                                                       \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            ::aeros::set_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            return AEROS_ERR_CUDA;                                             \
+        }                                                                      \
+    } while (0)
+
+// ---------------------------------------------------------------- FFT plan
+struct FftPlan {
+    int n;          // complex length = nlon / 2
+    int nstage;
+    int rad[12];
+};
+
+// ---------------------------------------------------------------- descriptors
+// Legendre synthesis column: Fourier row(s) of one spectral field.
+struct SynCol {
+    const double2 *src;  // nlm coefficients
+    int scale;           // per-l factor applied to the input (index into lfac table, 0 = 1)
+    int rowP;            // Fourier row for sum_l c Pbar
+    int rowD;            // Fourier row for sum_l c dPbar/dtheta, -1 = none
+    int pad;
+};
+
+// Fourier synthesis output field: grid = FFT^-1[ Nrm * sum_t (a_t + i b_t m/sin) F[src_t] ].
+struct FsynField {
+    int src0, src1;      // Fourier rows (-1 = none)
+    double a0, b0, a1, b1;
+    double *dst;         // grid field base (nlat x nlon)
+};
+
+// Fourier analysis input field: Fourier row = sqrt(2pi)/nlon * FFT[grid].
+struct FanaField {
+    const double *src;   // grid field base (nlat x nlon)
+    int row;             // Fourier row written
+    int pad;
+};
+
+// Legendre analysis output column:
+// out_lm = post(l) [ sum_j Pw X1 + sum_j dPw X2 ] + lfac3(l) sum_j Pw X3,
+// X_t = (a_t + i b_t m/sin) F[row_t].
+struct AnaCol {
+    double2 *dst;
+    int row1, row2, row3;
+    int post;            // lfac table index for the P/dP part (0 = 1)
+    int lf3;             // lfac table index for slot 3
+    int pad;
+    double a1, b1, a2, b2;
+};
+
+// per-l factor tables (device, each T+1 long)
+enum LFac { LF_ONE = 0, LF_INV_LL1 = 1, LF_LL1_A2 = 2, LF_F = 3, LF_G = 4, LF_COUNT = 5 };
+
+// ---------------------------------------------------------------- geometry
+struct Geometry {
+    int T = 0, nlon = 0, nlat = 0, nlm = 0, nh = 0, ms = 0;   // ms = T+1
+    std::vector<int> l_of_lm, m_of_lm, moff;
+    std::vector<double> x, w, sint;                          // (nlat)
+    std::vector<double> Ps, dPs;                             // [lm][j], j < nh
+    std::vector<double> PaT, dPaT;                           // [moff(m)*nh + j*K + (l-m)]
+};
+int grid_size(int trunc, int *nlon, int *nlat);
+int build_geometry(Geometry &g, int trunc, int nlon, int nlat);
+int fft_plan(int n, FftPlan &p);
+
+// Device-side copy of the transform tables.
+struct DevTables {
+    double *Ps = nullptr, *dPs = nullptr, *PaT = nullptr, *dPaT = nullptr;
+    double *sint = nullptr, *x = nullptr, *w = nullptr;
+    double *lfac = nullptr;      // LF_COUNT * (T+1)
+    double2 *tw = nullptr;       // n entries exp(-2 pi i t/n), n = nlon/2
+    double2 *twN = nullptr;      // nlon/2+1 entries exp(-2 pi i k/nlon)
+    int *moff = nullptr;         // (T+1)
+    int *l_of_lm = nullptr;
+    FftPlan plan{};
+};
+int upload_tables(const Geometry &g, DevTables &t);
+void free_tables(DevTables &t);
+
+// Launch context for the transform kernels.
+struct Ctx {
+    int T, nlon, nlat, nh, nlm, ms;
+    const DevTables *tab;
+    cudaStream_t stream;
+    long long *launches;         // launch counter (host)
+};
+
+// ---------------------------------------------------------------- kernels
+// Legendre synthesis plan: columns [0, ncolD_first) produce Pbar sums only,
+// [ncolD_first, ncol) also dPbar sums; tiles never straddle the boundary.
+struct SynPlan {
+    SynCol *cols_d = nullptr;
+    int *tiles_d = nullptr;
+    int ncol = 0, ncolD_first = 0, ntile = 0;
+};
+int make_syn_plan(const std::vector<SynCol> &colsP, const std::vector<SynCol> &colsPD, SynPlan &p);
+void free_syn_plan(SynPlan &p);
+// Legendre synthesis sums (FP64).
+int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow);
+// Fourier synthesis: nf fields, Fourier buffer F with nrow rows per latitude.
+int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow);
+// Fourier analysis.
+int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow);
+// Legendre analysis (FP64).
+int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
+
+// Elementwise helpers.
+int launch_laplacian(const Ctx &c, double2 *coeffs, int inverse, int nbatch);
+int launch_surface_integral(const Ctx &c, const double *field, double *partial, double *total, int nbatch);
+
+}  // namespace aeros

@@ -1,0 +1,1412 @@
+// dyn.cu -- the dry spectral time step on sm_103a (FP64 path).
+//
+// One step of aeros_timestep_step (src/dynamics/aeros_timestep.f90:776-1137,
+// dry Held-Suarez subset) for every ensemble member at once, as a CUDA graph
+// of these launches:
+//   1 Legendre synthesis sums of vor, div, T, lnps         (transforms.cu)
+//   2 longitude FFTs -> 7 nlev + 3 grid fields            (transforms.cu)
+//   3 column kernel: aeros_tendency column_terms + Held-Suarez forcing
+//   4 longitude FFTs of ae, an, Phi+K, dT/dt, dlnps/dt    (transforms.cu)
+//   5 Legendre analysis -> spectral tendencies            (transforms.cu)
+//   6 spectral kernel: vorticity leapfrog, semi-implicit solve, del^ndiff
+//     diffusion, RAW filter, time-level shift (in place)
+//   7-8 mass fixer: lnps synthesis + exp + quadrature, then the (0,0) fix
+// The start-up step (h = dt, old <- now, mass target capture) is its own graph.
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <cuda_runtime.h>
+#include "aeros_internal.h"
+#include "fft.cuh"
+#include "split.h"
+
+using namespace aeros;
+
+namespace {
+
+constexpr int kMaxLev = 32;   // warp-per-coefficient solve: one lane per level
+constexpr double kNrmD = 0.39894228040143267794;   // 1/sqrt(2 pi)
+
+// Per-level constants of the vertical coordinate (src/dynamics/aeros_vertical.f90).
+// A level is "pure" when both bounding half levels have A = 0 and the upper one
+// B > 0: then dlnp, alpha and c are pressure-independent and precomputed.
+struct LevConst {
+    double A0, A1, B0, B1, dB;
+    double dlnp, alpha, cfac;     // valid when pure
+    double lnbf, bfk;             // ln(bf), bf^kappa with p_full = bf ps (pure)
+    int pure;
+    int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
+};
+__constant__ LevConst c_lev[kMaxLev];
+
+struct HsConst {
+    double t_eq, t_min, dtheta_z, sigma_b, p0, k_s, k_f, lnp0;
+};
+__constant__ HsConst c_hs;
+
+// ---------------------------------------------------------------- column kernel
+// Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
+// dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy.  Outputs GA[e][f][j][i]:
+// ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.  One thread per column.
+__global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
+                                                int nlon, int nlat, int M, const double *__restrict__ xlat,
+                                                const double *__restrict__ phis, int hs_on,
+                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
+    const long ng = (long)nlon * nlat;
+    long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (gid >= ng * M) return;
+    const int e = (int)(gid / ng);
+    const long c = gid - e * ng;
+    const int j = (int)(c / nlon);
+    const double *Gf = G + (size_t)e * (7 * NL + 3) * ng + c;
+    double *Go = GA + (size_t)e * (4 * NL + 1) * ng + c;
+#define GF(f) Gf[(size_t)(f) * ng]
+#define GO(f) Go[(size_t)(f) * ng]
+    const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
+    const double ps = exp(lnps);
+    double dp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev], gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1],
+        phi[kMaxLev];
+    scum[0] = 0.0;
+    for (int k = 0; k < NL; ++k) {
+        const LevConst &L = c_lev[k];
+        double ph0 = L.A0 + L.B0 * ps, ph1 = L.A1 + L.B1 * ps;
+        double d = ph1 - ph0;
+        dp[k] = d;
+        if (L.pure) {
+            dlnp[k] = L.dlnp;
+            alpha[k] = L.alpha;
+            cfac[k] = L.cfac;
+        } else {
+            double dl, al;
+            if (ph0 <= 0.0) {
+                al = 0.69314718055994530942;   // ln 2 (Simmons-Burridge top layer)
+                dl = 0.0;                      // zero-pressure top: substituted 0
+            } else {
+                dl = log(ph1 / ph0);
+                al = 1.0 - (ph0 / d) * dl;
+            }
+            dlnp[k] = dl;
+            alpha[k] = al;
+            cfac[k] = (ps / d) * (L.B0 * dl + L.dB * al);
+        }
+        double u = GF(k), v = GF(NL + k), dv = GF(3 * NL + k);
+        double g = u * dpx + v * dpy;
+        gc[k] = g;
+        double cmass = d * dv + L.dB * ps * g;
+        cm[k] = cmass;
+        scum[k + 1] = scum[k] + cmass;
+    }
+    GO(4 * NL) = -scum[NL] / ps;
+    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474)
+    {
+        double phh = phis ? phis[c] : 0.0;
+        for (int k = NL - 1; k >= 0; --k) {
+            double t = GF(4 * NL + k);
+            phi[k] = phh + alpha[k] * kRd * t;
+            phh = phh + kRd * t * dlnp[k];
+        }
+    }
+    const double SN = scum[NL];
+    const double f = 2.0 * kOmega * xlat[j];
+    const double x2 = xlat[j] * xlat[j], c2 = 1.0 - x2, c4 = c2 * c2;
+    double dty = 0, ka = 0, psk = 0, lnpr = 0;
+    if (hs_on) {
+        dty = hs_dty[e];
+        ka = hs_ka[e];
+        lnpr = lnps - c_hs.lnp0;
+        psk = exp(kKappa * lnpr);   // (ps/p0)^kappa
+    }
+    double up = 0, vp = 0, tp = 0;                    // level k-1
+    double uc = GF(0), vc = GF(NL), tc = GF(4 * NL);  // level k
+    for (int k = 0; k < NL; ++k) {
+        const LevConst &L = c_lev[k];
+        double un = 0, vn = 0, tn = 0;
+        if (k + 1 < NL) {
+            un = GF(k + 1);
+            vn = GF(NL + k + 1);
+            tn = GF(4 * NL + k + 1);
+        }
+        const double d = dp[k];
+        const double omega = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cm[k]) / d;
+        const double mup = L.B0 * SN - scum[k];        // M at half level k (above)
+        const double mlo = L.B1 * SN - scum[k + 1];    // M at half level k+1 (below)
+        double vu = 0.5 * (((k < NL - 1) ? mlo * (un - uc) : 0.0) + ((k > 0) ? mup * (uc - up) : 0.0)) / d;
+        double vv = 0.5 * (((k < NL - 1) ? mlo * (vn - vc) : 0.0) + ((k > 0) ? mup * (vc - vp) : 0.0)) / d;
+        double vt = 0.5 * (((k < NL - 1) ? mlo * (tn - tc) : 0.0) + ((k > 0) ? mup * (tc - tp) : 0.0)) / d;
+        const double zf = GF(2 * NL + k) + f;
+        const double pgf = kRd * tc * cfac[k];
+        double ae = zf * vc - vu - pgf * dpx;
+        double an = -zf * uc - vv - pgf * dpy;
+        double ek = phi[k] + 0.5 * (uc * uc + vc * vc);
+        double dtdt = -(uc * GF(5 * NL + k) + vc * GF(6 * NL + k)) - vt + kKappa * tc * omega;
+        if (hs_on) {
+            // src/physics/aeros_held_suarez.f90:177-293
+            double pf, sig, lnpf, pfk;
+            if (L.pure) {
+                sig = 0.5 * (L.B0 + L.B1);
+                lnpf = L.lnbf + lnpr;
+                pfk = L.bfk * psk;
+            } else {
+                pf = 0.5 * ((L.A0 + L.B0 * ps) + (L.A1 + L.B1 * ps));
+                sig = pf / ps;
+                lnpf = log(pf / c_hs.p0);
+                pfk = exp(kKappa * lnpf);
+            }
+            double teq = (c_hs.t_eq - dty * x2 - c_hs.dtheta_z * lnpf * c2) * pfk;
+            teq = fmax(c_hs.t_min, teq);
+            double hf = fmax(0.0, (sig - c_hs.sigma_b) / (1.0 - c_hs.sigma_b));
+            double kt = ka + (c_hs.k_s - ka) * hf * c4;
+            double kv = c_hs.k_f * hf;
+            dtdt -= kt * (tc - teq);
+            ae -= kv * uc;
+            an -= kv * vc;
+        }
+        GO(k) = ae;
+        GO(NL + k) = an;
+        GO(2 * NL + k) = ek;
+        GO(3 * NL + k) = dtdt;
+        up = uc; vp = vc; tp = tc;
+        uc = un; vc = vn; tc = tn;
+    }
+#undef GF
+#undef GO
+}
+
+// ---------------------------------------------------------------- spectral kernel
+// Warp per (member, lm); lane k = level.  Semi-implicit correction form of
+// src/dynamics/aeros_semiimp.f90:462-571 (factors replaced by the explicit
+// inverse of I + alpha^2 h^2 lambda_l W, built in FP64 on the host), the
+// vorticity leapfrog (aeros_timestep.f90:1043-1047), implicit del^ndiff
+// diffusion (:1673-1726) and the RAW filter (:1762-1815).  In place: the
+// filtered X^n is written to the old slot, X^(n+1) to the now slot.
+struct SpecArgs {
+    double2 *vor, *div, *tmp, *lnps;          // now (in: X^n, out: X^(n+1))
+    double2 *vor_o, *div_o, *tmp_o, *lnps_o;  // old (in: X^(n-1), out: filtered X^n)
+    const double2 *tv, *td, *tt, *tp;         // tendencies
+    const double *GT, *TT, *WT;               // transposed [j][k] nlev x nlev
+    const double *nu, *pcoef;
+    const double *MinvT;                      // [l][j][k]
+    const double *dfac;                       // (T+1) diffusion factor for this h
+    const int *l_of_lm;
+    int nlm, NL, M;
+    double h, a1, astep, hh_old;
+    double half_nu, raw_alpha, raw_beta;
+    int semi_implicit, raw_on;
+    int *flag;                                // non-finite sentinel
+};
+
+__device__ __forceinline__ double2 shfl2(double2 v, int src) {
+    return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ double2 wsum2(double2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_spectral(SpecArgs a) {
+    __shared__ double sG[kMaxLev * kMaxLev], sT[kMaxLev * kMaxLev], sW[kMaxLev * kMaxLev];
+    __shared__ double sNu[kMaxLev], sPc[kMaxLev];
+    const int NL = a.NL;
+    for (int i = threadIdx.x; i < NL * NL; i += blockDim.x) {
+        sG[i] = a.GT[i];
+        sT[i] = a.TT[i];
+        sW[i] = a.WT[i];
+    }
+    for (int i = threadIdx.x; i < NL; i += blockDim.x) {
+        sNu[i] = a.nu[i];
+        sPc[i] = a.pcoef[i];
+    }
+    __syncthreads();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= a.nlm * a.M) return;
+    const int e = warp / a.nlm, lm = warp - e * a.nlm;
+    const int l = a.l_of_lm[lm];
+    const double lam = (double)l * (l + 1) / (kA * kA);
+    const bool act = lane < NL;
+    const int k = act ? lane : 0;
+    const size_t o = ((size_t)e * NL + k) * a.nlm + lm;
+    const size_t op = (size_t)e * a.nlm + lm;
+    const double2 z = make_double2(0.0, 0.0);
+    double2 vo = act ? a.vor_o[o] : z, vn = act ? a.vor[o] : z, tv = act ? a.tv[o] : z;
+    double2 dold = act ? a.div_o[o] : z, dnow = act ? a.div[o] : z, rd = act ? a.td[o] : z;
+    double2 told = act ? a.tmp_o[o] : z, tnow = act ? a.tmp[o] : z, rt = act ? a.tt[o] : z;
+    double2 pold = a.lnps_o[op], pnow = a.lnps[op], rp = a.tp[op];
+    const double h = a.h;
+    double2 vnew = make_double2(vo.x + h * tv.x, vo.y + h * tv.y);
+    double2 dnew, tnew, pnew;
+    if (a.semi_implicit) {
+        // L(X^n): ltnow = -tau dnow (lower), lpnow = -nu . dnow, ldnow = lam (G tnow + pcoef pnow)
+        double2 ltn = z, ldn = z, lds = z, wd = z;
+        for (int j = 0; j < NL; ++j) {
+            double2 dj = shfl2(dnow, j), tj = shfl2(tnow, j), oj = shfl2(dold, j);
+            double tk = sT[j * NL + k], gk = sG[j * NL + k], wk = sW[j * NL + k];
+            ltn.x -= tk * dj.x; ltn.y -= tk * dj.y;          // tau[k][j] = 0 for j > k
+            ldn.x += gk * tj.x; ldn.y += gk * tj.y;          // G[k][j] = 0 for j < k
+            wd.x += wk * oj.x; wd.y += wk * oj.y;
+        }
+        double2 nd = wsum2(act ? make_double2(sNu[k] * dnow.x, sNu[k] * dnow.y) : z);
+        double2 lpn = make_double2(-nd.x, -nd.y);
+        double pc = sPc[k];
+        ldn = make_double2(lam * (ldn.x + pc * pnow.x), lam * (ldn.y + pc * pnow.y));
+        double2 tst = make_double2(told.x + a.astep * (rt.x - ltn.x), told.y + a.astep * (rt.y - ltn.y));
+        double2 pst = make_double2(pold.x + a.astep * (rp.x - lpn.x), pold.y + a.astep * (rp.y - lpn.y));
+        for (int j = 0; j < NL; ++j) {
+            double2 tj = shfl2(tst, j);
+            double gk = sG[j * NL + k];
+            lds.x += gk * tj.x; lds.y += gk * tj.y;
+        }
+        lds = make_double2(lam * (lds.x + pc * pst.x), lam * (lds.y + pc * pst.y));
+        double2 rhs = make_double2(dold.x - a.hh_old * lam * wd.x + h * (rd.x + lds.x - ldn.x),
+                                   dold.y - a.hh_old * lam * wd.y + h * (rd.y + lds.y - ldn.y));
+        const double *Mi = a.MinvT + (size_t)l * NL * NL;
+        dnew = z;
+        for (int j = 0; j < NL; ++j) {
+            double2 rj = shfl2(rhs, j);
+            double mk = act ? Mi[j * NL + k] : 0.0;
+            dnew.x += mk * rj.x; dnew.y += mk * rj.y;
+        }
+        double2 db = make_double2(a.a1 * dnew.x + (1.0 - a.a1) * dold.x, a.a1 * dnew.y + (1.0 - a.a1) * dold.y);
+        double2 td = z;
+        for (int j = 0; j < NL; ++j) {
+            double2 bj = shfl2(db, j);
+            double tk = sT[j * NL + k];
+            td.x += tk * bj.x; td.y += tk * bj.y;
+        }
+        tnew = make_double2(told.x + h * (rt.x - td.x - ltn.x), told.y + h * (rt.y - td.y - ltn.y));
+        double2 nb = wsum2(act ? make_double2(sNu[k] * db.x, sNu[k] * db.y) : z);
+        pnew = make_double2(pold.x + h * (rp.x - nb.x - lpn.x), pold.y + h * (rp.y - nb.y - lpn.y));
+    } else {
+        dnew = make_double2(dold.x + h * rd.x, dold.y + h * rd.y);
+        tnew = make_double2(told.x + h * rt.x, told.y + h * rt.y);
+        pnew = make_double2(pold.x + h * rp.x, pold.y + h * rp.y);
+    }
+    const double fd = a.dfac[l];
+    vnew = make_double2(vnew.x * fd, vnew.y * fd);
+    dnew = make_double2(dnew.x * fd, dnew.y * fd);
+    tnew = make_double2(tnew.x * fd, tnew.y * fd);
+    if (a.raw_on) {
+        auto filt = [&](double2 xo, double2 &xn, double2 &xw) {
+            double dx = a.half_nu * (xo.x - 2.0 * xn.x + xw.x), dy = a.half_nu * (xo.y - 2.0 * xn.y + xw.y);
+            xn.x += a.raw_alpha * dx; xn.y += a.raw_alpha * dy;
+            xw.x -= a.raw_beta * dx; xw.y -= a.raw_beta * dy;
+        };
+        filt(vo, vn, vnew);
+        filt(dold, dnow, dnew);
+        filt(told, tnow, tnew);
+        filt(pold, pnow, pnew);
+    }
+    bool bad = !(isfinite(vnew.x) && isfinite(vnew.y) && isfinite(dnew.x) && isfinite(dnew.y) &&
+                 isfinite(tnew.x) && isfinite(tnew.y) && isfinite(pnew.x) && isfinite(pnew.y));
+    if (act) {
+        if (bad) atomicOr(a.flag, 1);
+        a.vor_o[o] = vn; a.div_o[o] = dnow; a.tmp_o[o] = tnow;
+        a.vor[o] = vnew; a.div[o] = dnew; a.tmp[o] = tnew;
+    }
+    if (lane == 0) {
+        a.lnps_o[op] = pnow;
+        a.lnps[op] = pnew;
+    }
+}
+
+// Copy X^n into the old slot (start-up step, aeros_timestep.f90:825-828).
+__global__ void k_copy(double2 *dst, const double2 *src, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------- mass fixer
+// Per (member, north latitude): synthesize lnps on the two mirrored rows,
+// exponentiate and sum each row (src/dynamics/aeros_timestep.f90:1253-1276).
+__global__ void k_mass_rows(const double2 *__restrict__ lnps, int M, int T, int nlm, int nh, int nlat, int nlon,
+                            const double *__restrict__ Ps, const int *__restrict__ moff, FftPlan plan,
+                            const double2 *__restrict__ tw, const double2 *__restrict__ twN,
+                            double *__restrict__ rows) {
+    extern __shared__ double2 sm[];
+    const int n = nlon / 2, ms = T + 1;
+    const int e = blockIdx.y, jn = blockIdx.x, js = nlat - 1 - jn;
+    double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * n;
+    const double2 *c = lnps + (size_t)e * nlm;
+    for (int m = threadIdx.x; m <= T; m += blockDim.x) {
+        double2 ev = make_double2(0, 0), od = make_double2(0, 0);
+        int mo = moff[m];
+        for (int l = m; l <= T; ++l) {
+            double p = Ps[(size_t)(mo + l - m) * nh + jn];
+            double2 v = c[mo + l - m];
+            if ((l - m) & 1) { od.x += p * v.x; od.y += p * v.y; }
+            else { ev.x += p * v.x; ev.y += p * v.y; }
+        }
+        Fn[m] = cadd(ev, od);
+        Fs[m] = csub(ev, od);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 2 * n; idx += blockDim.x) {
+        int r = idx / n, k = idx - r * n;
+        const double2 *F = r ? Fs : Fn;
+        double2 xk = make_double2(0, 0), xc = make_double2(0, 0);
+        int kc = n - k;
+        if (k <= T) { xk = F[k]; if (k == 0) xk.y = 0.0; }
+        if (kc <= T && kc < n) xc = F[kc];
+        double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
+        double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
+        double2 O = cmulconj(D, twN[k]);
+        A[idx] = make_double2((E.x - O.y) * kNrmD, (E.y + O.x) * kNrmD);
+    }
+    __syncthreads();
+    double2 *res = fft_rows<true>(A, B, 2, n, plan, tw, threadIdx.x, blockDim.x);
+    const double *rr = reinterpret_cast<const double *>(res);
+    __shared__ double red[2][128];
+    for (int r = 0; r < 2; ++r) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < nlon; i += blockDim.x) s += exp(rr[(size_t)r * nlon + i]);
+        red[r][threadIdx.x] = s;
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + o];
+            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        rows[(size_t)e * nlat + jn] = red[0][0];
+        rows[(size_t)e * nlat + js] = red[1][0];
+    }
+}
+
+// mode 0: capture the target; mode 1: restore it (aeros_timestep.f90:1225-1251).
+__global__ void k_mass_fix(double2 *lnps, int nlm, int M, const double *__restrict__ rows,
+                           const double *__restrict__ w, int nlat, int nlon, double c00, double *target,
+                           double *lnr_last, double *lnr_cum, int mode) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M) return;
+    const double dlon = 2.0 * kPi / nlon;
+    double t = 0.0;
+    for (int j = 0; j < nlat; ++j) t += w[j] * rows[(size_t)e * nlat + j] * dlon;
+    double mass = t * kA * kA / kGrav;
+    if (mode == 0) {
+        if (target[e] < 0.0) target[e] = mass;
+        return;
+    }
+    double lnr = log(target[e] / mass);
+    lnps[(size_t)e * nlm].x += lnr * c00;
+    lnr_last[e] = lnr;
+    lnr_cum[e] += lnr;
+}
+
+// ---------------------------------------------------------------- diagnostics
+__global__ void k_exp_inplace(double *p, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = exp(p[i]);
+}
+
+// Budget (src/aeros_budget.f90:61-142): per (member, latitude) row sums.
+// D[e][f][j][i]: u_k, v_k, T_k (3 nlev), ps.
+__global__ void k_budget_rows(const double *__restrict__ D, int NL, int nlon, int nlat,
+                              const double *__restrict__ phis, const double *__restrict__ xlat,
+                              double *__restrict__ out) {
+    __shared__ double red[3][128];
+    const int e = blockIdx.y, j = blockIdx.x;
+    const size_t ng = (size_t)nlon * nlat;
+    const double *De = D + (size_t)e * (3 * NL + 1) * ng;
+    const double coslat = sqrt((1.0 - xlat[j]) * (1.0 + xlat[j]));
+    double sm = 0, se = 0, sa = 0;
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+        size_t c = (size_t)j * nlon + i;
+        double ps = De[(size_t)3 * NL * ng + c];
+        double ce = 0, ca = 0;
+        for (int k = 0; k < NL; ++k) {
+            const LevConst &L = c_lev[k];
+            double dpk = (L.A1 + L.B1 * ps) - (L.A0 + L.B0 * ps);
+            double u = De[(size_t)k * ng + c], v = De[(size_t)(NL + k) * ng + c], t = De[(size_t)(2 * NL + k) * ng + c];
+            ce += dpk * (kCp * t + 0.5 * (u * u + v * v));
+            ca += dpk * (u + kOmega * kA * coslat) * kA * coslat;
+        }
+        if (phis) ce += phis[c] * ps;
+        sm += ps;
+        se += ce;
+        sa += ca;
+    }
+    red[0][threadIdx.x] = sm;
+    red[1][threadIdx.x] = se;
+    red[2][threadIdx.x] = sa;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; ++q) out[((size_t)e * nlat + j) * 3 + q] = red[q][0];
+}
+
+__global__ void k_budget_final(const double *__restrict__ rows, const double *__restrict__ w, int nlat, int nlon,
+                               int M, double *__restrict__ res) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M) return;
+    double dlon = 2.0 * kPi / nlon, s[3] = {0, 0, 0};
+    for (int j = 0; j < nlat; ++j) {
+        double area = w[j] * dlon * kA * kA;
+        for (int q = 0; q < 3; ++q) s[q] += area * rows[((size_t)e * nlat + j) * 3 + q];
+    }
+    for (int q = 0; q < 3; ++q) res[(size_t)e * 3 + q] = s[q] / kGrav;
+}
+
+// Zonal means (src/aeros_diagnostics.f90:153-241): one CTA per (level, lat, member).
+__global__ void k_zonal(const double *__restrict__ D, int NL, int nlon, int nlat, double *__restrict__ acc) {
+    __shared__ double red[4][128];
+    const int j = blockIdx.x, k = blockIdx.y, e = blockIdx.z;
+    const size_t ng = (size_t)nlon * nlat;
+    const double *De = D + (size_t)e * (3 * NL + 1) * ng;
+    const double *U = De + (size_t)k * ng + (size_t)j * nlon, *V = De + (size_t)(NL + k) * ng + (size_t)j * nlon,
+                 *Tt = De + (size_t)(2 * NL + k) * ng + (size_t)j * nlon;
+    const double rn = 1.0 / nlon;
+    double a = 0, b = 0, c = 0;
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) { a += U[i]; b += V[i]; c += Tt[i]; }
+    red[0][threadIdx.x] = a; red[1][threadIdx.x] = b; red[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    const double um = red[0][0] * rn, vm = red[1][0] * rn, tm = red[2][0] * rn;
+    __syncthreads();
+    double uv = 0, vt = 0, ek = 0, tv = 0;
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+        double up = U[i] - um, vp = V[i] - vm, tp = Tt[i] - tm;
+        uv += up * vp; vt += vp * tp; ek += 0.5 * (up * up + vp * vp); tv += tp * tp;
+    }
+    red[0][threadIdx.x] = uv; red[1][threadIdx.x] = vt; red[2][threadIdx.x] = ek; red[3][threadIdx.x] = tv;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const size_t F = (size_t)nlat * NL;
+        double *A = acc + (size_t)e * (7 * F + 2 * nlat);
+        size_t o = (size_t)k * nlat + j;
+        A[o] += um; A[F + o] += vm; A[2 * F + o] += tm;
+        A[3 * F + o] += red[0][0] * rn; A[4 * F + o] += red[1][0] * rn;
+        A[5 * F + o] += red[2][0] * rn; A[6 * F + o] += red[3][0] * rn;
+        if (k == 0) {
+            double ps = 0, us = 0;
+            const double *P = De + (size_t)3 * NL * ng + (size_t)j * nlon;
+            const double *Us = De + (size_t)(NL - 1) * ng + (size_t)j * nlon;
+            for (int i = 0; i < nlon; ++i) { ps += P[i]; us += Us[i]; }
+            A[7 * F + j] += ps * rn;
+            A[7 * F + nlat + j] += us * rn;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- host helpers
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int lu_inverse(std::vector<double> &A, int n, std::vector<double> &inv) {
+    // Doolittle with partial pivoting (src/dynamics/aeros_semiimp.f90:658-750),
+    // then solve for each unit vector.
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; ++k) {
+        int ip = k;
+        double amax = std::fabs(A[k * n + k]);
+        for (int i = k + 1; i < n; ++i)
+            if (std::fabs(A[i * n + k]) > amax) { amax = std::fabs(A[i * n + k]); ip = i; }
+        if (amax <= 0.0) return AEROS_ERR_SINGULAR;
+        piv[k] = ip;
+        if (ip != k)
+            for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[ip * n + j]);
+        for (int i = k + 1; i < n; ++i) {
+            A[i * n + k] /= A[k * n + k];
+            for (int j = k + 1; j < n; ++j) A[i * n + j] -= A[i * n + k] * A[k * n + j];
+        }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    std::vector<double> b(n);
+    for (int col = 0; col < n; ++col) {
+        std::fill(b.begin(), b.end(), 0.0);
+        b[col] = 1.0;
+        for (int k = 0; k < n; ++k) {
+            if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+            for (int j = k + 1; j < n; ++j) b[j] -= A[j * n + k] * b[k];
+        }
+        for (int k = n - 1; k >= 0; --k) {
+            for (int j = k + 1; j < n; ++j) b[k] -= A[k * n + j] * b[j];
+            b[k] /= A[k * n + k];
+        }
+        for (int r = 0; r < n; ++r) inv[(size_t)r * n + col] = b[r];
+    }
+    return AEROS_OK;
+}
+
+}  // namespace
+
+// =========================================================================
+struct aeros_dyn_s {
+    aeros_params par{};
+    Geometry g;
+    DevTables tab;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int M = 1, NL = 0;
+    long long launches = 0;
+    // vertical grid (host)
+    std::vector<double> A, B, sigma_half, sigma_full;
+    double ps_ref = 0, t_ref = 0;
+    // semi-implicit operators (host, row-major [k][j])
+    std::vector<double> Gm, Tm, Wm, nu, pcoef;
+    // device state
+    double2 *now = nullptr, *old = nullptr, *tnd = nullptr;   // each: M*(3 NL nlm + nlm)
+    double2 *FS = nullptr, *FA = nullptr;
+    double *G = nullptr, *GA = nullptr, *D = nullptr;          // grid fields, rhs, diagnostics
+    double *GT_d = nullptr, *TT_d = nullptr, *WT_d = nullptr, *nu_d = nullptr, *pc_d = nullptr;
+    double *Minv_d[2] = {nullptr, nullptr};                    // h = dt, 2 dt
+    double *dfac_d[2] = {nullptr, nullptr};
+    double *xlat_d = nullptr, *phis_d = nullptr;
+    bool phis_set = false;
+    double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
+    double *mass_rows = nullptr, *mass_tgt = nullptr, *lnr_last = nullptr, *lnr_cum = nullptr;
+    double *bud_rows = nullptr, *bud_res = nullptr, *zm = nullptr;
+    int nsample = 0;
+    int *flag = nullptr;
+    double c00 = 0;
+    int nrowS = 0, nrowA = 0;
+    SynPlan synS, synD;
+    FsynField *fsS = nullptr, *fsD = nullptr;
+    int nfsS = 0, nfsD = 0;
+    FanaField *faS = nullptr;
+    int nfaS = 0;
+    AnaCol *acS = nullptr;
+    int nacS = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // start-up, regular
+    long long graph_kernels[2] = {0, 0};
+    int nstep = 0;
+    std::vector<cudaEvent_t> *prof = nullptr;        // events recorded after each launch
+    std::vector<std::string> *prof_names = nullptr;
+    double2 *stage = nullptr;                        // host transfer staging
+    size_t stage_bytes = 0;
+    SplitCtx *split = nullptr;
+
+    size_t ns3() const { return (size_t)NL * g.nlm; }
+    size_t nstate() const { return (size_t)M * (3 * ns3() + g.nlm); }
+    double2 *vor(double2 *b) const { return b; }
+    double2 *div(double2 *b) const { return b + (size_t)M * ns3(); }
+    double2 *tmp(double2 *b) const { return b + (size_t)2 * M * ns3(); }
+    double2 *lnp(double2 *b) const { return b + (size_t)3 * M * ns3(); }
+    Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches}; }
+};
+
+namespace {
+
+using Dyn = aeros_dyn_s;
+
+// Record a profiling event after a launch (no-op outside aeros_dyn_profile_step).
+void mark(Dyn &d, const char *name) {
+    if (!d.prof) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, d.stream);
+    d.prof->push_back(e);
+    d.prof_names->push_back(name);
+}
+
+int build_vgrid(Dyn &d, const double *a_half, const double *b_half) {
+    const aeros_params &p = d.par;
+    const int n = p.nlev;
+    if (n < 2) return AEROS_ERR_ARG;
+    if (!(p.stretch_a > 0.0 && p.stretch_a <= 1.0)) return AEROS_ERR_ARG;
+    if (p.sigma_t < 0.0 || p.sigma_t >= 1.0) return AEROS_ERR_ARG;
+    d.A.assign(n + 1, 0.0);
+    d.B.assign(n + 1, 0.0);
+    d.sigma_half.assign(n + 1, 0.0);
+    d.sigma_full.assign(n, 0.0);
+    const double psr = p.ps_ref;
+    if (a_half && b_half) {
+        if (b_half[n] != 1.0 || a_half[n] != 0.0 || b_half[0] != 0.0) return AEROS_ERR_ARG;
+        for (int j = 0; j <= n; ++j) {
+            d.A[j] = a_half[j];
+            d.B[j] = b_half[j];
+            d.sigma_half[j] = d.A[j] / psr + d.B[j];
+        }
+    } else {
+        // src/dynamics/aeros_vertical.f90:230-283
+        double st = p.p_top / psr;
+        for (int j = 0; j <= n; ++j) {
+            double x = (double)j / n;
+            double s = 1.0 - (p.stretch_a * (1.0 - x) + (1.0 - p.stretch_a) * std::pow(1.0 - x, p.stretch_r));
+            d.sigma_half[j] = st + (1.0 - st) * s;
+        }
+        for (int j = 0; j <= n; ++j) {
+            if (p.sigma_t <= 0.0) d.B[j] = d.sigma_half[j];
+            else if (d.sigma_half[j] <= p.sigma_t) d.B[j] = 0.0;
+            else d.B[j] = (d.sigma_half[j] - p.sigma_t) / (1.0 - p.sigma_t);
+            d.A[j] = (d.sigma_half[j] - d.B[j]) * psr;
+        }
+        d.B[n] = 1.0; d.A[n] = 0.0; d.B[0] = 0.0; d.A[0] = p.p_top;
+        d.sigma_half[n] = 1.0;
+        d.sigma_half[0] = p.p_top / psr;
+    }
+    for (int k = 0; k < n; ++k) d.sigma_full[k] = 0.5 * (d.sigma_half[k + 1] + d.sigma_half[k]);
+    for (int j = 1; j <= n; ++j)
+        if (d.A[j] + d.B[j] * psr <= d.A[j - 1] + d.B[j - 1] * psr) return AEROS_ERR_ARG;
+    d.ps_ref = psr;
+    d.t_ref = p.t_ref;
+    return AEROS_OK;
+}
+
+// Semi-implicit operators (src/dynamics/aeros_semiimp.f90:171-276).
+void build_si(Dyn &d) {
+    const int n = d.NL;
+    std::vector<double> ph(n + 1), dp(n), al(n), dl(n);
+    for (int j = 0; j <= n; ++j) ph[j] = d.A[j] + d.B[j] * d.ps_ref;
+    for (int k = 0; k < n; ++k) {
+        dp[k] = ph[k + 1] - ph[k];
+        if (ph[k] <= 0.0) { al[k] = std::log(2.0); dl[k] = 0.0; }
+        else { dl[k] = std::log(ph[k + 1] / ph[k]); al[k] = 1.0 - (ph[k] / dp[k]) * dl[k]; }
+    }
+    d.Gm.assign((size_t)n * n, 0.0);
+    d.Tm.assign((size_t)n * n, 0.0);
+    d.Wm.assign((size_t)n * n, 0.0);
+    d.nu.assign(n, 0.0);
+    d.pcoef.assign(n, 0.0);
+    for (int k = 0; k < n; ++k) {
+        d.Gm[k * n + k] = kRd * al[k];
+        for (int j = k + 1; j < n; ++j) d.Gm[k * n + j] = kRd * dl[j];
+        d.Tm[k * n + k] = kKappa * d.t_ref * al[k];
+        for (int j = 0; j < k; ++j) d.Tm[k * n + j] = kKappa * d.t_ref * dl[k] * dp[j] / dp[k];
+        d.nu[k] = dp[k] / d.ps_ref;
+        d.pcoef[k] = kRd * d.t_ref;
+    }
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) {
+            double acc = d.pcoef[k] * d.nu[j];
+            for (int m = 0; m < n; ++m) acc += d.Gm[k * n + m] * d.Tm[m * n + j];
+            d.Wm[k * n + j] = acc;
+        }
+}
+
+template <typename T>
+int dalloc(T *&p, size_t n) {
+    if (cudaMalloc(&p, n * sizeof(T) + 16) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation failed");
+        return AEROS_ERR_NOMEM;
+    }
+    cudaMemset(p, 0, n * sizeof(T) + 16);
+    return AEROS_OK;
+}
+template <typename T>
+int dput(T *&p, const std::vector<T> &v) {
+    int rc = dalloc(p, v.size());
+    if (rc) return rc;
+    AEROS_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
+// Build the per-step descriptors (row layout documented at the top of the file).
+int build_descriptors(Dyn &d) {
+    const int NL = d.NL, M = d.M, nlm = d.g.nlm;
+    const size_t ng = (size_t)d.g.nlon * d.g.nlat;
+    const double ia = 1.0 / kA;
+    d.nrowS = 8 * NL + 2;
+    d.nrowA = 4 * NL + 1;
+    std::vector<SynCol> sp, spd;
+    std::vector<FsynField> fs;
+    std::vector<FanaField> fa;
+    std::vector<AnaCol> ac;
+    for (int e = 0; e < M; ++e) {
+        const int R = e * d.nrowS, RA = e * d.nrowA;
+        auto V = [&](int k) { return d.vor(d.now) + ((size_t)e * NL + k) * nlm; };
+        auto Dv = [&](int k) { return d.div(d.now) + ((size_t)e * NL + k) * nlm; };
+        auto Tv = [&](int k) { return d.tmp(d.now) + ((size_t)e * NL + k) * nlm; };
+        const double2 *Pv = d.lnp(d.now) + (size_t)e * nlm;
+        for (int k = 0; k < NL; ++k) sp.push_back(SynCol{V(k), LF_ONE, R + k, -1, 0});
+        for (int k = 0; k < NL; ++k) sp.push_back(SynCol{Dv(k), LF_ONE, R + NL + k, -1, 0});
+        for (int k = 0; k < NL; ++k) spd.push_back(SynCol{V(k), LF_G, R + 2 * NL + k, R + 5 * NL + 1 + k, 0});
+        for (int k = 0; k < NL; ++k) spd.push_back(SynCol{Dv(k), LF_F, R + 3 * NL + k, R + 6 * NL + 1 + k, 0});
+        for (int k = 0; k < NL; ++k) spd.push_back(SynCol{Tv(k), LF_ONE, R + 4 * NL + k, R + 7 * NL + 1 + k, 0});
+        spd.push_back(SynCol{Pv, LF_ONE, R + 5 * NL, R + 8 * NL + 1, 0});
+        double *Ge = d.G + (size_t)e * (7 * NL + 3) * ng;
+        auto GF = [&](int f) { return Ge + (size_t)f * ng; };
+        for (int k = 0; k < NL; ++k) {
+            const int Pz = R + k, PD = R + NL + k, Pzg = R + 2 * NL + k, PDf = R + 3 * NL + k, PT = R + 4 * NL + k;
+            const int Dzg = R + 5 * NL + 1 + k, DDf = R + 6 * NL + 1 + k, DT = R + 7 * NL + 1 + k;
+            fs.push_back(FsynField{PDf, Dzg, 0.0, 1.0, -1.0, 0.0, GF(k)});              // u
+            fs.push_back(FsynField{DDf, Pzg, -1.0, 0.0, 0.0, -1.0, GF(NL + k)});         // v
+            fs.push_back(FsynField{Pz, -1, 1.0, 0.0, 0.0, 0.0, GF(2 * NL + k)});          // vor
+            fs.push_back(FsynField{PD, -1, 1.0, 0.0, 0.0, 0.0, GF(3 * NL + k)});          // div
+            fs.push_back(FsynField{PT, -1, 1.0, 0.0, 0.0, 0.0, GF(4 * NL + k)});          // T
+            fs.push_back(FsynField{PT, -1, 0.0, ia, 0.0, 0.0, GF(5 * NL + k)});           // dT/dx
+            fs.push_back(FsynField{DT, -1, -ia, 0.0, 0.0, 0.0, GF(6 * NL + k)});          // dT/dy
+        }
+        fs.push_back(FsynField{R + 5 * NL, -1, 1.0, 0.0, 0.0, 0.0, GF(7 * NL)});
+        fs.push_back(FsynField{R + 5 * NL, -1, 0.0, ia, 0.0, 0.0, GF(7 * NL + 1)});
+        fs.push_back(FsynField{R + 8 * NL + 1, -1, -ia, 0.0, 0.0, 0.0, GF(7 * NL + 2)});
+        const double *GAe = d.GA + (size_t)e * (4 * NL + 1) * ng;
+        for (int f = 0; f < 4 * NL + 1; ++f) fa.push_back(FanaField{GAe + (size_t)f * ng, RA + f, 0});
+        for (int k = 0; k < NL; ++k) {
+            AnaCol c{};
+            c.dst = d.vor(d.tnd) + ((size_t)e * NL + k) * nlm;
+            c.row1 = RA + NL + k; c.a1 = 0.0; c.b1 = ia;       // an: i m F/(a sin), P
+            c.row2 = RA + k; c.a2 = -ia; c.b2 = 0.0;           // ae: -F/a, dP
+            c.row3 = -1; c.post = LF_ONE; c.lf3 = LF_ONE;
+            ac.push_back(c);
+            AnaCol q{};
+            q.dst = d.div(d.tnd) + ((size_t)e * NL + k) * nlm;
+            q.row1 = RA + k; q.a1 = 0.0; q.b1 = ia;           // ae: i m F/(a sin), P
+            q.row2 = RA + NL + k; q.a2 = ia; q.b2 = 0.0;       // an: F/a, dP
+            q.row3 = RA + 2 * NL + k; q.lf3 = LF_LL1_A2;       // -lap(Phi + K)
+            q.post = LF_ONE;
+            ac.push_back(q);
+            AnaCol t{};
+            t.dst = d.tmp(d.tnd) + ((size_t)e * NL + k) * nlm;
+            t.row1 = RA + 3 * NL + k; t.a1 = 1.0; t.b1 = 0.0;
+            t.row2 = -1; t.row3 = -1; t.post = LF_ONE; t.lf3 = LF_ONE;
+            ac.push_back(t);
+        }
+        AnaCol p{};
+        p.dst = d.lnp(d.tnd) + (size_t)e * nlm;
+        p.row1 = RA + 4 * NL; p.a1 = 1.0; p.b1 = 0.0;
+        p.row2 = -1; p.row3 = -1; p.post = LF_ONE; p.lf3 = LF_ONE;
+        ac.push_back(p);
+    }
+    int rc;
+    if ((rc = make_syn_plan(sp, spd, d.synS))) return rc;
+    if ((rc = dput(d.fsS, fs))) return rc;
+    if ((rc = dput(d.faS, fa))) return rc;
+    if ((rc = dput(d.acS, ac))) return rc;
+    d.nfsS = (int)fs.size();
+    d.nfaS = (int)fa.size();
+    d.nacS = (int)ac.size();
+    // diagnostics: u, v (from vor/div), T, lnps -> D[e][3 NL + 1][ng]; rows per
+    // member: PS, DS (div, f-scaled), PT, DT (vor, g-scaled), T, lnps.
+    std::vector<SynCol> dp1, dp2;
+    std::vector<FsynField> fd;
+    for (int e = 0; e < M; ++e) {
+        const int R = e * (5 * NL + 1);
+        for (int k = 0; k < NL; ++k) {
+            dp2.push_back(SynCol{d.div(d.now) + ((size_t)e * NL + k) * nlm, LF_F, R + k, R + NL + k, 0});
+            dp2.push_back(SynCol{d.vor(d.now) + ((size_t)e * NL + k) * nlm, LF_G, R + 2 * NL + k, R + 3 * NL + k, 0});
+            dp1.push_back(SynCol{d.tmp(d.now) + ((size_t)e * NL + k) * nlm, LF_ONE, R + 4 * NL + k, -1, 0});
+        }
+        dp1.push_back(SynCol{d.lnp(d.now) + (size_t)e * nlm, LF_ONE, R + 5 * NL, -1, 0});
+        double *De = d.D + (size_t)e * (3 * NL + 1) * ng;
+        for (int k = 0; k < NL; ++k) {
+            fd.push_back(FsynField{R + k, R + 3 * NL + k, 0.0, 1.0, -1.0, 0.0, De + (size_t)k * ng});
+            fd.push_back(FsynField{R + NL + k, R + 2 * NL + k, -1.0, 0.0, 0.0, -1.0, De + (size_t)(NL + k) * ng});
+            fd.push_back(FsynField{R + 4 * NL + k, -1, 1.0, 0.0, 0.0, 0.0, De + (size_t)(2 * NL + k) * ng});
+        }
+        fd.push_back(FsynField{R + 5 * NL, -1, 1.0, 0.0, 0.0, 0.0, De + (size_t)3 * NL * ng});
+    }
+    if ((rc = make_syn_plan(dp1, dp2, d.synD))) return rc;
+    if ((rc = dput(d.fsD, fd))) return rc;
+    d.nfsD = (int)fd.size();
+    return AEROS_OK;
+}
+
+int upload_level_consts(Dyn &d) {
+    const int n = d.NL;
+    std::vector<LevConst> L(n);
+    for (int k = 0; k < n; ++k) {
+        LevConst &c = L[k];
+        c.A0 = d.A[k]; c.A1 = d.A[k + 1]; c.B0 = d.B[k]; c.B1 = d.B[k + 1]; c.dB = c.B1 - c.B0;
+        c.topzero = (c.A0 <= 0.0 && c.B0 <= 0.0);
+        c.pure = (c.A0 == 0.0 && c.A1 == 0.0 && c.B1 > 0.0);
+        if (c.pure) {
+            if (c.B0 > 0.0) {
+                c.dlnp = std::log(c.B1 / c.B0);
+                c.alpha = 1.0 - (c.B0 / c.dB) * c.dlnp;
+            } else {
+                c.dlnp = 0.0;
+                c.alpha = std::log(2.0);
+            }
+            c.cfac = (c.B0 * c.dlnp + c.dB * c.alpha) / c.dB;
+            double bf = 0.5 * (c.B0 + c.B1);
+            c.lnbf = std::log(bf);
+            c.bfk = std::pow(bf, kKappa);
+        }
+    }
+    AEROS_CUDA(cudaMemcpyToSymbol(c_lev, L.data(), sizeof(LevConst) * n));
+    const aeros_params &p = d.par;
+    HsConst h{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
+              std::log(p.hs_p0)};
+    AEROS_CUDA(cudaMemcpyToSymbol(c_hs, &h, sizeof(h)));
+    return AEROS_OK;
+}
+
+// SI inverses and diffusion factors for h = dt (idx 0) and 2 dt (idx 1).
+int build_step_tables(Dyn &d) {
+    const int n = d.NL, T = d.g.T;
+    const double alpha = d.par.si_alpha;
+    for (int s = 0; s < 2; ++s) {
+        double h = d.par.dt * (s ? 2.0 : 1.0);
+        double hh = alpha * alpha * h * h;
+        std::vector<double> minvT((size_t)(T + 1) * n * n), A((size_t)n * n), inv;
+        for (int l = 0; l <= T; ++l) {
+            double lam = (double)l * (l + 1) / (kA * kA);
+            for (int k = 0; k < n; ++k)
+                for (int j = 0; j < n; ++j) A[k * n + j] = hh * lam * d.Wm[k * n + j] + (k == j ? 1.0 : 0.0);
+            int rc = lu_inverse(A, n, inv);
+            if (rc) return rc;
+            for (int k = 0; k < n; ++k)
+                for (int j = 0; j < n; ++j) minvT[(size_t)l * n * n + j * n + k] = inv[(size_t)k * n + j];
+        }
+        int rc = dput(d.Minv_d[s], minvT);
+        if (rc) return rc;
+        // diffusion (aeros_timestep.f90:559-563,1673-1726): 1/(1 + (h/tau)(l(l+1)/(T(T+1)))^(ndiff/2))
+        std::vector<double> f(T + 1);
+        double lref = (double)T * (T + 1), rate = h / (d.par.tau_diff * 3600.0);
+        for (int l = 0; l <= T; ++l) f[l] = 1.0 / (1.0 + rate * std::pow((double)l * (l + 1) / lref, d.par.ndiff / 2));
+        if ((rc = dput(d.dfac_d[s], f))) return rc;
+    }
+    std::vector<double> GT((size_t)n * n), TT((size_t)n * n), WT((size_t)n * n);
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) {
+            GT[j * n + k] = d.Gm[k * n + j];
+            TT[j * n + k] = d.Tm[k * n + j];
+            WT[j * n + k] = d.Wm[k * n + j];
+        }
+    int rc;
+    if ((rc = dput(d.GT_d, GT)) || (rc = dput(d.TT_d, TT)) || (rc = dput(d.WT_d, WT)) || (rc = dput(d.nu_d, d.nu)) ||
+        (rc = dput(d.pc_d, d.pcoef)))
+        return rc;
+    return AEROS_OK;
+}
+
+// ---- launch sequences ----
+int run_tendency(Dyn &d, int hs_on) {
+    Ctx c = d.ctx();
+    int rc;
+    const int rowsS = d.M * d.nrowS, rowsA = d.M * d.nrowA;
+    if (d.par.precision == AEROS_PREC_SPLIT && d.split)
+        rc = split_leg_synth(d.split, c, d.synS, d.FS, rowsS);
+    else
+        rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
+    if (rc) return rc;
+    mark(d, "legendre_synth");
+    if ((rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS))) return rc;
+    mark(d, "fourier_synth");
+    long ncol = (long)d.g.nlon * d.g.nlat * d.M;
+    k_column<<<(unsigned)((ncol + 127) / 128), 128, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
+                                                                  d.xlat_d, d.phis_set ? d.phis_d : nullptr, hs_on,
+                                                                  d.hs_dty_d, d.hs_ka_d);
+    ++d.launches;
+    AEROS_CUDA(cudaGetLastError());
+    mark(d, "column");
+    if ((rc = launch_fourier_anal(c, d.faS, d.nfaS, d.FA, rowsA))) return rc;
+    mark(d, "fourier_anal");
+    if (d.par.precision == AEROS_PREC_SPLIT && d.split)
+        rc = split_leg_anal(d.split, c, d.acS, d.nacS, d.FA, rowsA);
+    else
+        rc = launch_leg_anal_fp64(c, d.acS, d.nacS, d.FA, rowsA);
+    mark(d, "legendre_anal");
+    return rc;
+}
+
+int run_mass(Dyn &d, int mode) {
+    const int n = d.g.nlon / 2;
+    size_t smem = (size_t)(2 * d.g.ms + 4 * n) * sizeof(double2);
+    k_mass_rows<<<dim3(d.g.nh, d.M), 128, smem, d.stream>>>(d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat,
+                                                            d.g.nlon, d.tab.Ps, d.tab.moff, d.tab.plan, d.tab.tw,
+                                                            d.tab.twN, d.mass_rows);
+    mark(d, "mass_rows");
+    k_mass_fix<<<(d.M + 63) / 64, 64, 0, d.stream>>>(d.lnp(d.now), d.g.nlm, d.M, d.mass_rows, d.tab.w, d.g.nlat,
+                                                     d.g.nlon, d.c00, d.mass_tgt, d.lnr_last, d.lnr_cum, mode);
+    mark(d, "mass_fix");
+    d.launches += 2;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// One step, h = dt (start-up) or 2 dt.
+int enqueue_step(Dyn &d, bool startup) {
+    int rc;
+    const size_t nst = d.nstate();
+    if (startup) {
+        k_copy<<<256, 256, 0, d.stream>>>(d.old, d.now, nst);
+        ++d.launches;
+        mark(d, "copy");
+        if (d.par.mass_fixer && (rc = run_mass(d, 0))) return rc;
+    }
+    if ((rc = run_tendency(d, d.par.held_suarez))) return rc;
+    SpecArgs a{};
+    a.vor = d.vor(d.now); a.div = d.div(d.now); a.tmp = d.tmp(d.now); a.lnps = d.lnp(d.now);
+    a.vor_o = d.vor(d.old); a.div_o = d.div(d.old); a.tmp_o = d.tmp(d.old); a.lnps_o = d.lnp(d.old);
+    a.tv = d.vor(d.tnd); a.td = d.div(d.tnd); a.tt = d.tmp(d.tnd); a.tp = d.lnp(d.tnd);
+    a.GT = d.GT_d; a.TT = d.TT_d; a.WT = d.WT_d; a.nu = d.nu_d; a.pcoef = d.pc_d;
+    const int s = startup ? 0 : 1;
+    a.MinvT = d.Minv_d[s];
+    a.dfac = d.dfac_d[s];
+    a.l_of_lm = d.tab.l_of_lm;
+    a.nlm = d.g.nlm; a.NL = d.NL; a.M = d.M;
+    a.h = d.par.dt * (startup ? 1.0 : 2.0);
+    a.a1 = d.par.si_alpha;
+    a.astep = a.a1 * a.h;
+    a.hh_old = a.a1 * (1.0 - a.a1) * a.h * a.h;
+    a.half_nu = 0.5 * d.par.eps_filter;
+    a.raw_alpha = d.par.raw_alpha;
+    a.raw_beta = 1.0 - d.par.raw_alpha;
+    a.semi_implicit = d.par.semi_implicit;
+    a.raw_on = (!startup && d.par.eps_filter > 0.0) ? 1 : 0;
+    a.flag = d.flag;
+    long nw = (long)d.g.nlm * d.M;
+    k_spectral<<<(unsigned)((nw + 3) / 4), 128, 0, d.stream>>>(a);
+    ++d.launches;
+    AEROS_CUDA(cudaGetLastError());
+    mark(d, "spectral");
+    if (d.par.mass_fixer && (rc = run_mass(d, 1))) return rc;
+    return AEROS_OK;
+}
+
+int capture_graphs(Dyn &d) {
+    for (int s = 0; s < 2; ++s) {
+        cudaGraph_t g;
+        long long before = d.launches;
+        AEROS_CUDA(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(d, s == 0);
+        cudaError_t e = cudaStreamEndCapture(d.stream, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) {
+            set_error(std::string("graph capture: ") + cudaGetErrorString(e));
+            return AEROS_ERR_CUDA;
+        }
+        AEROS_CUDA(cudaGraphInstantiate(&d.graph[s], g, 0));
+        cudaGraphDestroy(g);
+        d.graph_kernels[s] = d.launches - before;
+        d.launches = before;
+    }
+    return AEROS_OK;
+}
+
+int ensure_stage(Dyn &d, size_t bytes) {
+    if (d.stage_bytes >= bytes) return AEROS_OK;
+    if (d.stage) cudaFree(d.stage);
+    d.stage = nullptr;
+    d.stage_bytes = 0;
+    if (cudaMalloc(&d.stage, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return AEROS_ERR_NOMEM;
+    }
+    d.stage_bytes = bytes;
+    return AEROS_OK;
+}
+
+// Copy (host or device) state arrays into / out of a device state buffer.
+int put_state(Dyn &d, double2 *buf, const double *vor, const double *div, const double *temp, const double *lnps) {
+    const size_t n3 = (size_t)d.M * d.ns3(), n1 = (size_t)d.M * d.g.nlm;
+    if (vor) AEROS_CUDA(cudaMemcpyAsync(d.vor(buf), vor, n3 * 16, cudaMemcpyDefault, d.stream));
+    if (div) AEROS_CUDA(cudaMemcpyAsync(d.div(buf), div, n3 * 16, cudaMemcpyDefault, d.stream));
+    if (temp) AEROS_CUDA(cudaMemcpyAsync(d.tmp(buf), temp, n3 * 16, cudaMemcpyDefault, d.stream));
+    if (lnps) AEROS_CUDA(cudaMemcpyAsync(d.lnp(buf), lnps, n1 * 16, cudaMemcpyDefault, d.stream));
+    AEROS_CUDA(cudaStreamSynchronize(d.stream));
+    return AEROS_OK;
+}
+int get_state(Dyn &d, double2 *buf, double *vor, double *div, double *temp, double *lnps) {
+    const size_t n3 = (size_t)d.M * d.ns3(), n1 = (size_t)d.M * d.g.nlm;
+    if (vor) AEROS_CUDA(cudaMemcpyAsync(vor, d.vor(buf), n3 * 16, cudaMemcpyDefault, d.stream));
+    if (div) AEROS_CUDA(cudaMemcpyAsync(div, d.div(buf), n3 * 16, cudaMemcpyDefault, d.stream));
+    if (temp) AEROS_CUDA(cudaMemcpyAsync(temp, d.tmp(buf), n3 * 16, cudaMemcpyDefault, d.stream));
+    if (lnps) AEROS_CUDA(cudaMemcpyAsync(lnps, d.lnp(buf), n1 * 16, cudaMemcpyDefault, d.stream));
+    AEROS_CUDA(cudaStreamSynchronize(d.stream));
+    return AEROS_OK;
+}
+
+int diagnose_device(Dyn &d) {
+    Ctx c = d.ctx();
+    int rc;
+    const int rows = d.M * (5 * d.NL + 1);
+    if ((rc = launch_leg_synth_fp64(c, d.synD, d.FS, rows))) return rc;
+    if ((rc = launch_fourier_synth(c, d.fsD, d.nfsD, d.FS, rows))) return rc;
+    const size_t ng = (size_t)d.g.nlon * d.g.nlat;
+    for (int e = 0; e < d.M; ++e) {
+        k_exp_inplace<<<64, 256, 0, d.stream>>>(d.D + ((size_t)e * (3 * d.NL + 1) + 3 * d.NL) * ng, ng);
+        ++d.launches;
+    }
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+void destroy(Dyn *d) {
+    if (!d) return;
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    for (auto &g : d->graph)
+        if (g) cudaGraphExecDestroy(g);
+    free_syn_plan(d->synS);
+    free_syn_plan(d->synD);
+    void *ps[] = {d->now, d->old, d->tnd, d->FS, d->FA, d->G, d->GA, d->D, d->GT_d, d->TT_d, d->WT_d, d->nu_d,
+                  d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
+                  d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
+                  d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    if (d->split) split_destroy(d->split);
+    free_tables(d->tab);
+    if (d->own_stream && d->stream) cudaStreamDestroy(d->stream);
+    delete d;
+}
+
+}  // namespace
+
+extern "C" {
+
+int aeros_params_default(aeros_params *p) {
+    if (!p) return AEROS_ERR_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->trunc = 31; p->nlon = -1; p->nlat = -1; p->nlev = 20; p->nmember = 1; p->precision = AEROS_PREC_FP64;
+    p->dt = 1800.0; p->eps_filter = 0.06; p->raw_alpha = 0.53; p->si_alpha = 0.5;
+    p->tau_diff = 6.0; p->ndiff = 6; p->semi_implicit = 1; p->held_suarez = 1; p->mass_fixer = 1;
+    p->stretch_a = 1.0; p->stretch_r = 2.0; p->sigma_t = 0.0; p->p_top = 1000.0; p->ps_ref = 1.0e5; p->t_ref = 300.0;
+    p->hs_t_equator = 315.0; p->hs_t_min = 200.0; p->hs_dt_y = 60.0; p->hs_dtheta_z = 10.0; p->hs_sigma_b = 0.7;
+    p->hs_p0 = 1.0e5; p->hs_k_a = 1.0 / (40.0 * 86400.0); p->hs_k_s = 1.0 / (4.0 * 86400.0);
+    p->hs_k_f = 1.0 / 86400.0;
+    return AEROS_OK;
+}
+
+int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_half, const double *b_half) {
+    if (!out || !p) return AEROS_ERR_ARG;
+    *out = nullptr;
+    // argument checks of aeros_timestep_init (src/dynamics/aeros_timestep.f90:478-503)
+    if (p->dt <= 0.0 || p->ndiff < 2 || (p->ndiff & 1) || p->tau_diff <= 0.0 || p->eps_filter < 0.0 ||
+        p->eps_filter >= 1.0 || p->raw_alpha <= 0.0 || p->raw_alpha > 1.0 || p->si_alpha < 0.5 || p->si_alpha > 1.0 ||
+        p->nmember < 1 || p->trunc < 1)
+        return AEROS_ERR_ARG;
+    if (p->nlev < 2 || p->nlev > kMaxLev) return p->nlev < 2 ? AEROS_ERR_ARG : AEROS_ERR_UNSUPPORTED;
+    if (p->precision != AEROS_PREC_FP64 && p->precision != AEROS_PREC_SPLIT) return AEROS_ERR_ARG;
+    Dyn *d = new Dyn;
+    d->par = *p;
+    d->M = p->nmember;
+    d->NL = p->nlev;
+    int rc = build_geometry(d->g, p->trunc, p->nlon, p->nlat);
+    if (!rc) rc = build_vgrid(*d, a_half, b_half);
+    if (rc) { delete d; return rc; }
+    build_si(*d);
+    if ((rc = upload_tables(d->g, d->tab))) { destroy(d); return rc; }
+    if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess) { destroy(d); return AEROS_ERR_CUDA; }
+    d->own_stream = true;
+    const size_t ng = (size_t)d->g.nlon * d->g.nlat, M = d->M, NL = d->NL;
+    const size_t nst = d->nstate();
+    if ((rc = dalloc(d->now, nst)) || (rc = dalloc(d->old, nst)) || (rc = dalloc(d->tnd, nst)) ||
+        (rc = dalloc(d->FS, (size_t)d->g.nlat * M * std::max(8 * NL + 2, 6 * NL + 2) * d->g.ms)) ||
+        (rc = dalloc(d->FA, (size_t)d->g.nlat * M * (4 * NL + 1) * d->g.ms)) ||
+        (rc = dalloc(d->G, M * (7 * NL + 3) * ng)) || (rc = dalloc(d->GA, M * (4 * NL + 1) * ng)) ||
+        (rc = dalloc(d->D, M * (3 * NL + 1) * ng)) || (rc = dalloc(d->mass_rows, M * d->g.nlat)) ||
+        (rc = dalloc(d->lnr_last, M)) || (rc = dalloc(d->lnr_cum, M)) || (rc = dalloc(d->bud_rows, M * d->g.nlat * 3)) ||
+        (rc = dalloc(d->bud_res, M * 3)) || (rc = dalloc(d->zm, M * (7 * NL * d->g.nlat + 2 * d->g.nlat))) ||
+        (rc = dalloc(d->flag, 1)) || (rc = dalloc(d->phis_d, ng))) {
+        destroy(d);
+        return rc;
+    }
+    std::vector<double> tgt(M, -1.0), dty(M, p->hs_dt_y), ka(M, p->hs_k_a);
+    if ((rc = dput(d->mass_tgt, tgt)) || (rc = dput(d->hs_dty_d, dty)) || (rc = dput(d->hs_ka_d, ka)) ||
+        (rc = dput(d->xlat_d, d->g.x))) {
+        destroy(d);
+        return rc;
+    }
+    // c00: the (0,0) coefficient of the constant field 1 (aeros_timestep.f90:578-588),
+    // read back from the quadrature of the analysis tables: sqrt(4 pi) in this normalization.
+    {
+        double s = 0.0;
+        for (int j = 0; j < d->g.nh; ++j) s += 2.0 * d->g.w[j] * d->g.Ps[j];
+        d->c00 = s * std::sqrt(2.0 * kPi);
+        if (std::fabs(d->c00) < 1e-12) { destroy(d); return AEROS_ERR_STATE; }
+    }
+    if ((rc = upload_level_consts(*d)) || (rc = build_step_tables(*d)) || (rc = build_descriptors(*d))) {
+        destroy(d);
+        return rc;
+    }
+    if (p->precision == AEROS_PREC_SPLIT) {
+        int rows = (int)(M * std::max(8 * NL + 2, 4 * NL + 1));
+        if ((rc = split_create(d->g, d->tab, rows, &d->split))) { destroy(d); return rc; }
+    }
+    if ((rc = capture_graphs(*d))) { destroy(d); return rc; }
+    *out = d;
+    return AEROS_OK;
+}
+
+int aeros_dyn_destroy(aeros_dyn_t h) {
+    if (!h) return AEROS_ERR_ARG;
+    destroy(h);
+    return AEROS_OK;
+}
+
+int aeros_dyn_info(aeros_dyn_t h, int *nlon, int *nlat, int *nlm, int *nlev, double *a_half, double *b_half,
+                   double *sigma_full, double *sinlat, double *gauss_w) {
+    if (!h) return AEROS_ERR_ARG;
+    if (nlon) *nlon = h->g.nlon;
+    if (nlat) *nlat = h->g.nlat;
+    if (nlm) *nlm = h->g.nlm;
+    if (nlev) *nlev = h->NL;
+    if (a_half) std::memcpy(a_half, h->A.data(), sizeof(double) * (h->NL + 1));
+    if (b_half) std::memcpy(b_half, h->B.data(), sizeof(double) * (h->NL + 1));
+    if (sigma_full) std::memcpy(sigma_full, h->sigma_full.data(), sizeof(double) * h->NL);
+    if (sinlat) std::memcpy(sinlat, h->g.x.data(), sizeof(double) * h->g.nlat);
+    if (gauss_w) std::memcpy(gauss_w, h->g.w.data(), sizeof(double) * h->g.nlat);
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_member_forcing(aeros_dyn_t h, int member, double dt_y, double k_a) {
+    if (!h || member < 0 || member >= h->M || k_a < 0.0) return AEROS_ERR_ARG;
+    AEROS_CUDA(cudaMemcpy(h->hs_dty_d + member, &dt_y, 8, cudaMemcpyHostToDevice));
+    AEROS_CUDA(cudaMemcpy(h->hs_ka_d + member, &k_a, 8, cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_state(aeros_dyn_t h, const double *vor, const double *div, const double *temp, const double *lnps) {
+    if (!h || !vor || !div || !temp || !lnps) return AEROS_ERR_ARG;
+    int rc = put_state(*h, h->now, vor, div, temp, lnps);
+    if (rc) return rc;
+    AEROS_CUDA(cudaMemset(h->flag, 0, sizeof(int)));
+    h->nstep = 0;
+    return AEROS_OK;
+}
+
+int aeros_dyn_get_state(aeros_dyn_t h, double *vor, double *div, double *temp, double *lnps) {
+    if (!h) return AEROS_ERR_ARG;
+    return get_state(*h, h->now, vor, div, temp, lnps);
+}
+
+int aeros_dyn_set_old_state(aeros_dyn_t h, const double *vor, const double *div, const double *temp,
+                            const double *lnps, int nstep) {
+    if (!h || !vor || !div || !temp || !lnps || nstep < 0) return AEROS_ERR_ARG;
+    int rc = put_state(*h, h->old, vor, div, temp, lnps);
+    if (rc) return rc;
+    h->nstep = nstep;
+    return AEROS_OK;
+}
+
+int aeros_dyn_get_old_state(aeros_dyn_t h, double *vor, double *div, double *temp, double *lnps) {
+    if (!h) return AEROS_ERR_ARG;
+    return get_state(*h, h->old, vor, div, temp, lnps);
+}
+
+int aeros_dyn_set_isothermal(aeros_dyn_t h, double temp, double ps) {
+    if (!h) return AEROS_ERR_ARG;
+    const double t_ = temp > 0 ? temp : h->t_ref, ps_ = ps > 0 ? ps : h->ps_ref;
+    std::vector<double2> s(h->nstate(), make_double2(0.0, 0.0));
+    const double y00 = std::sqrt(4.0 * std::acos(-1.0));
+    for (int e = 0; e < h->M; ++e) {
+        for (int k = 0; k < h->NL; ++k) s[(size_t)2 * h->M * h->ns3() + ((size_t)e * h->NL + k) * h->g.nlm] =
+            make_double2(t_ * y00, 0.0);
+        s[(size_t)3 * h->M * h->ns3() + (size_t)e * h->g.nlm] = make_double2(std::log(ps_) * y00, 0.0);
+    }
+    AEROS_CUDA(cudaMemcpy(h->now, s.data(), s.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    h->nstep = 0;
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis) {
+    if (!h || !phis) return AEROS_ERR_ARG;
+    AEROS_CUDA(cudaMemcpy(h->phis_d, phis, sizeof(double) * h->g.nlon * h->g.nlat, cudaMemcpyDefault));
+    if (!h->phis_set) {
+        // the graphs were captured without the surface geopotential
+        h->phis_set = true;
+        for (auto &g : h->graph)
+            if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        int rc = capture_graphs(*h);
+        if (rc) return rc;
+    }
+    return AEROS_OK;
+}
+
+int aeros_dyn_step_async(aeros_dyn_t h, int nsteps);
+int aeros_dyn_sync(aeros_dyn_t h);
+
+int aeros_dyn_step(aeros_dyn_t h, int nsteps) {
+    int rc = aeros_dyn_step_async(h, nsteps);
+    if (rc) return rc;
+    return aeros_dyn_sync(h);
+}
+
+int aeros_dyn_step_async(aeros_dyn_t h, int nsteps) {
+    if (!h || nsteps < 0) return AEROS_ERR_ARG;
+    for (int i = 0; i < nsteps; ++i) {
+        int s = h->nstep == 0 ? 0 : 1;
+        AEROS_CUDA(cudaGraphLaunch(h->graph[s], h->stream));
+        h->launches += h->graph_kernels[s];
+        h->nstep += 1;
+    }
+    return AEROS_OK;
+}
+
+int aeros_dyn_sync(aeros_dyn_t h) {
+    if (!h) return AEROS_ERR_ARG;
+    int flag = 0;
+    AEROS_CUDA(cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    if (flag) {
+        set_error("non-finite value in the spectral state");
+        return AEROS_ERR_NONFINITE;
+    }
+    return AEROS_OK;
+}
+
+int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int name_len, int *nk) {
+    if (!h || !ms || !nk || maxk < 1) return AEROS_ERR_ARG;
+    std::vector<cudaEvent_t> ev;
+    std::vector<std::string> nm;
+    cudaEvent_t e0;
+    AEROS_CUDA(cudaEventCreate(&e0));
+    AEROS_CUDA(cudaEventRecord(e0, h->stream));
+    h->prof = &ev;
+    h->prof_names = &nm;
+    int rc = enqueue_step(*h, h->nstep == 0);
+    h->prof = nullptr;
+    h->prof_names = nullptr;
+    if (rc) return rc;
+    h->nstep += 1;
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    int n = std::min((int)ev.size(), maxk);
+    cudaEvent_t prev = e0;
+    for (int i = 0; i < n; ++i) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, prev, ev[i]);
+        ms[i] = t;
+        prev = ev[i];
+        if (names && name_len > 0) {
+            std::strncpy(names + (size_t)i * name_len, nm[i].c_str(), name_len - 1);
+            names[(size_t)i * name_len + name_len - 1] = 0;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    cudaEventDestroy(e0);
+    *nk = n;
+    return AEROS_OK;
+}
+
+int aeros_dyn_tendency(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp, double *dlnps) {
+    if (!h) return AEROS_ERR_ARG;
+    int rc = run_tendency(*h, 0);
+    if (rc) return rc;
+    return get_state(*h, h->tnd, dvor, ddiv, dtemp, dlnps);
+}
+
+int aeros_dyn_diagnose(aeros_dyn_t h, double *u, double *v, double *temp, double *ps) {
+    if (!h) return AEROS_ERR_ARG;
+    int rc = diagnose_device(*h);
+    if (rc) return rc;
+    const size_t ng = (size_t)h->g.nlon * h->g.nlat, n3 = (size_t)h->NL * ng;
+    for (int e = 0; e < h->M; ++e) {
+        const double *De = h->D + (size_t)e * (3 * h->NL + 1) * ng;
+        if (u) AEROS_CUDA(cudaMemcpyAsync(u + e * n3, De, n3 * 8, cudaMemcpyDefault, h->stream));
+        if (v) AEROS_CUDA(cudaMemcpyAsync(v + e * n3, De + n3, n3 * 8, cudaMemcpyDefault, h->stream));
+        if (temp) AEROS_CUDA(cudaMemcpyAsync(temp + e * n3, De + 2 * n3, n3 * 8, cudaMemcpyDefault, h->stream));
+        if (ps) AEROS_CUDA(cudaMemcpyAsync(ps + e * ng, De + 3 * n3, ng * 8, cudaMemcpyDefault, h->stream));
+    }
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    return AEROS_OK;
+}
+
+int aeros_dyn_budget(aeros_dyn_t h, double *mass, double *energy, double *angmom) {
+    if (!h) return AEROS_ERR_ARG;
+    int rc = diagnose_device(*h);
+    if (rc) return rc;
+    k_budget_rows<<<dim3(h->g.nlat, h->M), 128, 0, h->stream>>>(h->D, h->NL, h->g.nlon, h->g.nlat,
+                                                               h->phis_set ? h->phis_d : nullptr, h->xlat_d,
+                                                               h->bud_rows);
+    k_budget_final<<<(h->M + 63) / 64, 64, 0, h->stream>>>(h->bud_rows, h->tab.w, h->g.nlat, h->g.nlon, h->M,
+                                                           h->bud_res);
+    h->launches += 2;
+    AEROS_CUDA(cudaGetLastError());
+    std::vector<double> r((size_t)3 * h->M);
+    AEROS_CUDA(cudaMemcpyAsync(r.data(), h->bud_res, r.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int e = 0; e < h->M; ++e) {
+        if (mass) mass[e] = r[3 * e];
+        if (energy) energy[e] = r[3 * e + 1];
+        if (angmom) angmom[e] = r[3 * e + 2];
+    }
+    return AEROS_OK;
+}
+
+int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target, double *lnr_last, double *lnr_cum) {
+    if (!h) return AEROS_ERR_ARG;
+    if (nstep) *nstep = h->nstep;
+    if (mass_target) AEROS_CUDA(cudaMemcpy(mass_target, h->mass_tgt, 8, cudaMemcpyDeviceToHost));
+    if (lnr_last) AEROS_CUDA(cudaMemcpy(lnr_last, h->lnr_last, 8, cudaMemcpyDeviceToHost));
+    if (lnr_cum) AEROS_CUDA(cudaMemcpy(lnr_cum, h->lnr_cum, 8, cudaMemcpyDeviceToHost));
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass) {
+    if (!h || mass <= 0.0) return AEROS_ERR_ARG;
+    std::vector<double> t(h->M, mass);
+    AEROS_CUDA(cudaMemcpy(h->mass_tgt, t.data(), 8 * h->M, cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
+int aeros_dyn_diag_accumulate(aeros_dyn_t h) {
+    if (!h) return AEROS_ERR_ARG;
+    int rc = diagnose_device(*h);
+    if (rc) return rc;
+    k_zonal<<<dim3(h->g.nlat, h->NL, h->M), 128, 0, h->stream>>>(h->D, h->NL, h->g.nlon, h->g.nlat, h->zm);
+    ++h->launches;
+    AEROS_CUDA(cudaGetLastError());
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    h->nsample += 1;
+    return AEROS_OK;
+}
+
+int aeros_dyn_diag_read(aeros_dyn_t h, int member, double *out, int *nsample) {
+    if (!h || !out || member < 0 || member >= h->M) return AEROS_ERR_ARG;
+    const size_t F = (size_t)h->g.nlat * h->NL, n = 7 * F + 2 * h->g.nlat;
+    std::vector<double> acc(n);
+    AEROS_CUDA(cudaMemcpy(acc.data(), h->zm + (size_t)member * n, n * 8, cudaMemcpyDeviceToHost));
+    double rn = h->nsample > 0 ? 1.0 / h->nsample : 0.0;
+    for (size_t i = 0; i < n; ++i) out[i] = acc[i] * rn;
+    if (nsample) *nsample = h->nsample;
+    return AEROS_OK;
+}
+
+int aeros_dyn_gwspeed(aeros_dyn_t h, double *cmax) {
+    if (!h || !cmax) return AEROS_ERR_ARG;
+    const int n = h->NL;
+    std::vector<double> x(n, 1.0 / std::sqrt((double)n)), y(n);
+    double lam = 0.0;
+    for (int it = 0; it < 200; ++it) {
+        for (int k = 0; k < n; ++k) {
+            y[k] = 0.0;
+            for (int j = 0; j < n; ++j) y[k] += h->Wm[k * n + j] * x[j];
+        }
+        double nrm = 0.0;
+        for (int k = 0; k < n; ++k) nrm += y[k] * y[k];
+        nrm = std::sqrt(nrm);
+        if (nrm <= 0.0) break;
+        for (int k = 0; k < n; ++k) x[k] = y[k] / nrm;
+        lam = 0.0;
+        for (int k = 0; k < n; ++k) lam += x[k] * y[k];
+    }
+    *cmax = std::sqrt(std::max(lam, 0.0));
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_stream(aeros_dyn_t h, void *stream) {
+    if (!h) return AEROS_ERR_ARG;
+    cudaStreamSynchronize(h->stream);
+    if (stream) {
+        if (h->own_stream) cudaStreamDestroy(h->stream);
+        h->stream = (cudaStream_t)stream;
+        h->own_stream = false;
+    }
+    return AEROS_OK;
+}
+
+int aeros_dyn_launch_count(aeros_dyn_t h, long long *count) {
+    if (!h || !count) return AEROS_ERR_ARG;
+    *count = h->launches;
+    return AEROS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,17 @@
+// split.h -- split-precision (Ozaki) Legendre contraction on the tensor cores.
+#pragma once
+#include "aeros_internal.h"
+
+namespace aeros {
+
+struct SplitCtx;
+
+// Build the sliced Legendre tables for geometry g; `max_rows` bounds the
+// Fourier rows per call.
+int split_create(const Geometry &g, const DevTables &t, int max_rows, SplitCtx **out);
+void split_destroy(SplitCtx *s);
+// Same contract as launch_leg_synth_fp64 / launch_leg_anal_fp64.
+int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int nrow);
+int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
+
+}  // namespace aeros

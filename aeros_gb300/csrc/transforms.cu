@@ -1,0 +1,499 @@
+// transforms.cu -- FP64 spherical-harmonic transform kernels for sm_103a.
+//
+// A synthesis is two launches: the per-m Legendre contraction (spectral ->
+// Fourier rows, hemisphere-folded) and the longitude FFT (Fourier rows ->
+// grid).  An analysis is the reverse.  Both mirror the per-m DGEMM structure
+// of mwm/A_scaling/src/aeros_bench_batched.f90:328-427, with SHTns'
+// orthonormal convention (src/aeros_spectral.f90:17-27): the Fourier
+// normalization 1/sqrt(2 pi) (synthesis) and sqrt(2 pi)/nlon (analysis) is
+// applied in the FFT kernels.
+#include <cuda_runtime.h>
+#include "aeros_internal.h"
+#include "fft.cuh"
+
+namespace aeros {
+
+constexpr double kNrm = 0.39894228040143267794;      // 1/sqrt(2 pi)
+constexpr double kSq2Pi = 2.50662827463100050242;    // sqrt(2 pi)
+
+// ============================================================ Fourier synthesis
+// grid[j][i] = FFT^-1[ X ],  X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m].
+// CTA = (field, group of LPB latitudes); each row uses 2 n complex of smem.
+__global__ void k_fourier_synth(const FsynField *__restrict__ fields, const double2 *__restrict__ F, int nrow,
+                                int ms, int T, int nlat, int nlon, int lpb, FftPlan plan,
+                                const double2 *__restrict__ tw, const double2 *__restrict__ twN,
+                                const double *__restrict__ isin) {
+    extern __shared__ double2 sm[];
+    const FsynField fd = fields[blockIdx.x];
+    const int n = nlon / 2;
+    const int j0 = blockIdx.y * lpb;
+    const int nr = min(lpb, nlat - j0);
+    double2 *A = sm, *B = sm + (size_t)lpb * n;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+
+    for (int idx = tid; idx < nr * n; idx += nthr) {
+        int r = idx / n, k = idx - r * n;
+        int j = j0 + r;
+        double is = isin[j];
+        // X[k] and X[n-k]
+        double2 xk = make_double2(0.0, 0.0), xc = make_double2(0.0, 0.0);
+        int kc = n - k;
+        const double2 *Fr = F + (size_t)j * nrow * ms;
+        if (k <= T) {
+            if (fd.src0 >= 0) {
+                double2 f = Fr[(size_t)fd.src0 * ms + k];
+                double bb = fd.b0 * k * is;
+                xk.x += fd.a0 * f.x - bb * f.y;
+                xk.y += fd.a0 * f.y + bb * f.x;
+            }
+            if (fd.src1 >= 0) {
+                double2 f = Fr[(size_t)fd.src1 * ms + k];
+                double bb = fd.b1 * k * is;
+                xk.x += fd.a1 * f.x - bb * f.y;
+                xk.y += fd.a1 * f.y + bb * f.x;
+            }
+            if (k == 0) xk.y = 0.0;
+        }
+        if (kc <= T && kc < n) {
+            if (fd.src0 >= 0) {
+                double2 f = Fr[(size_t)fd.src0 * ms + kc];
+                double bb = fd.b0 * kc * is;
+                xc.x += fd.a0 * f.x - bb * f.y;
+                xc.y += fd.a0 * f.y + bb * f.x;
+            }
+            if (fd.src1 >= 0) {
+                double2 f = Fr[(size_t)fd.src1 * ms + kc];
+                double bb = fd.b1 * kc * is;
+                xc.x += fd.a1 * f.x - bb * f.y;
+                xc.y += fd.a1 * f.y + bb * f.x;
+            }
+        }
+        // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O
+        double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
+        double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
+        double2 O = cmulconj(D, twN[k]);
+        A[(size_t)r * n + k] = make_double2((E.x - O.y) * kNrm, (E.y + O.x) * kNrm);
+    }
+    __syncthreads();
+    double2 *res = fft_rows<true>(A, B, nr, n, plan, tw, tid, nthr);
+    const double *rr = reinterpret_cast<const double *>(res);
+    for (int idx = tid; idx < nr * nlon; idx += nthr) {
+        int r = idx / nlon, i = idx - r * nlon;
+        fd.dst[(size_t)(j0 + r) * nlon + i] = rr[(size_t)r * 2 * n + i];
+    }
+}
+
+// ============================================================ Fourier analysis
+// F[j][row][m] = sqrt(2pi)/nlon * sum_i grid[j][i] e^{-i m lambda_i},  m = 0..T.
+__global__ void k_fourier_anal(const FanaField *__restrict__ fields, double2 *__restrict__ F, int nrow, int ms,
+                               int T, int nlat, int nlon, int lpb, FftPlan plan, const double2 *__restrict__ tw,
+                               const double2 *__restrict__ twN) {
+    extern __shared__ double2 sm[];
+    const FanaField fd = fields[blockIdx.x];
+    const int n = nlon / 2;
+    const int j0 = blockIdx.y * lpb;
+    const int nr = min(lpb, nlat - j0);
+    double2 *A = sm, *B = sm + (size_t)lpb * n;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    double *Ar = reinterpret_cast<double *>(A);
+    for (int idx = tid; idx < nr * nlon; idx += nthr) {
+        int r = idx / nlon, i = idx - r * nlon;
+        Ar[(size_t)r * 2 * n + i] = fd.src[(size_t)(j0 + r) * nlon + i];
+    }
+    __syncthreads();
+    double2 *Z = fft_rows<false>(A, B, nr, n, plan, tw, tid, nthr);
+    const double sc = kSq2Pi / nlon;
+    for (int idx = tid; idx < nr * ms; idx += nthr) {
+        int r = idx / ms, m = idx - r * ms;
+        double2 a = Z[(size_t)r * n + (m % n)];
+        double2 b = Z[(size_t)r * n + ((n - m) % n)];
+        // E = (a + conj b)/2, O = -i/2 (a - conj b),  X = E + e^{-2 pi i m/N} O
+        double2 E = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+        double2 O = make_double2(0.5 * (a.y + b.y), -0.5 * (a.x - b.x));
+        double2 X = cadd(E, cmul(twN[m], O));
+        if (m == 0) X.y = 0.0;
+        F[((size_t)(j0 + r) * nrow + fd.row) * ms + m] = make_double2(X.x * sc, X.y * sc);
+    }
+}
+
+static int fourier_lpb(int nlon) {
+    // two rows of n complex per latitude; keep <= 64 KB of shared memory
+    int n = nlon / 2;
+    int lpb = (64 * 1024) / (2 * n * (int)sizeof(double2));
+    if (lpb > 8) lpb = 8;
+    if (lpb < 1) lpb = 1;
+    return lpb;
+}
+
+int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    int lpb = fourier_lpb(c.nlon);
+    size_t smem = (size_t)2 * lpb * (c.nlon / 2) * sizeof(double2);
+    dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
+    if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fourier_synth<<<grid, 256, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+                                                   c.tab->tw, c.tab->twN, c.tab->sint);
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    int lpb = fourier_lpb(c.nlon);
+    size_t smem = (size_t)2 * lpb * (c.nlon / 2) * sizeof(double2);
+    dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
+    if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_anal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fourier_anal<<<grid, 256, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+                                                  c.tab->tw, c.tab->twN);
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// ============================================================ Legendre synthesis (FP64)
+// CTA = (m, column tile, latitude tile).  Thread pairs (j, c) accumulate the
+// even and odd (l - m) parts of sum_l c_lm Pbar_lm(x_j) [and dPbar], which
+// fold into the north row (E + O) and the south row (E - O; O - E for dPbar,
+// whose parity is opposite).
+constexpr int kSynJT = 32;   // latitudes per tile
+constexpr int kSynCT = 16;   // columns per tile
+constexpr int kSynKC = 16;   // degrees per smem chunk (even)
+constexpr int kSynThreads = 128;
+constexpr int kSynQ = kSynJT * kSynCT / kSynThreads;
+
+__global__ void __launch_bounds__(kSynThreads) k_leg_synth_fp64(
+    const SynCol *__restrict__ cols, int ncol, int ncolD_first, const int *__restrict__ tile_first,
+    const double *__restrict__ Ps, const double *__restrict__ dPs, const double *__restrict__ lfac,
+    const int *__restrict__ moff, double2 *__restrict__ F, int nrow, int ms, int T, int nh, int nlat) {
+    __shared__ double sP[kSynKC][kSynJT];
+    __shared__ double sD[kSynKC][kSynJT];
+    __shared__ double2 sC[kSynKC][kSynCT];
+    __shared__ SynCol sCol[kSynCT];
+
+    const int m = blockIdx.x;
+    const int c0 = tile_first[blockIdx.y];
+    const int c1 = tile_first[blockIdx.y + 1];
+    const int nct = c1 - c0;
+    const bool hasD = c0 >= ncolD_first;
+    const int j0 = blockIdx.z * kSynJT;
+    const int jt = min(kSynJT, nh - j0);
+    const int K = T - m + 1;
+    const int mo = moff[m];
+    const int tid = threadIdx.x;
+    if (tid < nct) sCol[tid] = cols[c0 + tid];
+
+    double2 pe[kSynQ], po[kSynQ], de[kSynQ], dq[kSynQ];
+#pragma unroll
+    for (int q = 0; q < kSynQ; ++q) pe[q] = po[q] = de[q] = dq[q] = make_double2(0.0, 0.0);
+
+    for (int k0 = 0; k0 < K; k0 += kSynKC) {
+        const int kc = min(kSynKC, K - k0);
+        __syncthreads();
+        for (int idx = tid; idx < kSynKC * kSynJT; idx += kSynThreads) {
+            int kk = idx / kSynJT, jj = idx - kk * kSynJT;
+            double p = 0.0, d = 0.0;
+            if (kk < kc && jj < jt) {
+                size_t o = (size_t)(mo + k0 + kk) * nh + j0 + jj;
+                p = Ps[o];
+                if (hasD) d = dPs[o];
+            }
+            sP[kk][jj] = p;
+            sD[kk][jj] = d;
+        }
+        for (int idx = tid; idx < kSynKC * kSynCT; idx += kSynThreads) {
+            int kk = idx / kSynCT, cc = idx - kk * kSynCT;
+            double2 v = make_double2(0.0, 0.0);
+            if (kk < kc && cc < nct) {
+                const SynCol &cd = sCol[cc];
+                v = cd.src[mo + k0 + kk];
+                if (cd.scale) {
+                    double s = lfac[cd.scale * ms + m + k0 + kk];
+                    v.x *= s;
+                    v.y *= s;
+                }
+            }
+            sC[kk][cc] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kSynQ; ++q) {
+            int p = tid + q * kSynThreads;
+            int jj = p % kSynJT, cc = p / kSynJT;
+            if (cc >= nct || jj >= jt) continue;
+            double2 ae = pe[q], ao = po[q], be = de[q], bo = dq[q];
+            for (int kk = 0; kk < kc; kk += 2) {
+                double2 cv = sC[kk][cc];
+                double pv = sP[kk][jj];
+                ae.x = fma(pv, cv.x, ae.x);
+                ae.y = fma(pv, cv.y, ae.y);
+                if (hasD) {
+                    double dv = sD[kk][jj];
+                    be.x = fma(dv, cv.x, be.x);
+                    be.y = fma(dv, cv.y, be.y);
+                }
+                if (kk + 1 < kc) {
+                    double2 cw = sC[kk + 1][cc];
+                    double pw = sP[kk + 1][jj];
+                    ao.x = fma(pw, cw.x, ao.x);
+                    ao.y = fma(pw, cw.y, ao.y);
+                    if (hasD) {
+                        double dw = sD[kk + 1][jj];
+                        bo.x = fma(dw, cw.x, bo.x);
+                        bo.y = fma(dw, cw.y, bo.y);
+                    }
+                }
+            }
+            pe[q] = ae; po[q] = ao; de[q] = be; dq[q] = bo;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kSynQ; ++q) {
+        int p = tid + q * kSynThreads;
+        int jj = p % kSynJT, cc = p / kSynJT;
+        if (cc >= nct || jj >= jt) continue;
+        const SynCol &cd = sCol[cc];
+        int jn = j0 + jj, js = nlat - 1 - jn;
+        F[((size_t)jn * nrow + cd.rowP) * ms + m] = cadd(pe[q], po[q]);
+        F[((size_t)js * nrow + cd.rowP) * ms + m] = csub(pe[q], po[q]);
+        if (hasD && cd.rowD >= 0) {
+            F[((size_t)jn * nrow + cd.rowD) * ms + m] = cadd(de[q], dq[q]);
+            F[((size_t)js * nrow + cd.rowD) * ms + m] = csub(dq[q], de[q]);
+        }
+    }
+}
+
+int make_syn_plan(const std::vector<SynCol> &colsP, const std::vector<SynCol> &colsPD, SynPlan &p) {
+    std::vector<SynCol> all(colsP);
+    all.insert(all.end(), colsPD.begin(), colsPD.end());
+    std::vector<int> tiles;
+    for (int c = 0; c < (int)colsP.size(); c += kSynCT) tiles.push_back(c);
+    for (int c = 0; c < (int)colsPD.size(); c += kSynCT) tiles.push_back((int)colsP.size() + c);
+    tiles.push_back((int)all.size());
+    p.ncol = (int)all.size();
+    p.ncolD_first = (int)colsP.size();
+    p.ntile = (int)tiles.size() - 1;
+    if (p.ncol == 0) return AEROS_OK;
+    AEROS_CUDA(cudaMalloc(&p.cols_d, all.size() * sizeof(SynCol)));
+    AEROS_CUDA(cudaMalloc(&p.tiles_d, tiles.size() * sizeof(int)));
+    AEROS_CUDA(cudaMemcpy(p.cols_d, all.data(), all.size() * sizeof(SynCol), cudaMemcpyHostToDevice));
+    AEROS_CUDA(cudaMemcpy(p.tiles_d, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
+void free_syn_plan(SynPlan &p) {
+    if (p.cols_d) cudaFree(p.cols_d);
+    if (p.tiles_d) cudaFree(p.tiles_d);
+    p = SynPlan{};
+}
+
+int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) {
+    if (p.ncol <= 0) return AEROS_OK;
+    dim3 grid(c.T + 1, p.ntile, (c.nh + kSynJT - 1) / kSynJT);
+    k_leg_synth_fp64<<<grid, kSynThreads, 0, c.stream>>>(p.cols_d, p.ncol, p.ncolD_first, p.tiles_d, c.tab->Ps,
+                                                         c.tab->dPs, c.tab->lfac, c.tab->moff, F, nrow, c.ms, c.T,
+                                                         c.nh, c.nlat);
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// ============================================================ Legendre analysis (FP64)
+// CTA = (m, column tile, l tile).  Warp = one output column, lanes = degrees
+// (split into j partitions when the tile is narrower than 32).  Inputs are
+// folded to even/odd latitude sums in shared memory.
+constexpr int kAnaCT = 8;       // columns (warps) per CTA
+constexpr int kAnaJC = 16;      // latitudes per smem chunk
+constexpr int kAnaLT = 32;
+
+__global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(
+    const AnaCol *__restrict__ cols, int ncol, const double *__restrict__ PaT, const double *__restrict__ dPaT,
+    const double *__restrict__ lfac, const double *__restrict__ isin, const int *__restrict__ moff,
+    const double2 *__restrict__ F, int nrow, int ms, int T, int nh, int nlat) {
+    __shared__ double sP[kAnaJC][kAnaLT];
+    __shared__ double sD[kAnaJC][kAnaLT];
+    __shared__ double2 sX[kAnaCT][3][2][kAnaJC];   // [col][slot][even/odd][j]
+    __shared__ AnaCol sCol[kAnaCT];
+
+    const int m = blockIdx.x;
+    const int K = T - m + 1;
+    const int l0 = blockIdx.z * kAnaLT;            // offset (l - m) of this tile
+    if (l0 >= K) return;
+    const int lt = min(kAnaLT, K - l0);
+    const int c0 = blockIdx.y * kAnaCT;
+    const int nct = min(kAnaCT, ncol - c0);
+    const int mo = moff[m];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid < nct) sCol[tid] = cols[c0 + tid];
+    __syncthreads();
+
+    // lane mapping: width LW (power of two >= lt), JP = 32/LW latitude partitions
+    int LW = 32;
+    while (LW / 2 >= lt && LW > 1) LW /= 2;
+    const int JP = 32 / LW;
+    const int lk = lane % LW, jp = lane / LW;
+    const bool lvalid = lk < lt;
+    const int par = (l0 + lk) & 1;                 // parity of l - m
+    const bool wvalid = warp < nct;
+    AnaCol cd;
+    if (wvalid) cd = sCol[warp];
+    double2 a1 = make_double2(0, 0), a2 = make_double2(0, 0), a3 = make_double2(0, 0);
+
+    for (int j0 = 0; j0 < nh; j0 += kAnaJC) {
+        const int jc = min(kAnaJC, nh - j0);
+        __syncthreads();
+        for (int idx = tid; idx < kAnaJC * kAnaLT; idx += blockDim.x) {
+            int jj = idx / kAnaLT, kk = idx - jj * kAnaLT;
+            double p = 0.0, d = 0.0;
+            if (jj < jc && kk < lt) {
+                size_t o = (size_t)mo * nh + (size_t)(j0 + jj) * K + l0 + kk;
+                p = PaT[o];
+                d = dPaT[o];
+            }
+            sP[jj][kk] = p;
+            sD[jj][kk] = d;
+        }
+        for (int idx = tid; idx < kAnaCT * 3 * kAnaJC; idx += blockDim.x) {
+            int cc = idx / (3 * kAnaJC);
+            int rem = idx - cc * 3 * kAnaJC;
+            int s = rem / kAnaJC, jj = rem - s * kAnaJC;
+            double2 e = make_double2(0, 0), o = make_double2(0, 0);
+            if (cc < nct && jj < jc) {
+                const AnaCol &q = sCol[cc];
+                int row = s == 0 ? q.row1 : (s == 1 ? q.row2 : q.row3);
+                if (row >= 0) {
+                    int jn = j0 + jj, js = nlat - 1 - jn;
+                    double2 fn = F[((size_t)jn * nrow + row) * ms + m];
+                    double2 fs = F[((size_t)js * nrow + row) * ms + m];
+                    if (s < 2) {
+                        double a = s == 0 ? q.a1 : q.a2, b = s == 0 ? q.b1 : q.b2;
+                        double bb = b * m * isin[jn];
+                        fn = make_double2(a * fn.x - bb * fn.y, a * fn.y + bb * fn.x);
+                        fs = make_double2(a * fs.x - bb * fs.y, a * fs.y + bb * fs.x);
+                    }
+                    e = cadd(fn, fs);
+                    o = csub(fn, fs);
+                }
+            }
+            sX[cc][s][0][jj] = e;
+            sX[cc][s][1][jj] = o;
+        }
+        __syncthreads();
+        if (wvalid && lvalid) {
+            for (int jj = jp; jj < jc; jj += JP) {
+                double p = sP[jj][lk], d = sD[jj][lk];
+                if (cd.row1 >= 0) {
+                    double2 x = sX[warp][0][par][jj];
+                    a1.x = fma(p, x.x, a1.x);
+                    a1.y = fma(p, x.y, a1.y);
+                }
+                if (cd.row2 >= 0) {
+                    double2 x = sX[warp][1][par ^ 1][jj];
+                    a2.x = fma(d, x.x, a2.x);
+                    a2.y = fma(d, x.y, a2.y);
+                }
+                if (cd.row3 >= 0) {
+                    double2 x = sX[warp][2][par][jj];
+                    a3.x = fma(p, x.x, a3.x);
+                    a3.y = fma(p, x.y, a3.y);
+                }
+            }
+        }
+    }
+    // reduce the latitude partitions
+    for (int off = LW; off < 32; off <<= 1) {
+        a1.x += __shfl_xor_sync(0xffffffffu, a1.x, off);
+        a1.y += __shfl_xor_sync(0xffffffffu, a1.y, off);
+        a2.x += __shfl_xor_sync(0xffffffffu, a2.x, off);
+        a2.y += __shfl_xor_sync(0xffffffffu, a2.y, off);
+        a3.x += __shfl_xor_sync(0xffffffffu, a3.x, off);
+        a3.y += __shfl_xor_sync(0xffffffffu, a3.y, off);
+    }
+    if (wvalid && lvalid && jp == 0) {
+        int l = m + l0 + lk;
+        double post = lfac[cd.post * ms + l];
+        double2 r = make_double2(post * (a1.x + a2.x), post * (a1.y + a2.y));
+        if (cd.row3 >= 0) {
+            double f3 = lfac[cd.lf3 * ms + l];
+            r.x += f3 * a3.x;
+            r.y += f3 * a3.y;
+        }
+        if (m == 0) r.y = 0.0;
+        cd.dst[mo + l0 + lk] = r;
+    }
+}
+
+int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
+    if (ncol <= 0) return AEROS_OK;
+    dim3 grid(c.T + 1, (ncol + kAnaCT - 1) / kAnaCT, (c.T + 1 + kAnaLT - 1) / kAnaLT);
+    k_leg_anal_fp64<<<grid, kAnaCT * 32, 0, c.stream>>>(cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac,
+                                                       c.tab->sint, c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// ============================================================ elementwise helpers
+__global__ void k_laplacian(double2 *c, int nlm, int nb, int inverse, const int *__restrict__ l_of_lm) {
+    const double a2 = kA * kA;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < (long)nlm * nb;
+         idx += (long)gridDim.x * blockDim.x) {
+        int lm = (int)(idx % nlm);
+        int l = l_of_lm[lm];
+        double ll = (double)l * (l + 1);
+        double2 v = c[idx];
+        double f;
+        if (inverse) {
+            if (l == 0) { c[idx] = make_double2(0.0, 0.0); continue; }
+            f = -a2 / ll;
+        } else {
+            f = -ll / a2;
+        }
+        c[idx] = make_double2(v.x * f, v.y * f);
+    }
+}
+
+int launch_laplacian(const Ctx &c, double2 *coeffs, int inverse, int nbatch) {
+    long n = (long)c.nlm * nbatch;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_laplacian<<<blocks, 256, 0, c.stream>>>(coeffs, c.nlm, nbatch, inverse, c.tab->l_of_lm);
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// Deterministic FP64 quadrature: one CTA per (field, latitude) sums the row
+// in a fixed tree, then one CTA per field accumulates the latitudes in order.
+__global__ void k_row_sums(const double *__restrict__ f, double *__restrict__ rows, int nlon, int nlat) {
+    __shared__ double s[256];
+    const double *row = f + ((size_t)blockIdx.y * nlat + blockIdx.x) * nlon;
+    double a = 0.0;
+    for (int i = threadIdx.x; i < nlon; i += blockDim.x) a += row[i];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) rows[(size_t)blockIdx.y * nlat + blockIdx.x] = s[0];
+}
+
+__global__ void k_quadrature(const double *__restrict__ rows, const double *__restrict__ w, double *total, int nlat,
+                             int nlon) {
+    if (threadIdx.x != 0) return;
+    const double dlon = 2.0 * kPi / nlon;
+    double t = 0.0;
+    for (int j = 0; j < nlat; ++j) t += w[j] * rows[(size_t)blockIdx.x * nlat + j] * dlon;
+    total[blockIdx.x] = t * kA * kA;
+}
+
+int launch_surface_integral(const Ctx &c, const double *field, double *partial, double *total, int nbatch) {
+    k_row_sums<<<dim3(c.nlat, nbatch), 256, 0, c.stream>>>(field, partial, c.nlon, c.nlat);
+    k_quadrature<<<nbatch, 32, 0, c.stream>>>(partial, c.tab->w, total, c.nlat, c.nlon);
+    if (c.launches) *c.launches += 2;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+}  // namespace aeros

@@ -1,0 +1,212 @@
+"""Python mirror of aeros' dry time step on the GPU library.
+
+`AerosDyn` plays the role of aeros_timestep_class + the aeros facade
+(src/dynamics/aeros_timestep.f90:435-448, src/aeros.f90:64-70) for an ensemble
+of `nmember` members that share truncation and levels.  State arrays are
+complex128 numpy arrays (host) or torch complex128 CUDA tensors (device):
+vor/div/temp (nmember, nlev, nlm), lnps (nmember, nlm); with nmember == 1 the
+leading member axis may be dropped.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from .params import AerosParams, held_suarez_params
+from .spectral import _ptr, _is_torch
+
+YEAR_SECONDS = 365.25 * 86400.0   # src/aeros_defs.f90:100
+
+
+class AerosDyn:
+    def __init__(self, params: AerosParams = None, a_half=None, b_half=None):
+        self.params = params if params is not None else held_suarez_params()
+        L = _capi.lib()
+        h = ctypes.c_void_p()
+        ah = None if a_half is None else np.ascontiguousarray(a_half, np.float64)
+        bh = None if b_half is None else np.ascontiguousarray(b_half, np.float64)
+        _capi.check(L.aeros_dyn_create(ctypes.byref(h), ctypes.byref(self.params),
+                                       None if ah is None else _ptr(ah), None if bh is None else _ptr(bh)),
+                    "aeros_dyn_create")
+        self._h = h
+        a, b, c, d = (ctypes.c_int() for _ in range(4))
+        L.aeros_dyn_info(h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d),
+                         None, None, None, None, None)
+        self.nlon, self.nlat, self.nlm, self.nlev = a.value, b.value, c.value, d.value
+        self.nmember = self.params.nmember
+        self.A = np.zeros(self.nlev + 1)
+        self.B = np.zeros(self.nlev + 1)
+        self.sigma_full = np.zeros(self.nlev)
+        self.sinlat = np.zeros(self.nlat)
+        self.gauss_w = np.zeros(self.nlat)
+        L.aeros_dyn_info(h, None, None, None, None, _ptr(self.A), _ptr(self.B), _ptr(self.sigma_full),
+                         _ptr(self.sinlat), _ptr(self.gauss_w))
+        self.time = 0.0
+        self.time_init = 0.0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _capi.lib().aeros_dyn_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    # ------------------------------------------------------------------ state
+    def _shape3(self):
+        return (self.nmember, self.nlev, self.nlm)
+
+    def _alloc(self, like=None):
+        if like is not None and _is_torch(like):
+            import torch
+            z = lambda s: torch.zeros(s, dtype=torch.complex128, device=like.device)
+        else:
+            z = lambda s: np.zeros(s, np.complex128)
+        return z(self._shape3()), z(self._shape3()), z(self._shape3()), z((self.nmember, self.nlm))
+
+    @staticmethod
+    def _c(a):
+        if _is_torch(a):
+            import torch
+            if a.is_cuda:
+                torch.cuda.current_stream(a.device).synchronize()
+            return a.contiguous()
+        return np.ascontiguousarray(a, np.complex128)
+
+    def set_state(self, vor, div, temp, lnps):
+        arrs = [self._c(x) for x in (vor, div, temp, lnps)]
+        n3 = self.nmember * self.nlev * self.nlm
+        for x, n in zip(arrs, (n3, n3, n3, self.nmember * self.nlm)):
+            if (x.numel() if _is_torch(x) else x.size) != n:
+                raise ValueError("state array has the wrong size")
+        _capi.check(_capi.lib().aeros_dyn_set_state(self._h, *[_ptr(x) for x in arrs]), "aeros_dyn_set_state")
+
+    def get_state(self, like=None, squeeze=True, out=None):
+        s = self._alloc(like) if out is None else tuple(out)
+        if like is not None and _is_torch(like) and like.is_cuda:
+            import torch
+            torch.cuda.current_stream(like.device).synchronize()
+        _capi.check(_capi.lib().aeros_dyn_get_state(self._h, *[_ptr(x) for x in s]), "aeros_dyn_get_state")
+        return self._squeeze(s) if squeeze else s
+
+    def set_old_state(self, vor, div, temp, lnps, nstep):
+        arrs = [self._c(x) for x in (vor, div, temp, lnps)]
+        _capi.check(_capi.lib().aeros_dyn_set_old_state(self._h, *[_ptr(x) for x in arrs], int(nstep)),
+                    "aeros_dyn_set_old_state")
+
+    def get_old_state(self, squeeze=True):
+        s = self._alloc()
+        _capi.check(_capi.lib().aeros_dyn_get_old_state(self._h, *[_ptr(x) for x in s]), "aeros_dyn_get_old_state")
+        return self._squeeze(s) if squeeze else s
+
+    def _squeeze(self, s):
+        if self.nmember == 1:
+            return tuple(x[0] for x in s)
+        return s
+
+    def set_isothermal(self, temp=-1.0, ps=-1.0):
+        _capi.check(_capi.lib().aeros_dyn_set_isothermal(self._h, float(temp), float(ps)), "aeros_dyn_set_isothermal")
+
+    def set_phis(self, phis):
+        p = np.ascontiguousarray(phis, np.float64)
+        _capi.check(_capi.lib().aeros_dyn_set_phis(self._h, _ptr(p)), "aeros_dyn_set_phis")
+
+    def set_member_forcing(self, member, dt_y, k_a):
+        _capi.check(_capi.lib().aeros_dyn_set_member_forcing(self._h, int(member), float(dt_y), float(k_a)),
+                    "aeros_dyn_set_member_forcing")
+
+    # ------------------------------------------------------------------ stepping
+    def step(self, nsteps=1):
+        _capi.check(_capi.lib().aeros_dyn_step(self._h, int(nsteps)), "aeros_dyn_step")
+
+    def step_async(self, nsteps=1):
+        """Enqueue steps (CUDA graphs) without waiting; pair with sync()."""
+        _capi.check(_capi.lib().aeros_dyn_step_async(self._h, int(nsteps)), "aeros_dyn_step_async")
+
+    def sync(self):
+        _capi.check(_capi.lib().aeros_dyn_sync(self._h), "aeros_dyn_sync")
+
+    def profile_step(self, maxk=32):
+        """One real step with events between its kernels: [(name, ms), ...]."""
+        ms = np.zeros(maxk)
+        names = ctypes.create_string_buffer(maxk * 32)
+        nk = ctypes.c_int()
+        _capi.check(_capi.lib().aeros_dyn_profile_step(self._h, maxk, _ptr(ms), names, 32, ctypes.byref(nk)),
+                    "aeros_dyn_profile_step")
+        raw = names.raw
+        out = []
+        for i in range(nk.value):
+            nm = raw[i * 32:(i + 1) * 32].split(b"\0", 1)[0].decode()
+            out.append((nm, float(ms[i])))
+        return out
+
+    def update(self, time_years):
+        """Advance to `time_years` with the step-count rule of aeros_update
+        (src/aeros.f90:202-241): n_target = nint((t - t0) yr / dt)."""
+        if time_years < self.time:
+            raise ValueError("cannot step backwards")
+        nstep = self.counters()[0]
+        target = int(np.rint((time_years - self.time_init) * YEAR_SECONDS / self.params.dt))
+        if target > nstep:
+            self.step(target - nstep)
+        self.time = time_years
+
+    def tendency(self):
+        s = self._alloc()
+        _capi.check(_capi.lib().aeros_dyn_tendency(self._h, *[_ptr(x) for x in s]), "aeros_dyn_tendency")
+        return self._squeeze(s)
+
+    def diagnose(self):
+        shp = (self.nmember, self.nlev, self.nlat, self.nlon)
+        u, v, t = np.zeros(shp), np.zeros(shp), np.zeros(shp)
+        ps = np.zeros((self.nmember, self.nlat, self.nlon))
+        _capi.check(_capi.lib().aeros_dyn_diagnose(self._h, _ptr(u), _ptr(v), _ptr(t), _ptr(ps)), "aeros_dyn_diagnose")
+        if self.nmember == 1:
+            return u[0], v[0], t[0], ps[0]
+        return u, v, t, ps
+
+    def budget(self):
+        m, e, a = (np.zeros(self.nmember) for _ in range(3))
+        _capi.check(_capi.lib().aeros_dyn_budget(self._h, _ptr(m), _ptr(e), _ptr(a)), "aeros_dyn_budget")
+        if self.nmember == 1:
+            return float(m[0]), float(e[0]), float(a[0])
+        return m, e, a
+
+    def counters(self):
+        n = ctypes.c_int()
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _capi.check(_capi.lib().aeros_dyn_counters(self._h, ctypes.byref(n), ctypes.byref(a), ctypes.byref(b),
+                                                   ctypes.byref(c)), "aeros_dyn_counters")
+        return n.value, a.value, b.value, c.value
+
+    def set_mass_target(self, mass):
+        _capi.check(_capi.lib().aeros_dyn_set_mass_target(self._h, float(mass)), "aeros_dyn_set_mass_target")
+
+    def diag_accumulate(self):
+        _capi.check(_capi.lib().aeros_dyn_diag_accumulate(self._h), "aeros_dyn_diag_accumulate")
+
+    def diag_read(self, member=0):
+        nl, n = self.nlat, self.nlev
+        out = np.zeros(7 * nl * n + 2 * nl)
+        ns = ctypes.c_int()
+        _capi.check(_capi.lib().aeros_dyn_diag_read(self._h, int(member), _ptr(out), ctypes.byref(ns)),
+                    "aeros_dyn_diag_read")
+        F = nl * n
+        names = ["u", "v", "temp", "uv", "vt", "eke", "tvar"]
+        d = {nm: out[i * F:(i + 1) * F].reshape(n, nl) for i, nm in enumerate(names)}
+        d["ps"] = out[7 * F:7 * F + nl]
+        d["u_sfc"] = out[7 * F + nl:]
+        d["nsample"] = ns.value
+        return d
+
+    def gwspeed(self):
+        c = ctypes.c_double()
+        _capi.check(_capi.lib().aeros_dyn_gwspeed(self._h, ctypes.byref(c)), "aeros_dyn_gwspeed")
+        return c.value
+
+    def set_stream(self, stream_ptr):
+        _capi.check(_capi.lib().aeros_dyn_set_stream(self._h, ctypes.c_void_p(stream_ptr)), "aeros_dyn_set_stream")
+
+    def launch_count(self):
+        c = ctypes.c_longlong()
+        _capi.lib().aeros_dyn_launch_count(self._h, ctypes.byref(c))
+        return c.value

@@ -131,6 +131,9 @@ int aeros_vordiv_from_uv(aeros_sht_t h, const double *u, const double *v,
                          double *vor, double *div, int nbatch);
 int aeros_gradient(aeros_sht_t h, const double *f, double *dfdx, double *dfdy, int nbatch);
 
+/* Number of this library's kernel launches issued by the handle so far. */
+int aeros_sht_launch_count(aeros_sht_t h, long long *count);
+
 /* ======================================================================== */
 /* Dry dynamics step: mirrors aeros_timestep / aeros facade                  */
 /* ======================================================================== */
@@ -212,6 +215,17 @@ int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis);
 /* Advance every member by nsteps dynamics steps.  Replaces nsteps calls of
  * aeros_timestep_step (src/dynamics/aeros_timestep.f90:776-1137), dry path. */
 int aeros_dyn_step(aeros_dyn_t h, int nsteps);
+
+/* Enqueue nsteps steps on the handle's stream and return at once (CUDA
+ * graphs; no host synchronization).  aeros_dyn_sync waits for them and
+ * reports AEROS_ERR_NONFINITE if any step produced a NaN/Inf. */
+int aeros_dyn_step_async(aeros_dyn_t h, int nsteps);
+int aeros_dyn_sync(aeros_dyn_t h);
+
+/* Run one step with a CUDA event after every kernel (no graph) and return the
+ * per-kernel durations in ms (up to maxk) and their names (name_len bytes
+ * each, may be NULL).  For measurement; the step is a real step. */
+int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int name_len, int *nk);
 
 /* Adiabatic spectral tendencies R(X^n) of the current state, no forcing:
  * replaces aeros_tendency_calc (src/dynamics/aeros_tendency.f90:338-360). */

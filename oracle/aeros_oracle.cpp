@@ -160,42 +160,43 @@ struct Sht {
     RFFT fft;
 };
 
-// Gauss-Legendre nodes on (-1,1), descending (north first), and weights
-// summing to 2.  Newton on P_n from the Chebyshev-like first guess, as in
-// mwm/A_scaling/src/aeros_bench_batched.f90:628-658; the weight is evaluated
-// at the converged node.
-void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+// Gauss-Legendre nodes on (-1,1), descending (north first), weights summing
+// to 2, and sin(colatitude).  Newton on P_n from the first guess of
+// mwm/A_scaling/src/aeros_bench_batched.f90:628-658, carried out in extended
+// precision so that the rounded node, weight and sin(theta) are accurate to
+// the last bit (sin(theta) comes from the unrounded node: near the poles it is
+// ill-conditioned in x, and a last-bit difference in x would move the polar
+// rows of Pbar_m^m by ~m x 1e-14).
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w, std::vector<double> &st) {
     x.assign(n, 0.0);
     w.assign(n, 0.0);
+    st.assign(n, 0.0);
+    auto pn = [n](long double z, long double &p, long double &dp) {
+        long double p1 = 1.0L, p2 = 0.0L;
+        for (int j = 1; j <= n; ++j) {
+            long double p3 = p2;
+            p2 = p1;
+            p1 = ((2.0L * j - 1.0L) * z * p2 - (j - 1.0L) * p3) / j;
+        }
+        p = p1;
+        dp = n * (z * p1 - p2) / (z * z - 1.0L);
+    };
     int mroots = (n + 1) / 2;
     for (int i = 1; i <= mroots; ++i) {
-        double z = std::cos(PI * (i - 0.25) / (n + 0.5));
-        double p1 = 0, p2 = 0, pp = 0;
+        long double z = std::cos(PI * (i - 0.25) / (n + 0.5)), p, dp;
         for (int it = 0; it < 100; ++it) {
-            p1 = 1.0; p2 = 0.0;
-            for (int j = 1; j <= n; ++j) {
-                double p3 = p2;
-                p2 = p1;
-                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-            }
-            pp = n * (z * p1 - p2) / (z * z - 1.0);
-            double z1 = z;
-            z = z1 - p1 / pp;
-            if (std::fabs(z - z1) <= 3.0e-15) break;
+            pn(z, p, dp);
+            long double z1 = z;
+            z = z1 - p / dp;
+            if (std::fabs((double)(z - z1)) <= 1.0e-18) break;
         }
-        p1 = 1.0; p2 = 0.0;
-        for (int j = 1; j <= n; ++j) {
-            double p3 = p2;
-            p2 = p1;
-            p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-        }
-        pp = n * (z * p1 - p2) / (z * z - 1.0);
-        x[i - 1] = z;
-        x[n - i] = -z;
-        w[i - 1] = 2.0 / ((1.0 - z * z) * pp * pp);
-        w[n - i] = w[i - 1];
+        pn(z, p, dp);
+        x[i - 1] = (double)z;
+        x[n - i] = -(double)z;
+        w[i - 1] = w[n - i] = (double)(2.0L / ((1.0L - z * z) * dp * dp));
+        st[i - 1] = st[n - i] = (double)std::sqrt((1.0L - z) * (1.0L + z));
     }
-    if (n % 2 == 1) x[n / 2] = 0.0;
+    if (n % 2 == 1) { x[n / 2] = 0.0; st[n / 2] = 1.0; }
 }
 
 // Normalized Pbar_l^m (integral over x of Pbar^2 = 1, no Condon-Shortley
@@ -264,10 +265,7 @@ Sht *sht_create(int trunc, int nlon, int nlat) {
             ++c;
         }
     }
-    gauss_legendre(s->nlat, s->x, s->w);
-    s->sint.resize(s->nlat);
-    for (int j = 0; j < s->nlat; ++j)
-        s->sint[j] = std::sqrt((1.0 - s->x[j]) * (1.0 + s->x[j]));
+    gauss_legendre(s->nlat, s->x, s->w, s->sint);
     build_tables(*s);
     s->fft.init(s->nlon);
     return s;

@@ -1,0 +1,234 @@
+"""GPU dynamics parity: the dry Held-Suarez step on the GPU (C-ABI) against
+the CPU oracle on the same seeded inputs.
+
+Bars (max |gpu - oracle| / scale):
+  tendencies of vorticity, temperature, ln ps    1e-12 of max |tendency|
+  divergence tendency                            max(1e-12, 20 x the oracle's own
+      change under 1-ulp input perturbations, measured in the test): dD/dt is
+      the small residual of the Coriolis, pressure-gradient and geopotential
+      terms, so any two FP64 implementations that sum in a different order
+      differ by ~eps x that cancellation ratio relative to dD/dt itself
+      (measured: 2e-13 at T21, 7e-13 at T42 for the oracle against itself)
+  state after one step (moving state)            1e-12 for vor, T, ln ps;
+                                                 1e-11 for D (carries h dD/dt)
+  state after 10 steps                           1e-10
+  mass fixer                                     target 1e-13 rel, ln r 1e-14 abs
+"""
+import numpy as np
+import pytest
+
+from tests._helpers import red_spectrum, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def noisy_state(o, sht, temp=264.0, noise=0.1, seed=0):
+    """Rest, isothermal T, ps = 1000 hPa, N(0, noise^2) K on grid T, analysed."""
+    o.set_isothermal(temp, 1.0e5)
+    vor, div, t, lnps = o.get_state()
+    rng = np.random.default_rng(seed)
+    tg = sht.synthesis(t) + rng.normal(0.0, noise, (o.nlev, o.nlat, o.nlon))
+    t = sht.analysis(tg)
+    return vor, div, t, lnps
+
+
+def moving_state(o, seed=3):
+    rng = np.random.default_rng(seed)
+    from oracle.pyoracle import OracleSHT
+    s = OracleSHT(o.params.trunc)
+    vor = 1e-5 * red_spectrum(rng, s.l_of_lm, s.m_of_lm, (o.nlev,), slope=-1.0)
+    div = 2e-6 * red_spectrum(rng, s.l_of_lm, s.m_of_lm, (o.nlev,), slope=-1.0)
+    vor[:, 0] = 0
+    div[:, 0] = 0
+    o.set_isothermal(264.0, 1.0e5)
+    _, _, t, lnps = o.get_state()
+    t = t + 1.0 * red_spectrum(rng, s.l_of_lm, s.m_of_lm, (o.nlev,), slope=-1.0)
+    lnps = lnps + 0.01 * red_spectrum(rng, s.l_of_lm, s.m_of_lm, (), slope=-1.0)
+    return vor, div, t, lnps
+
+
+def make_pair(trunc, nlev, **kw):
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from oracle.pyoracle import OracleDyn, OracleSHT
+    p = held_suarez_params(trunc=trunc, nlev=nlev, **kw)
+    return AerosDyn(p), OracleDyn(p), OracleSHT(trunc)
+
+
+def oracle_floor(o, st, which, reps=3):
+    """Relative change of the oracle's tendency field `which` when the input
+    state is perturbed at the last bit (its rounding sensitivity)."""
+    o.set_state(*st)
+    t0 = o.tendency()[which]
+    rng = np.random.default_rng(99)
+    worst = 0.0
+    for _ in range(reps):
+        o.set_state(*[x * (1 + 2.2e-16 * rng.standard_normal(x.shape)) for x in st])
+        worst = max(worst, relerr(o.tendency()[which], t0))
+    o.set_state(*st)
+    return worst
+
+
+@pytest.mark.parametrize("trunc,nlev", [(21, 12), (42, 20)])
+def test_adiabatic_tendency(gpulib, trunc, nlev):
+    g, o, s = make_pair(trunc, nlev)
+    st = moving_state(o)
+    o.set_state(*st)
+    g.set_state(*st)
+    tg = g.tendency()
+    to = o.tendency()
+    assert relerr(tg[0], to[0]) < 1e-12
+    assert relerr(tg[2], to[2]) < 1e-12
+    assert relerr(tg[3], to[3]) < 1e-12
+    assert relerr(tg[1], to[1]) < max(1e-12, 20 * oracle_floor(o, st, 1))
+
+
+def test_rest_state_tendency(gpulib):
+    """tests/test_tendency.f90:77-107: resting isothermal atmosphere has no tendency."""
+    g, o, s = make_pair(21, 12, held_suarez=0, p_top=0.0)
+    g.set_isothermal(280.0, 1.0e5)
+    tv, td, tt, tp = g.tendency()
+    assert np.max(np.abs(tv)) == 0.0
+    assert np.max(np.abs(td)) < 1e-12 * 1e-5
+    assert np.max(np.abs(tt)) < 1e-12 and np.max(np.abs(tp)) < 1e-12
+
+
+@pytest.mark.parametrize("trunc", [21, 31])
+def test_hs_steps_match_oracle(gpulib, trunc):
+    """Forced steps from a moving state: every term of the column is active."""
+    g, o, s = make_pair(trunc, 20)
+    st = moving_state(o, seed=21)
+    o.set_state(*st)
+    g.set_state(*st)
+    o.step(1)
+    g.step(1)
+    sg, so = g.get_state(), o.get_state()
+    assert relerr(sg[0], so[0]) < 1e-12
+    assert relerr(sg[1], so[1]) < 1e-11
+    assert relerr(sg[2], so[2]) < 1e-12
+    assert relerr(sg[3], so[3]) < 1e-12
+    o.step(9)
+    g.step(9)
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert relerr(a, b) < 1e-10
+    for a, b in zip(g.get_old_state(), o.get_old_state()):
+        assert relerr(a, b) < 1e-10
+    ng, mg, lg, cg = g.counters()
+    no, mo, lo, co = o.counters()
+    assert ng == no == 10
+    assert abs(mg - mo) / mo < 1e-13
+    assert abs(lg - lo) < 1e-14 and abs(cg - co) < 1e-13
+
+
+def test_hs_rest_noise_start(gpulib):
+    """Rest + 0.1 K noise (the Held-Suarez start): T and ln ps match from the
+    first step; vor and D start at round-off size (dzeta/dt is analytically 0
+    at rest) and are compared once populated, after 30 steps."""
+    g, o, s = make_pair(21, 20)
+    st = noisy_state(o, s)
+    o.set_state(*st)
+    g.set_state(*st)
+    o.step(1)
+    g.step(1)
+    sg, so = g.get_state(), o.get_state()
+    assert relerr(sg[2], so[2]) < 1e-12 and relerr(sg[3], so[3]) < 1e-12
+    o.step(29)
+    g.step(29)
+    sg, so = g.get_state(), o.get_state()
+    assert relerr(sg[0], so[0]) < 1e-10 and relerr(sg[1], so[1]) < 1e-10
+    assert relerr(sg[2], so[2]) < 1e-12 and relerr(sg[3], so[3]) < 1e-12
+
+
+def test_forced_moving_state_steps(gpulib):
+    """A state with winds and ln(ps) structure: every term of the column is active."""
+    g, o, s = make_pair(31, 20)
+    st = moving_state(o, seed=5)
+    o.set_state(*st)
+    g.set_state(*st)
+    o.step(3)
+    g.step(3)
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert relerr(a, b) < 1e-11
+
+
+def test_diagnose_budget_zonal(gpulib):
+    g, o, s = make_pair(21, 12)
+    st = moving_state(o, seed=7)
+    o.set_state(*st)
+    g.set_state(*st)
+    for a, b in zip(g.diagnose(), o.diagnose()):
+        assert relerr(a, b) < 1e-12
+    bg, bo = g.budget(), o.budget()
+    for a, b in zip(bg, bo):
+        assert abs(a - b) / abs(b) < 1e-12
+    g.diag_accumulate()
+    o.diag_accumulate()
+    dg, do = g.diag_read(), o.diag_read()
+    for k in ("u", "v", "temp", "uv", "vt", "eke", "tvar", "ps", "u_sfc"):
+        assert relerr(dg[k], do[k]) < 1e-11, k
+
+
+def test_ensemble_members_independent(gpulib):
+    """Members stepped together equal single-member runs with the same forcing."""
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from oracle.pyoracle import OracleDyn, OracleSHT
+    p = held_suarez_params(trunc=21, nlev=16, nmember=3)
+    g = AerosDyn(p)
+    s = OracleSHT(21)
+    states, oracles = [], []
+    for e, dty in enumerate((40.0, 60.0, 80.0)):
+        p1 = held_suarez_params(trunc=21, nlev=16)
+        o = OracleDyn(p1)
+        o.set_forcing(dty, p1.hs_k_a * (1 + 0.1 * e))
+        g.set_member_forcing(e, dty, p1.hs_k_a * (1 + 0.1 * e))
+        st = moving_state(o, seed=1000 + e)
+        o.set_state(*st)
+        states.append(st)
+        oracles.append(o)
+    g.set_state(*[np.stack([st[i] for st in states]) for i in range(4)])
+    g.step(4)
+    for o in oracles:
+        o.step(4)
+    gs = g.get_state()
+    for e, o in enumerate(oracles):
+        for a, b in zip([x[e] for x in gs], o.get_state()):
+            assert relerr(a, b) < 1e-10
+
+
+def test_restart_split_run_bitwise(gpulib):
+    """tests/test_restart.f90: a split run equals the continuous run bit for bit."""
+    g1, o, s = make_pair(21, 12)
+    st = noisy_state(o, s, seed=9)
+    g1.set_state(*st)
+    g1.step(6)
+    full = g1.get_state()
+    g2, _, _ = make_pair(21, 12)
+    g2.set_state(*st)
+    g2.step(3)
+    now, old = g2.get_state(), g2.get_old_state()
+    n, mt, _, _ = g2.counters()
+    g3, _, _ = make_pair(21, 12)
+    g3.set_state(*now)
+    g3.set_old_state(*old, nstep=n)
+    g3.set_mass_target(mt)
+    g3.step(3)
+    for a, b in zip(g3.get_state(), full):
+        assert np.array_equal(a, b)
+
+
+def test_nonfinite_state_is_reported(gpulib):
+    """A NaN planted in the input state comes back as AEROS_ERR_NONFINITE."""
+    from aeros_gb300._capi import AerosError, ERR_NONFINITE
+    g, o, s = make_pair(21, 12, mass_fixer=0)
+    g.set_isothermal(264.0, 1.0e5)
+    vor, div, t, lnps = g.get_state()
+    t = t.copy()
+    t[3, 5] = np.nan
+    g.set_state(vor, div, t, lnps)
+    with pytest.raises(AerosError) as ei:
+        g.step(1)
+    assert ei.value.code == ERR_NONFINITE
+    g.set_isothermal(264.0, 1.0e5)
+    g.set_state(*g.get_state())
+    g.step(1)
