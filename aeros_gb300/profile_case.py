@@ -1,0 +1,47 @@
+"""A fixed step workload for profiling one kernel under ncu.
+
+  python -m aeros_gb300.profile_case --trunc 42 --nlev 20 --members 16 --steps 3 [--precision fp64|split]
+
+Builds an ensemble of Held-Suarez members (rest + 0.1 K noise, one seed per
+member) and runs `steps` steps with direct launches (no graph), so that an
+ncu `-k <kernel> -s <n> -c <k>` selection sees a small, fixed number of
+launches.  With 16 members at T42L20 the grid fields of one launch (~235 MB)
+exceed the 129 MB L2, so DRAM counters measure real traffic.
+"""
+import argparse
+import sys
+
+import numpy as np
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--trunc", type=int, default=42)
+    ap.add_argument("--nlev", type=int, default=20)
+    ap.add_argument("--members", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    a = ap.parse_args(argv)
+    from .params import held_suarez_params, PREC_FP64, PREC_SPLIT
+    from .dynamics import AerosDyn
+    from .spectral import AerosSHT
+    p = held_suarez_params(trunc=a.trunc, nlev=a.nlev, nmember=a.members,
+                           precision=PREC_SPLIT if a.precision == "split" else PREC_FP64)
+    dyn = AerosDyn(p)
+    sht = AerosSHT(a.trunc, batch_max=a.nlev)
+    dyn.set_isothermal(264.0, 1.0e5)
+    vor, div, t, lnps = dyn.get_state(squeeze=False)
+    t = t.copy()
+    for e in range(a.members):
+        rng = np.random.default_rng(e)
+        tg = sht.synthesis(t[e]) + rng.normal(0.0, 0.1, (a.nlev, dyn.nlat, dyn.nlon))
+        t[e] = sht.analysis(tg)
+    dyn.set_state(vor, div, t, lnps)
+    for _ in range(a.steps):
+        ks = dyn.profile_step()
+    print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

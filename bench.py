@@ -45,6 +45,18 @@ def parse():
     return ap.parse_args()
 
 
+def reduce_time(local_s, world, backend="nccl"):
+    """Max over ranks of a per-rank time (the replicas share no data)."""
+    if world <= 1:
+        return local_s
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if backend == "nccl" else "cpu"
+    t = torch.tensor([float(local_s)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def rank_info():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -273,9 +285,7 @@ def run_gpu(args, rank, world, local):
     t_warm = e0.elapsed_time(e1) / 1e3 / K
     clk = clocks.stop()
     if world > 1:
-        tt = torch.tensor([t_gpu], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_gpu = float(tt.item())
+        t_gpu = reduce_time(t_gpu, world, backend="nccl")
         dist.barrier()
 
     # per-kernel durations (events between the step's launches), averaged

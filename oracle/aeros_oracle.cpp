@@ -1445,6 +1445,21 @@ int ora_dyn_si_linear(void *h, double *ldiv, double *ltemp, double *lps) {
     }
     return 0;
 }
+// Pointwise Held-Suarez functions (src/physics/aeros_held_suarez.f90:225-293).
+double ora_hs_teq(const aeros_params *p, double pres, double sinlat2, double coslat2) {
+    double pfac = pres / p->hs_p0;
+    double teq = (p->hs_t_equator - p->hs_dt_y * sinlat2 - p->hs_dtheta_z * std::log(pfac) * coslat2) *
+                 std::pow(pfac, KAPPA);
+    return std::max(p->hs_t_min, teq);
+}
+static double hs_hfac(const aeros_params *p, double sigma) {
+    return std::max(0.0, (sigma - p->hs_sigma_b) / (1.0 - p->hs_sigma_b));
+}
+double ora_hs_kt(const aeros_params *p, double sigma, double coslat4) {
+    return p->hs_k_a + (p->hs_k_s - p->hs_k_a) * hs_hfac(p, sigma) * coslat4;
+}
+double ora_hs_kv(const aeros_params *p, double sigma) { return p->hs_k_f * hs_hfac(p, sigma); }
+
 int ora_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);

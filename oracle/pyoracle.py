@@ -44,6 +44,10 @@ def lib():
         L.ora_dyn_step.argtypes = [vp, ctypes.c_int]
         L.ora_grid_size.argtypes = [ctypes.c_int, ip, ip]
         L.ora_set_threads.argtypes = [ctypes.c_int]
+        for name, n in (("ora_hs_teq", 3), ("ora_hs_kt", 2), ("ora_hs_kv", 1)):
+            fn = getattr(L, name)
+            fn.restype = ctypes.c_double
+            fn.argtypes = [vp] + [ctypes.c_double] * n
         _lib = L
     return _lib
 
@@ -54,6 +58,18 @@ def _p(a):
 
 def set_threads(n: int) -> int:
     return lib().ora_set_threads(int(n))
+
+
+def hs_teq(params, p, sinlat2, coslat2):
+    return lib().ora_hs_teq(ctypes.byref(params), p, sinlat2, coslat2)
+
+
+def hs_kt(params, sigma, coslat4):
+    return lib().ora_hs_kt(ctypes.byref(params), sigma, coslat4)
+
+
+def hs_kv(params, sigma):
+    return lib().ora_hs_kv(ctypes.byref(params), sigma)
 
 
 def grid_size(trunc):
