@@ -67,6 +67,7 @@ _PROTOS = {
     "aeros_vordiv_from_uv": [_vp, _vp, _vp, _vp, _vp, _i],
     "aeros_gradient": [_vp, _vp, _vp, _vp, _i],
     "aeros_sht_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "aeros_sht_synthesis_noalloc": [_vp, _vp, _vp, _i],
     "aeros_params_default": [ctypes.POINTER(AerosParams)],
     "aeros_dyn_create": [ctypes.POINTER(_vp), ctypes.POINTER(AerosParams), _vp, _vp],
     "aeros_dyn_destroy": [_vp],

@@ -249,7 +249,23 @@ int dispatch(aeros_sht_t h, int op, bool in_spec, int nin, int nout, const doubl
 
 namespace aeros {
 const char *last_error();
+
+// Read-only view of a handle for the other translation units of the library.
+struct ShtView {
+    const Geometry *g;
+    const DevTables *tab;
+    cudaStream_t stream;
+    long long *launches;
+};
+int sht_view(aeros_sht_t h, ShtView &v) {
+    if (!h) return AEROS_ERR_ARG;
+    v.g = &h->g;
+    v.tab = &h->tab;
+    v.stream = h->stream;
+    v.launches = &h->launches;
+    return AEROS_OK;
 }
+}  // namespace aeros
 
 extern "C" {
 

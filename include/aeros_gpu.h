@@ -134,6 +134,18 @@ int aeros_gradient(aeros_sht_t h, const double *f, double *dfdx, double *dfdy, i
 /* Number of this library's kernel launches issued by the handle so far. */
 int aeros_sht_launch_count(aeros_sht_t h, long long *count);
 
+/* Scalar synthesis that allocates nothing, for callers that cannot call
+ * cudaMalloc (device memory owned by another allocator or reserved up front,
+ * or a loop whose memory must not change once it runs).  No counterpart in
+ * the reference.  Same result as aeros_sht_synthesis; coeffs and field must
+ * be device pointers.  Its Fourier-row scratch (2^19 complex = 8 MiB) and
+ * descriptors live in static device arrays that every GPU loading the library
+ * holds until exit: nbatch <= 256 and nlat * nbatch * (T+1) <= 2^19, else
+ * AEROS_ERR_ARG.  All calls share those arrays, so calls that overlap on the
+ * GPU race.  The first call on a device resolves the arrays' addresses; make
+ * it before any stream capture.  Synchronous. */
+int aeros_sht_synthesis_noalloc(aeros_sht_t h, const double *coeffs, double *field, int nbatch);
+
 /* ======================================================================== */
 /* Dry dynamics step: mirrors aeros_timestep / aeros facade                  */
 /* ======================================================================== */
