@@ -35,13 +35,14 @@ struct LevConst {
     double A0, A1, B0, B1, dB;
     double dlnp, alpha, cfac;     // valid when pure
     double lnbf, bfk;             // ln(bf), bf^kappa with p_full = bf ps (pure)
+    double hf;                    // Held-Suarez max(0, (sigma - sigma_b)/(1 - sigma_b)) (pure)
     int pure;
     int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
 };
 __constant__ LevConst c_lev[kMaxLev];
 
 struct HsConst {
-    double t_eq, t_min, dtheta_z, sigma_b, p0, k_s, k_f, lnp0;
+    double t_eq, t_min, dtheta_z, sigma_b, p0, k_s, k_f, lnp0, rsb;   // rsb = 1/(1 - sigma_b)
 };
 __constant__ HsConst c_hs;
 
@@ -49,10 +50,10 @@ __constant__ HsConst c_hs;
 // Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
 // dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy.  Outputs GA[e][f][j][i]:
 // ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.  One thread per column.
-__global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
-                                                int nlon, int nlat, int M, const double *__restrict__ xlat,
-                                                const double *__restrict__ phis, int hs_on,
-                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
+__global__ void __launch_bounds__(64) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
+                                               int nlon, int nlat, int M, const double *__restrict__ xlat,
+                                               const double *__restrict__ phis, int hs_on,
+                                               const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
     const long ng = (long)nlon * nlat;
     long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (gid >= ng * M) return;
@@ -65,14 +66,16 @@ __global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, do
 #define GO(f) Go[(size_t)(f) * ng]
     const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
     const double ps = exp(lnps);
-    double dp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev], gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1],
+    // per-level column quantities; 1/dp replaces the reference's divisions by dp
+    double rdp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev], gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1],
         phi[kMaxLev];
     scum[0] = 0.0;
     for (int k = 0; k < NL; ++k) {
         const LevConst &L = c_lev[k];
-        double ph0 = L.A0 + L.B0 * ps, ph1 = L.A1 + L.B1 * ps;
-        double d = ph1 - ph0;
-        dp[k] = d;
+        const double ph0 = fma(L.B0, ps, L.A0), ph1 = fma(L.B1, ps, L.A1);
+        const double d = ph1 - ph0;
+        const double r = 1.0 / d;
+        rdp[k] = r;
         if (L.pure) {
             dlnp[k] = L.dlnp;
             alpha[k] = L.alpha;
@@ -84,16 +87,15 @@ __global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, do
                 dl = 0.0;                      // zero-pressure top: substituted 0
             } else {
                 dl = log(ph1 / ph0);
-                al = 1.0 - (ph0 / d) * dl;
+                al = 1.0 - (ph0 * r) * dl;
             }
             dlnp[k] = dl;
             alpha[k] = al;
-            cfac[k] = (ps / d) * (L.B0 * dl + L.dB * al);
+            cfac[k] = (ps * r) * (L.B0 * dl + L.dB * al);
         }
-        double u = GF(k), v = GF(NL + k), dv = GF(3 * NL + k);
-        double g = u * dpx + v * dpy;
+        const double g = GF(k) * dpx + GF(NL + k) * dpy;
         gc[k] = g;
-        double cmass = d * dv + L.dB * ps * g;
+        const double cmass = d * GF(3 * NL + k) + L.dB * ps * g;
         cm[k] = cmass;
         scum[k + 1] = scum[k] + cmass;
     }
@@ -102,20 +104,21 @@ __global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, do
     {
         double phh = phis ? phis[c] : 0.0;
         for (int k = NL - 1; k >= 0; --k) {
-            double t = GF(4 * NL + k);
-            phi[k] = phh + alpha[k] * kRd * t;
-            phh = phh + kRd * t * dlnp[k];
+            const double rt = kRd * GF(4 * NL + k);
+            phi[k] = fma(alpha[k], rt, phh);
+            phh = fma(rt, dlnp[k], phh);
         }
     }
     const double SN = scum[NL];
     const double f = 2.0 * kOmega * xlat[j];
     const double x2 = xlat[j] * xlat[j], c2 = 1.0 - x2, c4 = c2 * c2;
-    double dty = 0, ka = 0, psk = 0, lnpr = 0;
+    double dty = 0, ka = 0, psk = 0, lnpr = 0, tbase = 0;
     if (hs_on) {
         dty = hs_dty[e];
         ka = hs_ka[e];
         lnpr = lnps - c_hs.lnp0;
         psk = exp(kKappa * lnpr);   // (ps/p0)^kappa
+        tbase = c_hs.t_eq - dty * x2;
     }
     double up = 0, vp = 0, tp = 0;                    // level k-1
     double uc = GF(0), vc = GF(NL), tc = GF(4 * NL);  // level k
@@ -127,38 +130,37 @@ __global__ void __launch_bounds__(128) k_column(const double *__restrict__ G, do
             vn = GF(NL + k + 1);
             tn = GF(4 * NL + k + 1);
         }
-        const double d = dp[k];
-        const double omega = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cm[k]) / d;
+        const double r = rdp[k];
+        const double omega = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cm[k]) * r;
         const double mup = L.B0 * SN - scum[k];        // M at half level k (above)
         const double mlo = L.B1 * SN - scum[k + 1];    // M at half level k+1 (below)
-        double vu = 0.5 * (((k < NL - 1) ? mlo * (un - uc) : 0.0) + ((k > 0) ? mup * (uc - up) : 0.0)) / d;
-        double vv = 0.5 * (((k < NL - 1) ? mlo * (vn - vc) : 0.0) + ((k > 0) ? mup * (vc - vp) : 0.0)) / d;
-        double vt = 0.5 * (((k < NL - 1) ? mlo * (tn - tc) : 0.0) + ((k > 0) ? mup * (tc - tp) : 0.0)) / d;
+        const double hr = 0.5 * r;
+        const double vu = hr * (((k < NL - 1) ? mlo * (un - uc) : 0.0) + ((k > 0) ? mup * (uc - up) : 0.0));
+        const double vv = hr * (((k < NL - 1) ? mlo * (vn - vc) : 0.0) + ((k > 0) ? mup * (vc - vp) : 0.0));
+        const double vt = hr * (((k < NL - 1) ? mlo * (tn - tc) : 0.0) + ((k > 0) ? mup * (tc - tp) : 0.0));
         const double zf = GF(2 * NL + k) + f;
         const double pgf = kRd * tc * cfac[k];
         double ae = zf * vc - vu - pgf * dpx;
         double an = -zf * uc - vv - pgf * dpy;
-        double ek = phi[k] + 0.5 * (uc * uc + vc * vc);
+        const double ek = phi[k] + 0.5 * (uc * uc + vc * vc);
         double dtdt = -(uc * GF(5 * NL + k) + vc * GF(6 * NL + k)) - vt + kKappa * tc * omega;
         if (hs_on) {
             // src/physics/aeros_held_suarez.f90:177-293
-            double pf, sig, lnpf, pfk;
+            double lnpf, pfk, hf;
             if (L.pure) {
-                sig = 0.5 * (L.B0 + L.B1);
                 lnpf = L.lnbf + lnpr;
                 pfk = L.bfk * psk;
+                hf = L.hf;
             } else {
-                pf = 0.5 * ((L.A0 + L.B0 * ps) + (L.A1 + L.B1 * ps));
-                sig = pf / ps;
+                const double pf = 0.5 * (fma(L.B0, ps, L.A0) + fma(L.B1, ps, L.A1));
                 lnpf = log(pf / c_hs.p0);
                 pfk = exp(kKappa * lnpf);
+                hf = fmax(0.0, (pf / ps - c_hs.sigma_b) * c_hs.rsb);
             }
-            double teq = (c_hs.t_eq - dty * x2 - c_hs.dtheta_z * lnpf * c2) * pfk;
-            teq = fmax(c_hs.t_min, teq);
-            double hf = fmax(0.0, (sig - c_hs.sigma_b) / (1.0 - c_hs.sigma_b));
-            double kt = ka + (c_hs.k_s - ka) * hf * c4;
-            double kv = c_hs.k_f * hf;
+            const double teq = fmax(c_hs.t_min, (tbase - c_hs.dtheta_z * lnpf * c2) * pfk);
+            const double kt = ka + (c_hs.k_s - ka) * hf * c4;
             dtdt -= kt * (tc - teq);
+            const double kv = c_hs.k_f * hf;
             ae -= kv * uc;
             an -= kv * vc;
         }
@@ -837,12 +839,13 @@ int upload_level_consts(Dyn &d) {
             double bf = 0.5 * (c.B0 + c.B1);
             c.lnbf = std::log(bf);
             c.bfk = std::pow(bf, kKappa);
+            c.hf = std::max(0.0, (bf - d.par.hs_sigma_b) / (1.0 - d.par.hs_sigma_b));
         }
     }
     AEROS_CUDA(cudaMemcpyToSymbol(c_lev, L.data(), sizeof(LevConst) * n));
     const aeros_params &p = d.par;
     HsConst h{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
-              std::log(p.hs_p0)};
+              std::log(p.hs_p0), 1.0 / (1.0 - p.hs_sigma_b)};
     AEROS_CUDA(cudaMemcpyToSymbol(c_hs, &h, sizeof(h)));
     return AEROS_OK;
 }
@@ -900,7 +903,7 @@ int run_tendency(Dyn &d, int hs_on) {
     if ((rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS))) return rc;
     mark(d, "fourier_synth");
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
-    k_column<<<(unsigned)((ncol + 127) / 128), 128, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
+    k_column<<<(unsigned)((ncol + 63) / 64), 64, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
                                                                   d.xlat_d, d.phis_set ? d.phis_d : nullptr, hs_on,
                                                                   d.hs_dty_d, d.hs_ka_d);
     ++d.launches;

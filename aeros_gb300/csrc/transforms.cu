@@ -28,51 +28,42 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
     const int n = nlon / 2;
     const int j0 = blockIdx.y * lpb;
     const int nr = min(lpb, nlat - j0);
-    double2 *A = sm, *B = sm + (size_t)lpb * n;
+    double2 *A = sm, *B = sm + (size_t)lpb * n, *X = sm + (size_t)2 * lpb * n;
     const int tid = threadIdx.x, nthr = blockDim.x;
 
-    for (int idx = tid; idx < nr * n; idx += nthr) {
-        int r = idx / n, k = idx - r * n;
-        int j = j0 + r;
-        double is = isin[j];
-        // X[k] and X[n-k]
-        double2 xk = make_double2(0.0, 0.0), xc = make_double2(0.0, 0.0);
-        int kc = n - k;
+    // X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m], m = 0..T (imag of X_0 dropped)
+    for (int idx = tid; idx < nr * ms; idx += nthr) {
+        const int r = idx / ms, m = idx - r * ms;
+        const int j = j0 + r;
+        const double bs = m * isin[j];
         const double2 *Fr = F + (size_t)j * nrow * ms;
-        if (k <= T) {
-            if (fd.src0 >= 0) {
-                double2 f = Fr[(size_t)fd.src0 * ms + k];
-                double bb = fd.b0 * k * is;
-                xk.x += fd.a0 * f.x - bb * f.y;
-                xk.y += fd.a0 * f.y + bb * f.x;
-            }
-            if (fd.src1 >= 0) {
-                double2 f = Fr[(size_t)fd.src1 * ms + k];
-                double bb = fd.b1 * k * is;
-                xk.x += fd.a1 * f.x - bb * f.y;
-                xk.y += fd.a1 * f.y + bb * f.x;
-            }
-            if (k == 0) xk.y = 0.0;
+        double2 x = make_double2(0.0, 0.0);
+        if (fd.src0 >= 0) {
+            const double2 f = Fr[(size_t)fd.src0 * ms + m];
+            const double bb = fd.b0 * bs;
+            x.x = fd.a0 * f.x - bb * f.y;
+            x.y = fd.a0 * f.y + bb * f.x;
         }
-        if (kc <= T && kc < n) {
-            if (fd.src0 >= 0) {
-                double2 f = Fr[(size_t)fd.src0 * ms + kc];
-                double bb = fd.b0 * kc * is;
-                xc.x += fd.a0 * f.x - bb * f.y;
-                xc.y += fd.a0 * f.y + bb * f.x;
-            }
-            if (fd.src1 >= 0) {
-                double2 f = Fr[(size_t)fd.src1 * ms + kc];
-                double bb = fd.b1 * kc * is;
-                xc.x += fd.a1 * f.x - bb * f.y;
-                xc.y += fd.a1 * f.y + bb * f.x;
-            }
+        if (fd.src1 >= 0) {
+            const double2 f = Fr[(size_t)fd.src1 * ms + m];
+            const double bb = fd.b1 * bs;
+            x.x += fd.a1 * f.x - bb * f.y;
+            x.y += fd.a1 * f.y + bb * f.x;
         }
-        // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O
-        double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
-        double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
-        double2 O = cmulconj(D, twN[k]);
-        A[(size_t)r * n + k] = make_double2((E.x - O.y) * kNrm, (E.y + O.x) * kNrm);
+        if (m == 0) x.y = 0.0;
+        X[(size_t)r * ms + m] = make_double2(x.x * kNrm, x.y * kNrm);
+    }
+    __syncthreads();
+    // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O
+    for (int idx = tid; idx < nr * n; idx += nthr) {
+        const int r = idx / n, k = idx - r * n;
+        const int kc = n - k;
+        const double2 xk = k <= T ? X[(size_t)r * ms + k] : make_double2(0.0, 0.0);
+        const double2 xc = (kc <= T && kc < n) ? X[(size_t)r * ms + kc] : make_double2(0.0, 0.0);
+        const double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
+        const double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
+        const double2 O = cmulconj(D, twN[k]);
+        A[(size_t)r * n + k] = make_double2(E.x - O.y, E.y + O.x);
     }
     __syncthreads();
     double2 *res = fft_rows<true>(A, B, nr, n, plan, tw, tid, nthr);
@@ -128,7 +119,7 @@ static int fourier_lpb(int nlon) {
 int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     int lpb = fourier_lpb(c.nlon);
-    size_t smem = (size_t)2 * lpb * (c.nlon / 2) * sizeof(double2);
+    size_t smem = (size_t)(2 * (c.nlon / 2) + c.ms) * lpb * sizeof(double2);
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
     if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_fourier_synth<<<grid, 256, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
