@@ -1,0 +1,93 @@
+"""Split-precision (Ozaki, tcgen05 bf16 digits, FP64 recombination) path
+against the FP64 CPU oracle.
+
+Bar: 1e-10 relative (max |split - oracle| / max |oracle|) for every transform
+and for the step, the tolerance the split-precision form is specified to.  The
+errors actually reached are printed (pytest -s) and are ~1e-14.
+"""
+import numpy as np
+import pytest
+
+from tests._helpers import red_spectrum, relerr
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", params=[21, 42, 85, 170])
+def pair(request, gpulib):
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import PREC_SPLIT
+    from oracle.pyoracle import OracleSHT
+    T = request.param
+    return AerosSHT(T, batch_max=6, precision=PREC_SPLIT), OracleSHT(T)
+
+
+def test_split_scalar(pair):
+    g, o = pair
+    rng = np.random.default_rng(31)
+    c = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (3,))
+    e1 = relerr(g.synthesis(c), o.synthesis(c))
+    f = o.synthesis(c)
+    e2 = relerr(g.analysis(f), o.analysis(f))
+    print(f"T{o.trunc} split synthesis {e1:.2e} analysis {e2:.2e}")
+    assert e1 < TOL and e2 < TOL
+
+
+def test_split_vector_gradient_winds(pair):
+    g, o = pair
+    rng = np.random.default_rng(32)
+    s = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (2,))
+    t = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (2,))
+    s[:, 0] = 0
+    t[:, 0] = 0
+    errs = []
+    for a, b in zip(g.synthesis_vec(s, t), o.synthesis_vec(s, t)):
+        errs.append(relerr(a, b))
+    vth, vph = o.synthesis_vec(s, t)
+    for a, b in zip(g.analysis_vec(vth, vph), o.analysis_vec(vth, vph)):
+        errs.append(relerr(a, b))
+    for a, b in zip(g.gradient(s), o.gradient(s)):
+        errs.append(relerr(a, b))
+    vor, div = 1e-5 * s, 2e-6 * t
+    u, v = o.uv_from_vordiv(vor, div)
+    for a, b in zip(g.uv_from_vordiv(vor, div), (u, v)):
+        errs.append(relerr(a, b))
+    for a, b in zip(g.vordiv_from_uv(u, v), o.vordiv_from_uv(u, v)):
+        errs.append(relerr(a, b))
+    print(f"T{o.trunc} split vector/gradient/winds max {max(errs):.2e}")
+    assert max(errs) < TOL
+
+
+def test_split_round_trip_T341(gpulib):
+    """Size-independent property at the largest transform size:
+    analysis(synthesis(c)) = c for a band-limited spectrum."""
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import PREC_SPLIT
+    g = AerosSHT(341, batch_max=2, precision=PREC_SPLIT)
+    rng = np.random.default_rng(33)
+    c = red_spectrum(rng, g.l_of_lm, g.m_of_lm, (2,))
+    e = relerr(g.analysis(g.synthesis(c)), c)
+    print(f"T341 split round trip {e:.2e}")
+    assert e < TOL
+
+
+def test_split_dynamics_step(gpulib):
+    from aeros_gb300.params import held_suarez_params, PREC_SPLIT
+    from aeros_gb300.dynamics import AerosDyn
+    from oracle.pyoracle import OracleDyn
+    from tests.test_gpu_dyn import moving_state
+    p = held_suarez_params(trunc=42, nlev=20, precision=PREC_SPLIT)
+    g = AerosDyn(p)
+    o = OracleDyn(held_suarez_params(trunc=42, nlev=20))
+    st = moving_state(o, seed=41)
+    g.set_state(*st)
+    o.set_state(*st)
+    et = [relerr(a, b) for a, b in zip(g.tendency(), o.tendency())]
+    g.step(5)
+    o.step(5)
+    es = [relerr(a, b) for a, b in zip(g.get_state(), o.get_state())]
+    print("split T42L20 tendency errors", ["%.1e" % x for x in et], "state after 5 steps",
+          ["%.1e" % x for x in es])
+    assert max(et) < TOL and max(es) < TOL
