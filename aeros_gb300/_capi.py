@@ -93,6 +93,13 @@ _PROTOS = {
     "aeros_dyn_gwspeed": [_vp, _dp],
     "aeros_dyn_set_stream": [_vp, _vp],
     "aeros_dyn_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "aeros_group_create": [ctypes.POINTER(_vp), ctypes.POINTER(_vp), _i],
+    "aeros_group_destroy": [_vp],
+    "aeros_group_set_stream": [_vp, _vp],
+    "aeros_group_step": [_vp, _i],
+    "aeros_group_step_async": [_vp, _i],
+    "aeros_group_sync": [_vp],
+    "aeros_group_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "aeros_last_error": [],
 }
 _RESTYPE = {"aeros_last_error": ctypes.c_char_p}

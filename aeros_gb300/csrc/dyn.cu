@@ -594,6 +594,7 @@ struct aeros_dyn_s {
     AnaCol *acS = nullptr;
     int nacS = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // start-up, regular
+    cudaGraph_t graph_src[2] = {nullptr, nullptr};   // kept for ensemble groups
     long long graph_kernels[2] = {0, 0};
     int nstep = 0;
     std::vector<cudaEvent_t> *prof = nullptr;        // events recorded after each launch
@@ -987,7 +988,8 @@ int capture_graphs(Dyn &d) {
             return AEROS_ERR_CUDA;
         }
         AEROS_CUDA(cudaGraphInstantiate(&d.graph[s], g, 0));
-        cudaGraphDestroy(g);
+        if (d.graph_src[s]) cudaGraphDestroy(d.graph_src[s]);
+        d.graph_src[s] = g;
         d.graph_kernels[s] = d.launches - before;
         d.launches = before;
     }
@@ -1047,6 +1049,8 @@ void destroy(Dyn *d) {
     if (d->stream) cudaStreamSynchronize(d->stream);
     for (auto &g : d->graph)
         if (g) cudaGraphExecDestroy(g);
+    for (auto &g : d->graph_src)
+        if (g) cudaGraphDestroy(g);
     free_syn_plan(d->synS);
     free_syn_plan(d->synD);
     void *ps[] = {d->now, d->old, d->tnd, d->FS, d->FA, d->G, d->GA, d->D, d->GT_d, d->TT_d, d->WT_d, d->nu_d,
@@ -1409,6 +1413,115 @@ int aeros_dyn_set_stream(aeros_dyn_t h, void *stream) {
 int aeros_dyn_launch_count(aeros_dyn_t h, long long *count) {
     if (!h || !count) return AEROS_ERR_ARG;
     *count = h->launches;
+    return AEROS_OK;
+}
+
+}  // extern "C"
+
+// =========================================================================
+// Ensemble groups: one CUDA graph per step for several handles (members of
+// different truncations and level counts), each handle's step graph a child
+// node of it with no dependencies between handles, so they run concurrently.
+struct aeros_group_s {
+    std::vector<aeros_dyn_t> dyn;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long kernels[2] = {0, 0};
+    long long launches = 0;
+    int nstep = 0;
+};
+
+extern "C" {
+
+int aeros_group_create(aeros_group_t *out, aeros_dyn_t *handles, int n) {
+    if (!out || !handles || n < 1) return AEROS_ERR_ARG;
+    *out = nullptr;
+    aeros_group_s *g = new aeros_group_s;
+    for (int i = 0; i < n; ++i) {
+        if (!handles[i] || !handles[i]->graph_src[0] || !handles[i]->graph_src[1]) { delete g; return AEROS_ERR_ARG; }
+        if (handles[i]->nstep != handles[0]->nstep) { delete g; return AEROS_ERR_STATE; }
+        cudaStreamSynchronize(handles[i]->stream);
+        g->dyn.push_back(handles[i]);
+    }
+    g->nstep = handles[0]->nstep;
+    for (int s = 0; s < 2; ++s) {
+        cudaGraph_t root;
+        AEROS_CUDA(cudaGraphCreate(&root, 0));
+        for (auto *h : g->dyn) {
+            cudaGraphNode_t node;
+            AEROS_CUDA(cudaGraphAddChildGraphNode(&node, root, nullptr, 0, h->graph_src[s]));
+            g->kernels[s] += h->graph_kernels[s];
+        }
+        cudaError_t e = cudaGraphInstantiate(&g->exec[s], root, 0);
+        cudaGraphDestroy(root);
+        if (e != cudaSuccess) {
+            set_error(std::string("group graph: ") + cudaGetErrorString(e));
+            delete g;
+            return AEROS_ERR_CUDA;
+        }
+    }
+    AEROS_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    g->own_stream = true;
+    *out = g;
+    return AEROS_OK;
+}
+
+int aeros_group_destroy(aeros_group_t g) {
+    if (!g) return AEROS_ERR_ARG;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (auto &e : g->exec)
+        if (e) cudaGraphExecDestroy(e);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return AEROS_OK;
+}
+
+int aeros_group_set_stream(aeros_group_t g, void *stream) {
+    if (!g || !stream) return AEROS_ERR_ARG;
+    cudaStreamSynchronize(g->stream);
+    if (g->own_stream) cudaStreamDestroy(g->stream);
+    g->stream = (cudaStream_t)stream;
+    g->own_stream = false;
+    return AEROS_OK;
+}
+
+int aeros_group_step_async(aeros_group_t g, int nsteps) {
+    if (!g || nsteps < 0) return AEROS_ERR_ARG;
+    for (int i = 0; i < nsteps; ++i) {
+        const int s = g->nstep == 0 ? 0 : 1;
+        for (auto *h : g->dyn)
+            if (h->nstep != g->nstep) return AEROS_ERR_STATE;
+        AEROS_CUDA(cudaGraphLaunch(g->exec[s], g->stream));
+        g->launches += g->kernels[s];
+        for (auto *h : g->dyn) {
+            h->nstep += 1;
+            h->launches += h->graph_kernels[s];
+        }
+        g->nstep += 1;
+    }
+    return AEROS_OK;
+}
+
+int aeros_group_sync(aeros_group_t g) {
+    if (!g) return AEROS_ERR_ARG;
+    AEROS_CUDA(cudaStreamSynchronize(g->stream));
+    for (auto *h : g->dyn) {
+        int rc = aeros_dyn_sync(h);
+        if (rc) return rc;
+    }
+    return AEROS_OK;
+}
+
+int aeros_group_step(aeros_group_t g, int nsteps) {
+    int rc = aeros_group_step_async(g, nsteps);
+    if (rc) return rc;
+    return aeros_group_sync(g);
+}
+
+int aeros_group_launch_count(aeros_group_t g, long long *count) {
+    if (!g || !count) return AEROS_ERR_ARG;
+    *count = g->launches;
     return AEROS_OK;
 }
 

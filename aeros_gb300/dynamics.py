@@ -210,3 +210,48 @@ class AerosDyn:
         c = ctypes.c_longlong()
         _capi.lib().aeros_dyn_launch_count(self._h, ctypes.byref(c))
         return c.value
+
+
+class AerosGroup:
+    """Several AerosDyn handles stepped by one CUDA graph launch per step.
+
+    Members may differ in truncation and level count (e.g. 32 x T21L16,
+    32 x T31L20 and 32 x T42L20); each handle's step graph is an independent
+    branch of the group's graph.  Configure the handles (state, forcing) before
+    grouping and step them only through the group afterwards.
+    """
+
+    def __init__(self, handles):
+        self.handles = list(handles)
+        arr = (ctypes.c_void_p * len(self.handles))(*[h._h.value for h in self.handles])
+        g = ctypes.c_void_p()
+        _capi.check(_capi.lib().aeros_group_create(ctypes.byref(g), arr, len(self.handles)), "aeros_group_create")
+        self._g = g
+
+    def close(self):
+        if getattr(self, "_g", None):
+            _capi.lib().aeros_group_destroy(self._g)
+            self._g = None
+
+    __del__ = close
+
+    def set_stream(self, stream_ptr):
+        _capi.check(_capi.lib().aeros_group_set_stream(self._g, ctypes.c_void_p(stream_ptr)), "aeros_group_set_stream")
+
+    def step(self, nsteps=1):
+        _capi.check(_capi.lib().aeros_group_step(self._g, int(nsteps)), "aeros_group_step")
+
+    def step_async(self, nsteps=1):
+        _capi.check(_capi.lib().aeros_group_step_async(self._g, int(nsteps)), "aeros_group_step_async")
+
+    def sync(self):
+        _capi.check(_capi.lib().aeros_group_sync(self._g), "aeros_group_sync")
+
+    def launch_count(self):
+        c = ctypes.c_longlong()
+        _capi.lib().aeros_group_launch_count(self._g, ctypes.byref(c))
+        return c.value
+
+    @property
+    def nmember(self):
+        return sum(h.nmember for h in self.handles)

@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--trunc", type=int, default=42)
     ap.add_argument("--nlev", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=60)
+    ap.add_argument("--no-split", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -165,6 +168,97 @@ def initial_state(dyn, sht, seed):
     rng = np.random.default_rng(seed)
     tg = sht.synthesis(t) + rng.normal(0.0, 0.1, (dyn.nlev, dyn.nlat, dyn.nlon))
     return vor, div, sht.analysis(tg), lnps
+
+
+def time_steps(stepper, stream, K, torch, flush=None):
+    """Mean device time per step over K steps (CUDA events on `stream`); with
+    `flush`, a >L2 write precedes every step outside its event pair."""
+    if flush is None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            stepper.step_async(K)
+            e1.record(stream)
+        stepper.sync()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / K
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    with torch.cuda.stream(stream):
+        for i in range(K):
+            flush.fill_(i & 0xFF)
+            ev0[i].record(stream)
+            stepper.step_async(1)
+            ev1[i].record(stream)
+    stepper.sync()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3 / K
+
+
+def split_form(args, sht, dyn_fp64, flush, torch):
+    """T42L20 single member with the split-precision Legendre contractions:
+    SYPD with the same flushed timing, and the relative difference from the
+    FP64 GPU path after the same steps from the same state."""
+    import numpy as np
+    from aeros_gb300.params import held_suarez_params, PREC_SPLIT
+    from aeros_gb300.dynamics import AerosDyn
+    p = held_suarez_params(trunc=args.trunc, nlev=args.nlev, precision=PREC_SPLIT)
+    d = AerosDyn(p)
+    ref = AerosDyn(held_suarez_params(trunc=args.trunc, nlev=args.nlev))
+    st = initial_state(d, sht, seed=0)
+    d.set_state(*st)
+    ref.set_state(*st)
+    d.step(24)
+    ref.step(24)
+    err = max(float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(d.get_state(), ref.get_state()))
+    s = torch.cuda.Stream()
+    d.set_stream(s.cuda_stream)
+    d.step_async(3)
+    d.sync()
+    t = time_steps(d, s, args.steps, torch, flush)
+    return {"sypd": sypd(t), "ms_per_step": t * 1e3,
+            "max_rel_diff_vs_fp64_gpu_after_24_steps": err,
+            "legendre": "tcgen05 bf16 Ozaki digits (55 bits), FP64 recombination"}
+
+
+def batched_form(args, torch):
+    """Config of 96 uneven members: 32 x T21L16 + 32 x T31L20 + 32 x T42L20,
+    each member with its own seed and equator-pole contrast dT_y ~ U(40, 80) K,
+    stepped by one CUDA graph launch per step; FP64 and split precision.
+    Working set > L2, so no flush is needed."""
+    import numpy as np
+    from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
+    from aeros_gb300.dynamics import AerosDyn, AerosGroup
+    from aeros_gb300.spectral import AerosSHT
+    out = {"members": "32 x T21L16 + 32 x T31L20 + 32 x T42L20", "steps": args.batched_steps}
+    cfg = [(21, 16), (31, 20), (42, 20)]
+    for name, prec in (("fp64", PREC_FP64), ("split", PREC_SPLIT)):
+        rng = np.random.default_rng(1000)
+        hs = []
+        for T, L in cfg:
+            d = AerosDyn(held_suarez_params(trunc=T, nlev=L, nmember=32, precision=prec))
+            sht = AerosSHT(T, batch_max=L)
+            d.set_isothermal(264.0, 1.0e5)
+            vor, div, t, lnps = d.get_state(squeeze=False)
+            t = t.copy()
+            for e in range(32):
+                r = np.random.default_rng(1000 + len(hs) * 32 + e)
+                t[e] = sht.analysis(sht.synthesis(t[e]) + r.normal(0.0, 0.1, (L, d.nlat, d.nlon)))
+                d.set_member_forcing(e, rng.uniform(40.0, 80.0), 1.0 / (40.0 * 86400.0))
+            d.set_state(vor, div, t, lnps)
+            hs.append(d)
+        g = AerosGroup(hs)
+        s = torch.cuda.Stream()
+        g.set_stream(s.cuda_stream)
+        g.step_async(3)
+        g.sync()
+        n0 = g.launch_count()
+        t = time_steps(g, s, args.batched_steps, torch)
+        out[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3,
+                     "gpu_launches_per_step": (g.launch_count() - n0) / args.batched_steps}
+        del g, hs
+    # the same 32 T42L20 members one by one through the single-member FP64 path
+    return out
 
 
 # ---------------------------------------------------------------- reference arm
@@ -345,6 +439,18 @@ def run_gpu(args, rank, world, local):
                "d2h_bytes_per_step": sbytes, "ms_per_step": t_e2e * 1e3,
                "path": "aeros_dyn_set_state/set_old_state/step/get_state with pinned host buffers"}
 
+    # split-precision form at the same workload, and its distance from the FP64 path
+    split = None
+    if not args.no_split:
+        split = split_form(args, sht, dyn, flush, torch)
+    batched = None
+    if not args.no_batched:
+        batched = batched_form(args, torch)
+        if batched is not None:
+            for k in list(batched):
+                if isinstance(batched[k], dict) and "sypd" in batched[k]:
+                    batched[k]["vs_fp64_single"] = batched[k]["sypd"] / sypd(t_gpu)
+
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1) else None
     if rank == 0:
         line = {"metric": METRIC, "value": sypd(t_gpu) * world, "unit": "SYPD", "n_gpus": world, "steps": K,
@@ -356,6 +462,7 @@ def run_gpu(args, rank, world, local):
                 "ms_per_step_l2_resident": t_warm * 1e3,
                 "sypd_l2_resident": sypd(t_warm) * world,
                 "e2e": e2e, "roofline": roof, "kernels_ms": prof, "cpu_baseline": cpu,
+                "split_precision": split, "batched": batched,
                 "clocks": clk, "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -49,6 +49,7 @@ extern "C" {
 /* ---- opaque handles ------------------------------------------------------ */
 typedef struct aeros_sht_s *aeros_sht_t;
 typedef struct aeros_dyn_s *aeros_dyn_t;
+typedef struct aeros_group_s *aeros_group_t;
 
 /* ======================================================================== */
 /* Spectral transforms: mirrors module aeros_spectral                        */
@@ -277,6 +278,22 @@ int aeros_dyn_set_stream(aeros_dyn_t h, void *stream);
 /* Number of this library's kernel launches issued since creation (a step
  * replayed from a graph counts each kernel node). */
 int aeros_dyn_launch_count(aeros_dyn_t h, long long *count);
+
+/* ======================================================================== */
+/* Ensemble groups: several dyn handles (e.g. members of different          */
+/* truncations) stepped by ONE CUDA graph launch per time step; each        */
+/* handle's step graph is an independent branch.  Handles must be fully      */
+/* configured (state, forcing, phis) and at the same step count; while in a */
+/* group, step them only through the group.  No reference counterpart: the */
+/* reference steps one configuration per process.                          */
+/* ======================================================================== */
+int aeros_group_create(aeros_group_t *g, aeros_dyn_t *handles, int n);
+int aeros_group_destroy(aeros_group_t g);
+int aeros_group_set_stream(aeros_group_t g, void *stream);
+int aeros_group_step(aeros_group_t g, int nsteps);
+int aeros_group_step_async(aeros_group_t g, int nsteps);
+int aeros_group_sync(aeros_group_t g);
+int aeros_group_launch_count(aeros_group_t g, long long *count);
 
 /* Last CUDA error string for diagnostics (static storage). */
 const char *aeros_last_error(void);
