@@ -1257,7 +1257,7 @@ int aeros_dyn_sync(aeros_dyn_t h) {
         set_error("non-finite value in the spectral state");
         return AEROS_ERR_NONFINITE;
     }
-    return AEROS_OK;
+    return split_check(h->split);
 }
 
 int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int name_len, int *nk) {

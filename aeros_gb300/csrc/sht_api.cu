@@ -241,6 +241,7 @@ int dispatch(aeros_sht_t h, int op, bool in_spec, int nin, int nout, const doubl
         AEROS_CUDA(cudaMemcpyAsync(out0, do0, nO * 8, cudaMemcpyDefault, h->stream));
         if (nout > 1) AEROS_CUDA(cudaMemcpyAsync(out1, do1, nO * 8, cudaMemcpyDefault, h->stream));
         AEROS_CUDA(cudaStreamSynchronize(h->stream));
+        return split_check(h->split);
     }
     return AEROS_OK;
 }

@@ -1,21 +1,26 @@
 // split.cu -- split-precision (Ozaki) Legendre contractions on the tcgen05
 // tensor cores, FP64 in and out.
 //
-// Every FP64 operand is cut into S balanced base-2^b integer digits with one
+// Every FP64 operand is cut into S balanced base-2^B integer digits with one
 // power-of-two scale per row (tables) or per column (data):
-//     x = 2^(e - (S b - 1)) sum_s d_s 2^((S-1-s) b),   |d_s| <= 2^(b-1) (+1 top)
-// The digits are exact in bf16.  For every shift q = s + t <= S the digit
-// products d^A_s d^X_t are summed by tcgen05.mma (kind::f16, bf16 x bf16 ->
-// fp32) into one TMEM accumulator Y_q; all partial sums are integers below
-// 2^24, so the fp32 accumulation is exact.  The epilogue recombines
-//     result = 2^(e_r + e_c - 2(S b - 1)) sum_q Y_q 2^((2S-2-q) b)
-// in FP64.  (S, b) = (7, 8) for contraction lengths <= 126 and (8, 7) up to 441
-// (55 bits per operand; the bound (S+1) K (2^(b-1)+1)^2 < 2^24 keeps every
-// accumulator exact), so the result carries ~1e-16 of the row/column scale.
+//     x = 2^(e - 55) sum_s d_s 2^((S-1-s) B),   |d_s| <= 2^(B-1) (+1 top),
+// S B - 1 = 55 bits, (S, B) = (7, 8) for contraction lengths <= 126 and (8, 7)
+// up to 441.  The digits are exact in bf16.  For every shift q = s + t <= S-1
+// the digit products d^A_s d^X_t are summed by tcgen05.mma (kind::f16,
+// bf16 x bf16 -> fp32) into one TMEM accumulator Y_q; every partial sum is an
+// integer below S K (2^(B-1)+1)^2 < 2^24, so the fp32 accumulation is exact.
+// Shifts q >= S are dropped: they lie below 2^-53 of the row x column scale.
 //
-// Tables (Pbar, dPbar/dtheta, and their Gauss-weighted forms) are digitised
-// once per handle on the device.  Operands sit in shared memory in the
-// canonical K-major, no-swizzle layout (8-row x 16-byte core matrices).
+// No FP64 arithmetic touches the digits or the accumulators (GB300 runs FP64
+// ~60x slower than FP32/INT32): digits are cut from the IEEE bit pattern with
+// integer shifts, and the epilogue forms Z = sum_q Y_q 2^(40 - q B) exactly in
+// int64, adds the even and odd hemisphere parts as integers (their rows share
+// one exponent), and assembles the FP64 result from Z's bits.
+//
+// Tables (Pbar, dPbar/dtheta and their Gauss-weighted forms) are digitised once
+// per handle on the device into tile images in the canonical K-major,
+// no-swizzle layout (8-row x 16-byte core matrices), one image per (m, tile,
+// 64-wide chunk), which a CTA fetches with one cp.async.bulk.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -24,7 +29,6 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include "split.h"
-#include "fft.cuh"
 
 namespace aeros {
 
@@ -32,24 +36,34 @@ namespace {
 
 constexpr int kTM = 128;     // tile rows (M of one MMA)
 constexpr int kKC = 64;      // contraction chunk
-constexpr int kNTs = 64;     // synthesis tile columns (at most; 48 when S = 8)
-constexpr int kNTa = 48;     // analysis tile columns (4 outputs x 12)
+constexpr int kNTs = 64;     // synthesis tile columns: 32 complex fields x (re, im)
+constexpr int kNTa = 48;     // analysis tile columns: 2 folds x 3 slots x 4 fields x (re, im)
 constexpr int kTmemCols = 512;
 constexpr long long kWaitLimit = 1ll << 26;   // bounded mbarrier polls
+constexpr int kZShift = 40;  // Z = sum_q Y_q 2^(40 - q B)
+constexpr int kThreads = 512;  // 16 warps: 4 per SM sub-partition to hide latency
+constexpr int kSt = kKC + 1;   // staged-value row stride (doubles): conflict-free 8-byte reads
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// element (r, k) of a rows x kKC K-major tile, canonical no-swizzle layout
-__host__ __device__ __forceinline__ int cidx(int r, int k) {
-    return ((r >> 3) * (kKC / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+// Operand tiles are K-major with 128-byte rows (64 bf16 of the contraction,
+// zero past the chunk's length) in the 128-byte swizzle: the 16-byte chunk c of
+// row r sits at chunk c ^ (r & 7) of the row, 8-row groups are 1024 bytes apart,
+// and every tile starts on a 1024-byte boundary.  Element index of (r, k):
+__host__ __device__ __forceinline__ int swz(int r, int k) {
+    return r * 64 + ((((k >> 3) ^ r) & 7) << 3) + (k & 7);
 }
+constexpr int kSlice = 64;   // elements per tile row
 
+// smem descriptor of a swizzled K-major tile whose row 0 starts at saddr (plus
+// the byte offset of the K step inside the 128-byte row)
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)(128 >> 4) << 16;                    // LBO: next core matrix along K
-    d |= (uint64_t)(((kKC / 8) * 128) >> 4) << 32;      // SBO: next 8-row group
-    d |= (uint64_t)1 << 46;                             // tcgen05 descriptor version
+    d |= (uint64_t)1 << 16;                  // LBO (unused by swizzled K-major layouts)
+    d |= (uint64_t)(1024 >> 4) << 32;        // SBO: next 8-row group
+    d |= (uint64_t)1 << 46;                  // tcgen05 descriptor version
+    d |= (uint64_t)2 << 61;                  // 128-byte swizzle
     return d;
 }
 
@@ -68,6 +82,24 @@ __device__ __forceinline__ void mma_commit(uint64_t *mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)));
 }
 
+__device__ __forceinline__ void mbar_init(uint64_t *mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)));
+}
+
+// Bulk copy global -> shared of `bytes` (multiple of 16, both ends 16-byte
+// aligned), completing on `mbar` (which this call also arms).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
 // Bounded wait on an mbarrier phase; returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
     uint32_t done = 0;
@@ -82,265 +114,448 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
     return false;
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;");
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t *r);
+template <>
+__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+template <>
+__device__ __forceinline__ void tmem_ld<4>(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+template <>
+__device__ __forceinline__ void tmem_ld<2>(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;"); }
+
+// ------------------------------------------------------------------ integer digit arithmetic
+// Biased exponent field of x (0 for zero and subnormals).
+__device__ __forceinline__ int bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
+// Scale exponent e with |x| < 2^e for every x of a row/column whose largest
+// biased exponent is be (0 -> all zero, any e works).
+__device__ __forceinline__ int scale_exp(int be) { return be ? be - 1022 : 0; }
+
+// round(x 2^(55 - e)) as an integer, for |x| < 2^e; subnormals count as 0.
+__device__ __forceinline__ long long fixed55(double x, int e) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int be = (int)((bits >> 52) & 0x7FF);
+    if (be == 0) return 0;
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1020 - be + e;   // right shift; >= -2 because |x| < 2^e
+    long long v;
+    if (sh <= 0) v = (long long)(mant << (-sh));
+    else if (sh >= 54) v = 0;
+    else v = (long long)((mant + (1ull << (sh - 1))) >> sh);
+    return (bits >> 63) ? -v : v;
 }
 
-// 2^e as a double; 0 below the normal range (such products are below 1e-300)
-__device__ __forceinline__ double pow2(int e) {
-    if (e < -1022) return 0.0;
-    if (e > 1023) e = 1023;
-    return __longlong_as_double((long long)(e + 1023) << 52);
+// fp32 bit pattern of a small integer d (|d| < 2^22); its upper half is the
+// bf16 pattern, exact when |d| <= 256
+__device__ __forceinline__ uint32_t f32_bits(int d) {
+    return __float_as_uint(__int_as_float(0x4B400000 + d) - 12582912.0f);
+}
+// fp32 bit pattern of (byte k of x) - 128
+template <int k>
+__device__ __forceinline__ uint32_t f32_byte(uint32_t x) {
+    return __float_as_uint(__uint_as_float(__byte_perm(x, 0x4B000000u, 0x7650 + k)) - 8388736.0f);
 }
 
-// exponent e with |x| < 2^e (x != 0), via the bit pattern; clamped at -960 so
-// that the digit scaling 2^(S b - 1 - e) stays finite (smaller values round to 0)
-__device__ __forceinline__ int exp_above(double x) {
-    long long b = __double_as_longlong(x);
-    int be = (int)((b >> 52) & 0x7FF);
-    return max(be - 1022, -960);
-}
-
-// Balanced base-2^b digits of round(x 2^(Sb-1-e)), most significant first.
-__device__ __forceinline__ void digits(double x, int e, int S, int b, float *d) {
-    long long v = __double2ll_rn(x * pow2(S * b - 1 - e));
-    const long long half = 1ll << (b - 1), mask = (1ll << b) - 1;
-    for (int s = S - 1; s > 0; --s) {
-        long long r = ((v + half) & mask) - half;
-        d[s] = (float)r;
-        v = (v - r) >> b;
+// Balanced base-2^B digits of v (most significant first) as fp32 bit patterns.
+template <int S, int B>
+struct Digits {
+    static __device__ __forceinline__ void cut(long long v, uint32_t *h) {
+        constexpr unsigned long long half = 1ull << (B - 1);
+        unsigned long long C = 0;
+#pragma unroll
+        for (int i = 0; i < S - 1; ++i) C |= half << (i * B);
+        const unsigned long long u = (unsigned long long)v + C;
+#pragma unroll
+        for (int s = 1; s < S; ++s) h[s] = f32_bits((int)((u >> ((S - 1 - s) * B)) & ((1ull << B) - 1)) - (int)half);
+        h[0] = f32_bits((int)((long long)u >> ((S - 1) * B)));
     }
-    d[0] = (float)v;
+};
+// B = 8: the lower digits are the bytes of v + 0x808080808080, less 128.
+template <>
+struct Digits<7, 8> {
+    static __device__ __forceinline__ void cut(long long v, uint32_t *h) {
+        const unsigned long long u = (unsigned long long)v + 0x0000808080808080ull;
+        const uint32_t lo = (uint32_t)u, hi = (uint32_t)(u >> 32);
+        h[6] = f32_byte<0>(lo);
+        h[5] = f32_byte<1>(lo);
+        h[4] = f32_byte<2>(lo);
+        h[3] = f32_byte<3>(lo);
+        h[2] = f32_byte<0>(hi);
+        h[1] = f32_byte<1>(hi);
+        h[0] = f32_bits((int)hi >> 16);
+    }
+};
+
+// bf16 pair (lo, hi) from two fp32 patterns holding exact bf16 values
+__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) { return __byte_perm(lo, hi, 0x7632); }
+
+// Write the S digit slices of 8 consecutive contraction entries x[0..7] of tile
+// row n (16 bytes per slice) into the K-major tile images at `tile`
+// (slice stride `slice_elems`), scale exponent e.
+template <int S, int B>
+__device__ __forceinline__ void put8(const double *x, int e, __nv_bfloat16 *tile, size_t slice_elems, int n, int k0) {
+    uint32_t h[8][S];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) Digits<S, B>::cut(fixed55(x[i], e), h[i]);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        uint4 w;
+        w.x = pack_bf16(h[0][s], h[1][s]);
+        w.y = pack_bf16(h[2][s], h[3][s]);
+        w.z = pack_bf16(h[4][s], h[5][s]);
+        w.w = pack_bf16(h[6][s], h[7][s]);
+        *reinterpret_cast<uint4 *>(tile + (size_t)s * slice_elems + swz(n, k0)) = w;
+    }
 }
+
+// Accumulator Y (fp32 holding an exact integer) shifted into the Z window.
+template <int B>
+__device__ __forceinline__ long long zterm(uint32_t y, int q) {
+    const int v = __float2int_rn(__uint_as_float(y));
+    const int sh = kZShift - q * B;
+    return sh >= 0 ? ((long long)v << sh) : (long long)(v >> (-sh));
+}
+
+// z 2^E as a double (round to nearest, ties away); 0 below the normal range
+// (|z| < 2^63, so no overflow is possible for the exponents used here).
+__device__ __forceinline__ double z_to_f64(long long z, int E) {
+    const unsigned long long sgn = (unsigned long long)z & 0x8000000000000000ull;
+    const unsigned long long m = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
+    const int lz = __clzll((long long)m);
+    const unsigned long long n = m << (lz & 63);               // leading one at bit 63
+    const unsigned long long r = (n >> 11) + ((n >> 10) & 1);  // 53-bit mantissa, 2^53 on carry
+    const int be = 63 - lz + E + 1023;
+    // (be - 1) 2^52 + r carries a rounded-up mantissa into the exponent
+    const unsigned long long bits = sgn | (((unsigned long long)(be - 1) << 52) + r);
+    return (m == 0 || be <= 0) ? 0.0 : __longlong_as_double((long long)bits);
+}
+
+// Result exponent: sum_k A B = Z 2^(e_row + e_col - 2B - 38).
+template <int B>
+__device__ __forceinline__ int zexp(int er, int ec) { return er + ec - 2 * B - 38; }
 
 // ------------------------------------------------------------------ table prep
-// Synthesis table digits: block (m, lat tile t, chunk ch, slice s) = 128 x 64 bf16
-// tile image; row r = blk*32 + jj (blk: Pbar even, Pbar odd, dPbar even, dPbar odd
-// in l - m), column k = l - m within the chunk.
+// Synthesis tables: tile image (m, lat tile t, chunk ch): rows r = blk*32 + jj
+// (blk: Pbar even, Pbar odd, dPbar even, dPbar odd in l - m; latitude t*32+jj),
+// columns = l - m within the chunk.  Even and odd rows of one latitude share
+// their scale so the epilogue can add them as integers.
 __global__ void k_prep_synth_exp(const double *__restrict__ Ps, const double *__restrict__ dPs,
                                  const int *__restrict__ moff, int T, int nh, int ntl, int *__restrict__ rexp) {
-    const int m = blockIdx.x, t = blockIdx.y, r = threadIdx.x;   // 128 threads
-    const int blk = r >> 5, jj = r & 31, j = t * 32 + jj;
-    const int K = T - m + 1;
-    double amax = 0.0;
+    const int m = blockIdx.x, t = blockIdx.y, p = threadIdx.x >> 5, jj = threadIdx.x & 31;   // 64 threads
+    const int j = t * 32 + jj, K = T - m + 1;
+    int be = 0;
     if (j < nh)
-        for (int k = (blk & 1); k < K; k += 2) {
-            double v = (blk < 2 ? Ps : dPs)[(size_t)(moff[m] + k) * nh + j];
-            amax = fmax(amax, fabs(v));
-        }
-    rexp[((size_t)m * ntl + t) * kTM + r] = amax > 0.0 ? exp_above(amax) : 0;
+        for (int k = 0; k < K; ++k) be = max(be, bexp((p ? dPs : Ps)[(size_t)(moff[m] + k) * nh + j]));
+    const int e = scale_exp(be);
+    int *re = rexp + ((size_t)m * ntl + t) * kTM;
+    re[(2 * p) * 32 + jj] = e;
+    re[(2 * p + 1) * 32 + jj] = e;
 }
 
+template <int S, int B>
 __global__ void k_prep_synth_dig(const double *__restrict__ Ps, const double *__restrict__ dPs,
-                                 const int *__restrict__ moff, const int *__restrict__ cbase, int T, int nh, int ntl,
-                                 int S, int b, const int *__restrict__ rexp, __nv_bfloat16 *__restrict__ dig) {
+                                 const int *__restrict__ moff, const long long *__restrict__ sbase, int T, int nh,
+                                 int ntl, const int *__restrict__ rexp, __nv_bfloat16 *__restrict__ dig) {
     const int m = blockIdx.x, t = blockIdx.y, ch = blockIdx.z;
-    const int K = T - m + 1;
-    if (ch * kKC >= ((K + 15) & ~15)) return;
-    for (int idx = threadIdx.x; idx < kTM * kKC; idx += blockDim.x) {
-        const int r = idx / kKC, kk = idx - r * kKC;
-        const int blk = r >> 5, jj = r & 31, j = t * 32 + jj, k = ch * kKC + kk;
-        double v = 0.0;
-        if (j < nh && k < K && ((k & 1) == (blk & 1))) v = (blk < 2 ? Ps : dPs)[(size_t)(moff[m] + k) * nh + j];
-        float d[8];
-        const int e = rexp[((size_t)m * ntl + t) * kTM + r];
-        digits(v, e, S, b, d);
-        const size_t base = (((size_t)(cbase[m] + ch) * ntl + t) * S) * (kTM * kKC);
-        for (int s = 0; s < S; ++s) dig[base + (size_t)s * kTM * kKC + cidx(r, kk)] = __float2bfloat16(d[s]);
+    const int K = T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
+    if (ch >= nch) return;
+    __nv_bfloat16 *tile = dig + sbase[m] + ((size_t)t * nch + ch) * S * kTM * kSlice;
+    for (int idx = threadIdx.x; idx < kTM * 8; idx += blockDim.x) {
+        const int r = idx >> 3, k0 = (idx & 7) * 8;
+        const int blk = r >> 5, j = t * 32 + (r & 31);
+        double x[8];
+        for (int i = 0; i < 8; ++i) {
+            const int k = ch * kKC + k0 + i;
+            x[i] = (j < nh && k < K && ((k & 1) == (blk & 1))) ? (blk < 2 ? Ps : dPs)[(size_t)(moff[m] + k) * nh + j]
+                                                                : 0.0;
+        }
+        put8<S, B>(x, rexp[((size_t)m * ntl + t) * kTM + r], tile, (size_t)kTM * kSlice, r, k0);
     }
 }
 
-// Analysis table digits: block (m, l tile t, chunk ch over latitudes, slice s);
-// row r = blk*32 + pos with l = m + 64 t + 2 pos + (blk & 1); blk < 2: w Pbar,
-// else w dPbar; column = latitude within the chunk.
+// Analysis tables: tile image (m, l tile t, chunk ch over latitudes): row
+// r = blk*32 + pos with l = m + 64 t + 2 pos + (blk & 1); blk < 2: w Pbar,
+// else w dPbar; columns = latitude within the chunk.
 __global__ void k_prep_anal_exp(const double *__restrict__ PaT, const double *__restrict__ dPaT,
                                 const int *__restrict__ moff, int T, int nh, int ntlA, int *__restrict__ rexp) {
     const int m = blockIdx.x, t = blockIdx.y, r = threadIdx.x;
-    const int blk = r >> 5, pos = r & 31;
-    const int K = T - m + 1;
+    const int blk = r >> 5, pos = r & 31, K = T - m + 1;
     const int k = 64 * t + 2 * pos + (blk & 1);
-    double amax = 0.0;
+    int be = 0;
     if (k < K)
-        for (int j = 0; j < nh; ++j) {
-            double v = (blk < 2 ? PaT : dPaT)[(size_t)moff[m] * nh + (size_t)j * K + k];
-            amax = fmax(amax, fabs(v));
-        }
-    rexp[((size_t)m * ntlA + t) * kTM + r] = amax > 0.0 ? exp_above(amax) : 0;
+        for (int j = 0; j < nh; ++j) be = max(be, bexp((blk < 2 ? PaT : dPaT)[(size_t)moff[m] * nh + (size_t)j * K + k]));
+    rexp[((size_t)m * ntlA + t) * kTM + r] = scale_exp(be);
 }
 
+template <int S, int B>
 __global__ void k_prep_anal_dig(const double *__restrict__ PaT, const double *__restrict__ dPaT,
-                                const int *__restrict__ moff, int T, int nh, int ntlA, int nchA, int S, int b,
-                                const int *__restrict__ rexp, __nv_bfloat16 *__restrict__ dig) {
+                                const int *__restrict__ moff, const long long *__restrict__ abase, int T, int nh,
+                                int ntlA, int KpA, const int *__restrict__ rexp, __nv_bfloat16 *__restrict__ dig) {
     const int m = blockIdx.x, t = blockIdx.y, ch = blockIdx.z;
     const int K = T - m + 1;
-    if (64 * t >= K) return;
-    for (int idx = threadIdx.x; idx < kTM * kKC; idx += blockDim.x) {
-        const int r = idx / kKC, jj = idx - r * kKC;
+    const int nch = (KpA + kKC - 1) / kKC;
+    if (64 * t >= K || ch >= nch) return;
+    __nv_bfloat16 *tile = dig + abase[m] + ((size_t)t * nch + ch) * S * kTM * kSlice;
+    for (int idx = threadIdx.x; idx < kTM * 8; idx += blockDim.x) {
+        const int r = idx >> 3, j0 = (idx & 7) * 8;
         const int blk = r >> 5, pos = r & 31;
-        const int k = 64 * t + 2 * pos + (blk & 1), j = ch * kKC + jj;
-        double v = 0.0;
-        if (k < K && j < nh) v = (blk < 2 ? PaT : dPaT)[(size_t)moff[m] * nh + (size_t)j * K + k];
-        float d[8];
-        digits(v, rexp[((size_t)m * ntlA + t) * kTM + r], S, b, d);
-        const size_t base = ((((size_t)m * ntlA + t) * nchA + ch) * S) * (kTM * kKC);
-        for (int s = 0; s < S; ++s) dig[base + (size_t)s * kTM * kKC + cidx(r, jj)] = __float2bfloat16(d[s]);
+        const int k = 64 * t + 2 * pos + (blk & 1);
+        double x[8];
+        for (int i = 0; i < 8; ++i) {
+            const int j = ch * kKC + j0 + i;
+            x[i] = (k < K && j < nh) ? (blk < 2 ? PaT : dPaT)[(size_t)moff[m] * nh + (size_t)j * K + k] : 0.0;
+        }
+        put8<S, B>(x, rexp[((size_t)m * ntlA + t) * kTM + r], tile, (size_t)kTM * kSlice, r, j0);
     }
 }
 
-// ------------------------------------------------------------------ common MMA loop
-// Issue the digit-pair products of one chunk: D_q += A_s B_t^T for s + t = q <= S.
-__device__ __forceinline__ void issue_chunk(uint32_t tmem, const __nv_bfloat16 *sA, const __nv_bfloat16 *sB, int S,
-                                            int NT, int tile_b_elems, uint32_t *inited) {
+// ------------------------------------------------------------------ common MMA issue
+// D_q += A_s B_t^T over one chunk for every s + t = q <= S - 1.  Consecutive
+// MMAs go to different accumulators (t runs fastest), so no MMA waits on the
+// accumulation of the one before it.
+template <int S>
+__device__ __forceinline__ void issue_chunk(uint32_t tmem, const __nv_bfloat16 *sA, const __nv_bfloat16 *sB, int NT,
+                                            int kc, bool first) {
     const uint32_t id = idesc_bf16(kTM, NT);
-    for (int q = 0; q <= S; ++q)
-        for (int s = 0; s < S; ++s) {
-            const int t = q - s;
-            if (t < 0 || t >= S) continue;
-            const uint32_t aA = smem_u32(sA + (size_t)s * kTM * kKC);
-            const uint32_t aB = smem_u32(sB + (size_t)t * tile_b_elems);
-            for (int k0 = 0; k0 < kKC; k0 += 16) {
-                uint32_t acc = (*inited >> q) & 1u;
-                mma_bf16(tmem + (uint32_t)(q * NT), sdesc(aA + (k0 / 8) * 128), sdesc(aB + (k0 / 8) * 128),
-                         id, acc);
-                *inited |= 1u << q;
-            }
-        }
+    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+#pragma unroll 1
+    for (int k0 = 0; k0 < kc; k0 += 16)
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int t = 0; t < S - s; ++t)
+                mma_bf16(tmem + (uint32_t)((s + t) * NT), sdesc(a0 + (uint32_t)(s * kTM * kSlice * 2 + k0 * 2)),
+                         sdesc(b0 + (uint32_t)(t * NT * kSlice * 2 + k0 * 2)), id,
+                         (first && s == 0 && k0 == 0) ? 0u : 1u);
 }
 
 // ------------------------------------------------------------------ synthesis kernel
 struct SynSplitArgs {
     const SynCol *cols;
-    int ncol, ncolD_first;
+    int ncol;
     const double *lfac;
-    const int *moff, *cbase;
+    const int *moff;
+    const long long *sbase;
     const __nv_bfloat16 *dig;
     const int *rexp;
     double2 *F;
-    int nrow, ms, T, nh, nlat, ntl, S, b, NT;
+    int nrow, ms, T, nh, nlat, ntl;
     int *err;
 };
 
-__global__ void __launch_bounds__(128, 1) k_split_synth(SynSplitArgs a) {
+// Synthesis smem: A [S][128][64] | B [S][64][64] bf16 | stage [64][65] doubles.
+template <int S>
+constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + (size_t)kNTs * kSt * 8; }
+template <int S>
+constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + (size_t)kNTa * kSt * 8; }
+
+template <int S, int B>
+__global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
-    __nv_bfloat16 *sB = sA + (size_t)a.S * kTM * kKC;
-    __shared__ __align__(8) uint64_t mbar;
+    __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
+    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTs * kKC);   // [64 cols][kSt]
+    __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[kNTs];
     __shared__ SynCol scol[kNTs / 2];
+    __shared__ int anyD, fail;
 
+    if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
+        if (threadIdx.x == 0) atomicOr(a.err, 2);
+        return;
+    }
     const int m = blockIdx.x, t = blockIdx.y, nt = blockIdx.z;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = a.T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
     const int mo = a.moff[m];
-    const int NT = a.NT;
-    const int c0 = nt * (NT / 2);
-    const int ncl = min(NT / 2, a.ncol - c0);
+    const int c0 = nt * (kNTs / 2);
+    const int ncl = min(kNTs / 2, a.ncol - c0);
     if (ncl <= 0) return;
     if (tid < ncl) scol[tid] = a.cols[c0 + tid];
+    if (tid < kNTs) cexp[tid] = 0;
+    if (tid == 0) { anyD = 0; fail = 0; }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    if (tid == 0) {
+        mbar_init(&mbarA);
+        mbar_init(&mbarM);
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
     __syncthreads();
-    // column exponents over the full contraction (re/im of each field)
-    if (tid < NT) {
-        const int cc = tid >> 1, comp = tid & 1;
-        int e = -2000;
-        if (cc < ncl) {
-            const SynCol &sc = scol[cc];
-            for (int k = 0; k < K; ++k) {
-                double2 v = sc.src[mo + k];
-                double x = comp ? v.y : v.x;
-                if (sc.scale) x *= a.lfac[sc.scale * a.ms + m + k];
-                if (x != 0.0) e = max(e, exp_above(x));
-            }
+    const __nv_bfloat16 *gA = a.dig + a.sbase[m] + (size_t)t * nch * S * kTM * kSlice;
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    if (tid < ncl && scol[tid].rowD >= 0) anyD = 1;
+
+    // value k of complex column cc (scaled input coefficient)
+    auto coef = [&](int cc, int k) -> double2 {
+        const SynCol &sc = scol[cc];
+        double2 v = sc.src[mo + k];
+        if (sc.scale) {
+            const double f = a.lfac[sc.scale * a.ms + m + k];
+            v.x *= f;
+            v.y *= f;
         }
-        cexp[tid] = e == -2000 ? 0 : e;
+        return v;
+    };
+    // phase 1: column scales over the full contraction, chunk 0 staged
+    const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+    for (int base = 0; base < ncl * nk8; base += kThreads) {
+        const int task = base + tid;
+        const bool valid = task < ncl * nk8;
+        const int cc = valid ? task / nk8 : -1, k0 = valid ? (task - cc * nk8) * 8 : 0;
+        int br = 0, bi = 0;
+        double re[8], im[8], f[8];
+        const double2 *src = valid ? scol[cc].src + mo + k0 : nullptr;
+        const int sci = valid ? scol[cc].scale : 0;
+        const double *lf = a.lfac + sci * a.ms + m + k0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {   // all loads first
+            const bool in = valid && k0 + i < K;
+            const double2 v = in ? __ldg(src + i) : make_double2(0.0, 0.0);
+            re[i] = v.x;
+            im[i] = v.y;
+            f[i] = in && sci ? __ldg(lf + i) : 1.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (sci) {
+                re[i] *= f[i];
+                im[i] *= f[i];
+            }
+            br = max(br, bexp(re[i]));
+            bi = max(bi, bexp(im[i]));
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, cc);
+        br = __reduce_max_sync(peers, br);
+        bi = __reduce_max_sync(peers, bi);
+        if (valid && lane == __ffs(peers) - 1) {
+            atomicMax(&cexp[2 * cc], br);
+            atomicMax(&cexp[2 * cc + 1], bi);
+        }
+        if (valid && k0 < kc0)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                stage[(2 * cc) * kSt + k0 + i] = re[i];
+                stage[(2 * cc + 1) * kSt + k0 + i] = im[i];
+            }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
-    const int tileB = NT * kKC;
-    uint32_t inited = 0;
     bool ok = true;
     for (int ch = 0; ch < nch && ok; ++ch) {
-        // A: precomputed digit tile image (S x 128 x 64 bf16), straight copy
-        const uint4 *gA = reinterpret_cast<const uint4 *>(a.dig + (((size_t)(a.cbase[m] + ch) * a.ntl + t) * a.S) *
-                                                                        (kTM * kKC));
-        uint4 *s4 = reinterpret_cast<uint4 *>(sA);
-        const int nA4 = a.S * kTM * kKC * 2 / 16;
-        for (int i = tid; i < nA4; i += blockDim.x) s4[i] = gA[i];
-        // B: digits of the data columns for this chunk
-        for (int idx = tid; idx < NT * kKC; idx += blockDim.x) {
-            const int n = idx / kKC, kk = idx - n * kKC;
-            const int cc = n >> 1, comp = n & 1, k = ch * kKC + kk;
-            double x = 0.0;
-            if (cc < ncl && k < K) {
-                const SynCol &sc = scol[cc];
-                double2 v = sc.src[mo + k];
-                x = comp ? v.y : v.x;
-                if (sc.scale) x *= a.lfac[sc.scale * a.ms + m + k];
+        const int kc = min(kKC, Kp - ch * kKC);
+        if (ch > 0) {
+            for (int task = tid; task < ncl * (kc / 8); task += kThreads) {
+                const int cc = task / (kc / 8), k0 = (task - cc * (kc / 8)) * 8;
+                for (int i = 0; i < 8; ++i) {
+                    const int k = ch * kKC + k0 + i;
+                    const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
+                    stage[(2 * cc) * kSt + k0 + i] = v.x;
+                    stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
+                }
             }
-            float d[8];
-            digits(x, cexp[n], a.S, a.b, d);
-            for (int s = 0; s < a.S; ++s) sB[(size_t)s * tileB + cidx(n, kk)] = __float2bfloat16(d[s]);
+            __syncthreads();
+        }
+        // digits of the data columns (columns of absent fields are zero)
+        // lanes take consecutive tile rows n: 16-byte digit stores fill whole core matrices
+        for (int task = tid; task < kNTs * (kc / 8); task += kThreads) {
+            const int n = task % kNTs, k0 = (task / kNTs) * 8;
+            double x[8];
+            if ((n >> 1) < ncl) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = 0.0;
+            }
+            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTs * kSlice, n, k0);
         }
         asm volatile("fence.proxy.async.shared::cta;");
         __syncthreads();
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            issue_chunk(tmem, sA, sB, a.S, NT, tileB, &inited);
-            mma_commit(&mbar);
+            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                issue_chunk<S>(tmem, sA, sB, kNTs, kc, ch == 0);
+                mma_commit(&mbarM);
+            } else {
+                fail = 1;
+                mbar_arrive(&mbarM);
+            }
         }
-        ok = mbar_wait(&mbar, (uint32_t)(ch & 1));
+        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
         asm volatile("tcgen05.fence::after_thread_sync;");
         __syncthreads();
+        ok = ok && !fail;
+        if (ok && tid == 0 && ch + 1 < nch) {
+            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+        }
     }
     if (!ok) {
         if (tid == 0) atomicOr(a.err, 1);
     } else {
-        // epilogue: warp w owns row block w (P even, P odd, dP even, dP odd), lane = latitude
-        double *stage = reinterpret_cast<double *>(smraw);   // [4][32][NT]
-        const int re = a.rexp[((size_t)m * a.ntl + t) * kTM + tid];
-        const int sh = 2 * (a.S * a.b - 1);
-        for (int c16 = 0; c16 < NT; c16 += 16) {
-            double acc[16];
-            for (int i = 0; i < 16; ++i) acc[i] = 0.0;
-            for (int q = a.S; q >= 0; --q) {
-                uint32_t r[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * NT + c16), r);
-                for (int i = 0; i < 16; ++i) {
-                    const int ce = cexp[c16 + i];
-                    acc[i] = fma((double)__uint_as_float(r[i]), pow2(re + ce - sh + (2 * a.S - 2 - q) * a.b), acc[i]);
-                }
+        // epilogue 1: warp w reads TMEM lane quarter w % 4 = row block (P even,
+        // P odd, dP even, dP odd; lane = latitude) and columns 16 (w / 4) .. +16
+        long long *zst = reinterpret_cast<long long *>(smraw);   // [128 rows][65]
+        const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+        if (quarter < 2 || anyD) {
+            for (int h = 0; h < 16; h += 8) {
+                long long z[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) z[i] = 0;
+                uint32_t r[S][8];
+#pragma unroll
+                for (int q = 0; q < S; ++q)
+                    tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
+                tmem_wait_ld();
+#pragma unroll
+                for (int q = 0; q < S; ++q)
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * 65 + c16 + h + i] = z[i];
             }
-            for (int i = 0; i < 16; ++i) stage[((size_t)warp * 32 + lane) * NT + c16 + i] = acc[i];
         }
         __syncthreads();
-        for (int idx = tid; idx < 32 * ncl; idx += blockDim.x) {
+        // epilogue 2: hemispheres as integer sums, then FP64
+        const int *re = a.rexp + ((size_t)m * a.ntl + t) * kTM;
+        for (int idx = tid; idx < 32 * ncl; idx += kThreads) {
             const int jj = idx / ncl, cc = idx - jj * ncl;
             const int jn = t * 32 + jj;
             if (jn >= a.nh) continue;
             const int js = a.nlat - 1 - jn;
             const SynCol &sc = scol[cc];
-            const double *E = stage + ((size_t)0 * 32 + jj) * NT + 2 * cc;
-            const double *O = stage + ((size_t)1 * 32 + jj) * NT + 2 * cc;
-            a.F[((size_t)jn * a.nrow + sc.rowP) * a.ms + m] = make_double2(E[0] + O[0], E[1] + O[1]);
-            a.F[((size_t)js * a.nrow + sc.rowP) * a.ms + m] = make_double2(E[0] - O[0], E[1] - O[1]);
+            const int ecr = scale_exp(cexp[2 * cc]), eci = scale_exp(cexp[2 * cc + 1]);
+            const long long *E = zst + (size_t)(0 * 32 + jj) * 65 + 2 * cc;
+            const long long *O = zst + (size_t)(1 * 32 + jj) * 65 + 2 * cc;
+            const int eP = re[jj];
+            a.F[((size_t)jn * a.nrow + sc.rowP) * a.ms + m] =
+                make_double2(z_to_f64(E[0] + O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] + O[1], zexp<B>(eP, eci)));
+            a.F[((size_t)js * a.nrow + sc.rowP) * a.ms + m] =
+                make_double2(z_to_f64(E[0] - O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] - O[1], zexp<B>(eP, eci)));
             if (sc.rowD >= 0) {
-                const double *dE = stage + ((size_t)2 * 32 + jj) * NT + 2 * cc;
-                const double *dO = stage + ((size_t)3 * 32 + jj) * NT + 2 * cc;
-                a.F[((size_t)jn * a.nrow + sc.rowD) * a.ms + m] = make_double2(dE[0] + dO[0], dE[1] + dO[1]);
-                a.F[((size_t)js * a.nrow + sc.rowD) * a.ms + m] = make_double2(dO[0] - dE[0], dO[1] - dE[1]);
+                const long long *dE = zst + (size_t)(2 * 32 + jj) * 65 + 2 * cc;
+                const long long *dO = zst + (size_t)(3 * 32 + jj) * 65 + 2 * cc;
+                const int eD = re[64 + jj];
+                a.F[((size_t)jn * a.nrow + sc.rowD) * a.ms + m] = make_double2(
+                    z_to_f64(dE[0] + dO[0], zexp<B>(eD, ecr)), z_to_f64(dE[1] + dO[1], zexp<B>(eD, eci)));
+                a.F[((size_t)js * a.nrow + sc.rowD) * a.ms + m] = make_double2(
+                    z_to_f64(dO[0] - dE[0], zexp<B>(eD, ecr)), z_to_f64(dO[1] - dE[1], zexp<B>(eD, eci)));
             }
         }
     }
@@ -355,23 +570,36 @@ struct AnaSplitArgs {
     int ncol;
     const double *lfac, *isin;
     const int *moff;
+    const long long *abase;
     const __nv_bfloat16 *dig;
     const int *rexp;
     const double2 *F;
-    int nrow, ms, T, nh, nlat, ntlA, nchA, S, b;
+    int nrow, ms, T, nh, nlat, ntlA, KpA;
     int *err;
 };
 
-// B column n (0..47) of output col cc = n / 12: slot = (n % 12) / 4, fold = (n % 4) / 2 (0 even, 1 odd), comp = n % 2.
-__global__ void __launch_bounds__(128, 1) k_split_anal(AnaSplitArgs a) {
+// B column of (fold, slot, field cc, comp): fold 0 = north + south, 1 = north - south;
+// slot s scales Fourier row s of the field by (a_s + i b_s m / sin) (slots 0, 1).
+__host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
+    return fold * 24 + slot * 8 + cc * 2 + comp;
+}
+
+template <int S, int B>
+__global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
-    __nv_bfloat16 *sB = sA + (size_t)a.S * kTM * kKC;
-    __shared__ __align__(8) uint64_t mbar;
+    __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
+    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // [48 cols][kSt]
+    __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[kNTa];
     __shared__ AnaCol scol[kNTa / 12];
+    __shared__ int fail;
 
+    if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
+        if (threadIdx.x == 0) atomicOr(a.err, 2);
+        return;
+    }
     const int m = blockIdx.x, t = blockIdx.y, nt = blockIdx.z;
     const int K = a.T - m + 1;
     if (64 * t >= K) return;
@@ -379,111 +607,171 @@ __global__ void __launch_bounds__(128, 1) k_split_anal(AnaSplitArgs a) {
     const int c0 = nt * (kNTa / 12);
     const int ncl = min(kNTa / 12, a.ncol - c0);
     if (ncl <= 0) return;
+    const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
     if (tid < ncl) scol[tid] = a.cols[c0 + tid];
+    if (tid < kNTa) cexp[tid] = 0;
+    if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    if (tid == 0) {
+        mbar_init(&mbarA);
+        mbar_init(&mbarM);
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
     __syncthreads();
+    const __nv_bfloat16 *gA = a.dig + a.abase[m] + (size_t)t * nch * S * kTM * kSlice;
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
 
-    // value of B column n at latitude j (north index j < nh)
-    auto bval = [&](int n, int j) -> double {
-        const int cc = n / 12, rem = n - cc * 12, slot = rem >> 2, fold = (rem >> 1) & 1, comp = rem & 1;
-        if (cc >= ncl || j >= a.nh) return 0.0;
+    // the four B values (fold x comp) of field cc, slot s at north latitude j
+    auto bvals = [&](int cc, int slot, int j, double *v) {
         const AnaCol &q = scol[cc];
         const int row = slot == 0 ? q.row1 : (slot == 1 ? q.row2 : q.row3);
-        if (row < 0) return 0.0;
-        const int js = a.nlat - 1 - j;
+        if (row < 0 || j >= a.nh) { v[0] = v[1] = v[2] = v[3] = 0.0; return; }
         double2 fn = a.F[((size_t)j * a.nrow + row) * a.ms + m];
-        double2 fs = a.F[((size_t)js * a.nrow + row) * a.ms + m];
+        double2 fs = a.F[((size_t)(a.nlat - 1 - j) * a.nrow + row) * a.ms + m];
         if (slot < 2) {
             const double aa = slot == 0 ? q.a1 : q.a2, bb = (slot == 0 ? q.b1 : q.b2) * m * a.isin[j];
             fn = make_double2(aa * fn.x - bb * fn.y, aa * fn.y + bb * fn.x);
             fs = make_double2(aa * fs.x - bb * fs.y, aa * fs.y + bb * fs.x);
         }
-        const double2 v = fold ? make_double2(fn.x - fs.x, fn.y - fs.y) : make_double2(fn.x + fs.x, fn.y + fs.y);
-        return comp ? v.y : v.x;
+        v[0] = fn.x + fs.x;   // fold 0 re
+        v[1] = fn.y + fs.y;   // fold 0 im
+        v[2] = fn.x - fs.x;   // fold 1 re
+        v[3] = fn.y - fs.y;   // fold 1 im
     };
-    if (tid < kNTa) {
-        int e = -2000;
-        for (int j = 0; j < a.nh; ++j) {
-            double x = bval(tid, j);
-            if (x != 0.0) e = max(e, exp_above(x));
+    // phase 1: column scales over all latitudes, chunk 0 staged
+    const int kc0 = min(kKC, KpA);
+    for (int base = 0; base < ncl * 3 * KpA; base += kThreads) {
+        const int task = base + tid;
+        const bool valid = task < ncl * 3 * KpA;
+        const int j = task % KpA, cs = valid ? task / KpA : -1, cc = cs / 3, slot = cs - cc * 3;
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
+        if (valid) bvals(cc, slot, j, v);
+        const unsigned peers = __match_any_sync(0xffffffffu, cs);
+        const bool leader = valid && lane == __ffs(peers) - 1;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            const int n = acol(f >> 1, slot, cc, f & 1);
+            const int be = __reduce_max_sync(peers, bexp(v[f]));
+            if (leader) atomicMax(&cexp[n], be);
+            if (valid && j < kc0) stage[n * kSt + j] = v[f];
         }
-        cexp[tid] = e == -2000 ? 0 : e;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
-    const int tileB = kNTa * kKC;
-    uint32_t inited = 0;
     bool ok = true;
-    for (int ch = 0; ch < a.nchA && ok; ++ch) {
-        const uint4 *gA = reinterpret_cast<const uint4 *>(
-            a.dig + ((((size_t)m * a.ntlA + t) * a.nchA + ch) * a.S) * (kTM * kKC));
-        uint4 *s4 = reinterpret_cast<uint4 *>(sA);
-        const int nA4 = a.S * kTM * kKC * 2 / 16;
-        for (int i = tid; i < nA4; i += blockDim.x) s4[i] = gA[i];
-        for (int idx = tid; idx < kNTa * kKC; idx += blockDim.x) {
-            const int n = idx / kKC, jj = idx - n * kKC;
-            float d[8];
-            digits(bval(n, ch * kKC + jj), cexp[n], a.S, a.b, d);
-            for (int s = 0; s < a.S; ++s) sB[(size_t)s * tileB + cidx(n, jj)] = __float2bfloat16(d[s]);
+    for (int ch = 0; ch < nch && ok; ++ch) {
+        const int kc = min(kKC, KpA - ch * kKC);
+        if (ch > 0) {
+            for (int task = tid; task < ncl * 3 * kc; task += kThreads) {
+                const int jl = task % kc, cs = task / kc, cc = cs / 3, slot = cs - cc * 3;
+                double v[4];
+                bvals(cc, slot, ch * kKC + jl, v);
+#pragma unroll
+                for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
+            }
+            __syncthreads();
+        }
+        for (int task = tid; task < kNTa * (kc / 8); task += kThreads) {
+            const int n = task % kNTa, k0 = (task / kNTa) * 8;
+            const int cc = (n % 8) >> 1;
+            double x[8];
+            if (cc < ncl) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = 0.0;
+            }
+            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTa * kSlice, n, k0);
         }
         asm volatile("fence.proxy.async.shared::cta;");
         __syncthreads();
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            issue_chunk(tmem, sA, sB, a.S, kNTa, tileB, &inited);
-            mma_commit(&mbar);
+            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                issue_chunk<S>(tmem, sA, sB, kNTa, kc, ch == 0);
+                mma_commit(&mbarM);
+            } else {
+                fail = 1;
+                mbar_arrive(&mbarM);
+            }
         }
-        ok = mbar_wait(&mbar, (uint32_t)(ch & 1));
+        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
         asm volatile("tcgen05.fence::after_thread_sync;");
         __syncthreads();
+        ok = ok && !fail;
+        if (ok && tid == 0 && ch + 1 < nch) {
+            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+        }
     }
     if (!ok) {
         if (tid == 0) atomicOr(a.err, 1);
     } else {
-        double *stage = reinterpret_cast<double *>(smraw);   // [128 rows][48 cols]
-        const int re = a.rexp[((size_t)m * a.ntlA + t) * kTM + tid];
-        const int sh = 2 * (a.S * a.b - 1);
-        for (int c16 = 0; c16 < kNTa; c16 += 16) {
-            double acc[16];
-            for (int i = 0; i < 16; ++i) acc[i] = 0.0;
-            for (int q = a.S; q >= 0; --q) {
-                uint32_t r[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(q * kNTa + c16), r);
-                for (int i = 0; i < 16; ++i)
-                    acc[i] = fma((double)__uint_as_float(r[i]),
-                                 pow2(re + cexp[c16 + i] - sh + (2 * a.S - 2 - q) * a.b), acc[i]);
-            }
-            for (int i = 0; i < 16; ++i) stage[(size_t)tid * kNTa + c16 + i] = acc[i];
+        // epilogue 1: only the columns a row uses.  P rows (lane quarters 0, 1;
+        // parity par) use fold par of slots 0 and 2 (16 columns), dP rows
+        // (quarters 2, 3) fold 1 - par of slot 1 (8 columns); the four warps
+        // of a quarter split them.
+        double *sd = reinterpret_cast<double *>(sB);   // [128 rows][17]
+        const int quarter = warp & 3, g = warp >> 2, par = quarter & 1;
+        const int row = quarter * 32 + lane;
+        const int er = a.rexp[((size_t)m * a.ntlA + t) * kTM + row];
+        const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
+        if (quarter < 2) {
+            const int n0 = acol(par, g < 2 ? 0 : 2, 0, 0) + (g & 1) * 4;
+            long long z[4] = {0, 0, 0, 0};
+            uint32_t r[S][4];
+#pragma unroll
+            for (int q = 0; q < S; ++q) tmem_ld<4>(tl + (uint32_t)(q * kNTa + n0), r[q]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) z[i] += zterm<B>(r[q][i], q);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                sd[(size_t)row * 17 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
+        } else {
+            const int n0 = acol(1 - par, 1, 0, 0) + g * 2;
+            long long z[2] = {0, 0};
+            uint32_t r[S][2];
+#pragma unroll
+            for (int q = 0; q < S; ++q) tmem_ld<2>(tl + (uint32_t)(q * kNTa + n0), r[q]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+#pragma unroll
+                for (int i = 0; i < 2; ++i) z[i] += zterm<B>(r[q][i], q);
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+                sd[(size_t)row * 17 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
         }
         __syncthreads();
-        // combine: l = m + 64 t + 2 pos + par; P rows blk = par, dP rows blk = 2 + par
-        for (int idx = tid; idx < 64 * ncl; idx += blockDim.x) {
+        // epilogue 2: combine P and dP parts; l = m + 64 t + 2 pos + par
+        for (int idx = tid; idx < 64 * ncl; idx += kThreads) {
             const int lk = idx / ncl, cc = idx - lk * ncl;
-            const int pos = lk >> 1, par = lk & 1;
+            const int pos = lk >> 1, pr = lk & 1;
             const int k = 64 * t + lk;
             if (k >= K) continue;
             const AnaCol &q = scol[cc];
             const int l = m + k;
-            const double *rp = stage + (size_t)(par * 32 + pos) * kNTa + cc * 12;
-            const double *rd = stage + (size_t)((2 + par) * 32 + pos) * kNTa + cc * 12;
-            // columns: slot*4 + fold*2 + comp; P uses fold = par, dP uses fold = 1 - par
+            const double *rp = sd + (size_t)(pr * 32 + pos) * 17;         // slot 0 at [0..8), slot 2 at [8..16)
+            const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * 17;   // slot 1 at [0..8)
             double xr = 0.0, xi = 0.0;
-            if (q.row1 >= 0) { xr += rp[0 * 4 + par * 2]; xi += rp[0 * 4 + par * 2 + 1]; }
-            if (q.row2 >= 0) { xr += rd[1 * 4 + (1 - par) * 2]; xi += rd[1 * 4 + (1 - par) * 2 + 1]; }
+            if (q.row1 >= 0) { xr += rp[cc * 2]; xi += rp[cc * 2 + 1]; }
+            if (q.row2 >= 0) { xr += rd[cc * 2]; xi += rd[cc * 2 + 1]; }
             const double post = a.lfac[q.post * a.ms + l];
             xr *= post;
             xi *= post;
             if (q.row3 >= 0) {
                 const double f3 = a.lfac[q.lf3 * a.ms + l];
-                xr += f3 * rp[2 * 4 + par * 2];
-                xi += f3 * rp[2 * 4 + par * 2 + 1];
+                xr += f3 * rp[8 + cc * 2];
+                xi += f3 * rp[8 + cc * 2 + 1];
             }
             if (m == 0) xi = 0.0;
             q.dst[a.moff[m] + k] = make_double2(xr, xi);
@@ -497,11 +785,29 @@ __global__ void __launch_bounds__(128, 1) k_split_anal(AnaSplitArgs a) {
 }  // namespace
 
 struct SplitCtx {
-    int T = 0, nh = 0, ntl = 0, ntlA = 0, nchA = 0, S = 7, b = 8, NTs = 64;
+    int T = 0, nh = 0, ntl = 0, ntlA = 0, KpA = 0, S = 7, B = 8;
     __nv_bfloat16 *digS = nullptr, *digA = nullptr;
-    int *rexpS = nullptr, *rexpA = nullptr, *cbase = nullptr, *err = nullptr;
-    size_t smemS = 0, smemA = 0;
+    long long *sbase = nullptr, *abase = nullptr;
+    int *rexpS = nullptr, *rexpA = nullptr, *err = nullptr;
 };
+
+namespace {
+
+template <int S, int B>
+int prep_tables(SplitCtx *s, const Geometry &g, const DevTables &t, int nchS) {
+    k_prep_synth_dig<S, B><<<dim3(g.T + 1, s->ntl, nchS), 256>>>(t.Ps, t.dPs, t.moff, s->sbase, g.T, g.nh, s->ntl,
+                                                                s->rexpS, s->digS);
+    k_prep_anal_dig<S, B><<<dim3(g.T + 1, s->ntlA, (s->KpA + kKC - 1) / kKC), 256>>>(
+        t.PaT, t.dPaT, t.moff, s->abase, g.T, g.nh, s->ntlA, s->KpA, s->rexpA, s->digA);
+    AEROS_CUDA(cudaGetLastError());
+    AEROS_CUDA(cudaFuncSetAttribute(k_split_synth<S, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)synth_smem<S>()));
+    AEROS_CUDA(cudaFuncSetAttribute(k_split_anal<S, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)anal_smem<S>()));
+    return AEROS_OK;
+}
+
+}  // namespace
 
 int split_create(const Geometry &g, const DevTables &t, int /*max_rows*/, SplitCtx **out) {
     *out = nullptr;
@@ -509,26 +815,31 @@ int split_create(const Geometry &g, const DevTables &t, int /*max_rows*/, SplitC
     s->T = g.T;
     s->nh = g.nh;
     const int kmax = std::max(((g.T + 1) + 15) & ~15, (g.nh + 15) & ~15);
-    if (kmax <= 126) { s->S = 7; s->b = 8; s->NTs = 64; }
-    else if (kmax <= 441) { s->S = 8; s->b = 7; s->NTs = 48; }
+    if (kmax <= 126) { s->S = 7; s->B = 8; }
+    else if (kmax <= 441) { s->S = 8; s->B = 7; }
     else { delete s; set_error("split path: contraction longer than 441"); return AEROS_ERR_UNSUPPORTED; }
     s->ntl = (g.nh + 31) / 32;
     s->ntlA = (g.T + 1 + 63) / 64;
-    s->nchA = ((g.nh + 15) / 16 * 16 + kKC - 1) / kKC;
-    std::vector<int> cb(g.T + 1);
-    int tot = 0;
+    s->KpA = (g.nh + 15) & ~15;
+    const size_t tile = (size_t)s->S * kTM * kSlice;   // elements of one (m, tile, chunk) image
+    const int nchA = (s->KpA + kKC - 1) / kKC;
+    std::vector<long long> sb(g.T + 1), ab(g.T + 1);
+    long long totS = 0, totA = 0;
+    int nchS = 1;
     for (int m = 0; m <= g.T; ++m) {
-        cb[m] = tot;
-        int Kp = ((g.T - m + 1) + 15) & ~15;
-        tot += (Kp + kKC - 1) / kKC;
+        const int K = g.T - m + 1, Kp = (K + 15) & ~15;
+        sb[m] = totS;
+        totS += (long long)s->ntl * ((Kp + kKC - 1) / kKC) * tile;
+        nchS = std::max(nchS, (Kp + kKC - 1) / kKC);
+        ab[m] = totA;
+        totA += (long long)((K + 63) / 64) * nchA * tile;
     }
-    const size_t tile = (size_t)kTM * kKC;
-    const size_t nS = (size_t)tot * s->ntl * s->S * tile;
-    const size_t nA = (size_t)(g.T + 1) * s->ntlA * s->nchA * s->S * tile;
-    bool okm = cudaMalloc(&s->digS, nS * 2) == cudaSuccess && cudaMalloc(&s->digA, nA * 2) == cudaSuccess &&
+    bool okm = cudaMalloc(&s->digS, (size_t)totS * 2) == cudaSuccess &&
+               cudaMalloc(&s->digA, (size_t)totA * 2) == cudaSuccess &&
+               cudaMalloc(&s->sbase, sizeof(long long) * (g.T + 1)) == cudaSuccess &&
+               cudaMalloc(&s->abase, sizeof(long long) * (g.T + 1)) == cudaSuccess &&
                cudaMalloc(&s->rexpS, sizeof(int) * (g.T + 1) * s->ntl * kTM) == cudaSuccess &&
                cudaMalloc(&s->rexpA, sizeof(int) * (g.T + 1) * s->ntlA * kTM) == cudaSuccess &&
-               cudaMalloc(&s->cbase, sizeof(int) * (g.T + 1)) == cudaSuccess &&
                cudaMalloc(&s->err, sizeof(int)) == cudaSuccess;
     if (!okm) {
         cudaGetLastError();
@@ -536,32 +847,25 @@ int split_create(const Geometry &g, const DevTables &t, int /*max_rows*/, SplitC
         set_error("split path: table allocation failed");
         return AEROS_ERR_NOMEM;
     }
-    cudaMemset(s->err, 0, sizeof(int));
-    cudaMemset(s->digS, 0, nS * 2);
-    cudaMemset(s->digA, 0, nA * 2);
-    AEROS_CUDA(cudaMemcpy(s->cbase, cb.data(), sizeof(int) * cb.size(), cudaMemcpyHostToDevice));
-    k_prep_synth_exp<<<dim3(g.T + 1, s->ntl), kTM>>>(t.Ps, t.dPs, t.moff, g.T, g.nh, s->ntl, s->rexpS);
-    int nchmax = ((g.T + 1 + 15) / 16 * 16 + kKC - 1) / kKC;
-    k_prep_synth_dig<<<dim3(g.T + 1, s->ntl, nchmax), 256>>>(t.Ps, t.dPs, t.moff, s->cbase, g.T, g.nh, s->ntl, s->S,
-                                                            s->b, s->rexpS, s->digS);
+    AEROS_CUDA(cudaMemset(s->err, 0, sizeof(int)));
+    AEROS_CUDA(cudaMemcpy(s->sbase, sb.data(), sizeof(long long) * sb.size(), cudaMemcpyHostToDevice));
+    AEROS_CUDA(cudaMemcpy(s->abase, ab.data(), sizeof(long long) * ab.size(), cudaMemcpyHostToDevice));
+    k_prep_synth_exp<<<dim3(g.T + 1, s->ntl), 64>>>(t.Ps, t.dPs, t.moff, g.T, g.nh, s->ntl, s->rexpS);
     k_prep_anal_exp<<<dim3(g.T + 1, s->ntlA), kTM>>>(t.PaT, t.dPaT, t.moff, g.T, g.nh, s->ntlA, s->rexpA);
-    k_prep_anal_dig<<<dim3(g.T + 1, s->ntlA, s->nchA), 256>>>(t.PaT, t.dPaT, t.moff, g.T, g.nh, s->ntlA, s->nchA,
-                                                             s->S, s->b, s->rexpA, s->digA);
-    AEROS_CUDA(cudaGetLastError());
-    AEROS_CUDA(cudaDeviceSynchronize());
-    s->smemS = (size_t)s->S * (kTM + s->NTs) * kKC * 2;
-    s->smemA = (size_t)s->S * (kTM + kNTa) * kKC * 2;
-    s->smemS = std::max(s->smemS, (size_t)4 * 32 * s->NTs * 8);
-    s->smemA = std::max(s->smemA, (size_t)kTM * kNTa * 8);
-    AEROS_CUDA(cudaFuncSetAttribute(k_split_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smemS));
-    AEROS_CUDA(cudaFuncSetAttribute(k_split_anal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smemA));
+    int rc = s->S == 7 ? prep_tables<7, 8>(s, g, t, nchS) : prep_tables<8, 7>(s, g, t, nchS);
+    if (rc == AEROS_OK) rc = cudaDeviceSynchronize() == cudaSuccess ? AEROS_OK : AEROS_ERR_CUDA;
+    if (rc != AEROS_OK) {
+        split_destroy(s);
+        if (rc == AEROS_ERR_CUDA) set_error("split path: table preparation failed");
+        return rc;
+    }
     *out = s;
     return AEROS_OK;
 }
 
 void split_destroy(SplitCtx *s) {
     if (!s) return;
-    void *ps[] = {s->digS, s->digA, s->rexpS, s->rexpA, s->cbase, s->err};
+    void *ps[] = {s->digS, s->digA, s->sbase, s->abase, s->rexpS, s->rexpA, s->err};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete s;
@@ -569,10 +873,11 @@ void split_destroy(SplitCtx *s) {
 
 int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int nrow) {
     if (p.ncol <= 0) return AEROS_OK;
-    SynSplitArgs a{p.cols_d, p.ncol, p.ncolD_first, c.tab->lfac, c.tab->moff, s->cbase, s->digS, s->rexpS, F,
-                   nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->S, s->b, s->NTs, s->err};
-    dim3 grid(c.T + 1, s->ntl, (p.ncol + s->NTs / 2 - 1) / (s->NTs / 2));
-    k_split_synth<<<grid, 128, s->smemS, c.stream>>>(a);
+    SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
+                   nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err};
+    dim3 grid(c.T + 1, s->ntl, (p.ncol + kNTs / 2 - 1) / (kNTs / 2));
+    if (s->S == 7) k_split_synth<7, 8><<<grid, kThreads, synth_smem<7>(), c.stream>>>(a);
+    else k_split_synth<8, 7><<<grid, kThreads, synth_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -580,10 +885,11 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
 
 int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
     if (ncol <= 0) return AEROS_OK;
-    AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->digA, s->rexpA, F, nrow, c.ms, c.T,
-                   c.nh, c.nlat, s->ntlA, s->nchA, s->S, s->b, s->err};
+    AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
+                   c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err};
     dim3 grid(c.T + 1, s->ntlA, (ncol + kNTa / 12 - 1) / (kNTa / 12));
-    k_split_anal<<<grid, 128, s->smemA, c.stream>>>(a);
+    if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
+    else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -591,6 +897,18 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, co
 
 int split_error(SplitCtx *s, int *flag) {
     return cudaMemcpy(flag, s->err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess ? AEROS_OK : AEROS_ERR_CUDA;
+}
+
+int split_check(SplitCtx *s) {
+    if (!s) return AEROS_OK;
+    int flag = 0;
+    if (split_error(s, &flag) != AEROS_OK) return AEROS_ERR_CUDA;
+    if (flag) {
+        set_error(flag & 2 ? "split path: shared memory not 1024-byte aligned"
+                           : "split path: tensor-core wait gave up (bounded mbarrier wait)");
+        return AEROS_ERR_CUDA;
+    }
+    return AEROS_OK;
 }
 
 }  // namespace aeros

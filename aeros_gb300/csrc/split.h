@@ -13,5 +13,10 @@ void split_destroy(SplitCtx *s);
 // Same contract as launch_leg_synth_fp64 / launch_leg_anal_fp64.
 int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int nrow);
 int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
+// Sticky device error flag of the split kernels (1: an mbarrier wait gave up,
+// 2: misaligned shared memory); read after the stream has synchronised.
+int split_error(SplitCtx *s, int *flag);
+// AEROS_OK, or AEROS_ERR_CUDA with the last-error text set when the flag is up.
+int split_check(SplitCtx *s);
 
 }  // namespace aeros

@@ -218,7 +218,7 @@ def split_form(args, sht, dyn_fp64, flush, torch):
     t = time_steps(d, s, args.steps, torch, flush)
     return {"sypd": sypd(t), "ms_per_step": t * 1e3,
             "max_rel_diff_vs_fp64_gpu_after_24_steps": err,
-            "legendre": "tcgen05 bf16 Ozaki digits (55 bits), FP64 recombination"}
+            "legendre": "tcgen05 bf16 Ozaki digits (55 bits), exact int64 recombination"}
 
 
 def batched_form(args, torch):

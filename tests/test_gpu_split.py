@@ -1,4 +1,4 @@
-"""Split-precision (Ozaki, tcgen05 bf16 digits, FP64 recombination) path
+"""Split-precision (Ozaki, tcgen05 bf16 digits, exact integer recombination) path
 against the FP64 CPU oracle.
 
 Bar: 1e-10 relative (max |split - oracle| / max |oracle|) for every transform
