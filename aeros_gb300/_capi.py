@@ -100,6 +100,14 @@ _PROTOS = {
     "aeros_group_step_async": [_vp, _i],
     "aeros_group_sync": [_vp],
     "aeros_group_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "aeros_sht_synthesis_ad": [_vp, _vp, _vp, _i],
+    "aeros_sht_analysis_ad": [_vp, _vp, _vp, _i],
+    "aeros_sht_synthesis_vec_ad": [_vp, _vp, _vp, _vp, _vp, _i],
+    "aeros_sht_analysis_vec_ad": [_vp, _vp, _vp, _vp, _vp, _i],
+    "aeros_dyn_state_size": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "aeros_dyn_step_ad": [_vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "aeros_dyn_window_forward": [_vp, _i, _i, _vp],
+    "aeros_dyn_window_backward": [_vp, _vp, _vp, _vp, _vp],
     "aeros_last_error": [],
 }
 _RESTYPE = {"aeros_last_error": ctypes.c_char_p}

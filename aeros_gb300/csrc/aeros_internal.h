@@ -102,7 +102,7 @@ struct DevTables {
     double2 *tw = nullptr;       // n entries exp(-2 pi i t/n), n = nlon/2
     double2 *twN = nullptr;      // nlon/2+1 entries exp(-2 pi i k/nlon)
     int *moff = nullptr;         // (T+1)
-    int *l_of_lm = nullptr;
+    int *l_of_lm = nullptr, *m_of_lm = nullptr;
     FftPlan plan{};
 };
 int upload_tables(const Geometry &g, DevTables &t);
@@ -136,6 +136,12 @@ int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2
 int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
 
 // Elementwise helpers.
+// Diagonal operators used by the adjoints (transforms.cu):
+// y (+)= c Dm^dm (l(l+1))^lp x over nf spectral fields, Dm = (2 - delta_m0) nlon / 2 pi,
+// l = 0 -> 0 when lp < 0; and g[f][j][i] *= c w_j^wp.
+void launch_spec_axpy(cudaStream_t st, double2 *y, const double2 *x, int nf, const Ctx &c, double f, int dm, int lp,
+                      int accumulate);
+void launch_grid_wscale(cudaStream_t st, double *g, int nf, const Ctx &c, double f, int wp);
 int launch_laplacian(const Ctx &c, double2 *coeffs, int inverse, int nbatch);
 int launch_surface_integral(const Ctx &c, const double *field, double *partial, double *total, int nbatch);
 

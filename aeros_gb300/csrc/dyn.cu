@@ -557,6 +557,9 @@ int lu_inverse(std::vector<double> &A, int n, std::vector<double> &inv) {
 }  // namespace
 
 // =========================================================================
+struct AdjCtx;                      // adjoint workspace (dyn_adjoint.cuh)
+void adj_release(AdjCtx *a);
+
 struct aeros_dyn_s {
     aeros_params par{};
     Geometry g;
@@ -602,6 +605,7 @@ struct aeros_dyn_s {
     double2 *stage = nullptr;                        // host transfer staging
     size_t stage_bytes = 0;
     SplitCtx *split = nullptr;
+    AdjCtx *adj = nullptr;
 
     size_t ns3() const { return (size_t)NL * g.nlm; }
     size_t nstate() const { return (size_t)M * (3 * ns3() + g.nlm); }
@@ -1060,6 +1064,7 @@ void destroy(Dyn *d) {
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->split) split_destroy(d->split);
+    if (d->adj) adj_release(d->adj);
     free_tables(d->tab);
     if (d->own_stream && d->stream) cudaStreamDestroy(d->stream);
     delete d;
@@ -1348,8 +1353,8 @@ int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target, double *l
 }
 
 int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass) {
-    if (!h || mass <= 0.0) return AEROS_ERR_ARG;
-    std::vector<double> t(h->M, mass);
+    if (!h || mass == 0.0 || !std::isfinite(mass)) return AEROS_ERR_ARG;
+    std::vector<double> t(h->M, mass > 0.0 ? mass : -1.0);   // negative: capture again at the next start-up
     AEROS_CUDA(cudaMemcpy(h->mass_tgt, t.data(), 8 * h->M, cudaMemcpyHostToDevice));
     return AEROS_OK;
 }
@@ -1526,3 +1531,5 @@ int aeros_group_launch_count(aeros_group_t g, long long *count) {
 }
 
 }  // extern "C"
+
+#include "dyn_adjoint.cuh"

@@ -207,12 +207,13 @@ int upload_tables(const Geometry &g, DevTables &t) {
     if ((rc = upload(t.twN, twN.data(), n + 1))) return rc;
     if ((rc = upload(t.moff, g.moff.data(), g.moff.size()))) return rc;
     if ((rc = upload(t.l_of_lm, g.l_of_lm.data(), g.l_of_lm.size()))) return rc;
+    if ((rc = upload(t.m_of_lm, g.m_of_lm.data(), g.m_of_lm.size()))) return rc;
     if ((rc = fft_plan(n, t.plan))) return rc;
     return AEROS_OK;
 }
 
 void free_tables(DevTables &t) {
-    void *ps[] = {t.Ps, t.dPs, t.PaT, t.dPaT, t.sint, t.x, t.w, t.lfac, t.tw, t.twN, t.moff, t.l_of_lm};
+    void *ps[] = {t.Ps, t.dPs, t.PaT, t.dPaT, t.sint, t.x, t.w, t.lfac, t.tw, t.twN, t.moff, t.l_of_lm, t.m_of_lm};
     for (void *p : ps)
         if (p) cudaFree(p);
     t = DevTables{};

@@ -39,6 +39,8 @@ struct aeros_sht_s {
     double2 *F2 = nullptr;                // second Fourier buffer (analysis)
     double *stage = nullptr;              // host-pointer staging
     size_t stage_bytes = 0;
+    double *adbuf = nullptr;              // adjoint transforms: grid and spectral scratch
+    size_t ad_bytes = 0;
     double *partial = nullptr, *totals = nullptr;
     long long launches = 0;
     std::map<DescKey, DescSet> cache;
@@ -316,6 +318,7 @@ int aeros_sht_destroy(aeros_sht_t h) {
     if (h->F) cudaFree(h->F);
     if (h->F2) cudaFree(h->F2);
     if (h->stage) cudaFree(h->stage);
+    if (h->adbuf) cudaFree(h->adbuf);
     if (h->partial) cudaFree(h->partial);
     if (h->totals) cudaFree(h->totals);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -438,6 +441,98 @@ int aeros_sht_launch_count(aeros_sht_t h, long long *count) {
     if (!h || !count) return AEROS_ERR_ARG;
     *count = h->launches;
     return AEROS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- adjoints
+// With W = diag(Gauss weight of the row) and Dm = diag((2 - delta_m0) nlon/2pi),
+// L = diag(l(l+1)) (exact identities of the discrete operators):
+//   synthesis^T = Dm analysis W^-1,          analysis^T = W synthesis Dm^-1,
+//   synthesis_vec^T = Dm L analysis_vec W^-1, analysis_vec^T = W synthesis_vec (Dm L)^-1.
+namespace {
+
+int ensure_ad(aeros_sht_s *h, size_t bytes) {
+    if (h->ad_bytes >= bytes) return AEROS_OK;
+    if (h->adbuf) cudaFree(h->adbuf);
+    h->adbuf = nullptr;
+    h->ad_bytes = 0;
+    if (cudaMalloc(&h->adbuf, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("adjoint transform scratch allocation failed");
+        return AEROS_ERR_NOMEM;
+    }
+    h->ad_bytes = bytes;
+    return AEROS_OK;
+}
+
+// grid -> spectral adjoints (synthesis^T for nvec = 1, synthesis_vec^T for 2)
+int grid_to_spec_ad(aeros_sht_s *h, int nvec, const double *g0, const double *g1, double *c0, double *c1, int nb) {
+    if (!h || !g0 || !c0 || (nvec == 2 && (!g1 || !c1)) || nb < 1 || nb > h->batch_max) return AEROS_ERR_ARG;
+    const size_t ng = (size_t)h->g.nlon * h->g.nlat * nb, ns = (size_t)h->g.nlm * nb;
+    int rc;
+    if ((rc = ensure_ad(h, 2 * ng * sizeof(double) + 2 * ns * sizeof(double2)))) return rc;
+    double *G0 = h->adbuf, *G1 = G0 + ng;
+    double2 *C0 = reinterpret_cast<double2 *>(G1 + ng), *C1 = C0 + ns;
+    Ctx c = h->ctx();
+    AEROS_CUDA(cudaMemcpyAsync(G0, g0, ng * 8, cudaMemcpyDefault, h->stream));
+    if (nvec == 2) AEROS_CUDA(cudaMemcpyAsync(G1, g1, ng * 8, cudaMemcpyDefault, h->stream));
+    launch_grid_wscale(h->stream, G0, nvec * nb, c, 1.0, -1);
+    rc = nvec == 1 ? aeros_sht_analysis(h, G0, reinterpret_cast<double *>(C0), nb)
+                   : aeros_sht_analysis_vec(h, G0, G1, reinterpret_cast<double *>(C0), reinterpret_cast<double *>(C1), nb);
+    if (rc) return rc;
+    launch_spec_axpy(h->stream, C0, C0, nvec * nb, c, 1.0, 1, nvec == 2 ? 1 : 0, 0);
+    AEROS_CUDA(cudaMemcpyAsync(c0, C0, ns * 16, cudaMemcpyDefault, h->stream));
+    if (nvec == 2) AEROS_CUDA(cudaMemcpyAsync(c1, C1, ns * 16, cudaMemcpyDefault, h->stream));
+    if (!is_device(c0) || (nvec == 2 && !is_device(c1))) AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// spectral -> grid adjoints (analysis^T for nvec = 1, analysis_vec^T for 2)
+int spec_to_grid_ad(aeros_sht_s *h, int nvec, const double *c0, const double *c1, double *g0, double *g1, int nb) {
+    if (!h || !c0 || !g0 || (nvec == 2 && (!c1 || !g1)) || nb < 1 || nb > h->batch_max) return AEROS_ERR_ARG;
+    const size_t ng = (size_t)h->g.nlon * h->g.nlat * nb, ns = (size_t)h->g.nlm * nb;
+    int rc;
+    if ((rc = ensure_ad(h, 2 * ng * sizeof(double) + 2 * ns * sizeof(double2)))) return rc;
+    double *G0 = h->adbuf, *G1 = G0 + ng;
+    double2 *C0 = reinterpret_cast<double2 *>(G1 + ng), *C1 = C0 + ns;
+    Ctx c = h->ctx();
+    AEROS_CUDA(cudaMemcpyAsync(C0, c0, ns * 16, cudaMemcpyDefault, h->stream));
+    if (nvec == 2) AEROS_CUDA(cudaMemcpyAsync(C1, c1, ns * 16, cudaMemcpyDefault, h->stream));
+    launch_spec_axpy(h->stream, C0, C0, nvec * nb, c, 1.0, -1, nvec == 2 ? -1 : 0, 0);
+    rc = nvec == 1 ? aeros_sht_synthesis(h, reinterpret_cast<double *>(C0), G0, nb)
+                   : aeros_sht_synthesis_vec(h, reinterpret_cast<double *>(C0), reinterpret_cast<double *>(C1), G0, G1,
+                                             nb);
+    if (rc) return rc;
+    launch_grid_wscale(h->stream, G0, nvec * nb, c, 1.0, 1);
+    AEROS_CUDA(cudaMemcpyAsync(g0, G0, ng * 8, cudaMemcpyDefault, h->stream));
+    if (nvec == 2) AEROS_CUDA(cudaMemcpyAsync(g1, G1, ng * 8, cudaMemcpyDefault, h->stream));
+    if (!is_device(g0) || (nvec == 2 && !is_device(g1))) AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int aeros_sht_synthesis_ad(aeros_sht_t h, const double *field_ad, double *coeffs_ad, int nbatch) {
+    return grid_to_spec_ad(h, 1, field_ad, nullptr, coeffs_ad, nullptr, nbatch);
+}
+
+int aeros_sht_analysis_ad(aeros_sht_t h, const double *coeffs_ad, double *field_ad, int nbatch) {
+    return spec_to_grid_ad(h, 1, coeffs_ad, nullptr, field_ad, nullptr, nbatch);
+}
+
+int aeros_sht_synthesis_vec_ad(aeros_sht_t h, const double *vth_ad, const double *vph_ad, double *slm_ad,
+                               double *tlm_ad, int nbatch) {
+    return grid_to_spec_ad(h, 2, vth_ad, vph_ad, slm_ad, tlm_ad, nbatch);
+}
+
+int aeros_sht_analysis_vec_ad(aeros_sht_t h, const double *slm_ad, const double *tlm_ad, double *vth_ad,
+                              double *vph_ad, int nbatch) {
+    return spec_to_grid_ad(h, 2, slm_ad, tlm_ad, vth_ad, vph_ad, nbatch);
 }
 
 }  // extern "C"

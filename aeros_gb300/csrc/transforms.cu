@@ -1,3 +1,4 @@
+#include <algorithm>
 // transforms.cu -- FP64 spherical-harmonic transform kernels for sm_103a.
 //
 // A synthesis is two launches: the per-m Legendre contraction (spectral ->
@@ -425,6 +426,50 @@ int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const dou
 }
 
 // ============================================================ elementwise helpers
+// y (+)= f Dm^dm (l(l+1))^lp x  (adjoint factors; see aeros_internal.h)
+__global__ void k_spec_axpy(double2 *__restrict__ y, const double2 *__restrict__ x, int nf, int nlm,
+                            const int *__restrict__ l_of_lm, const int *__restrict__ m_of_lm, int nlon, double f0,
+                            int dm, int lp, int accumulate) {
+    const size_t n = (size_t)nf * nlm;
+    const double dfull = nlon / (2.0 * kPi);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int lm = (int)(i % nlm), l = l_of_lm[lm];
+        const double D = (m_of_lm[lm] == 0 ? 1.0 : 2.0) * dfull, ll = (double)l * (l + 1);
+        double f = f0;
+        if (dm > 0) f *= D;
+        if (dm < 0) f /= D;
+        if (lp > 0) f *= ll;
+        if (lp < 0) f = l > 0 ? f / ll : 0.0;
+        const double2 v = x[i];
+        double2 r = make_double2(f * v.x, f * v.y);
+        if (accumulate) r = make_double2(y[i].x + r.x, y[i].y + r.y);
+        y[i] = r;
+    }
+}
+
+__global__ void k_grid_wscale(double *__restrict__ g, int nf, int nlat, int nlon, const double *__restrict__ w,
+                              double f, int wp) {
+    const size_t n = (size_t)nf * nlat * nlon;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)((i / nlon) % nlat);
+        g[i] *= wp > 0 ? f * w[j] : (wp < 0 ? f / w[j] : f);
+    }
+}
+
+static unsigned grid_blocks(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 4096); }
+
+void launch_spec_axpy(cudaStream_t st, double2 *y, const double2 *x, int nf, const Ctx &c, double f, int dm, int lp,
+                      int accumulate) {
+    k_spec_axpy<<<grid_blocks((size_t)nf * c.nlm), 256, 0, st>>>(y, x, nf, c.nlm, c.tab->l_of_lm, c.tab->m_of_lm,
+                                                                 c.nlon, f, dm, lp, accumulate);
+    if (c.launches) ++*c.launches;
+}
+
+void launch_grid_wscale(cudaStream_t st, double *g, int nf, const Ctx &c, double f, int wp) {
+    k_grid_wscale<<<grid_blocks((size_t)nf * c.nlon * c.nlat), 256, 0, st>>>(g, nf, c.nlat, c.nlon, c.tab->w, f, wp);
+    if (c.launches) ++*c.launches;
+}
+
 __global__ void k_laplacian(double2 *c, int nlm, int nb, int inverse, const int *__restrict__ l_of_lm) {
     const double a2 = kA * kA;
     for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < (long)nlm * nb;

@@ -211,6 +211,57 @@ class AerosDyn:
         _capi.lib().aeros_dyn_launch_count(self._h, ctypes.byref(c))
         return c.value
 
+    # ------------------------------------------------------------------ adjoint
+    # Packed state: vor (M, nlev, nlm) | div | temp | lnps (M, nlm), complex128.
+    def pack(self, vor, div, temp, lnps):
+        M = self.nmember
+        parts = [np.asarray(vor, np.complex128).reshape(M, -1), np.asarray(div, np.complex128).reshape(M, -1),
+                 np.asarray(temp, np.complex128).reshape(M, -1), np.asarray(lnps, np.complex128).reshape(M, -1)]
+        return np.concatenate([p.ravel() for p in parts])
+
+    def unpack(self, x):
+        M, n3 = self.nmember, self.nmember * self.nlev * self.nlm
+        s3 = self._shape3()
+        out = (x[:n3].reshape(s3), x[n3:2 * n3].reshape(s3), x[2 * n3:3 * n3].reshape(s3),
+               x[3 * n3:].reshape(M, self.nlm))
+        return self._squeeze(out)
+
+    def state_size(self):
+        n = ctypes.c_longlong()
+        _capi.check(_capi.lib().aeros_dyn_state_size(self._h, ctypes.byref(n)), "aeros_dyn_state_size")
+        return n.value
+
+    def step_ad(self, old_ad, now_ad):
+        """Adjoint of the next step (state unchanged): packed adjoints of the
+        post-step (old, now) slots -> packed adjoints of the pre-step slots,
+        and per-member d/dk_a, d/ddT_y."""
+        n = self.state_size()
+        oi = np.ascontiguousarray(old_ad, np.complex128)
+        ni = np.ascontiguousarray(now_ad, np.complex128)
+        assert oi.size == n and ni.size == n
+        oo, no = np.zeros(n, np.complex128), np.zeros(n, np.complex128)
+        ka, dty = np.zeros(self.nmember), np.zeros(self.nmember)
+        _capi.check(_capi.lib().aeros_dyn_step_ad(self._h, _ptr(oi), _ptr(ni), _ptr(oo), _ptr(no), _ptr(ka),
+                                                  _ptr(dty)), "aeros_dyn_step_ad")
+        return oo, no, ka, dty
+
+    def window_forward(self, nsteps, ckpt_every=12):
+        """Step nsteps with checkpoints; J per member (window-mean kinetic energy, J)."""
+        J = np.zeros(self.nmember)
+        _capi.check(_capi.lib().aeros_dyn_window_forward(self._h, int(nsteps), int(ckpt_every), _ptr(J)),
+                    "aeros_dyn_window_forward")
+        return J
+
+    def window_backward(self):
+        """Gradient of sum(J) w.r.t. the window's initial state (packed now, old)
+        and the members' k_a, dT_y."""
+        n = self.state_size()
+        now, old = np.zeros(n, np.complex128), np.zeros(n, np.complex128)
+        ka, dty = np.zeros(self.nmember), np.zeros(self.nmember)
+        _capi.check(_capi.lib().aeros_dyn_window_backward(self._h, _ptr(now), _ptr(old), _ptr(ka), _ptr(dty)),
+                    "aeros_dyn_window_backward")
+        return now, old, ka, dty
+
 
 class AerosGroup:
     """Several AerosDyn handles stepped by one CUDA graph launch per step.

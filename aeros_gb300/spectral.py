@@ -147,6 +147,38 @@ class AerosSHT:
                                                        self._nb_grid(a)), "aeros_sht_analysis_vec")
         return s, t
 
+    # ---- adjoints (Euclidean inner products of the arrays; m = 0 imaginary
+    # parts are not degrees of freedom)
+    def synthesis_ad(self, field_ad):
+        """coeffs_ad = synthesis^T field_ad."""
+        f = self._grid_in(field_ad)
+        c = self._spec_out(f, tuple(f.shape[:-2]))
+        _capi.check(_capi.lib().aeros_sht_synthesis_ad(self._h, _ptr(f), _ptr(c), self._nb_grid(f)),
+                    "aeros_sht_synthesis_ad")
+        return c
+
+    def analysis_ad(self, coeffs_ad):
+        """field_ad = analysis^T coeffs_ad."""
+        c = self._spec_in(coeffs_ad)
+        f = self._grid_out(c, tuple(c.shape[:-1]))
+        _capi.check(_capi.lib().aeros_sht_analysis_ad(self._h, _ptr(c), _ptr(f), self._nb_spec(c)),
+                    "aeros_sht_analysis_ad")
+        return f
+
+    def synthesis_vec_ad(self, vth_ad, vph_ad):
+        a, b = self._grid_in(vth_ad), self._grid_in(vph_ad)
+        s, t = self._spec_out(a, tuple(a.shape[:-2])), self._spec_out(a, tuple(a.shape[:-2]))
+        _capi.check(_capi.lib().aeros_sht_synthesis_vec_ad(self._h, _ptr(a), _ptr(b), _ptr(s), _ptr(t),
+                                                           self._nb_grid(a)), "aeros_sht_synthesis_vec_ad")
+        return s, t
+
+    def analysis_vec_ad(self, slm_ad, tlm_ad):
+        s, t = self._spec_in(slm_ad), self._spec_in(tlm_ad)
+        a, b = self._grid_out(s, tuple(s.shape[:-1])), self._grid_out(s, tuple(s.shape[:-1]))
+        _capi.check(_capi.lib().aeros_sht_analysis_vec_ad(self._h, _ptr(s), _ptr(t), _ptr(a), _ptr(b),
+                                                          self._nb_spec(s)), "aeros_sht_analysis_vec_ad")
+        return a, b
+
     def gradient(self, coeffs):
         """(dF/dtheta, (1/sin theta) dF/dphi) on the unit sphere (SHsph_to_spat)."""
         c = self._spec_in(coeffs)

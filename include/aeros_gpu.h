@@ -259,6 +259,8 @@ int aeros_dyn_budget(aeros_dyn_t h, double *mass, double *energy, double *angmom
  * corrections of member 0 (src/dynamics/aeros_timestep.f90:1225-1301). */
 int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target,
                        double *lnr_last, double *lnr_cum);
+/* Set every member's target mass [kg]; a negative value clears it, so the
+ * next start-up step captures it again (restarting from a new state). */
 int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass);
 
 /* Zonal-mean statistics (src/aeros_diagnostics.f90:153-276): accumulate one
@@ -294,6 +296,50 @@ int aeros_group_step(aeros_group_t g, int nsteps);
 int aeros_group_step_async(aeros_group_t g, int nsteps);
 int aeros_group_sync(aeros_group_t g);
 int aeros_group_launch_count(aeros_group_t g, long long *count);
+
+/* ======================================================================== */
+/* Differentiation: adjoints of the transforms and of the step              */
+/* (no reference counterpart: aeros has no adjoint).  Inner products are     */
+/* the Euclidean ones of the arrays: sum of grid values, and sum over        */
+/* (l, m) of Re(conj(a) b) for spectral arrays; m = 0 imaginary parts are    */
+/* not degrees of freedom.  Same argument conventions (host or device        */
+/* pointers, batches) as the forward transforms.                             */
+/* ======================================================================== */
+/* coeffs_ad = synthesis^T field_ad */
+int aeros_sht_synthesis_ad(aeros_sht_t h, const double *field_ad, double *coeffs_ad, int nbatch);
+/* field_ad = analysis^T coeffs_ad */
+int aeros_sht_analysis_ad(aeros_sht_t h, const double *coeffs_ad, double *field_ad, int nbatch);
+/* (slm_ad, tlm_ad) = synthesis_vec^T (vth_ad, vph_ad) */
+int aeros_sht_synthesis_vec_ad(aeros_sht_t h, const double *vth_ad, const double *vph_ad, double *slm_ad,
+                               double *tlm_ad, int nbatch);
+/* (vth_ad, vph_ad) = analysis_vec^T (slm_ad, tlm_ad) */
+int aeros_sht_analysis_vec_ad(aeros_sht_t h, const double *slm_ad, const double *tlm_ad, double *vth_ad,
+                              double *vph_ad, int nbatch);
+
+/* Complex entries of a packed state: M (3 nlev + 1) nlm, laid out as
+ * vor (M, nlev, nlm) | div | temp | lnps (M, nlm) -- the order of
+ * aeros_dyn_set_state's four arrays, concatenated. */
+int aeros_dyn_state_size(aeros_dyn_t h, long long *n);
+
+/* Adjoint of the next step (the one aeros_dyn_step(h, 1) would take from the
+ * current state; the state is left unchanged).  In: adjoints of the post-step
+ * old slot (the RAW-filtered X^n) and now slot (X^(n+1)), packed.  Out:
+ * adjoints of the pre-step old (X^(n-1)) and now (X^n) slots, packed, and per
+ * member d/dk_a, d/ddT_y (any output may be NULL). */
+int aeros_dyn_step_ad(aeros_dyn_t h, const double *old_ad_in, const double *now_ad_in, double *old_ad_out,
+                      double *now_ad_out, double *ka_ad, double *dty_ad);
+
+/* Forward half of the window pair: step nsteps from the current state,
+ * keeping a checkpoint every ckpt_every steps, and return per member
+ * J = (1/nsteps) sum_{n=1..nsteps} sum_k int (u^2 + v^2)/2 dp_k/g dA [J],
+ * the window mean of the kinetic part of aeros_budget's energy. */
+int aeros_dyn_window_forward(aeros_dyn_t h, int nsteps, int ckpt_every, double *J);
+
+/* Backward half: gradient of sum_e J_e with respect to the state at the start
+ * of the window (packed, now and old slots; the old slot's is zero when the
+ * window starts at step 0) and to each member's k_a and dT_y.  Segments are
+ * recomputed from the checkpoints; the handle is left at the end of the window. */
+int aeros_dyn_window_backward(aeros_dyn_t h, double *now_ad, double *old_ad, double *ka_ad, double *dty_ad);
 
 /* Last CUDA error string for diagnostics (static storage). */
 const char *aeros_last_error(void);
