@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -219,6 +220,54 @@ def split_form(args, sht, dyn_fp64, flush, torch):
     return {"sypd": sypd(t), "ms_per_step": t * 1e3,
             "max_rel_diff_vs_fp64_gpu_after_24_steps": err,
             "legendre": "tcgen05 bf16 Ozaki digits (55 bits), exact int64 recombination"}
+
+
+def adjoint_form(args):
+    """Differentiation form: gradient of the window-mean kinetic energy over a
+    96-step T42L20 window (dt 1800 s, checkpoints every 12 steps) from a seeded
+    red-spectrum state (vorticity 1e-5/l^2 s^-1, divergence 0.2 of it,
+    temperature 1 K/l about 264 K, seed 2); forward and backward wall time
+    (synchronised) and a central-difference check of dJ/dk_a."""
+    import numpy as np
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from aeros_gb300.spectral import AerosSHT
+    d = AerosDyn(held_suarez_params(trunc=args.trunc, nlev=args.nlev))
+    s = AerosSHT(args.trunc, batch_max=1)
+    rng = np.random.default_rng(2)
+    L, M = np.asarray(s.l_of_lm, float), np.asarray(s.m_of_lm)
+
+    def red(shape, slope):
+        c = (rng.standard_normal(shape + (len(L),)) + 1j * rng.standard_normal(shape + (len(L),))) * (L + 1) ** slope
+        c[..., M == 0] = c[..., M == 0].real
+        return c
+    d.set_isothermal(264.0, 1.0e5)
+    _, _, t, lnps = d.get_state()
+    vor, div = 1e-5 * red((d.nlev,), -2.0), 2e-6 * red((d.nlev,), -2.0)
+    vor[:, 0] = 0
+    div[:, 0] = 0
+    x0 = (vor, div, t + red((d.nlev,), -1.0), lnps)
+    nst, every = 96, 12
+    ka0 = d.params.hs_k_a
+
+    def J(ka=ka0):
+        d.set_member_forcing(0, d.params.hs_dt_y, ka)
+        d.set_mass_target(-1.0)
+        d.set_state(*x0)
+        return float(d.window_forward(nst, every)[0])
+    J()
+    d.window_backward()   # warm-up
+    t0 = time.perf_counter()
+    j0 = J()
+    t1 = time.perf_counter()
+    _, _, ka_b, dty_b = d.window_backward()
+    t2 = time.perf_counter()
+    e = 1e-4 * ka0
+    fd = (J(ka0 + e) - J(ka0 - e)) / (2 * e)
+    return {"workload": f"T{args.trunc}L{args.nlev} window of {nst} steps, checkpoints every {every}",
+            "J": j0, "forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+            "backward_over_forward": (t2 - t1) / (t1 - t0), "dJ_dka": float(ka_b[0]), "dJ_ddTy": float(dty_b[0]),
+            "fd_rel_err_ka": abs(fd - ka_b[0]) / abs(ka_b[0])}
 
 
 def batched_form(args, torch):
@@ -451,6 +500,10 @@ def run_gpu(args, rank, world, local):
                 if isinstance(batched[k], dict) and "sypd" in batched[k]:
                     batched[k]["vs_fp64_single"] = batched[k]["sypd"] / sypd(t_gpu)
 
+    adjoint = None
+    if not args.no_adjoint and rank == 0:
+        adjoint = adjoint_form(args)
+
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1) else None
     if rank == 0:
         line = {"metric": METRIC, "value": sypd(t_gpu) * world, "unit": "SYPD", "n_gpus": world, "steps": K,
@@ -462,7 +515,7 @@ def run_gpu(args, rank, world, local):
                 "ms_per_step_l2_resident": t_warm * 1e3,
                 "sypd_l2_resident": sypd(t_warm) * world,
                 "e2e": e2e, "roofline": roof, "kernels_ms": prof, "cpu_baseline": cpu,
-                "split_precision": split, "batched": batched,
+                "split_precision": split, "batched": batched, "adjoint": adjoint,
                 "clocks": clk, "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if world > 1:

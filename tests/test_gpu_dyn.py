@@ -232,3 +232,17 @@ def test_nonfinite_state_is_reported(gpulib):
     g.set_isothermal(264.0, 1.0e5)
     g.set_state(*g.get_state())
     g.step(1)
+
+
+def test_held_suarez_climate_short(gpulib):
+    """A short T21L8 Held-Suarez climate (300 days, the last 100 averaged, two
+    members) develops the published circulation: westerly jets near +-45 deg in
+    the upper troposphere, poleward [v'T'] with its maximum low down, tropical
+    surface easterlies."""
+    from aeros_gb300.hs_climate import run
+    r = run(trunc=21, nlev=8, days=300, spinup=200, members=2)
+    print("T21L8 300-day HS summary", {k: r[k] for k in ("jet_nh", "jet_sh", "vT_max", "u_surface_tropics_min")})
+    for jet in (r["jet_nh"], r["jet_sh"]):
+        assert jet["u_max"] > 15.0 and 25.0 < abs(jet["lat"]) < 65.0 and jet["p_hpa"] < 500.0
+    assert r["vT_max"]["value"] > 5.0 and r["vT_max"]["p_hpa"] > 600.0
+    assert r["u_surface_tropics_min"] < 0.0
