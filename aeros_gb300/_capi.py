@@ -108,6 +108,8 @@ _PROTOS = {
     "aeros_dyn_step_ad": [_vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "aeros_dyn_window_forward": [_vp, _i, _i, _vp],
     "aeros_dyn_window_backward": [_vp, _vp, _vp, _vp, _vp],
+    "aeros_dyn_autotune": [_vp, _i, _dp, _dp],
+    "aeros_dyn_tune_get": [_vp, _vp],
     "aeros_last_error": [],
 }
 _RESTYPE = {"aeros_last_error": ctypes.c_char_p}

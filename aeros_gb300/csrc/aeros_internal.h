@@ -108,13 +108,25 @@ struct DevTables {
 int upload_tables(const Geometry &g, DevTables &t);
 void free_tables(DevTables &t);
 
+// Launch shapes chosen by the autotuner (0 / defaults: the built-in heuristics).
+struct Tune {
+    int fs_lpb = 0, fs_thr = 256;   // Fourier synthesis: latitudes per CTA, threads
+    int fa_lpb = 0, fa_thr = 256;   // Fourier analysis
+    int la_ct = 8;                  // FP64 Legendre analysis: output columns (warps) per CTA: 4, 8 or 16
+    int col_thr = 64;               // column kernel threads per CTA
+    int spec_warps = 4;             // spectral kernel warps per CTA
+};
+
 // Launch context for the transform kernels.
 struct Ctx {
     int T, nlon, nlat, nh, nlm, ms;
     const DevTables *tab;
     cudaStream_t stream;
     long long *launches;         // launch counter (host)
+    const Tune *tune = nullptr;  // launch shapes (nullptr: defaults)
 };
+// Largest latitude count per Fourier CTA that fits `smem_per_lat` bytes in 200 KB.
+int fourier_lpb_limit(size_t smem_per_lat);
 
 // ---------------------------------------------------------------- kernels
 // Legendre synthesis plan: columns [0, ncolD_first) produce Pbar sums only,

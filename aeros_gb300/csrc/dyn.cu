@@ -50,7 +50,7 @@ __constant__ HsConst c_hs;
 // Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
 // dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy.  Outputs GA[e][f][j][i]:
 // ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.  One thread per column.
-__global__ void __launch_bounds__(64) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
+__global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
                                                int nlon, int nlat, int M, const double *__restrict__ xlat,
                                                const double *__restrict__ phis, int hs_on,
                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
@@ -209,7 +209,7 @@ __device__ __forceinline__ double2 wsum2(double2 v) {
     return v;
 }
 
-__global__ void __launch_bounds__(128) k_spectral(SpecArgs a) {
+__global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
     __shared__ double sG[kMaxLev * kMaxLev], sT[kMaxLev * kMaxLev], sW[kMaxLev * kMaxLev];
     __shared__ double sNu[kMaxLev], sPc[kMaxLev];
     const int NL = a.NL;
@@ -559,6 +559,10 @@ int lu_inverse(std::vector<double> &A, int n, std::vector<double> &inv) {
 // =========================================================================
 struct AdjCtx;                      // adjoint workspace (dyn_adjoint.cuh)
 void adj_release(AdjCtx *a);
+struct aeros_dyn_s;
+namespace {
+bool tune_load(aeros_dyn_s &d);   // dyn_tune.cuh
+}
 
 struct aeros_dyn_s {
     aeros_params par{};
@@ -606,6 +610,7 @@ struct aeros_dyn_s {
     size_t stage_bytes = 0;
     SplitCtx *split = nullptr;
     AdjCtx *adj = nullptr;
+    Tune tune;                                       // launch shapes (aeros_dyn_autotune)
 
     size_t ns3() const { return (size_t)NL * g.nlm; }
     size_t nstate() const { return (size_t)M * (3 * ns3() + g.nlm); }
@@ -613,7 +618,7 @@ struct aeros_dyn_s {
     double2 *div(double2 *b) const { return b + (size_t)M * ns3(); }
     double2 *tmp(double2 *b) const { return b + (size_t)2 * M * ns3(); }
     double2 *lnp(double2 *b) const { return b + (size_t)3 * M * ns3(); }
-    Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches}; }
+    Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches, &tune}; }
 };
 
 namespace {
@@ -908,7 +913,8 @@ int run_tendency(Dyn &d, int hs_on) {
     if ((rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS))) return rc;
     mark(d, "fourier_synth");
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
-    k_column<<<(unsigned)((ncol + 63) / 64), 64, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
+    const int ct = d.tune.col_thr;
+    k_column<<<(unsigned)((ncol + ct - 1) / ct), ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
                                                                   d.xlat_d, d.phis_set ? d.phis_d : nullptr, hs_on,
                                                                   d.hs_dty_d, d.hs_ka_d);
     ++d.launches;
@@ -971,7 +977,8 @@ int enqueue_step(Dyn &d, bool startup) {
     a.raw_on = (!startup && d.par.eps_filter > 0.0) ? 1 : 0;
     a.flag = d.flag;
     long nw = (long)d.g.nlm * d.M;
-    k_spectral<<<(unsigned)((nw + 3) / 4), 128, 0, d.stream>>>(a);
+    const int sw = d.tune.spec_warps;
+    k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "spectral");
@@ -1143,6 +1150,7 @@ int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_ha
         int rows = (int)(M * std::max(8 * NL + 2, 4 * NL + 1));
         if ((rc = split_create(d->g, d->tab, rows, &d->split))) { destroy(d); return rc; }
     }
+    tune_load(*d);   // launch shapes of an earlier aeros_dyn_autotune (AEROS_TUNE_CACHE)
     if ((rc = capture_graphs(*d))) { destroy(d); return rc; }
     *out = d;
     return AEROS_OK;
@@ -1533,3 +1541,4 @@ int aeros_group_launch_count(aeros_group_t g, long long *count) {
 }  // extern "C"
 
 #include "dyn_adjoint.cuh"
+#include "dyn_tune.cuh"

@@ -117,13 +117,17 @@ static int fourier_lpb(int nlon) {
     return lpb;
 }
 
+int fourier_lpb_limit(size_t smem_per_lat) { return (int)std::max<size_t>(1, (200 * 1024) / smem_per_lat); }
+
 int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    int lpb = fourier_lpb(c.nlon);
-    size_t smem = (size_t)(2 * (c.nlon / 2) + c.ms) * lpb * sizeof(double2);
+    const size_t per_lat = (size_t)(2 * (c.nlon / 2) + c.ms) * sizeof(double2);
+    int lpb = c.tune && c.tune->fs_lpb > 0 ? std::min(c.tune->fs_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
+    const int thr = c.tune ? c.tune->fs_thr : 256;
+    size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
     if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fourier_synth<<<grid, 256, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+    k_fourier_synth<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
                                                    c.tab->tw, c.tab->twN, c.tab->sint);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
@@ -132,11 +136,13 @@ int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const 
 
 int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    int lpb = fourier_lpb(c.nlon);
-    size_t smem = (size_t)2 * lpb * (c.nlon / 2) * sizeof(double2);
+    const size_t per_lat = (size_t)2 * (c.nlon / 2) * sizeof(double2);
+    int lpb = c.tune && c.tune->fa_lpb > 0 ? std::min(c.tune->fa_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
+    const int thr = c.tune ? c.tune->fa_thr : 256;
+    size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
     if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_anal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_fourier_anal<<<grid, 256, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+    k_fourier_anal<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
                                                   c.tab->tw, c.tab->twN);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
@@ -294,10 +300,10 @@ int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) 
 // CTA = (m, column tile, l tile).  Warp = one output column, lanes = degrees
 // (split into j partitions when the tile is narrower than 32).  Inputs are
 // folded to even/odd latitude sums in shared memory.
-constexpr int kAnaCT = 8;       // columns (warps) per CTA
 constexpr int kAnaJC = 16;      // latitudes per smem chunk
 constexpr int kAnaLT = 32;
 
+template <int kAnaCT>   // output columns (warps) per CTA
 __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(
     const AnaCol *__restrict__ cols, int ncol, const double *__restrict__ PaT, const double *__restrict__ dPaT,
     const double *__restrict__ lfac, const double *__restrict__ isin, const int *__restrict__ moff,
@@ -417,9 +423,15 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(
 
 int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
     if (ncol <= 0) return AEROS_OK;
-    dim3 grid(c.T + 1, (ncol + kAnaCT - 1) / kAnaCT, (c.T + 1 + kAnaLT - 1) / kAnaLT);
-    k_leg_anal_fp64<<<grid, kAnaCT * 32, 0, c.stream>>>(cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac,
-                                                       c.tab->sint, c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+    const int ct = c.tune ? c.tune->la_ct : 8;
+    auto go = [&](auto kern, int CT) {
+        dim3 grid(c.T + 1, (ncol + CT - 1) / CT, (c.T + 1 + kAnaLT - 1) / kAnaLT);
+        kern<<<grid, CT * 32, 0, c.stream>>>(cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac, c.tab->sint,
+                                             c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+    };
+    if (ct == 4) go(k_leg_anal_fp64<4>, 4);
+    else if (ct == 16) go(k_leg_anal_fp64<16>, 16);
+    else go(k_leg_anal_fp64<8>, 8);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;

@@ -211,6 +211,21 @@ class AerosDyn:
         _capi.lib().aeros_dyn_launch_count(self._h, ctypes.byref(c))
         return c.value
 
+    # ------------------------------------------------------------------ autotuner
+    TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps")
+
+    def autotune(self, reps=3):
+        """Choose launch shapes by timing whole steps; returns (ms before, ms after, shapes)."""
+        b, a = ctypes.c_double(), ctypes.c_double()
+        _capi.check(_capi.lib().aeros_dyn_autotune(self._h, int(reps), ctypes.byref(b), ctypes.byref(a)),
+                    "aeros_dyn_autotune")
+        return b.value, a.value, self.tune_shapes()
+
+    def tune_shapes(self):
+        v = np.zeros(7, np.int32)
+        _capi.check(_capi.lib().aeros_dyn_tune_get(self._h, _ptr(v)), "aeros_dyn_tune_get")
+        return dict(zip(self.TUNE_KEYS, (int(x) for x in v)))
+
     # ------------------------------------------------------------------ adjoint
     # Packed state: vor (M, nlev, nlm) | div | temp | lnps (M, nlm), complex128.
     def pack(self, vor, div, temp, lnps):

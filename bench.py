@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner of the batched form")
     return ap.parse_args()
 
 
@@ -274,7 +275,9 @@ def batched_form(args, torch):
     """Config of 96 uneven members: 32 x T21L16 + 32 x T31L20 + 32 x T42L20,
     each member with its own seed and equator-pole contrast dT_y ~ U(40, 80) K,
     stepped by one CUDA graph launch per step; FP64 and split precision.
-    Working set > L2, so no flush is needed."""
+    Each member handle's launch shapes are chosen by the autotuner before the
+    group is built (outside the timed region).  Working set > L2, so no flush
+    is needed."""
     import numpy as np
     from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
     from aeros_gb300.dynamics import AerosDyn, AerosGroup
@@ -295,6 +298,10 @@ def batched_form(args, torch):
                 t[e] = sht.analysis(sht.synthesis(t[e]) + r.normal(0.0, 0.1, (L, d.nlat, d.nlon)))
                 d.set_member_forcing(e, rng.uniform(40.0, 80.0), 1.0 / (40.0 * 86400.0))
             d.set_state(vor, div, t, lnps)
+            if not args.no_tune:
+                b0, b1, shp = d.autotune(reps=3)
+                out.setdefault("autotune", {}).setdefault(name, {})[f"T{T}L{L}x32"] = {
+                    "ms_before": b0, "ms_after": b1, "shapes": shp}
             hs.append(d)
         g = AerosGroup(hs)
         s = torch.cuda.Stream()
