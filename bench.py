@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the T85/T170/T341 transform sweep")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner of the batched form")
     return ap.parse_args()
 
@@ -221,6 +222,72 @@ def split_form(args, sht, dyn_fp64, flush, torch):
     return {"sypd": sypd(t), "ms_per_step": t * 1e3,
             "max_rel_diff_vs_fp64_gpu_after_24_steps": err,
             "legendre": "tcgen05 bf16 Ozaki digits (55 bits), exact int64 recombination"}
+
+
+def transform_sweep(args, torch):
+    """Standalone transforms at T85, T170 and T341 (256x128, 512x256, 1024x512
+    grids), batch 240 = 30 levels x 8 fields of seeded complex Gaussian
+    coefficients with variance proportional to (l+1)^-3 and real m = 0 (seed 1),
+    device pointers.  FP64 and split precision: synthesis and analysis time
+    (CUDA events on the handle's stream, mean of 5 after 2 warm-up calls), the
+    FP64-equivalent Legendre rate 2 nlat nlm B / t per direction, the split
+    form's relative difference from the FP64 path and its round-trip error."""
+    import numpy as np
+    from aeros_gb300 import _capi
+    from aeros_gb300.spectral import AerosSHT, _ptr
+    L = _capi.lib()
+    B = 240
+    out = {"batch": B}
+    stream = torch.cuda.Stream()
+    for T in (85, 170, 341):
+        hs = [AerosSHT(T, batch_max=B, precision=p) for p in (0, 1)]
+        for h in hs:
+            _capi.check(L.aeros_sht_set_stream(h._h, ctypes_void(stream.cuda_stream)), "aeros_sht_set_stream")
+        h0 = hs[0]
+        rng = np.random.default_rng(1)
+        l = np.asarray(h0.l_of_lm, float)
+        c = (rng.standard_normal((B, h0.nlm)) + 1j * rng.standard_normal((B, h0.nlm))) * (l + 1.0) ** -1.5
+        c[:, np.asarray(h0.m_of_lm) == 0] = c[:, np.asarray(h0.m_of_lm) == 0].real
+        cd = torch.from_numpy(c).cuda()
+        g = [torch.empty((B, h0.nlat, h0.nlon), dtype=torch.float64, device="cuda") for _ in hs]
+        cb = [torch.empty_like(cd) for _ in hs]
+        torch.cuda.synchronize()
+
+        def timeit(fn):
+            for _ in range(2):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(5):
+                fn()
+            e1.record(stream)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / 5.0
+        res = {}
+        flops = 2.0 * h0.nlat * h0.nlm * B
+        for i, name in enumerate(("fp64", "split")):
+            h = hs[i]
+            ts = timeit(lambda: _capi.check(L.aeros_sht_synthesis(h._h, _ptr(cd), _ptr(g[i]), B), "synthesis"))
+            ta = timeit(lambda: _capi.check(L.aeros_sht_analysis(h._h, _ptr(g[i]), _ptr(cb[i]), B), "analysis"))
+            res[name] = {"synthesis_ms": ts, "analysis_ms": ta,
+                         "legendre_equiv_gflops_synthesis": flops / (ts * 1e-3) / 1e9,
+                         "legendre_equiv_gflops_analysis": flops / (ta * 1e-3) / 1e9}
+        torch.cuda.synchronize()
+        rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+        # split analysis of the split synthesis -> round trip; FP64 path as the reference point
+        res["split_vs_fp64_synthesis"] = rel(g[1], g[0])
+        res["split_vs_fp64_analysis"] = rel(cb[1], cb[0])
+        res["split_round_trip"] = rel(cb[1], cd)
+        res["fp64_round_trip"] = rel(cb[0], cd)
+        res["grid"] = f"{h0.nlon}x{h0.nlat}"
+        out[f"T{T}"] = res
+        del hs, g, cb, cd
+    return out
+
+
+def ctypes_void(p):
+    import ctypes
+    return ctypes.c_void_p(p)
 
 
 def adjoint_form(args):
@@ -510,6 +577,9 @@ def run_gpu(args, rank, world, local):
     adjoint = None
     if not args.no_adjoint and rank == 0:
         adjoint = adjoint_form(args)
+    sweep = None
+    if not args.no_sweep and rank == 0:
+        sweep = transform_sweep(args, torch)
 
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1) else None
     if rank == 0:
@@ -522,7 +592,7 @@ def run_gpu(args, rank, world, local):
                 "ms_per_step_l2_resident": t_warm * 1e3,
                 "sypd_l2_resident": sypd(t_warm) * world,
                 "e2e": e2e, "roofline": roof, "kernels_ms": prof, "cpu_baseline": cpu,
-                "split_precision": split, "batched": batched, "adjoint": adjoint,
+                "split_precision": split, "batched": batched, "adjoint": adjoint, "transform_sweep": sweep,
                 "clocks": clk, "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if world > 1:

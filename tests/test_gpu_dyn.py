@@ -246,3 +246,38 @@ def test_held_suarez_climate_short(gpulib):
         assert jet["u_max"] > 15.0 and 25.0 < abs(jet["lat"]) < 65.0 and jet["p_hpa"] < 500.0
     assert r["vT_max"]["value"] > 5.0 and r["vT_max"]["p_hpa"] > 600.0
     assert r["u_surface_tropics_min"] < 0.0
+
+
+def test_config_T31L20_480_steps(gpulib):
+    """The plain-method configuration: T31L20 Held-Suarez from rest (T = 264 K,
+    ps = 1000 hPa) plus N(0, 0.1^2) K on the grid temperature (seed 0), dt =
+    1800 s, 480 steps (10 days), compared with the oracle at step 1 (tendencies)
+    and every 48 steps (state).  The step-1 tendencies of D, T and ln ps agree
+    to the parity bars (the vorticity tendency of a rest state is round-off in
+    both and is compared in absolute terms); the state difference is reported
+    daily and stays below 1e-9 relative over the 10 days."""
+    import os
+    from oracle.pyoracle import OracleSHT, set_threads
+    set_threads(os.cpu_count() or 1)
+    g, o, s = make_pair(31, 20)
+    o.set_isothermal(264.0, 1.0e5)
+    vor, div, t, lnps = o.get_state()
+    rng = np.random.default_rng(0)
+    t = s.analysis(s.synthesis(t) + rng.normal(0.0, 0.1, (20, s.nlat, s.nlon)))
+    g.set_state(vor, div, t, lnps)
+    o.set_state(vor, div, t, lnps)
+    tg, to = g.tendency(), o.tendency()
+    assert np.max(np.abs(tg[0] - to[0])) < 1e-20
+    e_div = relerr(tg[1], to[1])
+    e_t, e_p = relerr(tg[2], to[2]), relerr(tg[3], to[3])
+    print(f"T31L20 step-1 tendencies: div {e_div:.1e}  T {e_t:.1e}  lnps {e_p:.1e}")
+    assert e_t < 1e-12 and e_p < 1e-12 and e_div < 1e-11
+    daily = []
+    for day in range(10):
+        g.step(48)
+        o.step(48)
+        daily.append(max(relerr(a, b) for a, b in zip(g.get_state()[1:], o.get_state()[1:])))
+    ev = relerr(g.get_state()[0], o.get_state()[0])
+    print("T31L20 daily max relative state difference (div, T, lnps):", ["%.1e" % x for x in daily],
+          f"vorticity at day 10 {ev:.1e}")
+    assert max(daily) < 1e-9 and ev < 1e-6

@@ -91,3 +91,28 @@ def test_split_dynamics_step(gpulib):
     print("split T42L20 tendency errors", ["%.1e" % x for x in et], "state after 5 steps",
           ["%.1e" % x for x in es])
     assert max(et) < TOL and max(es) < TOL
+
+
+@pytest.mark.parametrize("T,B", [(85, 240), (170, 240), (341, 30)])
+def test_transform_sweep_vs_oracle(gpulib, T, B):
+    """The transform sweep workload (30 levels x 8 fields at T85/T170; 30 fields
+    at T341 to bound the oracle's time): seeded complex Gaussian coefficients with
+    variance (l+1)^-3.  FP64 path <= 1e-12, split path <= 1e-10 against the
+    oracle, forward and inverse."""
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import PREC_SPLIT, PREC_FP64
+    from oracle.pyoracle import OracleSHT, set_threads
+    import os
+    set_threads(os.cpu_count() or 1)
+    o = OracleSHT(T)
+    rng = np.random.default_rng(1)
+    l = o.l_of_lm.astype(float)
+    c = (rng.standard_normal((B, o.nlm)) + 1j * rng.standard_normal((B, o.nlm))) * (l + 1.0) ** -1.5
+    c[:, o.m_of_lm == 0] = c[:, o.m_of_lm == 0].real
+    fo = o.synthesis(c)
+    co = o.analysis(fo)
+    for prec, tol in ((PREC_FP64, 1e-12), (PREC_SPLIT, 1e-10)):
+        g = AerosSHT(T, batch_max=B, precision=prec)
+        es, ea = relerr(g.synthesis(c), fo), relerr(g.analysis(fo), co)
+        print(f"T{T} B={B} precision {prec}: synthesis {es:.2e} analysis {ea:.2e}")
+        assert es < tol and ea < tol
