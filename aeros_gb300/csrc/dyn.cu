@@ -609,6 +609,7 @@ struct aeros_dyn_s {
     double2 *stage = nullptr;                        // host transfer staging
     size_t stage_bytes = 0;
     SplitCtx *split = nullptr;
+    SplitDft *dft = nullptr;                         // split form's longitude DFT products
     AdjCtx *adj = nullptr;
     Tune tune;                                       // launch shapes (aeros_dyn_autotune)
 
@@ -910,7 +911,11 @@ int run_tendency(Dyn &d, int hs_on) {
         rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
     if (rc) return rc;
     mark(d, "legendre_synth");
-    if ((rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS))) return rc;
+    if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_synth(d.dft))
+        rc = split_fourier_synth(d.dft, c, d.fsS, d.nfsS, d.FS, rowsS);
+    else
+        rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS);
+    if (rc) return rc;
     mark(d, "fourier_synth");
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
     const int ct = d.tune.col_thr;
@@ -920,7 +925,11 @@ int run_tendency(Dyn &d, int hs_on) {
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "column");
-    if ((rc = launch_fourier_anal(c, d.faS, d.nfaS, d.FA, rowsA))) return rc;
+    if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_anal(d.dft))
+        rc = split_fourier_anal(d.dft, c, d.faS, d.nfaS, d.FA, rowsA);
+    else
+        rc = launch_fourier_anal(c, d.faS, d.nfaS, d.FA, rowsA);
+    if (rc) return rc;
     mark(d, "fourier_anal");
     if (d.par.precision == AEROS_PREC_SPLIT && d.split)
         rc = split_leg_anal(d.split, c, d.acS, d.nacS, d.FA, rowsA);
@@ -1071,6 +1080,7 @@ void destroy(Dyn *d) {
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->split) split_destroy(d->split);
+    if (d->dft) split_dft_destroy(d->dft);
     if (d->adj) adj_release(d->adj);
     free_tables(d->tab);
     if (d->own_stream && d->stream) cudaStreamDestroy(d->stream);
@@ -1149,6 +1159,7 @@ int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_ha
     if (p->precision == AEROS_PREC_SPLIT) {
         int rows = (int)(M * std::max(8 * NL + 2, 4 * NL + 1));
         if ((rc = split_create(d->g, d->tab, rows, &d->split))) { destroy(d); return rc; }
+        if ((rc = split_dft_create(d->g, &d->dft))) { destroy(d); return rc; }
     }
     tune_load(*d);   // launch shapes of an earlier aeros_dyn_autotune (AEROS_TUNE_CACHE)
     if ((rc = capture_graphs(*d))) { destroy(d); return rc; }
@@ -1270,7 +1281,8 @@ int aeros_dyn_sync(aeros_dyn_t h) {
         set_error("non-finite value in the spectral state");
         return AEROS_ERR_NONFINITE;
     }
-    return split_check(h->split);
+    int rc = split_check(h->split);
+    return rc ? rc : split_dft_check(h->dft);
 }
 
 int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int name_len, int *nk) {

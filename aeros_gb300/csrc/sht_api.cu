@@ -45,6 +45,7 @@ struct aeros_sht_s {
     long long launches = 0;
     std::map<DescKey, DescSet> cache;
     SplitCtx *split = nullptr;
+    SplitDft *dft = nullptr;              // split form's longitude DFT products
 
     Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches}; }
 };
@@ -202,6 +203,8 @@ int run_synth(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, v
     } else {
         if ((rc = launch_leg_synth_fp64(c, d->syn, h->F, d->nrow))) return rc;
     }
+    if (h->precision == AEROS_PREC_SPLIT && split_dft_has_synth(h->dft))
+        return split_fourier_synth(h->dft, c, d->fsyn, d->nfsyn, h->F, d->nrow);
     return launch_fourier_synth(c, d->fsyn, d->nfsyn, h->F, d->nrow);
 }
 
@@ -210,7 +213,11 @@ int run_anal(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, vo
     int rc = get_desc(h, op, i0, i1, o0, o1, nb, d);
     if (rc) return rc;
     Ctx c = h->ctx();
-    if ((rc = launch_fourier_anal(c, d->fana, d->nfana, h->F, d->nrow))) return rc;
+    if (h->precision == AEROS_PREC_SPLIT && split_dft_has_anal(h->dft))
+        rc = split_fourier_anal(h->dft, c, d->fana, d->nfana, h->F, d->nrow);
+    else
+        rc = launch_fourier_anal(c, d->fana, d->nfana, h->F, d->nrow);
+    if (rc) return rc;
     if (h->precision == AEROS_PREC_SPLIT && h->split)
         return split_leg_anal(h->split, c, d->ana, d->nana, h->F, d->nrow);
     return launch_leg_anal_fp64(c, d->ana, d->nana, h->F, d->nrow);
@@ -243,7 +250,8 @@ int dispatch(aeros_sht_t h, int op, bool in_spec, int nin, int nout, const doubl
         AEROS_CUDA(cudaMemcpyAsync(out0, do0, nO * 8, cudaMemcpyDefault, h->stream));
         if (nout > 1) AEROS_CUDA(cudaMemcpyAsync(out1, do1, nO * 8, cudaMemcpyDefault, h->stream));
         AEROS_CUDA(cudaStreamSynchronize(h->stream));
-        return split_check(h->split);
+        if ((rc = split_check(h->split))) return rc;
+        return split_dft_check(h->dft);
     }
     return AEROS_OK;
 }
@@ -314,6 +322,7 @@ int aeros_sht_destroy(aeros_sht_t h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto &kv : h->cache) free_desc(kv.second);
     if (h->split) split_destroy(h->split);
+    if (h->dft) split_dft_destroy(h->dft);
     free_tables(h->tab);
     if (h->F) cudaFree(h->F);
     if (h->F2) cudaFree(h->F2);
@@ -352,6 +361,7 @@ int aeros_sht_set_precision(aeros_sht_t h, int mode) {
     if (mode == AEROS_PREC_SPLIT && !h->split) {
         int rc = split_create(h->g, h->tab, 4 * h->batch_max, &h->split);
         if (rc) return rc;
+        if ((rc = split_dft_create(h->g, &h->dft))) return rc;
     }
     h->precision = mode;
     return AEROS_OK;

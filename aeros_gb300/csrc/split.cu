@@ -20,7 +20,7 @@
 // Tables (Pbar, dPbar/dtheta and their Gauss-weighted forms) are digitised once
 // per handle on the device into tile images in the canonical K-major,
 // no-swizzle layout (8-row x 16-byte core matrices), one image per (m, tile,
-// 64-wide chunk), which a CTA fetches with one cp.async.bulk.
+// kKC-wide chunk), which a CTA fetches with one cp.async.bulk.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -29,220 +29,15 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include "split.h"
+#include "split_common.cuh"
 
 namespace aeros {
 
 namespace {
 
-constexpr int kTM = 128;     // tile rows (M of one MMA)
-constexpr int kKC = 64;      // contraction chunk
-constexpr int kNTs = 64;     // synthesis tile columns: 32 complex fields x (re, im)
-constexpr int kNTa = 48;     // analysis tile columns: 2 folds x 3 slots x 4 fields x (re, im)
-constexpr int kTmemCols = 512;
-constexpr long long kWaitLimit = 1ll << 26;   // bounded mbarrier polls
-constexpr int kZShift = 40;  // Z = sum_q Y_q 2^(40 - q B)
-constexpr int kThreads = 512;  // 16 warps: 4 per SM sub-partition to hide latency
-constexpr int kSt = kKC + 1;   // staged-value row stride (doubles): conflict-free 8-byte reads
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Operand tiles are K-major with 128-byte rows (64 bf16 of the contraction,
-// zero past the chunk's length) in the 128-byte swizzle: the 16-byte chunk c of
-// row r sits at chunk c ^ (r & 7) of the row, 8-row groups are 1024 bytes apart,
-// and every tile starts on a 1024-byte boundary.  Element index of (r, k):
-__host__ __device__ __forceinline__ int swz(int r, int k) {
-    return r * 64 + ((((k >> 3) ^ r) & 7) << 3) + (k & 7);
-}
-constexpr int kSlice = 64;   // elements per tile row
-
-// smem descriptor of a swizzled K-major tile whose row 0 starts at saddr (plus
-// the byte offset of the K step inside the 128-byte row)
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-    d |= (uint64_t)1 << 16;                  // LBO (unused by swizzled K-major layouts)
-    d |= (uint64_t)(1024 >> 4) << 32;        // SBO: next 8-row group
-    d |= (uint64_t)1 << 46;                  // tcgen05 descriptor version
-    d |= (uint64_t)2 << 61;                  // 128-byte swizzle
-    return d;
-}
-
-__device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
-        "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *mbar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)));
-}
-
-// Bulk copy global -> shared of `bytes` (multiple of 16, both ends 16-byte
-// aligned), completing on `mbar` (which this call also arms).
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes));
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(mbar))
-                 : "memory");
-}
-
-// Bounded wait on an mbarrier phase; returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase) {
-    uint32_t done = 0;
-    for (long long it = 0; it < kWaitLimit; ++it) {
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(smem_u32(mbar)), "r"(phase));
-        if (done) return true;
-        if (it > 64) __nanosleep(64);
-    }
-    return false;
-}
-
-template <int N>
-__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t *r);
-template <>
-__device__ __forceinline__ void tmem_ld<8>(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
-}
-template <>
-__device__ __forceinline__ void tmem_ld<4>(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(taddr));
-}
-template <>
-__device__ __forceinline__ void tmem_ld<2>(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;"); }
-
-// ------------------------------------------------------------------ integer digit arithmetic
-// Biased exponent field of x (0 for zero and subnormals).
-__device__ __forceinline__ int bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
-// Scale exponent e with |x| < 2^e for every x of a row/column whose largest
-// biased exponent is be (0 -> all zero, any e works).
-__device__ __forceinline__ int scale_exp(int be) { return be ? be - 1022 : 0; }
-
-// round(x 2^(55 - e)) as an integer, for |x| < 2^e; subnormals count as 0.
-__device__ __forceinline__ long long fixed55(double x, int e) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int be = (int)((bits >> 52) & 0x7FF);
-    if (be == 0) return 0;
-    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1020 - be + e;   // right shift; >= -2 because |x| < 2^e
-    long long v;
-    if (sh <= 0) v = (long long)(mant << (-sh));
-    else if (sh >= 54) v = 0;
-    else v = (long long)((mant + (1ull << (sh - 1))) >> sh);
-    return (bits >> 63) ? -v : v;
-}
-
-// fp32 bit pattern of a small integer d (|d| < 2^22); its upper half is the
-// bf16 pattern, exact when |d| <= 256
-__device__ __forceinline__ uint32_t f32_bits(int d) {
-    return __float_as_uint(__int_as_float(0x4B400000 + d) - 12582912.0f);
-}
-// fp32 bit pattern of (byte k of x) - 128
-template <int k>
-__device__ __forceinline__ uint32_t f32_byte(uint32_t x) {
-    return __float_as_uint(__uint_as_float(__byte_perm(x, 0x4B000000u, 0x7650 + k)) - 8388736.0f);
-}
-
-// Balanced base-2^B digits of v (most significant first) as fp32 bit patterns.
-template <int S, int B>
-struct Digits {
-    static __device__ __forceinline__ void cut(long long v, uint32_t *h) {
-        constexpr unsigned long long half = 1ull << (B - 1);
-        unsigned long long C = 0;
-#pragma unroll
-        for (int i = 0; i < S - 1; ++i) C |= half << (i * B);
-        const unsigned long long u = (unsigned long long)v + C;
-#pragma unroll
-        for (int s = 1; s < S; ++s) h[s] = f32_bits((int)((u >> ((S - 1 - s) * B)) & ((1ull << B) - 1)) - (int)half);
-        h[0] = f32_bits((int)((long long)u >> ((S - 1) * B)));
-    }
-};
-// B = 8: the lower digits are the bytes of v + 0x808080808080, less 128.
-template <>
-struct Digits<7, 8> {
-    static __device__ __forceinline__ void cut(long long v, uint32_t *h) {
-        const unsigned long long u = (unsigned long long)v + 0x0000808080808080ull;
-        const uint32_t lo = (uint32_t)u, hi = (uint32_t)(u >> 32);
-        h[6] = f32_byte<0>(lo);
-        h[5] = f32_byte<1>(lo);
-        h[4] = f32_byte<2>(lo);
-        h[3] = f32_byte<3>(lo);
-        h[2] = f32_byte<0>(hi);
-        h[1] = f32_byte<1>(hi);
-        h[0] = f32_bits((int)hi >> 16);
-    }
-};
-
-// bf16 pair (lo, hi) from two fp32 patterns holding exact bf16 values
-__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) { return __byte_perm(lo, hi, 0x7632); }
-
-// Write the S digit slices of 8 consecutive contraction entries x[0..7] of tile
-// row n (16 bytes per slice) into the K-major tile images at `tile`
-// (slice stride `slice_elems`), scale exponent e.
-template <int S, int B>
-__device__ __forceinline__ void put8(const double *x, int e, __nv_bfloat16 *tile, size_t slice_elems, int n, int k0) {
-    uint32_t h[8][S];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) Digits<S, B>::cut(fixed55(x[i], e), h[i]);
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        uint4 w;
-        w.x = pack_bf16(h[0][s], h[1][s]);
-        w.y = pack_bf16(h[2][s], h[3][s]);
-        w.z = pack_bf16(h[4][s], h[5][s]);
-        w.w = pack_bf16(h[6][s], h[7][s]);
-        *reinterpret_cast<uint4 *>(tile + (size_t)s * slice_elems + swz(n, k0)) = w;
-    }
-}
-
-// Accumulator Y (fp32 holding an exact integer) shifted into the Z window.
-template <int B>
-__device__ __forceinline__ long long zterm(uint32_t y, int q) {
-    const int v = __float2int_rn(__uint_as_float(y));
-    const int sh = kZShift - q * B;
-    return sh >= 0 ? ((long long)v << sh) : (long long)(v >> (-sh));
-}
-
-// z 2^E as a double (round to nearest, ties away); 0 below the normal range
-// (|z| < 2^63, so no overflow is possible for the exponents used here).
-__device__ __forceinline__ double z_to_f64(long long z, int E) {
-    const unsigned long long sgn = (unsigned long long)z & 0x8000000000000000ull;
-    const unsigned long long m = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
-    const int lz = __clzll((long long)m);
-    const unsigned long long n = m << (lz & 63);               // leading one at bit 63
-    const unsigned long long r = (n >> 11) + ((n >> 10) & 1);  // 53-bit mantissa, 2^53 on carry
-    const int be = 63 - lz + E + 1023;
-    // (be - 1) 2^52 + r carries a rounded-up mantissa into the exponent
-    const unsigned long long bits = sgn | (((unsigned long long)(be - 1) << 52) + r);
-    return (m == 0 || be <= 0) ? 0.0 : __longlong_as_double((long long)bits);
-}
-
-// Result exponent: sum_k A B = Z 2^(e_row + e_col - 2B - 38).
-template <int B>
-__device__ __forceinline__ int zexp(int er, int ec) { return er + ec - 2 * B - 38; }
+constexpr int kNTs = kNTile;   // synthesis tile columns: 16 complex fields x (re, im)
+constexpr int kNTa = kNTile;   // analysis tile columns: 2 folds x 3 slots x 2 fields x (re, im), 24 used
+constexpr int kFa = 2;         // analysis fields per tile
 
 // ------------------------------------------------------------------ table prep
 // Synthesis tables: tile image (m, lat tile t, chunk ch): rows r = blk*32 + jj
@@ -270,8 +65,8 @@ __global__ void k_prep_synth_dig(const double *__restrict__ Ps, const double *__
     const int K = T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
     if (ch >= nch) return;
     __nv_bfloat16 *tile = dig + sbase[m] + ((size_t)t * nch + ch) * S * kTM * kSlice;
-    for (int idx = threadIdx.x; idx < kTM * 8; idx += blockDim.x) {
-        const int r = idx >> 3, k0 = (idx & 7) * 8;
+    for (int idx = threadIdx.x; idx < kTM * (kKC / 8); idx += blockDim.x) {
+        const int r = idx / (kKC / 8), k0 = (idx % (kKC / 8)) * 8;
         const int blk = r >> 5, j = t * 32 + (r & 31);
         double x[8];
         for (int i = 0; i < 8; ++i) {
@@ -306,8 +101,8 @@ __global__ void k_prep_anal_dig(const double *__restrict__ PaT, const double *__
     const int nch = (KpA + kKC - 1) / kKC;
     if (64 * t >= K || ch >= nch) return;
     __nv_bfloat16 *tile = dig + abase[m] + ((size_t)t * nch + ch) * S * kTM * kSlice;
-    for (int idx = threadIdx.x; idx < kTM * 8; idx += blockDim.x) {
-        const int r = idx >> 3, j0 = (idx & 7) * 8;
+    for (int idx = threadIdx.x; idx < kTM * (kKC / 8); idx += blockDim.x) {
+        const int r = idx / (kKC / 8), j0 = (idx % (kKC / 8)) * 8;
         const int blk = r >> 5, pos = r & 31;
         const int k = 64 * t + 2 * pos + (blk & 1);
         double x[8];
@@ -317,26 +112,6 @@ __global__ void k_prep_anal_dig(const double *__restrict__ PaT, const double *__
         }
         put8<S, B>(x, rexp[((size_t)m * ntlA + t) * kTM + r], tile, (size_t)kTM * kSlice, r, j0);
     }
-}
-
-// ------------------------------------------------------------------ common MMA issue
-// D_q += A_s B_t^T over one chunk for every s + t = q <= S - 1.  Consecutive
-// MMAs go to different accumulators (t runs fastest), so no MMA waits on the
-// accumulation of the one before it.
-template <int S>
-__device__ __forceinline__ void issue_chunk(uint32_t tmem, const __nv_bfloat16 *sA, const __nv_bfloat16 *sB, int NT,
-                                            int kc, bool first) {
-    const uint32_t id = idesc_bf16(kTM, NT);
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-#pragma unroll 1
-    for (int k0 = 0; k0 < kc; k0 += 16)
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-#pragma unroll
-            for (int t = 0; t < S - s; ++t)
-                mma_bf16(tmem + (uint32_t)((s + t) * NT), sdesc(a0 + (uint32_t)(s * kTM * kSlice * 2 + k0 * 2)),
-                         sdesc(b0 + (uint32_t)(t * NT * kSlice * 2 + k0 * 2)), id,
-                         (first && s == 0 && k0 == 0) ? 0u : 1u);
 }
 
 // ------------------------------------------------------------------ synthesis kernel
@@ -360,11 +135,11 @@ template <int S>
 constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + (size_t)kNTa * kSt * 8; }
 
 template <int S, int B>
-__global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynSplitArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
     __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
-    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTs * kKC);   // [64 cols][kSt]
+    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTs * kKC);   // [kNTs cols][kSt]
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[kNTs];
@@ -511,7 +286,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynSplitArgs a) {
     } else {
         // epilogue 1: warp w reads TMEM lane quarter w % 4 = row block (P even,
         // P odd, dP even, dP odd; lane = latitude) and columns 16 (w / 4) .. +16
-        long long *zst = reinterpret_cast<long long *>(smraw);   // [128 rows][65]
+        long long *zst = reinterpret_cast<long long *>(smraw);   // [128 rows][kNTs + 1]
         const int quarter = warp & 3, c16 = (warp >> 2) * 16;
         if (quarter < 2 || anyD) {
             for (int h = 0; h < 16; h += 8) {
@@ -528,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynSplitArgs a) {
 #pragma unroll
                     for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
-                for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * 65 + c16 + h + i] = z[i];
+                for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * (kNTs + 1) + c16 + h + i] = z[i];
             }
         }
         __syncthreads();
@@ -541,16 +316,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynSplitArgs a) {
             const int js = a.nlat - 1 - jn;
             const SynCol &sc = scol[cc];
             const int ecr = scale_exp(cexp[2 * cc]), eci = scale_exp(cexp[2 * cc + 1]);
-            const long long *E = zst + (size_t)(0 * 32 + jj) * 65 + 2 * cc;
-            const long long *O = zst + (size_t)(1 * 32 + jj) * 65 + 2 * cc;
+            const long long *E = zst + (size_t)(0 * 32 + jj) * (kNTs + 1) + 2 * cc;
+            const long long *O = zst + (size_t)(1 * 32 + jj) * (kNTs + 1) + 2 * cc;
             const int eP = re[jj];
             a.F[((size_t)jn * a.nrow + sc.rowP) * a.ms + m] =
                 make_double2(z_to_f64(E[0] + O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] + O[1], zexp<B>(eP, eci)));
             a.F[((size_t)js * a.nrow + sc.rowP) * a.ms + m] =
                 make_double2(z_to_f64(E[0] - O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] - O[1], zexp<B>(eP, eci)));
             if (sc.rowD >= 0) {
-                const long long *dE = zst + (size_t)(2 * 32 + jj) * 65 + 2 * cc;
-                const long long *dO = zst + (size_t)(3 * 32 + jj) * 65 + 2 * cc;
+                const long long *dE = zst + (size_t)(2 * 32 + jj) * (kNTs + 1) + 2 * cc;
+                const long long *dO = zst + (size_t)(3 * 32 + jj) * (kNTs + 1) + 2 * cc;
                 const int eD = re[64 + jj];
                 a.F[((size_t)jn * a.nrow + sc.rowD) * a.ms + m] = make_double2(
                     z_to_f64(dE[0] + dO[0], zexp<B>(eD, ecr)), z_to_f64(dE[1] + dO[1], zexp<B>(eD, eci)));
@@ -581,19 +356,21 @@ struct AnaSplitArgs {
 // B column of (fold, slot, field cc, comp): fold 0 = north + south, 1 = north - south;
 // slot s scales Fourier row s of the field by (a_s + i b_s m / sin) (slots 0, 1).
 __host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
-    return fold * 24 + slot * 8 + cc * 2 + comp;
+    return fold * 12 + slot * 4 + cc * 2 + comp;
 }
 
 template <int S, int B>
-__global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
     __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
-    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // [48 cols][kSt]
+    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // [kNTa cols][kSt]
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[kNTa];
-    __shared__ AnaCol scol[kNTa / 12];
+    __shared__ AnaCol scol[kFa];
+    __shared__ int skind[kFa][2];      // slot scaling: 0 real (b = 0), 1 imaginary (a = 0), 2 general
+    __shared__ double sbm[kFa][2];     // b m of the slot
     __shared__ int fail;
 
     if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
@@ -604,13 +381,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
     const int K = a.T - m + 1;
     if (64 * t >= K) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int c0 = nt * (kNTa / 12);
-    const int ncl = min(kNTa / 12, a.ncol - c0);
+    const int c0 = nt * kFa;
+    const int ncl = min(kFa, a.ncol - c0);
     if (ncl <= 0) return;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
     if (tid < ncl) scol[tid] = a.cols[c0 + tid];
     if (tid < kNTa) cexp[tid] = 0;
     if (tid == 0) fail = 0;
+    if (tid < 2 * ncl) {
+        const AnaCol q = a.cols[c0 + (tid >> 1)];
+        const int sl = tid & 1;
+        const double aa = sl == 0 ? q.a1 : q.a2, bb = sl == 0 ? q.b1 : q.b2;
+        skind[tid >> 1][sl] = (__double_as_longlong(bb) << 1) == 0 ? 0 : ((__double_as_longlong(aa) << 1) == 0 ? 1 : 2);
+        sbm[tid >> 1][sl] = bb * m;
+    }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(kTmemCols));
@@ -630,17 +414,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
         const AnaCol &q = scol[cc];
         const int row = slot == 0 ? q.row1 : (slot == 1 ? q.row2 : q.row3);
         if (row < 0 || j >= a.nh) { v[0] = v[1] = v[2] = v[3] = 0.0; return; }
-        double2 fn = a.F[((size_t)j * a.nrow + row) * a.ms + m];
-        double2 fs = a.F[((size_t)(a.nlat - 1 - j) * a.nrow + row) * a.ms + m];
+        const double2 fn = a.F[((size_t)j * a.nrow + row) * a.ms + m];
+        const double2 fs = a.F[((size_t)(a.nlat - 1 - j) * a.nrow + row) * a.ms + m];
+        // fold first (the scaling is linear), then scale by (a + i b m / sin)
+        const double er = fn.x + fs.x, ei = fn.y + fs.y, orr = fn.x - fs.x, oi = fn.y - fs.y;
         if (slot < 2) {
-            const double aa = slot == 0 ? q.a1 : q.a2, bb = (slot == 0 ? q.b1 : q.b2) * m * a.isin[j];
-            fn = make_double2(aa * fn.x - bb * fn.y, aa * fn.y + bb * fn.x);
-            fs = make_double2(aa * fs.x - bb * fs.y, aa * fs.y + bb * fs.x);
+            const int kd = skind[cc][slot];
+            const double aa = slot == 0 ? q.a1 : q.a2;
+            if (kd == 0) {
+                v[0] = aa * er; v[1] = aa * ei; v[2] = aa * orr; v[3] = aa * oi;
+            } else {
+                const double bb = sbm[cc][slot] * a.isin[j];
+                if (kd == 1) {
+                    v[0] = -bb * ei; v[1] = bb * er; v[2] = -bb * oi; v[3] = bb * orr;
+                } else {
+                    v[0] = fma(aa, er, -bb * ei); v[1] = fma(aa, ei, bb * er);
+                    v[2] = fma(aa, orr, -bb * oi); v[3] = fma(aa, oi, bb * orr);
+                }
+            }
+        } else {
+            v[0] = er; v[1] = ei; v[2] = orr; v[3] = oi;
         }
-        v[0] = fn.x + fs.x;   // fold 0 re
-        v[1] = fn.y + fs.y;   // fold 0 im
-        v[2] = fn.x - fs.x;   // fold 1 re
-        v[3] = fn.y - fs.y;   // fold 1 im
     };
     // phase 1: column scales over all latitudes, chunk 0 staged
     const int kc0 = min(kKC, KpA);
@@ -679,9 +473,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
         }
         for (int task = tid; task < kNTa * (kc / 8); task += kThreads) {
             const int n = task % kNTa, k0 = (task / kNTa) * 8;
-            const int cc = (n % 8) >> 1;
+            const int cc = (n % 4) >> 1;
             double x[8];
-            if (cc < ncl) {
+            if (n < 24 && cc < ncl) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
             } else {
@@ -714,16 +508,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
         if (tid == 0) atomicOr(a.err, 1);
     } else {
         // epilogue 1: only the columns a row uses.  P rows (lane quarters 0, 1;
-        // parity par) use fold par of slots 0 and 2 (16 columns), dP rows
-        // (quarters 2, 3) fold 1 - par of slot 1 (8 columns); the four warps
-        // of a quarter split them.
-        double *sd = reinterpret_cast<double *>(sB);   // [128 rows][17]
+        // parity par) use fold par of slots 0 and 2 (4 columns each), dP rows
+        // (quarters 2, 3) fold 1 - par of slot 1 (4 columns); the two warps of
+        // a quarter split them.
+        double *sd = reinterpret_cast<double *>(sB);   // [128 rows][9]
         const int quarter = warp & 3, g = warp >> 2, par = quarter & 1;
         const int row = quarter * 32 + lane;
         const int er = a.rexp[((size_t)m * a.ntlA + t) * kTM + row];
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
         if (quarter < 2) {
-            const int n0 = acol(par, g < 2 ? 0 : 2, 0, 0) + (g & 1) * 4;
+            const int n0 = acol(par, g == 0 ? 0 : 2, 0, 0);
             long long z[4] = {0, 0, 0, 0};
             uint32_t r[S][4];
 #pragma unroll
@@ -735,7 +529,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
                 for (int i = 0; i < 4; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
             for (int i = 0; i < 4; ++i)
-                sd[(size_t)row * 17 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
+                sd[(size_t)row * 9 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
         } else {
             const int n0 = acol(1 - par, 1, 0, 0) + g * 2;
             long long z[2] = {0, 0};
@@ -749,7 +543,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
                 for (int i = 0; i < 2; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
             for (int i = 0; i < 2; ++i)
-                sd[(size_t)row * 17 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
+                sd[(size_t)row * 9 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
         }
         __syncthreads();
         // epilogue 2: combine P and dP parts; l = m + 64 t + 2 pos + par
@@ -760,8 +554,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
             if (k >= K) continue;
             const AnaCol &q = scol[cc];
             const int l = m + k;
-            const double *rp = sd + (size_t)(pr * 32 + pos) * 17;         // slot 0 at [0..8), slot 2 at [8..16)
-            const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * 17;   // slot 1 at [0..8)
+            const double *rp = sd + (size_t)(pr * 32 + pos) * 9;         // slot 0 at [0..4), slot 2 at [4..8)
+            const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * 9;   // slot 1 at [0..4)
             double xr = 0.0, xi = 0.0;
             if (q.row1 >= 0) { xr += rp[cc * 2]; xi += rp[cc * 2 + 1]; }
             if (q.row2 >= 0) { xr += rd[cc * 2]; xi += rd[cc * 2 + 1]; }
@@ -770,8 +564,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_anal(AnaSplitArgs a) {
             xi *= post;
             if (q.row3 >= 0) {
                 const double f3 = a.lfac[q.lf3 * a.ms + l];
-                xr += f3 * rp[8 + cc * 2];
-                xi += f3 * rp[8 + cc * 2 + 1];
+                xr += f3 * rp[4 + cc * 2];
+                xi += f3 * rp[4 + cc * 2 + 1];
             }
             if (m == 0) xi = 0.0;
             q.dst[a.moff[m] + k] = make_double2(xr, xi);
@@ -887,7 +681,7 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, co
     if (ncol <= 0) return AEROS_OK;
     AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
                    c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err};
-    dim3 grid(c.T + 1, s->ntlA, (ncol + kNTa / 12 - 1) / (kNTa / 12));
+    dim3 grid(c.T + 1, s->ntlA, (ncol + kFa - 1) / kFa);
     if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
     else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;

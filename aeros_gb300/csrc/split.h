@@ -19,4 +19,18 @@ int split_error(SplitCtx *s, int *flag);
 // AEROS_OK, or AEROS_ERR_CUDA with the last-error text set when the flag is up.
 int split_check(SplitCtx *s);
 
+// Longitude transforms of the split form as exact-digit DFT products on the
+// tensor cores (split_dft.cu).  Same contracts as launch_fourier_synth /
+// launch_fourier_anal; a direction whose contraction exceeds 441 is not built
+// (has_* false) and keeps the FFT.  Creation returns a null context when the
+// environment sets AEROS_SPLIT_FFT=1 (the FFT is kept in both directions).
+struct SplitDft;
+int split_dft_create(const Geometry &g, SplitDft **out);
+void split_dft_destroy(SplitDft *s);
+bool split_dft_has_synth(const SplitDft *s);
+bool split_dft_has_anal(const SplitDft *s);
+int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow);
+int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow);
+int split_dft_check(SplitDft *s);
+
 }  // namespace aeros

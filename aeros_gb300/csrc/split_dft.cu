@@ -1,0 +1,452 @@
+// split_dft.cu -- the longitude transforms of the split-precision form as
+// exact-digit DFT products on the tcgen05 tensor cores.
+//
+// GB300 executes FP64 at ~1/60 of its FP32/INT32 rate, and a real FFT of
+// length nlon is FP64-bound.  In the split form the Fourier stage is instead
+//   synthesis: grid[j][i] = sum_k A_s[i][k] X[j][k],  k = 2m + (0: re, 1: im),
+//              A_s[i][2m] = w_m cos(m lambda_i), A_s[i][2m+1] = -w_m sin(m lambda_i),
+//              w_m = (2 - delta_m0)/sqrt(2 pi) (the inverse real DFT of the
+//              truncated spectrum, as in aeros_spectral's SH_to_spat);
+//   analysis:  F[j][2m + c] = sum_i A_a[2m + c][i] grid[j][i],
+//              A_a[2m][i] = s cos(m lambda_i), A_a[2m+1][i] = -s sin(m lambda_i),
+//              s = sqrt(2 pi)/nlon (spat_to_SH's longitude sum);
+// with lambda_i = 2 pi i / nlon.  Both are products of a fixed FP64 table (cut
+// once into digit tile images) with data columns, one per (field, latitude),
+// done by the same Ozaki scheme as the Legendre sums (split_common.cuh): exact
+// digit products accumulated per shift in TMEM, int64 recombination, FP64
+// assembled from the bits.  Used for contraction lengths up to 128 (nlon <= 128
+// for the analysis, T <= 63 for the synthesis), where it beats the FFT; larger
+// grids keep the FFT.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include "split.h"
+#include "split_common.cuh"
+
+namespace aeros {
+
+namespace {
+
+constexpr int kNT = kNTile;   // data columns per tile
+
+template <int S>
+constexpr size_t gemm_smem() { return (size_t)S * (kTM + kNT) * kKC * 2 + (size_t)kNT * kSt * 8; }
+
+// ---------------------------------------------------------------- table digits
+__global__ void k_gemm_prep_exp(const double *__restrict__ T, int Mpad, int K, int *__restrict__ rexp) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= Mpad) return;
+    int be = 0;
+    for (int k = 0; k < K; ++k) be = max(be, bexp(T[(size_t)r * K + k]));
+    rexp[r] = scale_exp(be);
+}
+
+template <int S, int B>
+__global__ void k_gemm_prep_dig(const double *__restrict__ T, int K, int nch, const int *__restrict__ rexp,
+                                __nv_bfloat16 *__restrict__ dig) {
+    const int mt = blockIdx.x, ch = blockIdx.y;
+    __nv_bfloat16 *tile = dig + ((size_t)mt * nch + ch) * S * kTM * kSlice;
+    for (int idx = threadIdx.x; idx < kTM * (kKC / 8); idx += blockDim.x) {
+        const int r = idx / (kKC / 8), k0 = (idx % (kKC / 8)) * 8, row = mt * kTM + r;
+        double x[8];
+        for (int i = 0; i < 8; ++i) {
+            const int k = ch * kKC + k0 + i;
+            x[i] = k < K ? T[(size_t)row * K + k] : 0.0;
+        }
+        put8<S, B>(x, rexp[row], tile, (size_t)kTM * kSlice, r, k0);
+    }
+}
+
+// ---------------------------------------------------------------- data columns
+// Synthesis column (field f, latitude j): X_m = sum_t (a_t + i b_t m / sin_j) F[j][src_t][m].
+// The factors are classified with integer tests on their bits, and m / sin_j
+// comes from a table, so the FP64 pipe sees only the products that remain.
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ bool is_one(double v) { return __double_as_longlong(v) == 0x3FF0000000000000ll; }
+
+struct DftSynthP {
+    const FsynField *fields;
+    int nf, nrow, ms, nlat, nlon;
+    const double2 *F;
+    const double *msin;   // [nlat][ms]: m / sin(theta_j)
+    __device__ int ncol() const { return nf * nlat; }
+    __device__ int nrows() const { return nlon; }
+    __device__ void bvals8(int col, int k0, double *x) const {
+        const int f = col / nlat, j = col - f * nlat;
+        const FsynField fd = fields[f];
+        const double2 *Fr = F + (size_t)j * nrow * ms;
+        const double *mb = msin + (size_t)j * ms;
+        // kind: 0 absent, 1 copy (a = 1, b = 0), 2 real (b = 0), 3 imaginary (a = 0), 4 general
+        auto kind = [](int src, double a, double b) {
+            if (src < 0) return 0;
+            if (is_zero(b)) return is_one(a) ? 1 : 2;
+            return is_zero(a) ? 3 : 4;
+        };
+        const int k0k = kind(fd.src0, fd.a0, fd.b0), k1k = kind(fd.src1, fd.a1, fd.b1);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int m = (k0 >> 1) + t;
+            double xr = 0.0, xi = 0.0;
+            if (m < ms) {
+                const double bs = mb[m];
+                auto term = [&](int kd, int src, double a, double b, double &r, double &i) {
+                    const double2 v = Fr[(size_t)src * ms + m];
+                    if (kd == 1) { r = v.x; i = v.y; }
+                    else if (kd == 2) { r = a * v.x; i = a * v.y; }
+                    else {
+                        const double bb = b * bs;
+                        if (kd == 3) { r = -bb * v.y; i = bb * v.x; }
+                        else { r = fma(a, v.x, -bb * v.y); i = fma(a, v.y, bb * v.x); }
+                    }
+                };
+                if (k0k) term(k0k, fd.src0, fd.a0, fd.b0, xr, xi);
+                if (k1k) {
+                    double r, i;
+                    term(k1k, fd.src1, fd.a1, fd.b1, r, i);
+                    xr = k0k ? xr + r : r;
+                    xi = k0k ? xi + i : i;
+                }
+                if (m == 0) xi = 0.0;
+            }
+            x[2 * t] = xr;
+            x[2 * t + 1] = xi;
+        }
+    }
+    __device__ void store(int row, int col, double v) const {
+        if (row >= nlon) return;
+        const int f = col / nlat, j = col - f * nlat;
+        fields[f].dst[(size_t)j * nlon + row] = v;
+    }
+};
+
+// Analysis column (field f, latitude j): the grid row itself.
+struct DftAnalP {
+    const FanaField *fields;
+    int nf, nrow, ms, nlat, nlon;
+    double2 *F;
+    __device__ int ncol() const { return nf * nlat; }
+    __device__ int nrows() const { return 2 * ms; }
+    __device__ void bvals8(int col, int k0, double *x) const {
+        const int f = col / nlat, j = col - f * nlat;
+        const double *src = fields[f].src + (size_t)j * nlon;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = k0 + i < nlon ? src[k0 + i] : 0.0;
+    }
+    __device__ void store(int row, int col, double v) const {
+        if (row >= 2 * ms) return;
+        const int f = col / nlat, j = col - f * nlat, m = row >> 1;
+        reinterpret_cast<double *>(F)[(((size_t)j * nrow + fields[f].row) * ms + m) * 2 + (row & 1)] = v;
+    }
+};
+
+// ---------------------------------------------------------------- the product
+// CTA (M tile mt, column tile ct): rows mt*128.. of the table times 64 data
+// columns, over the whole contraction in 64-wide chunks.
+template <int S, int B, class P>
+__global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch, const __nv_bfloat16 *dig,
+                                                            const int *rexp, int *err) {
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    if (smem_u32(smraw) & 1023u) {
+        if (threadIdx.x == 0) atomicOr(err, 2);
+        return;
+    }
+    __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
+    __nv_bfloat16 *sB = sA + (size_t)S * kTM * kSlice;
+    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNT * kSlice);   // [kNT cols][kSt]
+    __shared__ __align__(8) uint64_t mbarA, mbarM;
+    __shared__ uint32_t tmem_base;
+    __shared__ int cexp[kNT];
+    __shared__ int fail;
+
+    const int mt = blockIdx.x, ct = blockIdx.y;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Kp = (K + 15) & ~15;
+    const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
+    if (ncl <= 0) return;
+    if (tid < kNT) cexp[tid] = 0;
+    if (tid == 0) fail = 0;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&mbarA);
+        mbar_init(&mbarM);
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    __syncthreads();
+    const __nv_bfloat16 *gA = dig + (size_t)mt * nch * S * kTM * kSlice;
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    // phase 1: column scales over the whole contraction, chunk 0 staged
+    const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+    for (int base = 0; base < ncl * nk8; base += kThreads) {
+        const int task = base + tid;
+        const bool valid = task < ncl * nk8;
+        const int n = valid ? task / nk8 : -1, k0 = valid ? (task - n * nk8) * 8 : 0;
+        double x[8];
+        if (valid) p.bvals8(c0 + n, k0, x);
+        else
+#pragma unroll
+            for (int i = 0; i < 8; ++i) x[i] = 0.0;
+        int be = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) be = max(be, k0 + i < K ? bexp(x[i]) : 0);
+        const unsigned peers = __match_any_sync(0xffffffffu, n);
+        be = __reduce_max_sync(peers, be);
+        if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[n], be);
+        if (valid && k0 < kc0)
+#pragma unroll
+            for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = k0 + i < K ? x[i] : 0.0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+    for (int ch = 0; ch < nch && ok; ++ch) {
+        const int kc = min(kKC, Kp - ch * kKC);
+        if (ch > 0) {
+            for (int task = tid; task < ncl * (kc / 8); task += kThreads) {
+                const int n = task / (kc / 8), k0 = (task - n * (kc / 8)) * 8;
+                double x[8];
+                p.bvals8(c0 + n, ch * kKC + k0, x);
+                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = ch * kKC + k0 + i < K ? x[i] : 0.0;
+            }
+            __syncthreads();
+        }
+        for (int task = tid; task < kNT * (kc / 8); task += kThreads) {
+            const int n = task % kNT, k0 = (task / kNT) * 8;
+            double x[8];
+            if (n < ncl) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) x[i] = 0.0;
+            }
+            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNT * kSlice, n, k0);
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        __syncthreads();
+        if (tid == 0) {
+            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                issue_chunk<S>(tmem, sA, sB, kNT, kc, ch == 0);
+                mma_commit(&mbarM);
+            } else {
+                fail = 1;
+                mbar_arrive(&mbarM);
+            }
+        }
+        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncthreads();
+        ok = ok && !fail;
+        if (ok && tid == 0 && ch + 1 < nch)
+            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(err, 1);
+    } else {
+        // warp w: TMEM lane quarter w % 4 (rows), columns 16 (w / 4) .. +16
+        const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+        const int row = quarter * 32 + lane;
+        const int grow = mt * kTM + row;
+        const int er = rexp[grow];
+        for (int h = 0; h < 16; h += 8) {
+            uint32_t r[S][8];
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+                tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNT + c16 + h), r[q]);
+            tmem_wait_ld();
+            long long z[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) z[i] = 0;
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+            if (grow < p.nrows())
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int n = c16 + h + i;
+                    if (n < ncl) p.store(grow, c0 + n, z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n]))));
+                }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+}  // namespace
+
+// One direction's table: Mpad x K FP64 values cut into (M tile, K chunk) images.
+struct DftPart {
+    int S = 0, B = 0, K = 0, nch = 0, nmt = 0, M = 0;
+    __nv_bfloat16 *dig = nullptr;
+    int *rexp = nullptr;
+};
+
+struct SplitDft {
+    DftPart syn, ana;
+    double *msin = nullptr;   // [nlat][ms] m / sin(theta_j)
+    int *err = nullptr;
+};
+
+namespace {
+
+template <int S, int B>
+int prep_part(DftPart &d, const double *Td) {
+    k_gemm_prep_exp<<<(d.nmt * kTM + 127) / 128, 128>>>(Td, d.nmt * kTM, d.K, d.rexp);
+    k_gemm_prep_dig<S, B><<<dim3(d.nmt, d.nch), 256>>>(Td, d.K, d.nch, d.rexp, d.dig);
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+// Build one part from a host table (rows M, contraction K); S = 0 marks "not supported".
+int build_part(DftPart &d, const std::vector<double> &T, int M, int K) {
+    // the product beats the FFT only for short rows (measured: T42 and below);
+    // longer contractions keep the FFT
+    if (K <= 126) { d.S = 7; d.B = 8; }
+    else if (K <= 128) { d.S = 8; d.B = 7; }
+    else { d.S = 0; return AEROS_OK; }
+    d.K = K;
+    d.M = M;
+    d.nmt = (M + kTM - 1) / kTM;
+    d.nch = ((K + 15) / 16 * 16 + kKC - 1) / kKC;
+    const size_t Mpad = (size_t)d.nmt * kTM;
+    std::vector<double> Tp(Mpad * K, 0.0);
+    std::copy(T.begin(), T.end(), Tp.begin());
+    double *Td = nullptr;
+    const size_t ndig = (size_t)d.nmt * d.nch * d.S * kTM * kSlice;
+    if (cudaMalloc(&Td, Tp.size() * 8) != cudaSuccess || cudaMalloc(&d.rexp, Mpad * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&d.dig, ndig * 2) != cudaSuccess) {
+        cudaGetLastError();
+        if (Td) cudaFree(Td);
+        set_error("split DFT: table allocation failed");
+        return AEROS_ERR_NOMEM;
+    }
+    AEROS_CUDA(cudaMemcpy(Td, Tp.data(), Tp.size() * 8, cudaMemcpyHostToDevice));
+    int rc = d.S == 7 ? prep_part<7, 8>(d, Td) : prep_part<8, 7>(d, Td);
+    if (rc == AEROS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = AEROS_ERR_CUDA;
+    cudaFree(Td);
+    if (rc) return rc;
+    if (d.S == 7)
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)gemm_smem<7>()));
+    else
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)gemm_smem<8>()));
+    if (d.S == 7)
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftAnalP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)gemm_smem<7>()));
+    else
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftAnalP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)gemm_smem<8>()));
+    return AEROS_OK;
+}
+
+void free_part(DftPart &d) {
+    if (d.dig) cudaFree(d.dig);
+    if (d.rexp) cudaFree(d.rexp);
+    d = DftPart{};
+}
+
+template <class P>
+void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err) {
+    dim3 grid(d.nmt, (ncol + kNT - 1) / kNT);
+    if (d.S == 7)
+        k_split_gemm<7, 8, P><<<grid, kThreads, gemm_smem<7>(), c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
+    else
+        k_split_gemm<8, 7, P><<<grid, kThreads, gemm_smem<8>(), c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
+    if (c.launches) ++*c.launches;
+}
+
+}  // namespace
+
+int split_dft_create(const Geometry &g, SplitDft **out) {
+    *out = nullptr;
+    const char *keep_fft = std::getenv("AEROS_SPLIT_FFT");
+    if (keep_fft && keep_fft[0] == '1') return AEROS_OK;
+    SplitDft *s = new SplitDft;
+    const int nlon = g.nlon, ms = g.T + 1;
+    const long double pi = 3.141592653589793238462643383279502884L;
+    const long double nrm = 1.0L / std::sqrt(2.0L * pi), sc = std::sqrt(2.0L * pi) / nlon;
+    // synthesis: rows i (longitude), columns 2m + (re, im)
+    std::vector<double> As((size_t)nlon * 2 * ms), Aa((size_t)2 * ms * nlon);
+    for (int i = 0; i < nlon; ++i)
+        for (int m = 0; m < ms; ++m) {
+            // reduce m i mod nlon before the angle so large products stay exact
+            const long double ang = 2.0L * pi * (long double)(((long long)m * i) % nlon) / nlon;
+            const long double w = (m == 0 ? 1.0L : 2.0L) * nrm;
+            As[(size_t)i * 2 * ms + 2 * m] = (double)(w * std::cos(ang));
+            As[(size_t)i * 2 * ms + 2 * m + 1] = (double)(-w * std::sin(ang));
+            Aa[(size_t)(2 * m) * nlon + i] = (double)(sc * std::cos(ang));
+            Aa[(size_t)(2 * m + 1) * nlon + i] = (double)(-sc * std::sin(ang));
+        }
+    int rc = build_part(s->syn, As, nlon, 2 * ms);
+    if (!rc) rc = build_part(s->ana, Aa, 2 * ms, nlon);
+    if (!rc) {
+        std::vector<double> msin((size_t)g.nlat * ms);
+        for (int j = 0; j < g.nlat; ++j)
+            for (int m = 0; m < ms; ++m) msin[(size_t)j * ms + m] = m / g.sint[j];
+        if (cudaMalloc(&s->msin, msin.size() * 8) != cudaSuccess ||
+            cudaMemcpy(s->msin, msin.data(), msin.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = AEROS_ERR_NOMEM;
+    }
+    if (!rc && cudaMalloc(&s->err, sizeof(int)) != cudaSuccess) rc = AEROS_ERR_NOMEM;
+    if (!rc && cudaMemset(s->err, 0, sizeof(int)) != cudaSuccess) rc = AEROS_ERR_CUDA;
+    if (rc) {
+        split_dft_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return AEROS_OK;
+}
+
+void split_dft_destroy(SplitDft *s) {
+    if (!s) return;
+    free_part(s->syn);
+    free_part(s->ana);
+    if (s->msin) cudaFree(s->msin);
+    if (s->err) cudaFree(s->err);
+    delete s;
+}
+
+bool split_dft_has_synth(const SplitDft *s) { return s && s->syn.S > 0; }
+bool split_dft_has_anal(const SplitDft *s) { return s && s->ana.S > 0; }
+
+int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    DftSynthP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, s->msin};
+    launch_gemm(s->syn, c, p, nf * c.nlat, s->err);
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    DftAnalP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F};
+    launch_gemm(s->ana, c, p, nf * c.nlat, s->err);
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+int split_dft_check(SplitDft *s) {
+    if (!s) return AEROS_OK;
+    int flag = 0;
+    if (cudaMemcpy(&flag, s->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return AEROS_ERR_CUDA;
+    if (flag) {
+        set_error(flag & 2 ? "split DFT: shared memory not 1024-byte aligned"
+                           : "split DFT: tensor-core wait gave up (bounded mbarrier wait)");
+        return AEROS_ERR_CUDA;
+    }
+    return AEROS_OK;
+}
+
+}  // namespace aeros
