@@ -49,37 +49,48 @@ __constant__ HsConst c_hs;
 // ---------------------------------------------------------------- column kernel
 // Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
 // dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy.  Outputs GA[e][f][j][i]:
-// ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.  One thread per column.
+// ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.
+// LPC lanes (adjacent in a warp) share a column, each owning a contiguous chunk
+// of levels.  The two vertical sums (mass flux from the top, geopotential from
+// the surface) are passed from lane to lane in level order, so every rounding
+// is the one-lane kernel's and the results do not depend on LPC.
+template <int LPC>
 __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
-                                               int nlon, int nlat, int M, const double *__restrict__ xlat,
-                                               const double *__restrict__ phis, int hs_on,
-                                               const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
+                                                int nlon, int nlat, int M, const double *__restrict__ xlat,
+                                                const double *__restrict__ phis, int hs_on,
+                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
+    constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
     const long ng = (long)nlon * nlat;
-    long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (gid >= ng * M) return;
-    const int e = (int)(gid / ng);
-    const long c = gid - e * ng;
+    const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long gid = gt / LPC;
+    const int q = (int)(gt % LPC);
+    const int base = (threadIdx.x & 31) - q;          // first lane of this column's group
+    const bool act = gid < ng * M;
+    const int e = act ? (int)(gid / ng) : 0;
+    const long c = act ? gid - (long)e * ng : 0;
     const int j = (int)(c / nlon);
     const double *Gf = G + (size_t)e * (7 * NL + 3) * ng + c;
     double *Go = GA + (size_t)e * (4 * NL + 1) * ng + c;
 #define GF(f) Gf[(size_t)(f) * ng]
 #define GO(f) Go[(size_t)(f) * ng]
-    const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
+    const int C = (NL + LPC - 1) / LPC;
+    const int k0 = min(NL, q * C), k1 = min(NL, k0 + C), nk = k1 - k0;
+    const double lnps = act ? GF(7 * NL) : 0.0, dpx = act ? GF(7 * NL + 1) : 0.0, dpy = act ? GF(7 * NL + 2) : 0.0;
     const double ps = exp(lnps);
-    // per-level column quantities; 1/dp replaces the reference's divisions by dp
-    double rdp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev], gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1],
-        phi[kMaxLev];
-    scum[0] = 0.0;
-    for (int k = 0; k < NL; ++k) {
+    // per-level column quantities of this lane's levels; 1/dp replaces the reference's divisions by dp
+    double rdp[kChunk], dlnp[kChunk], alpha[kChunk], cfac[kChunk], gc[kChunk], cm[kChunk], scum[kChunk + 1],
+        phi[kChunk];
+    for (int i = 0; i < nk; ++i) {
+        const int k = k0 + i;
         const LevConst &L = c_lev[k];
         const double ph0 = fma(L.B0, ps, L.A0), ph1 = fma(L.B1, ps, L.A1);
         const double d = ph1 - ph0;
         const double r = 1.0 / d;
-        rdp[k] = r;
+        rdp[i] = r;
         if (L.pure) {
-            dlnp[k] = L.dlnp;
-            alpha[k] = L.alpha;
-            cfac[k] = L.cfac;
+            dlnp[i] = L.dlnp;
+            alpha[i] = L.alpha;
+            cfac[i] = L.cfac;
         } else {
             double dl, al;
             if (ph0 <= 0.0) {
@@ -89,27 +100,42 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
                 dl = log(ph1 / ph0);
                 al = 1.0 - (ph0 * r) * dl;
             }
-            dlnp[k] = dl;
-            alpha[k] = al;
-            cfac[k] = (ps * r) * (L.B0 * dl + L.dB * al);
+            dlnp[i] = dl;
+            alpha[i] = al;
+            cfac[i] = (ps * r) * (L.B0 * dl + L.dB * al);
         }
-        const double g = GF(k) * dpx + GF(NL + k) * dpy;
-        gc[k] = g;
-        const double cmass = d * GF(3 * NL + k) + L.dB * ps * g;
-        cm[k] = cmass;
-        scum[k + 1] = scum[k] + cmass;
+        const double g = act ? GF(k) * dpx + GF(NL + k) * dpy : 0.0;
+        gc[i] = g;
+        cm[i] = d * (act ? GF(3 * NL + k) : 0.0) + L.dB * ps * g;
     }
-    GO(4 * NL) = -scum[NL] / ps;
-    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474)
-    {
-        double phh = phis ? phis[c] : 0.0;
-        for (int k = NL - 1; k >= 0; --k) {
-            const double rt = kRd * GF(4 * NL + k);
-            phi[k] = fma(alpha[k], rt, phh);
-            phh = fma(rt, dlnp[k], phh);
+    // mass flux sum from the top, lane by lane in level order
+    double sacc = 0.0;
+#pragma unroll
+    for (int r = 0; r < LPC; ++r) {
+        if (q == r) {
+            for (int i = 0; i < nk; ++i) {
+                scum[i] = sacc;
+                sacc = sacc + cm[i];
+            }
+            scum[nk] = sacc;
         }
+        if (LPC > 1) sacc = __shfl_sync(0xffffffffu, sacc, base + r);
     }
-    const double SN = scum[NL];
+    const double SN = sacc;
+    if (act && q == 0) GO(4 * NL) = -SN / ps;
+    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474), lane by lane from the surface
+    double phh = (act && phis) ? phis[c] : 0.0;
+#pragma unroll
+    for (int r = LPC - 1; r >= 0; --r) {
+        if (q == r)
+            for (int i = nk - 1; i >= 0; --i) {
+                const double rt = kRd * GF(4 * NL + k0 + i);
+                phi[i] = fma(alpha[i], rt, phh);
+                phh = fma(rt, dlnp[i], phh);
+            }
+        if (LPC > 1) phh = __shfl_sync(0xffffffffu, phh, base + r);
+    }
+    if (!act) return;
     const double f = 2.0 * kOmega * xlat[j];
     const double x2 = xlat[j] * xlat[j], c2 = 1.0 - x2, c4 = c2 * c2;
     double dty = 0, ka = 0, psk = 0, lnpr = 0, tbase = 0;
@@ -120,29 +146,27 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         psk = exp(kKappa * lnpr);   // (ps/p0)^kappa
         tbase = c_hs.t_eq - dty * x2;
     }
-    double up = 0, vp = 0, tp = 0;                    // level k-1
-    double uc = GF(0), vc = GF(NL), tc = GF(4 * NL);  // level k
-    for (int k = 0; k < NL; ++k) {
+    for (int i = 0; i < nk; ++i) {
+        const int k = k0 + i;
         const LevConst &L = c_lev[k];
-        double un = 0, vn = 0, tn = 0;
-        if (k + 1 < NL) {
-            un = GF(k + 1);
-            vn = GF(NL + k + 1);
-            tn = GF(4 * NL + k + 1);
-        }
-        const double r = rdp[k];
-        const double omega = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cm[k]) * r;
-        const double mup = L.B0 * SN - scum[k];        // M at half level k (above)
-        const double mlo = L.B1 * SN - scum[k + 1];    // M at half level k+1 (below)
+        const double uc = GF(k), vc = GF(NL + k), tc = GF(4 * NL + k);
+        const double up = k > 0 ? GF(k - 1) : 0.0, vp = k > 0 ? GF(NL + k - 1) : 0.0,
+                     tp = k > 0 ? GF(4 * NL + k - 1) : 0.0;
+        const double un = k + 1 < NL ? GF(k + 1) : 0.0, vn = k + 1 < NL ? GF(NL + k + 1) : 0.0,
+                     tn = k + 1 < NL ? GF(4 * NL + k + 1) : 0.0;
+        const double r = rdp[i];
+        const double omega = cfac[i] * gc[i] - (scum[i] * dlnp[i] + alpha[i] * cm[i]) * r;
+        const double mup = L.B0 * SN - scum[i];        // M at half level k (above)
+        const double mlo = L.B1 * SN - scum[i + 1];    // M at half level k+1 (below)
         const double hr = 0.5 * r;
         const double vu = hr * (((k < NL - 1) ? mlo * (un - uc) : 0.0) + ((k > 0) ? mup * (uc - up) : 0.0));
         const double vv = hr * (((k < NL - 1) ? mlo * (vn - vc) : 0.0) + ((k > 0) ? mup * (vc - vp) : 0.0));
         const double vt = hr * (((k < NL - 1) ? mlo * (tn - tc) : 0.0) + ((k > 0) ? mup * (tc - tp) : 0.0));
         const double zf = GF(2 * NL + k) + f;
-        const double pgf = kRd * tc * cfac[k];
+        const double pgf = kRd * tc * cfac[i];
         double ae = zf * vc - vu - pgf * dpx;
         double an = -zf * uc - vv - pgf * dpy;
-        const double ek = phi[k] + 0.5 * (uc * uc + vc * vc);
+        const double ek = phi[i] + 0.5 * (uc * uc + vc * vc);
         double dtdt = -(uc * GF(5 * NL + k) + vc * GF(6 * NL + k)) - vt + kKappa * tc * omega;
         if (hs_on) {
             // src/physics/aeros_held_suarez.f90:177-293
@@ -168,8 +192,6 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         GO(NL + k) = an;
         GO(2 * NL + k) = ek;
         GO(3 * NL + k) = dtdt;
-        up = uc; vp = vc; tp = tc;
-        uc = un; vc = vn; tc = tn;
     }
 #undef GF
 #undef GO
@@ -266,11 +288,15 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
         double2 rhs = make_double2(dold.x - a.hh_old * lam * wd.x + h * (rd.x + lds.x - ldn.x),
                                    dold.y - a.hh_old * lam * wd.y + h * (rd.y + lds.y - ldn.y));
         const double *Mi = a.MinvT + (size_t)l * NL * NL;
+        double mrow[kMaxLev];   // this lane's row of the inverse, loaded before the solve
+#pragma unroll
+        for (int j = 0; j < kMaxLev; ++j) mrow[j] = (act && j < NL) ? Mi[j * NL + k] : 0.0;
         dnew = z;
-        for (int j = 0; j < NL; ++j) {
+#pragma unroll
+        for (int j = 0; j < kMaxLev; ++j) {
+            if (j >= NL) break;
             double2 rj = shfl2(rhs, j);
-            double mk = act ? Mi[j * NL + k] : 0.0;
-            dnew.x += mk * rj.x; dnew.y += mk * rj.y;
+            dnew.x += mrow[j] * rj.x; dnew.y += mrow[j] * rj.y;
         }
         double2 db = make_double2(a.a1 * dnew.x + (1.0 - a.a1) * dold.x, a.a1 * dnew.y + (1.0 - a.a1) * dold.y);
         double2 td = z;
@@ -324,10 +350,16 @@ __global__ void k_copy(double2 *dst, const double2 *src, size_t n) {
 // ---------------------------------------------------------------- mass fixer
 // Per (member, north latitude): synthesize lnps on the two mirrored rows,
 // exponentiate and sum each row (src/dynamics/aeros_timestep.f90:1253-1276).
-__global__ void k_mass_rows(const double2 *__restrict__ lnps, int M, int T, int nlm, int nh, int nlat, int nlon,
-                            const double *__restrict__ Ps, const int *__restrict__ moff, FftPlan plan,
-                            const double2 *__restrict__ tw, const double2 *__restrict__ twN,
-                            double *__restrict__ rows) {
+// The last block of a member to finish (counted in done[e]) forms the mass and
+// captures the target (mode 0) or restores it (mode 1, aeros_timestep.f90:1225-1251);
+// it sums the rows in latitude order, so the result does not depend on which
+// block finishes last.
+__global__ void k_mass(double2 *__restrict__ lnps, int M, int T, int nlm, int nh, int nlat, int nlon,
+                       const double *__restrict__ Ps, const int *__restrict__ moff, FftPlan plan,
+                       const double2 *__restrict__ tw, const double2 *__restrict__ twN, double *__restrict__ rows,
+                       const double *__restrict__ w, double c00, double *__restrict__ target,
+                       double *__restrict__ lnr_last, double *__restrict__ lnr_cum, unsigned *__restrict__ done,
+                       int mode) {
     extern __shared__ double2 sm[];
     const int n = nlon / 2, ms = T + 1;
     const int e = blockIdx.y, jn = blockIdx.x, js = nlat - 1 - jn;
@@ -375,27 +407,27 @@ __global__ void k_mass_rows(const double2 *__restrict__ lnps, int M, int T, int 
         }
         __syncthreads();
     }
+    __shared__ bool last;
     if (threadIdx.x == 0) {
         rows[(size_t)e * nlat + jn] = red[0][0];
         rows[(size_t)e * nlat + js] = red[1][0];
+        __threadfence();
+        last = atomicAdd(done + e, 1u) == (unsigned)(nh - 1);
     }
-}
-
-// mode 0: capture the target; mode 1: restore it (aeros_timestep.f90:1225-1251).
-__global__ void k_mass_fix(double2 *lnps, int nlm, int M, const double *__restrict__ rows,
-                           const double *__restrict__ w, int nlat, int nlon, double c00, double *target,
-                           double *lnr_last, double *lnr_cum, int mode) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M) return;
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    done[e] = 0;   // ready for the next launch
+    __threadfence();
+    const volatile double *re = rows + (size_t)e * nlat;
     const double dlon = 2.0 * kPi / nlon;
     double t = 0.0;
-    for (int j = 0; j < nlat; ++j) t += w[j] * rows[(size_t)e * nlat + j] * dlon;
-    double mass = t * kA * kA / kGrav;
+    for (int j = 0; j < nlat; ++j) t += w[j] * re[j] * dlon;
+    const double mass = t * kA * kA / kGrav;
     if (mode == 0) {
         if (target[e] < 0.0) target[e] = mass;
         return;
     }
-    double lnr = log(target[e] / mass);
+    const double lnr = log(target[e] / mass);
     lnps[(size_t)e * nlm].x += lnr * c00;
     lnr_last[e] = lnr;
     lnr_cum[e] += lnr;
@@ -588,6 +620,7 @@ struct aeros_dyn_s {
     bool phis_set = false;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
     double *mass_rows = nullptr, *mass_tgt = nullptr, *lnr_last = nullptr, *lnr_cum = nullptr;
+    unsigned *mass_done = nullptr;                   // per-member block counter of k_mass
     double *bud_rows = nullptr, *bud_res = nullptr, *zm = nullptr;
     int nsample = 0;
     int *flag = nullptr;
@@ -918,10 +951,15 @@ int run_tendency(Dyn &d, int hs_on) {
     if (rc) return rc;
     mark(d, "fourier_synth");
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
-    const int ct = d.tune.col_thr;
-    k_column<<<(unsigned)((ncol + ct - 1) / ct), ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M,
-                                                                  d.xlat_d, d.phis_set ? d.phis_d : nullptr, hs_on,
-                                                                  d.hs_dty_d, d.hs_ka_d);
+    const int ct = d.tune.col_thr, lpc = d.tune.col_lanes;
+    const unsigned nb = (unsigned)((ncol * lpc + ct - 1) / ct);
+    auto go = [&](auto kern) {
+        kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
+                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d);
+    };
+    if (lpc == 4) go(k_column<4>);
+    else if (lpc == 2) go(k_column<2>);
+    else go(k_column<1>);
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "column");
@@ -942,14 +980,12 @@ int run_tendency(Dyn &d, int hs_on) {
 int run_mass(Dyn &d, int mode) {
     const int n = d.g.nlon / 2;
     size_t smem = (size_t)(2 * d.g.ms + 4 * n) * sizeof(double2);
-    k_mass_rows<<<dim3(d.g.nh, d.M), 128, smem, d.stream>>>(d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat,
-                                                            d.g.nlon, d.tab.Ps, d.tab.moff, d.tab.plan, d.tab.tw,
-                                                            d.tab.twN, d.mass_rows);
-    mark(d, "mass_rows");
-    k_mass_fix<<<(d.M + 63) / 64, 64, 0, d.stream>>>(d.lnp(d.now), d.g.nlm, d.M, d.mass_rows, d.tab.w, d.g.nlat,
-                                                     d.g.nlon, d.c00, d.mass_tgt, d.lnr_last, d.lnr_cum, mode);
-    mark(d, "mass_fix");
-    d.launches += 2;
+    k_mass<<<dim3(d.g.nh, d.M), 128, smem, d.stream>>>(d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat,
+                                                       d.g.nlon, d.tab.Ps, d.tab.moff, d.tab.plan, d.tab.tw,
+                                                       d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt,
+                                                       d.lnr_last, d.lnr_cum, d.mass_done, mode);
+    mark(d, "mass");
+    d.launches += 1;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
 }
@@ -1076,7 +1112,7 @@ void destroy(Dyn *d) {
     void *ps[] = {d->now, d->old, d->tnd, d->FS, d->FA, d->G, d->GA, d->D, d->GT_d, d->TT_d, d->WT_d, d->nu_d,
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
-                  d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage};
+                  d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->split) split_destroy(d->split);
@@ -1134,7 +1170,7 @@ int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_ha
         (rc = dalloc(d->D, M * (3 * NL + 1) * ng)) || (rc = dalloc(d->mass_rows, M * d->g.nlat)) ||
         (rc = dalloc(d->lnr_last, M)) || (rc = dalloc(d->lnr_cum, M)) || (rc = dalloc(d->bud_rows, M * d->g.nlat * 3)) ||
         (rc = dalloc(d->bud_res, M * 3)) || (rc = dalloc(d->zm, M * (7 * NL * d->g.nlat + 2 * d->g.nlat))) ||
-        (rc = dalloc(d->flag, 1)) || (rc = dalloc(d->phis_d, ng))) {
+        (rc = dalloc(d->flag, 1)) || (rc = dalloc(d->phis_d, ng)) || (rc = dalloc(d->mass_done, M))) {
         destroy(d);
         return rc;
     }

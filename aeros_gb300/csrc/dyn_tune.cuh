@@ -57,7 +57,9 @@ bool tune_load(Dyn &d) {
         std::istringstream in(line);
         std::string k;
         Tune t;
-        if (!(in >> k >> t.fs_lpb >> t.fs_thr >> t.fa_lpb >> t.fa_thr >> t.la_ct >> t.col_thr >> t.spec_warps)) continue;
+        if (!(in >> k >> t.fs_lpb >> t.fs_thr >> t.fa_lpb >> t.fa_thr >> t.la_ct >> t.col_thr >> t.spec_warps >>
+              t.col_lanes))
+            continue;
         if (k != key) continue;
         d.tune = t;
         found = true;
@@ -71,7 +73,7 @@ void tune_store(Dyn &d) {
     std::ofstream f(path, std::ios::app);
     const Tune &t = d.tune;
     f << tune_key(d) << " " << t.fs_lpb << " " << t.fs_thr << " " << t.fa_lpb << " " << t.fa_thr << " " << t.la_ct
-      << " " << t.col_thr << " " << t.spec_warps << "\n";
+      << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << "\n";
 }
 
 int recapture(Dyn &d) {
@@ -135,7 +137,13 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
             for (int ct : {4, 8, 16})
                 if (ct != d.tune.la_ct) { Tune t = d.tune; t.la_ct = ct; trial(t); }
         for (int ct : {32, 64, 128, 256})
-            if (ct != d.tune.col_thr) { Tune t = d.tune; t.col_thr = ct; trial(t); }
+            for (int lp : {1, 2, 4})
+                if (ct != d.tune.col_thr || lp != d.tune.col_lanes) {
+                    Tune t = d.tune;
+                    t.col_thr = ct;
+                    t.col_lanes = lp;
+                    trial(t);
+                }
         for (int sw : {1, 2, 4, 8})
             if (sw != d.tune.spec_warps) { Tune t = d.tune; t.spec_warps = sw; trial(t); }
     }
@@ -156,12 +164,12 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
     return AEROS_OK;
 }
 
-// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps.
-int aeros_dyn_tune_get(aeros_dyn_t h, int *shape7) {
-    if (!h || !shape7) return AEROS_ERR_ARG;
+// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes.
+int aeros_dyn_tune_get(aeros_dyn_t h, int *shape8) {
+    if (!h || !shape8) return AEROS_ERR_ARG;
     const Tune &t = h->tune;
-    const int v[7] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr, t.spec_warps};
-    std::memcpy(shape7, v, sizeof(v));
+    const int v[8] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr, t.spec_warps, t.col_lanes};
+    std::memcpy(shape8, v, sizeof(v));
     return AEROS_OK;
 }
 
