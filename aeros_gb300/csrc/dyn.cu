@@ -35,6 +35,7 @@ struct LevConst {
     double A0, A1, B0, B1, dB;
     double dlnp, alpha, cfac;     // valid when pure
     double lnbf, bfk;             // ln(bf), bf^kappa with p_full = bf ps (pure)
+    double rdB;                   // 1 / (B1 - B0) (pure): 1/dp = rdB / ps
     double hf;                    // Held-Suarez max(0, (sigma - sigma_b)/(1 - sigma_b)) (pure)
     int pure;
     int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     const int C = (NL + LPC - 1) / LPC;
     const int k0 = min(NL, q * C), k1 = min(NL, k0 + C), nk = k1 - k0;
     const double lnps = act ? GF(7 * NL) : 0.0, dpx = act ? GF(7 * NL + 1) : 0.0, dpy = act ? GF(7 * NL + 2) : 0.0;
-    const double ps = exp(lnps);
+    const double ps = exp(lnps), rps = 1.0 / ps;
     // per-level column quantities of this lane's levels; 1/dp replaces the reference's divisions by dp
     double rdp[kChunk], dlnp[kChunk], alpha[kChunk], cfac[kChunk], gc[kChunk], cm[kChunk], scum[kChunk + 1],
         phi[kChunk];
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         const LevConst &L = c_lev[k];
         const double ph0 = fma(L.B0, ps, L.A0), ph1 = fma(L.B1, ps, L.A1);
         const double d = ph1 - ph0;
-        const double r = 1.0 / d;
+        const double r = L.pure ? L.rdB * rps : 1.0 / d;
         rdp[i] = r;
         if (L.pure) {
             dlnp[i] = L.dlnp;
@@ -264,29 +265,27 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
     double2 vnew = make_double2(vo.x + h * tv.x, vo.y + h * tv.y);
     double2 dnew, tnew, pnew;
     if (a.semi_implicit) {
-        // L(X^n): ltnow = -tau dnow (lower), lpnow = -nu . dnow, ldnow = lam (G tnow + pcoef pnow)
-        double2 ltn = z, ldn = z, lds = z, wd = z;
+        // Correction form with W = G tau + pcoef nu^T folded in (the same linear map
+        // as the reference's sequence, four level-matrix products instead of six):
+        //   rhs = dold + h rd + h lam [G (told - tnow + a rt) + pcoef (pold - pnow + a rp)]
+        //         + lam W (h a dnow - a1 (1 - a1) h^2 dold),           a = a1 h
+        //   dnew = Minv rhs,  db = a1 dnew + (1 - a1) dold
+        //   tnew = told + h (rt - tau (db - dnow)),  pnew = pold + h (rp - nu . (db - dnow))
+        const double2 pz = make_double2(pold.x - pnow.x + a.astep * rp.x, pold.y - pnow.y + a.astep * rp.y);
+        const double ha = h * a.astep;
+        const double2 y = act ? make_double2(told.x - tnow.x + a.astep * rt.x, told.y - tnow.y + a.astep * rt.y) : z;
+        const double2 x = act ? make_double2(ha * dnow.x - a.hh_old * dold.x, ha * dnow.y - a.hh_old * dold.y) : z;
+        double2 gy = z, wx = z;
         for (int j = 0; j < NL; ++j) {
-            double2 dj = shfl2(dnow, j), tj = shfl2(tnow, j), oj = shfl2(dold, j);
-            double tk = sT[j * NL + k], gk = sG[j * NL + k], wk = sW[j * NL + k];
-            ltn.x -= tk * dj.x; ltn.y -= tk * dj.y;          // tau[k][j] = 0 for j > k
-            ldn.x += gk * tj.x; ldn.y += gk * tj.y;          // G[k][j] = 0 for j < k
-            wd.x += wk * oj.x; wd.y += wk * oj.y;
+            const double2 yj = shfl2(y, j), xj = shfl2(x, j);
+            const double gk = sG[j * NL + k], wk = sW[j * NL + k];   // G[k][j], W[k][j]
+            gy.x += gk * yj.x; gy.y += gk * yj.y;
+            wx.x += wk * xj.x; wx.y += wk * xj.y;
         }
-        double2 nd = wsum2(act ? make_double2(sNu[k] * dnow.x, sNu[k] * dnow.y) : z);
-        double2 lpn = make_double2(-nd.x, -nd.y);
-        double pc = sPc[k];
-        ldn = make_double2(lam * (ldn.x + pc * pnow.x), lam * (ldn.y + pc * pnow.y));
-        double2 tst = make_double2(told.x + a.astep * (rt.x - ltn.x), told.y + a.astep * (rt.y - ltn.y));
-        double2 pst = make_double2(pold.x + a.astep * (rp.x - lpn.x), pold.y + a.astep * (rp.y - lpn.y));
-        for (int j = 0; j < NL; ++j) {
-            double2 tj = shfl2(tst, j);
-            double gk = sG[j * NL + k];
-            lds.x += gk * tj.x; lds.y += gk * tj.y;
-        }
-        lds = make_double2(lam * (lds.x + pc * pst.x), lam * (lds.y + pc * pst.y));
-        double2 rhs = make_double2(dold.x - a.hh_old * lam * wd.x + h * (rd.x + lds.x - ldn.x),
-                                   dold.y - a.hh_old * lam * wd.y + h * (rd.y + lds.y - ldn.y));
+        const double pc = sPc[k], hl = h * lam;
+        double2 rhs = make_double2(dold.x + h * rd.x + hl * (gy.x + pc * pz.x) + lam * wx.x,
+                                   dold.y + h * rd.y + hl * (gy.y + pc * pz.y) + lam * wx.y);
+        if (!act) rhs = z;
         const double *Mi = a.MinvT + (size_t)l * NL * NL;
         double mrow[kMaxLev];   // this lane's row of the inverse, loaded before the solve
 #pragma unroll
@@ -298,16 +297,17 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
             double2 rj = shfl2(rhs, j);
             dnew.x += mrow[j] * rj.x; dnew.y += mrow[j] * rj.y;
         }
-        double2 db = make_double2(a.a1 * dnew.x + (1.0 - a.a1) * dold.x, a.a1 * dnew.y + (1.0 - a.a1) * dold.y);
-        double2 td = z;
+        const double2 db = make_double2(a.a1 * dnew.x + (1.0 - a.a1) * dold.x, a.a1 * dnew.y + (1.0 - a.a1) * dold.y);
+        const double2 ed = act ? make_double2(db.x - dnow.x, db.y - dnow.y) : z;
+        double2 te = z;
         for (int j = 0; j < NL; ++j) {
-            double2 bj = shfl2(db, j);
-            double tk = sT[j * NL + k];
-            td.x += tk * bj.x; td.y += tk * bj.y;
+            const double2 ej = shfl2(ed, j);
+            const double tk = sT[j * NL + k];   // tau[k][j]
+            te.x += tk * ej.x; te.y += tk * ej.y;
         }
-        tnew = make_double2(told.x + h * (rt.x - td.x - ltn.x), told.y + h * (rt.y - td.y - ltn.y));
-        double2 nb = wsum2(act ? make_double2(sNu[k] * db.x, sNu[k] * db.y) : z);
-        pnew = make_double2(pold.x + h * (rp.x - nb.x - lpn.x), pold.y + h * (rp.y - nb.y - lpn.y));
+        tnew = make_double2(told.x + h * (rt.x - te.x), told.y + h * (rt.y - te.y));
+        const double2 ne = wsum2(act ? make_double2(sNu[k] * ed.x, sNu[k] * ed.y) : z);
+        pnew = make_double2(pold.x + h * (rp.x - ne.x), pold.y + h * (rp.y - ne.y));
     } else {
         dnew = make_double2(dold.x + h * rd.x, dold.y + h * rd.y);
         tnew = make_double2(told.x + h * rt.x, told.y + h * rt.y);
@@ -880,6 +880,7 @@ int upload_level_consts(Dyn &d) {
                 c.alpha = std::log(2.0);
             }
             c.cfac = (c.B0 * c.dlnp + c.dB * c.alpha) / c.dB;
+            c.rdB = 1.0 / c.dB;
             double bf = 0.5 * (c.B0 + c.B1);
             c.lnbf = std::log(bf);
             c.bfk = std::pow(bf, kKappa);

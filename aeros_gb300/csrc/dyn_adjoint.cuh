@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
 #define AB(f) Ab[(size_t)(f) * ng]
 #define GB(f) Bo[(size_t)(f) * ng]
         const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
-        const double ps = exp(lnps);
+        const double ps = exp(lnps), rps = 1.0 / ps;
         // ---- forward recomputation (k_column)
         double ph0[kMaxLev], ph1[kMaxLev], dp[kMaxLev], rdp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev],
             gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1];
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
             ph0[k] = fma(L.B0, ps, L.A0);
             ph1[k] = fma(L.B1, ps, L.A1);
             dp[k] = ph1[k] - ph0[k];
-            const double r = 1.0 / dp[k];
+            const double r = L.pure ? L.rdB * rps : 1.0 / dp[k];
             rdp[k] = r;
             if (L.pure) {
                 dlnp[k] = L.dlnp;
