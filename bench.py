@@ -520,10 +520,13 @@ def run_gpu(args, rank, world, local):
     hbm_gbs, bf16_tf, peak_src = measured_peaks()
     fp64_tf = fp64_peak_tflops(torch)
     traffic = None
-    tp = os.path.join(ROOT, "profiles", f"{dom}_T{args.trunc}L{args.nlev}.json")
+    tp = os.path.join(ROOT, "profiles", f"dram_traffic_T{args.trunc}L{args.nlev}.txt")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and parts[0] == dom:
+                    traffic = float(parts[1])
     if kind == "flops":
         achieved = amount / (prof[dom] / 1e3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_tf, "unit": "TFLOP/s",
