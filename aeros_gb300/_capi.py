@@ -79,6 +79,7 @@ _PROTOS = {
     "aeros_dyn_get_old_state": [_vp, _vp, _vp, _vp, _vp],
     "aeros_dyn_set_isothermal": [_vp, _d, _d],
     "aeros_dyn_set_phis": [_vp, _vp],
+    "aeros_dyn_hs_perturb": [_vp, _d],
     "aeros_dyn_step": [_vp, _i],
     "aeros_dyn_step_async": [_vp, _i],
     "aeros_dyn_sync": [_vp],

@@ -1275,6 +1275,27 @@ int aeros_dyn_set_isothermal(aeros_dyn_t h, double temp, double ps) {
     return AEROS_OK;
 }
 
+int aeros_dyn_hs_perturb(aeros_dyn_t h, double amp) {
+    // aeros_hs_perturb (src/physics/aeros_held_suarez.f90:295-336), every member
+    if (!h) return AEROS_ERR_ARG;
+    const int T = h->g.T, NL = h->NL, nlm = h->g.nlm;
+    std::vector<double2> t((size_t)h->M * NL * nlm);
+    double2 *dt = h->tmp(h->now);
+    AEROS_CUDA(cudaMemcpyAsync(t.data(), dt, t.size() * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int e = 0; e < h->M; ++e)
+        for (int k = 1; k <= NL; ++k)
+            for (int m = 1; m <= std::min(8, T); ++m)
+                for (int l = m; l <= std::min(m + 4, T); ++l) {
+                    double2 &c = t[((size_t)e * NL + (k - 1)) * nlm + m * (2 * T + 1 - m) / 2 + l];
+                    c.x += amp * std::cos((double)(3 * l + 5 * m + k));
+                    c.y += amp * std::sin((double)(7 * l + 2 * m + 3 * k));
+                }
+    AEROS_CUDA(cudaMemcpyAsync(dt, t.data(), t.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    return AEROS_OK;
+}
+
 int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis) {
     if (!h || !phis) return AEROS_ERR_ARG;
     AEROS_CUDA(cudaMemcpy(h->phis_d, phis, sizeof(double) * h->g.nlon * h->g.nlat, cudaMemcpyDefault));

@@ -106,6 +106,10 @@ class AerosDyn:
     def set_isothermal(self, temp=-1.0, ps=-1.0):
         _capi.check(_capi.lib().aeros_dyn_set_isothermal(self._h, float(temp), float(ps)), "aeros_dyn_set_isothermal")
 
+    def hs_perturb(self, amp=1.0):
+        """Deterministic Held-Suarez temperature seed (aeros_hs_perturb)."""
+        _capi.check(_capi.lib().aeros_dyn_hs_perturb(self._h, float(amp)), "aeros_dyn_hs_perturb")
+
     def set_phis(self, phis):
         p = np.ascontiguousarray(phis, np.float64)
         _capi.check(_capi.lib().aeros_dyn_set_phis(self._h, _ptr(p)), "aeros_dyn_set_phis")

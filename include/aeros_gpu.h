@@ -221,6 +221,11 @@ int aeros_dyn_get_old_state(aeros_dyn_t h, double *vor, double *div, double *tem
  * for all members.  Replaces aeros_set_isothermal (src/aeros.f90:130-183). */
 int aeros_dyn_set_isothermal(aeros_dyn_t h, double temp, double ps);
 
+/* Deterministic temperature seed of every member's current state: T_lm,k +=
+ * amp (cos(3l + 5m + k), sin(7l + 2m + 3k)) for m = 1..8, l = m..m+4, k = 1..nlev.
+ * Replaces aeros_hs_perturb (src/physics/aeros_held_suarez.f90:295-336). */
+int aeros_dyn_hs_perturb(aeros_dyn_t h, double amp);
+
 /* Surface geopotential (nlon, nlat) [m2 s-2], shared by all members.
  * Replaces aeros_timestep_set_phis (src/dynamics/aeros_timestep.f90:1817-1844). */
 int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis);

@@ -1035,6 +1035,20 @@ void set_isothermal(Dyn &d, double temp, double ps) {
     d.nstep = 0;
 }
 
+// aeros_hs_perturb (src/physics/aeros_held_suarez.f90:295-336): a deterministic
+// temperature seed on zonal wavenumbers 1-8, degrees m..m+4, every level
+// (k is the 1-based level index of the formula).
+void hs_perturb(Dyn &d, double amp) {
+    const int T = d.sht->T;
+    for (int k = 1; k <= d.nlev; ++k)
+        for (int m = 1; m <= std::min(8, T); ++m)
+            for (int l = m; l <= std::min(m + 4, T); ++l) {
+                const int lm = m * (2 * T + 1 - m) / 2 + l;
+                d.now.temp[(size_t)(k - 1) * d.nlm + lm] +=
+                    cd(amp * std::cos((double)(3 * l + 5 * m + k)), amp * std::sin((double)(7 * l + 2 * m + 3 * k)));
+            }
+}
+
 // aeros_timestep_diagnose (src/dynamics/aeros_timestep.f90:1873-1919)
 void diagnose(Dyn &d, double *u, double *v, double *t, double *ps) {
     const Sht &s = *d.sht;
@@ -1258,6 +1272,10 @@ int ora_dyn_set_old_state(void *h, const double *vor, const double *div, const d
 }
 int ora_dyn_set_isothermal(void *h, double temp, double ps) {
     set_isothermal(*(Dyn *)h, temp, ps);
+    return 0;
+}
+int ora_dyn_hs_perturb(void *h, double amp) {
+    hs_perturb(*(Dyn *)h, amp);
     return 0;
 }
 int ora_dyn_set_phis(void *h, const double *phis) {

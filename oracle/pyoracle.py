@@ -32,13 +32,14 @@ def lib():
                      "ora_sht_laplacian", "ora_sht_surface_integral", "ora_uv_from_vordiv",
                      "ora_vordiv_from_uv", "ora_gradient", "ora_dyn_info", "ora_dyn_set_state",
                      "ora_dyn_get_state", "ora_dyn_get_old_state", "ora_dyn_set_old_state",
-                     "ora_dyn_set_isothermal", "ora_dyn_set_phis", "ora_dyn_set_forcing",
+                     "ora_dyn_set_isothermal", "ora_dyn_set_phis", "ora_dyn_set_forcing", "ora_dyn_hs_perturb",
                      "ora_dyn_step", "ora_dyn_tendency", "ora_dyn_tendency_forced",
                      "ora_dyn_grid_rhs", "ora_dyn_diagnose", "ora_dyn_counters",
                      "ora_dyn_set_mass_target", "ora_dyn_budget", "ora_dyn_diag_accumulate",
                      "ora_dyn_diag_read", "ora_dyn_gwspeed", "ora_dyn_si_linear"]:
             getattr(L, name).restype = ctypes.c_int
         L.ora_dyn_set_isothermal.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+        L.ora_dyn_hs_perturb.argtypes = [vp, ctypes.c_double]
         L.ora_dyn_set_forcing.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.ora_dyn_set_mass_target.argtypes = [vp, ctypes.c_double]
         L.ora_dyn_step.argtypes = [vp, ctypes.c_int]
@@ -237,6 +238,9 @@ class OracleDyn:
 
     def set_isothermal(self, temp=-1.0, ps=-1.0):
         lib().ora_dyn_set_isothermal(self._h, float(temp), float(ps))
+
+    def hs_perturb(self, amp=1.0):
+        lib().ora_dyn_hs_perturb(self._h, float(amp))
 
     def set_phis(self, phis):
         phis = np.ascontiguousarray(phis, np.float64)

@@ -281,3 +281,13 @@ def test_config_T31L20_480_steps(gpulib):
     print("T31L20 daily max relative state difference (div, T, lnps):", ["%.1e" % x for x in daily],
           f"vorticity at day 10 {ev:.1e}")
     assert max(daily) < 1e-9 and ev < 1e-6
+
+
+def test_hs_perturb_matches_oracle(gpulib):
+    g, o, s = make_pair(42, 20)
+    g.set_isothermal(264.0, 1.0e5)
+    o.set_isothermal(264.0, 1.0e5)
+    g.hs_perturb(1.0)
+    o.hs_perturb(1.0)
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert np.array_equal(a, b)

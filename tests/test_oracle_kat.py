@@ -395,3 +395,24 @@ def test_restart_split_run_bitwise():
     c.step(3)
     for x, y in zip(c.get_state(), a.get_state()):
         assert np.array_equal(x, y)
+
+
+def test_hs_perturb_formula():
+    """aeros_hs_perturb (src/physics/aeros_held_suarez.f90:295-336): T_lm,k +=
+    amp (cos(3l + 5m + k), sin(7l + 2m + 3k)) for m = 1..min(8, T),
+    l = m..min(m+4, T), k = 1..nlev, added to the isothermal state."""
+    from oracle.pyoracle import OracleDyn
+    from aeros_gb300.params import held_suarez_params
+    T, nlev, amp = 21, 5, 0.7
+    o = OracleDyn(held_suarez_params(trunc=T, nlev=nlev))
+    o.set_isothermal(264.0, 1.0e5)
+    _, _, t0, _ = o.get_state()
+    o.hs_perturb(amp)
+    _, _, t1, _ = o.get_state()
+    exp = t0.copy()
+    for k in range(1, nlev + 1):
+        for m in range(1, min(8, T) + 1):
+            for l in range(m, min(m + 4, T) + 1):
+                lm = m * (2 * T + 1 - m) // 2 + l
+                exp[k - 1, lm] += amp * np.cos(3 * l + 5 * m + k) + 1j * amp * np.sin(7 * l + 2 * m + 3 * k)
+    assert np.array_equal(t1, exp)
