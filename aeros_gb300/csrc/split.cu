@@ -235,18 +235,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     bool ok = true;
     for (int ch = 0; ch < nch && ok; ++ch) {
         const int kc = min(kKC, Kp - ch * kKC);
-        if (ch > 0) {
-            for (int task = tid; task < ncl * (kc / 8); task += kThreads) {
-                const int cc = task / (kc / 8), k0 = (task - cc * (kc / 8)) * 8;
-                for (int i = 0; i < 8; ++i) {
-                    const int k = ch * kKC + k0 + i;
-                    const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
-                    stage[(2 * cc) * kSt + k0 + i] = v.x;
-                    stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
-                }
-            }
-            __syncthreads();
-        }
         // digits of the data columns (columns of absent fields are zero)
         // lanes take consecutive tile rows n: 16-byte digit stores fill whole core matrices
         for (int task = tid; task < kNTs * (kc / 8); task += kThreads) {
@@ -273,10 +261,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
                 mbar_arrive(&mbarM);
             }
         }
+        // the next chunk's coefficients while the tensor core works on this one
+        if (ch + 1 < nch) {
+            const int kn = min(kKC, Kp - (ch + 1) * kKC);
+            for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
+                const int cc = task / (kn / 8), k0 = (task - cc * (kn / 8)) * 8;
+                for (int i = 0; i < 8; ++i) {
+                    const int k = (ch + 1) * kKC + k0 + i;
+                    const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
+                    stage[(2 * cc) * kSt + k0 + i] = v.x;
+                    stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
+                }
+            }
+        }
         ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
         asm volatile("tcgen05.fence::after_thread_sync;");
-        __syncthreads();
-        ok = ok && !fail;
+        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
         if (ok && tid == 0 && ch + 1 < nch) {
             bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
         }
@@ -461,16 +461,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     bool ok = true;
     for (int ch = 0; ch < nch && ok; ++ch) {
         const int kc = min(kKC, KpA - ch * kKC);
-        if (ch > 0) {
-            for (int task = tid; task < ncl * 3 * kc; task += kThreads) {
-                const int jl = task % kc, cs = task / kc, cc = cs / 3, slot = cs - cc * 3;
-                double v[4];
-                bvals(cc, slot, ch * kKC + jl, v);
-#pragma unroll
-                for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
-            }
-            __syncthreads();
-        }
         for (int task = tid; task < kNTa * (kc / 8); task += kThreads) {
             const int n = task % kNTa, k0 = (task / kNTa) * 8;
             const int cc = (n % 4) >> 1;
@@ -496,10 +486,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
                 mbar_arrive(&mbarM);
             }
         }
+        // the next chunk's grid values while the tensor core works on this one
+        if (ch + 1 < nch) {
+            const int kn = min(kKC, KpA - (ch + 1) * kKC);
+            for (int task = tid; task < ncl * 3 * kn; task += kThreads) {
+                const int jl = task % kn, cs = task / kn, cc = cs / 3, slot = cs - cc * 3;
+                double v[4];
+                bvals(cc, slot, (ch + 1) * kKC + jl, v);
+#pragma unroll
+                for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
+            }
+        }
         ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
         asm volatile("tcgen05.fence::after_thread_sync;");
-        __syncthreads();
-        ok = ok && !fail;
+        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
         if (ok && tid == 0 && ch + 1 < nch) {
             bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
         }

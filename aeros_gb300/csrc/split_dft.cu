@@ -209,15 +209,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     bool ok = true;
     for (int ch = 0; ch < nch && ok; ++ch) {
         const int kc = min(kKC, Kp - ch * kKC);
-        if (ch > 0) {
-            for (int task = tid; task < ncl * (kc / 8); task += kThreads) {
-                const int n = task / (kc / 8), k0 = (task - n * (kc / 8)) * 8;
-                double x[8];
-                p.bvals8(c0 + n, ch * kKC + k0, x);
-                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = ch * kKC + k0 + i < K ? x[i] : 0.0;
-            }
-            __syncthreads();
-        }
         for (int task = tid; task < kNT * (kc / 8); task += kThreads) {
             const int n = task % kNT, k0 = (task / kNT) * 8;
             double x[8];
@@ -242,10 +233,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                 mbar_arrive(&mbarM);
             }
         }
+        // the next chunk's data values while the tensor core works on this one
+        if (ch + 1 < nch) {
+            const int kn = min(kKC, Kp - (ch + 1) * kKC);
+            for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
+                const int n = task / (kn / 8), k0 = (task - n * (kn / 8)) * 8;
+                double x[8];
+                p.bvals8(c0 + n, (ch + 1) * kKC + k0, x);
+                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = (ch + 1) * kKC + k0 + i < K ? x[i] : 0.0;
+            }
+        }
         ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
         asm volatile("tcgen05.fence::after_thread_sync;");
-        __syncthreads();
-        ok = ok && !fail;
+        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
         if (ok && tid == 0 && ch + 1 < nch)
             bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
     }

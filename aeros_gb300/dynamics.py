@@ -149,7 +149,8 @@ class AerosDyn:
         if time_years < self.time:
             raise ValueError("cannot step backwards")
         nstep = self.counters()[0]
-        target = int(np.rint((time_years - self.time_init) * YEAR_SECONDS / self.params.dt))
+        x = (time_years - self.time_init) * YEAR_SECONDS / self.params.dt
+        target = int(np.sign(x) * np.floor(abs(x) + 0.5))   # Fortran nint: halves away from zero
         if target > nstep:
             self.step(target - nstep)
         self.time = time_years
