@@ -221,23 +221,25 @@ template <int B>
 __device__ __forceinline__ int zexp(int er, int ec) { return er + ec - 2 * B - 38; }
 
 // ------------------------------------------------------------------ common MMA issue
-// D_q += A_s B_t^T over one chunk for every s + t = q <= S - 1.  Consecutive
-// MMAs go to different accumulators (t runs fastest), so no MMA waits on the
-// accumulation of the one before it.
+// D_q += A_s B_t^T over one chunk for every s + t = q <= S - 1.  The data
+// slices B_0 .. B_{S-1} lie back to back in shared memory (slice t = rows
+// t NT .. of one (S NT)-row K-major matrix) and the accumulators D_0 .. D_{S-1}
+// back to back in TMEM columns, so for one s all t <= S - 1 - s are a single
+// MMA with N = (S - s) NT: D[:, s NT ..) += A_s [B_0 .. B_{S-1-s}]^T.  S MMAs
+// per 16-deep k step instead of S (S + 1) / 2 narrow ones.  The first MMA of a
+// tile (s = 0) spans every accumulator and initialises them.
 template <int S>
 __device__ __forceinline__ void issue_chunk(uint32_t tmem, const __nv_bfloat16 *sA, const __nv_bfloat16 *sB, int NT,
                                             int kc, bool first) {
-    const uint32_t id = idesc_bf16(kTM, NT);
+    static_assert(S * kNTile <= 256 && kNTile % 16 == 0, "one MMA spans at most 256 columns, N a multiple of 16");
     const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
 #pragma unroll 1
     for (int k0 = 0; k0 < kc; k0 += 16)
 #pragma unroll
         for (int s = 0; s < S; ++s)
-#pragma unroll
-            for (int t = 0; t < S - s; ++t)
-                mma_bf16(tmem + (uint32_t)((s + t) * NT), sdesc(a0 + (uint32_t)(s * kTM * kSlice * 2 + (k0 / 8) * 128)),
-                         sdesc(b0 + (uint32_t)(t * NT * kSlice * 2 + (k0 / 8) * 128)), id,
-                         (first && s == 0 && k0 == 0) ? 0u : 1u);
+            mma_bf16(tmem + (uint32_t)(s * NT), sdesc(a0 + (uint32_t)(s * kTM * kSlice * 2 + (k0 / 8) * 128)),
+                     sdesc(b0 + (uint32_t)((k0 / 8) * 128)), idesc_bf16(kTM, (S - s) * NT),
+                     (first && s == 0 && k0 == 0) ? 0u : 1u);
 }
 
 }  // namespace
