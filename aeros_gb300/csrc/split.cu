@@ -132,8 +132,11 @@ struct SynSplitArgs {
 template <int S>
 constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + (size_t)kNTs * kSt * 8; }
 template <int S>
-constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + (size_t)kNTa * kSt * 8; }
+constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + 2 * (size_t)kNTa * kSt * 8; }
 
+// One CTA per (m, latitude tile, group slot z): it steps through column groups
+// z, z + gridDim.z, ... (16 complex columns each) with its TMEM, barriers and
+// (for a one-chunk contraction) the table tile kept.
 template <int S, int B>
 __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -150,16 +153,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int m = blockIdx.x, t = blockIdx.y, nt = blockIdx.z;
+    const int m = blockIdx.x, t = blockIdx.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = a.T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
     const int mo = a.moff[m];
-    const int c0 = nt * (kNTs / 2);
-    const int ncl = min(kNTs / 2, a.ncol - c0);
-    if (ncl <= 0) return;
-    if (tid < ncl) scol[tid] = a.cols[c0 + tid];
-    if (tid < kNTs) cexp[tid] = 0;
-    if (tid == 0) { anyD = 0; fail = 0; }
+    const int ngrp = (a.ncol + kNTs / 2 - 1) / (kNTs / 2);
+    if ((int)blockIdx.z >= ngrp) return;
+    if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(kTmemCols));
@@ -173,167 +173,201 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     __syncthreads();
     const __nv_bfloat16 *gA = a.dig + a.sbase[m] + (size_t)t * nch * S * kTM * kSlice;
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    if (tid < ncl && scol[tid].rowD >= 0) anyD = 1;
-
-    // value k of complex column cc (scaled input coefficient)
-    auto coef = [&](int cc, int k) -> double2 {
-        const SynCol &sc = scol[cc];
-        double2 v = sc.src[mo + k];
-        if (sc.scale) {
-            const double f = a.lfac[sc.scale * a.ms + m + k];
-            v.x *= f;
-            v.y *= f;
-        }
-        return v;
-    };
-    // phase 1: column scales over the full contraction, chunk 0 staged
-    const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
-    for (int base = 0; base < ncl * nk8; base += kThreads) {
-        const int task = base + tid;
-        const bool valid = task < ncl * nk8;
-        const int cc = valid ? task / nk8 : -1, k0 = valid ? (task - cc * nk8) * 8 : 0;
-        int br = 0, bi = 0;
-        double re[8], im[8], f[8];
-        const double2 *src = valid ? scol[cc].src + mo + k0 : nullptr;
-        const int sci = valid ? scol[cc].scale : 0;
-        const double *lf = a.lfac + sci * a.ms + m + k0;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {   // all loads first
-            const bool in = valid && k0 + i < K;
-            const double2 v = in ? __ldg(src + i) : make_double2(0.0, 0.0);
-            re[i] = v.x;
-            im[i] = v.y;
-            f[i] = in && sci ? __ldg(lf + i) : 1.0;
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (sci) {
-                re[i] *= f[i];
-                im[i] *= f[i];
-            }
-            br = max(br, bexp(re[i]));
-            bi = max(bi, bexp(im[i]));
-        }
-        const unsigned peers = __match_any_sync(0xffffffffu, cc);
-        br = __reduce_max_sync(peers, br);
-        bi = __reduce_max_sync(peers, bi);
-        if (valid && lane == __ffs(peers) - 1) {
-            atomicMax(&cexp[2 * cc], br);
-            atomicMax(&cexp[2 * cc + 1], bi);
-        }
-        if (valid && k0 < kc0)
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                stage[(2 * cc) * kSt + k0 + i] = re[i];
-                stage[(2 * cc + 1) * kSt + k0 + i] = im[i];
-            }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
+    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+    const int jj = lane, jn = t * 32 + jj, js = a.nlat - 1 - jn;
+    const int *re = a.rexp + ((size_t)m * a.ntl + t) * kTM;
+    const int eRow = re[quarter * 32 + jj];
+    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
+    uint32_t nl = 1;           // table loads issued (thread 0's count)
     bool ok = true;
-    for (int ch = 0; ch < nch && ok; ++ch) {
-        const int kc = min(kKC, Kp - ch * kKC);
-        // digits of the data columns (columns of absent fields are zero)
-        // lanes take consecutive tile rows n: 16-byte digit stores fill whole core matrices
-        for (int task = tid; task < kNTs * (kc / 8); task += kThreads) {
-            const int n = task % kNTs, k0 = (task / kNTs) * 8;
-            double x[8];
-            if ((n >> 1) < ncl) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) x[i] = 0.0;
-            }
-            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTs * kSlice, n, k0);
-        }
-        asm volatile("fence.proxy.async.shared::cta;");
+
+    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gridDim.z) {
+        const int c0 = grp * (kNTs / 2);
+        const int ncl = min(kNTs / 2, a.ncol - c0);
+        if (tid < ncl) scol[tid] = a.cols[c0 + tid];
+        if (tid < kNTs) cexp[tid] = 0;
+        if (tid == 0) anyD = 0;
         __syncthreads();
-        if (tid == 0) {
-            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                issue_chunk<S>(tmem, sA, sB, kNTs, kc, ch == 0);
-                mma_commit(&mbarM);
-            } else {
-                fail = 1;
-                mbar_arrive(&mbarM);
+        if (tid < ncl && scol[tid].rowD >= 0) anyD = 1;
+        // value k of complex column cc (scaled input coefficient)
+        auto coef = [&](int cc, int k) -> double2 {
+            const SynCol &sc = scol[cc];
+            double2 v = sc.src[mo + k];
+            if (sc.scale) {
+                const double f = a.lfac[sc.scale * a.ms + m + k];
+                v.x *= f;
+                v.y *= f;
+            }
+            return v;
+        };
+        // phase 1: column scales over the full contraction, chunk 0 staged
+        const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+        for (int base = 0; base < ncl * nk8; base += kThreads) {
+            const int task = base + tid;
+            const bool valid = task < ncl * nk8;
+            const int cc = valid ? task / nk8 : -1, k0 = valid ? (task - cc * nk8) * 8 : 0;
+            int br = 0, bi = 0;
+            double re8[8], im8[8], f[8];
+            const double2 *src = valid ? scol[cc].src + mo + k0 : nullptr;
+            const int sci = valid ? scol[cc].scale : 0;
+            const double *lf = a.lfac + sci * a.ms + m + k0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {   // all loads first
+                const bool in = valid && k0 + i < K;
+                const double2 v = in ? __ldg(src + i) : make_double2(0.0, 0.0);
+                re8[i] = v.x;
+                im8[i] = v.y;
+                f[i] = in && sci ? __ldg(lf + i) : 1.0;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (sci) {
+                    re8[i] *= f[i];
+                    im8[i] *= f[i];
+                }
+                br = max(br, bexp(re8[i]));
+                bi = max(bi, bexp(im8[i]));
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, cc);
+            br = __reduce_max_sync(peers, br);
+            bi = __reduce_max_sync(peers, bi);
+            if (valid && lane == __ffs(peers) - 1) {
+                atomicMax(&cexp[2 * cc], br);
+                atomicMax(&cexp[2 * cc + 1], bi);
+            }
+            if (valid && k0 < kc0)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    stage[(2 * cc) * kSt + k0 + i] = re8[i];
+                    stage[(2 * cc + 1) * kSt + k0 + i] = im8[i];
+                }
+        }
+        __syncthreads();
+        for (int ch = 0; ch < nch && ok; ++ch) {
+            const int kc = min(kKC, Kp - ch * kKC);
+            // digits of the data columns (columns of absent fields are zero)
+            // lanes take consecutive tile rows n: 16-byte digit stores fill whole core matrices
+            for (int task = tid; task < kNTs * (kc / 8); task += kThreads) {
+                const int n = task % kNTs, k0 = (task / kNTs) * 8;
+                double x[8];
+                if ((n >> 1) < ncl) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) x[i] = 0.0;
+                }
+                put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTs * kSlice, n, k0);
+            }
+            asm volatile("fence.proxy.async.shared::cta;");
+            __syncthreads();
+            // a one-chunk table stays in shared memory after its first wait
+            const bool needA = nch > 1 || na == 0;
+            if (tid == 0) {
+                if (!needA || mbar_wait(&mbarA, na & 1u)) {
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    issue_chunk<S>(tmem, sA, sB, kNTs, kc, ch == 0);
+                    mma_commit(&mbarM);
+                } else {
+                    fail = 1;
+                    mbar_arrive(&mbarM);
+                }
+            }
+            if (needA) ++na;
+            // the next chunk's coefficients while the tensor core works on this one
+            if (ch + 1 < nch) {
+                const int kn = min(kKC, Kp - (ch + 1) * kKC);
+                for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
+                    const int cc = task / (kn / 8), k0 = (task - cc * (kn / 8)) * 8;
+                    for (int i = 0; i < 8; ++i) {
+                        const int k = (ch + 1) * kKC + k0 + i;
+                        const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
+                        stage[(2 * cc) * kSt + k0 + i] = v.x;
+                        stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
+                    }
+                }
+            }
+            ok = mbar_wait(&mbarM, nm & 1u);
+            ++nm;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
+            // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next group
+            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || grp + (int)gridDim.z < ngrp)) {
+                bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
+                          &mbarA);
+                ++nl;
             }
         }
-        // the next chunk's coefficients while the tensor core works on this one
-        if (ch + 1 < nch) {
-            const int kn = min(kKC, Kp - (ch + 1) * kKC);
-            for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
-                const int cc = task / (kn / 8), k0 = (task - cc * (kn / 8)) * 8;
-                for (int i = 0; i < 8; ++i) {
-                    const int k = (ch + 1) * kKC + k0 + i;
-                    const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
-                    stage[(2 * cc) * kSt + k0 + i] = v.x;
-                    stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
+        if (!ok) break;
+        // epilogue: warp w holds TMEM lane quarter w % 4 (row block P even,
+        // P odd, dP even, dP odd; lane = latitude) for columns 16 (w / 4) .. +16.
+        // The odd blocks go through shared memory (sB + stage, free now) to the
+        // even blocks' warps, which add the hemispheres as integers and store.
+        long long *zodd = reinterpret_cast<long long *>(sB);   // [2 blocks][32 lanes][kNTs + 1]
+        const bool live = quarter < 2 || anyD;
+        // the 8 accumulated columns c16 + h .. + 8 of this warp's lane quarter
+        auto zcols = [&](int h, long long *z) {
+            uint32_t r[S][8];
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+                tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) z[i] = 0;
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+        };
+        if (live && (quarter & 1))
+#pragma unroll 1
+            for (int h = 0; h < 16; h += 8) {
+                long long z[8];
+                zcols(h, z);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    zodd[((size_t)(quarter >> 1) * 32 + lane) * (kNTs + 1) + c16 + h + i] = z[i];
+            }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        // tcgen05.ld is warp-collective: the whole warp loads, lanes past the
+        // last latitude only skip the stores
+        if (live && !(quarter & 1)) {
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const long long *O = zodd + ((size_t)(quarter >> 1) * 32 + lane) * (kNTs + 1) + c16;
+            const bool dP = quarter == 2;
+#pragma unroll 1
+            for (int h = 0; h < 16; h += 8) {
+                if (((c16 + h) >> 1) >= ncl) break;
+                long long z[8];
+                zcols(h, z);
+#pragma unroll
+                for (int i = 0; i < 8; i += 2) {
+                    const int cc = (c16 + h + i) >> 1;
+                    if (cc >= ncl || jn >= a.nh) break;
+                    const SynCol &sc = scol[cc];
+                    const int row = dP ? sc.rowD : sc.rowP;
+                    if (row < 0) continue;
+                    const int ecr = zexp<B>(eRow, scale_exp(cexp[2 * cc]));
+                    const int eci = zexp<B>(eRow, scale_exp(cexp[2 * cc + 1]));
+                    const long long oe = O[h + i], oi = O[h + i + 1];
+                    // P: north E + O, south E - O; dP/dtheta is odd about the equator: south O - E
+                    const double2 nv = make_double2(z_to_f64(z[i] + oe, ecr), z_to_f64(z[i + 1] + oi, eci));
+                    const double2 sv = dP ? make_double2(z_to_f64(oe - z[i], ecr), z_to_f64(oi - z[i + 1], eci))
+                                          : make_double2(z_to_f64(z[i] - oe, ecr), z_to_f64(z[i + 1] - oi, eci));
+                    a.F[((size_t)jn * a.nrow + row) * a.ms + m] = nv;
+                    a.F[((size_t)js * a.nrow + row) * a.ms + m] = sv;
                 }
             }
         }
-        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
-        if (ok && tid == 0 && ch + 1 < nch) {
-            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();   // zodd (= sB, stage), scol and cexp are rewritten by the next group
     }
-    if (!ok) {
-        if (tid == 0) atomicOr(a.err, 1);
-    } else {
-        // epilogue 1: warp w reads TMEM lane quarter w % 4 = row block (P even,
-        // P odd, dP even, dP odd; lane = latitude) and columns 16 (w / 4) .. +16
-        long long *zst = reinterpret_cast<long long *>(smraw);   // [128 rows][kNTs + 1]
-        const int quarter = warp & 3, c16 = (warp >> 2) * 16;
-        if (quarter < 2 || anyD) {
-            for (int h = 0; h < 16; h += 8) {
-                long long z[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) z[i] = 0;
-                uint32_t r[S][8];
-#pragma unroll
-                for (int q = 0; q < S; ++q)
-                    tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
-                tmem_wait_ld();
-#pragma unroll
-                for (int q = 0; q < S; ++q)
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * (kNTs + 1) + c16 + h + i] = z[i];
-            }
-        }
-        __syncthreads();
-        // epilogue 2: hemispheres as integer sums, then FP64
-        const int *re = a.rexp + ((size_t)m * a.ntl + t) * kTM;
-        for (int idx = tid; idx < 32 * ncl; idx += kThreads) {
-            const int jj = idx / ncl, cc = idx - jj * ncl;
-            const int jn = t * 32 + jj;
-            if (jn >= a.nh) continue;
-            const int js = a.nlat - 1 - jn;
-            const SynCol &sc = scol[cc];
-            const int ecr = scale_exp(cexp[2 * cc]), eci = scale_exp(cexp[2 * cc + 1]);
-            const long long *E = zst + (size_t)(0 * 32 + jj) * (kNTs + 1) + 2 * cc;
-            const long long *O = zst + (size_t)(1 * 32 + jj) * (kNTs + 1) + 2 * cc;
-            const int eP = re[jj];
-            a.F[((size_t)jn * a.nrow + sc.rowP) * a.ms + m] =
-                make_double2(z_to_f64(E[0] + O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] + O[1], zexp<B>(eP, eci)));
-            a.F[((size_t)js * a.nrow + sc.rowP) * a.ms + m] =
-                make_double2(z_to_f64(E[0] - O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] - O[1], zexp<B>(eP, eci)));
-            if (sc.rowD >= 0) {
-                const long long *dE = zst + (size_t)(2 * 32 + jj) * (kNTs + 1) + 2 * cc;
-                const long long *dO = zst + (size_t)(3 * 32 + jj) * (kNTs + 1) + 2 * cc;
-                const int eD = re[64 + jj];
-                a.F[((size_t)jn * a.nrow + sc.rowD) * a.ms + m] = make_double2(
-                    z_to_f64(dE[0] + dO[0], zexp<B>(eD, ecr)), z_to_f64(dE[1] + dO[1], zexp<B>(eD, eci)));
-                a.F[((size_t)js * a.nrow + sc.rowD) * a.ms + m] = make_double2(
-                    z_to_f64(dO[0] - dE[0], zexp<B>(eD, ecr)), z_to_f64(dO[1] - dE[1], zexp<B>(eD, eci)));
-            }
-        }
-    }
+    if (!ok && tid == 0) atomicOr(a.err, 1);
+    // a table chunk still in flight must land before the CTA exits (bounded wait)
+    if (tid == 0 && nl > na) (void)mbar_wait(&mbarA, na & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
@@ -359,42 +393,37 @@ __host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
     return fold * 12 + slot * 4 + cc * 2 + comp;
 }
 
+// One CTA per (m, l tile, group slot z): it steps through column groups
+// z, z + gridDim.z, ... with its TMEM, barriers and (for a one-chunk
+// contraction) the table tile kept.  Software pipeline: the next group's grid
+// values are gathered (and its column scales formed) into the second stage
+// buffer while the tensor core works on the current group.
 template <int S, int B>
 __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
     __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
-    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // [kNTa cols][kSt]
+    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // 2 x [kNTa cols][kSt]
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
-    __shared__ int cexp[kNTa];
-    __shared__ AnaCol scol[kFa];
-    __shared__ int skind[kFa][2];      // slot scaling: 0 real (b = 0), 1 imaginary (a = 0), 2 general
-    __shared__ double sbm[kFa][2];     // b m of the slot
+    __shared__ int cexp[2][kNTa];
+    __shared__ AnaCol scol[2][kFa];
+    __shared__ int skind[2][kFa][2];   // slot scaling: 0 real (b = 0), 1 imaginary (a = 0), 2 general
+    __shared__ double sbm[2][kFa][2];  // b m of the slot
     __shared__ int fail;
 
     if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int m = blockIdx.x, t = blockIdx.y, nt = blockIdx.z;
+    const int m = blockIdx.x, t = blockIdx.y;
     const int K = a.T - m + 1;
-    if (64 * t >= K) return;
+    const int ngrp = (a.ncol + kFa - 1) / kFa;
+    if (64 * t >= K || (int)blockIdx.z >= ngrp) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int c0 = nt * kFa;
-    const int ncl = min(kFa, a.ncol - c0);
-    if (ncl <= 0) return;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
-    if (tid < ncl) scol[tid] = a.cols[c0 + tid];
-    if (tid < kNTa) cexp[tid] = 0;
+    const int gstep = gridDim.z;
     if (tid == 0) fail = 0;
-    if (tid < 2 * ncl) {
-        const AnaCol q = a.cols[c0 + (tid >> 1)];
-        const int sl = tid & 1;
-        const double aa = sl == 0 ? q.a1 : q.a2, bb = sl == 0 ? q.b1 : q.b2;
-        skind[tid >> 1][sl] = (__double_as_longlong(bb) << 1) == 0 ? 0 : ((__double_as_longlong(aa) << 1) == 0 ? 1 : 2);
-        sbm[tid >> 1][sl] = bb * m;
-    }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                      "r"(kTmemCols));
@@ -405,13 +434,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         mbar_init(&mbarM);
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    __syncthreads();
     const __nv_bfloat16 *gA = a.dig + a.abase[m] + (size_t)t * nch * S * kTM * kSlice;
-    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
 
-    // the four B values (fold x comp) of field cc, slot s at north latitude j
-    auto bvals = [&](int cc, int slot, int j, double *v) {
-        const AnaCol &q = scol[cc];
+    // group metadata into buffer b (scale classes of the two slots)
+    auto set_meta = [&](int grp, int b) {
+        const int c0 = grp * kFa, ncl = min(kFa, a.ncol - c0);
+        if (tid < ncl) scol[b][tid] = a.cols[c0 + tid];
+        if (tid < kNTa) cexp[b][tid] = 0;
+        if (tid < 2 * ncl) {
+            const AnaCol q = a.cols[c0 + (tid >> 1)];
+            const int sl = tid & 1;
+            const double aa = sl == 0 ? q.a1 : q.a2, bb = sl == 0 ? q.b1 : q.b2;
+            skind[b][tid >> 1][sl] =
+                (__double_as_longlong(bb) << 1) == 0 ? 0 : ((__double_as_longlong(aa) << 1) == 0 ? 1 : 2);
+            sbm[b][tid >> 1][sl] = bb * m;
+        }
+    };
+    // the four B values (fold x comp) of field cc, slot s at north latitude j (buffer b)
+    auto bvals = [&](int b, int cc, int slot, int j, double *v) {
+        const AnaCol &q = scol[b][cc];
         const int row = slot == 0 ? q.row1 : (slot == 1 ? q.row2 : q.row3);
         if (row < 0 || j >= a.nh) { v[0] = v[1] = v[2] = v[3] = 0.0; return; }
         const double2 fn = a.F[((size_t)j * a.nrow + row) * a.ms + m];
@@ -419,12 +460,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         // fold first (the scaling is linear), then scale by (a + i b m / sin)
         const double er = fn.x + fs.x, ei = fn.y + fs.y, orr = fn.x - fs.x, oi = fn.y - fs.y;
         if (slot < 2) {
-            const int kd = skind[cc][slot];
+            const int kd = skind[b][cc][slot];
             const double aa = slot == 0 ? q.a1 : q.a2;
             if (kd == 0) {
                 v[0] = aa * er; v[1] = aa * ei; v[2] = aa * orr; v[3] = aa * oi;
             } else {
-                const double bb = sbm[cc][slot] * a.isin[j];
+                const double bb = sbm[b][cc][slot] * a.isin[j];
                 if (kd == 1) {
                     v[0] = -bb * ei; v[1] = bb * er; v[2] = -bb * oi; v[3] = bb * orr;
                 } else {
@@ -436,77 +477,104 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             v[0] = er; v[1] = ei; v[2] = orr; v[3] = oi;
         }
     };
-    // phase 1: column scales over all latitudes, chunk 0 staged
-    const int kc0 = min(kKC, KpA);
-    for (int base = 0; base < ncl * 3 * KpA; base += kThreads) {
-        const int task = base + tid;
-        const bool valid = task < ncl * 3 * KpA;
-        const int j = task % KpA, cs = valid ? task / KpA : -1, cc = cs / 3, slot = cs - cc * 3;
-        double v[4] = {0.0, 0.0, 0.0, 0.0};
-        if (valid) bvals(cc, slot, j, v);
-        const unsigned peers = __match_any_sync(0xffffffffu, cs);
-        const bool leader = valid && lane == __ffs(peers) - 1;
+    // phase 1 of group grp into buffer b: column scales over all latitudes, chunk 0 staged
+    auto gather = [&](int grp, int b) {
+        const int ncl = min(kFa, a.ncol - grp * kFa);
+        double *stage = stage0 + (size_t)b * kNTa * kSt;
+        const int kc0 = min(kKC, KpA);
+        for (int base = 0; base < ncl * 3 * KpA; base += kThreads) {
+            const int task = base + tid;
+            const bool valid = task < ncl * 3 * KpA;
+            const int j = task % KpA, cs = valid ? task / KpA : -1, cc = cs / 3, slot = cs - cc * 3;
+            double v[4] = {0.0, 0.0, 0.0, 0.0};
+            if (valid) bvals(b, cc, slot, j, v);
+            const unsigned peers = __match_any_sync(0xffffffffu, cs);
+            const bool leader = valid && lane == __ffs(peers) - 1;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
-            const int n = acol(f >> 1, slot, cc, f & 1);
-            const int be = __reduce_max_sync(peers, bexp(v[f]));
-            if (leader) atomicMax(&cexp[n], be);
-            if (valid && j < kc0) stage[n * kSt + j] = v[f];
+            for (int f = 0; f < 4; ++f) {
+                const int n = acol(f >> 1, slot, cc, f & 1);
+                const int be = __reduce_max_sync(peers, bexp(v[f]));
+                if (leader) atomicMax(&cexp[b][n], be);
+                if (valid && j < kc0) stage[n * kSt + j] = v[f];
+            }
         }
-    }
+    };
+
+    set_meta(blockIdx.z, 0);
+    __syncthreads();
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    gather(blockIdx.z, 0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
+    const int er = a.rexp[((size_t)m * a.ntlA + t) * kTM + (warp & 3) * 32 + lane];   // this thread's epilogue row
+    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
+    uint32_t nl = 1;           // table loads issued (thread 0's count)
     bool ok = true;
-    for (int ch = 0; ch < nch && ok; ++ch) {
-        const int kc = min(kKC, KpA - ch * kKC);
-        for (int task = tid; task < kNTa * (kc / 8); task += kThreads) {
-            const int n = task % kNTa, k0 = (task / kNTa) * 8;
-            const int cc = (n % 4) >> 1;
-            double x[8];
-            if (n < 24 && cc < ncl) {
+
+    int cb = 0;   // buffer of the current group
+    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gstep, cb ^= 1) {
+        const int ncl = min(kFa, a.ncol - grp * kFa);
+        const bool more = grp + gstep < ngrp;
+        double *stage = stage0 + (size_t)cb * kNTa * kSt;
+        if (more) set_meta(grp + gstep, cb ^ 1);   // ordered before its gather by the sync below
+        for (int ch = 0; ch < nch && ok; ++ch) {
+            const int kc = min(kKC, KpA - ch * kKC);
+            // digits: all 8 warps, 4 contraction entries per task
+            for (int task = tid; task < kNTa * (kc / 4); task += kThreads) {
+                const int n = task % kNTa, k0 = (task / kNTa) * 4;
+                const int cc = (n % 4) >> 1;
+                double x[4];
+                if (n < 24 && cc < ncl) {
 #pragma unroll
-                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
-            } else {
+                    for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
+                } else {
 #pragma unroll
-                for (int i = 0; i < 8; ++i) x[i] = 0.0;
+                    for (int i = 0; i < 4; ++i) x[i] = 0.0;
+                }
+                put4<S, B>(x, scale_exp(cexp[cb][n]), sB, (size_t)kNTa * kSlice, n, k0);
             }
-            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTa * kSlice, n, k0);
-        }
-        asm volatile("fence.proxy.async.shared::cta;");
-        __syncthreads();
-        if (tid == 0) {
-            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                issue_chunk<S>(tmem, sA, sB, kNTa, kc, ch == 0);
-                mma_commit(&mbarM);
-            } else {
-                fail = 1;
-                mbar_arrive(&mbarM);
+            asm volatile("fence.proxy.async.shared::cta;");
+            __syncthreads();
+            // a one-chunk table stays in shared memory after its first wait
+            const bool needA = nch > 1 || na == 0;
+            if (tid == 0) {
+                if (!needA || mbar_wait(&mbarA, na & 1u)) {
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    issue_chunk<S>(tmem, sA, sB, kNTa, kc, ch == 0);
+                    mma_commit(&mbarM);
+                } else {
+                    fail = 1;
+                    mbar_arrive(&mbarM);
+                }
             }
-        }
-        // the next chunk's grid values while the tensor core works on this one
-        if (ch + 1 < nch) {
-            const int kn = min(kKC, KpA - (ch + 1) * kKC);
-            for (int task = tid; task < ncl * 3 * kn; task += kThreads) {
-                const int jl = task % kn, cs = task / kn, cc = cs / 3, slot = cs - cc * 3;
-                double v[4];
-                bvals(cc, slot, (ch + 1) * kKC + jl, v);
+            if (needA) ++na;
+            // while the tensor core works: the next chunk's grid values, or the next group's
+            if (ch + 1 < nch) {
+                const int kn = min(kKC, KpA - (ch + 1) * kKC);
+                for (int task = tid; task < ncl * 3 * kn; task += kThreads) {
+                    const int jl = task % kn, cs = task / kn, cc = cs / 3, slot = cs - cc * 3;
+                    double v[4];
+                    bvals(cb, cc, slot, (ch + 1) * kKC + jl, v);
 #pragma unroll
-                for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
+                    for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
+                }
+            } else if (more) {
+                gather(grp + gstep, cb ^ 1);
+            }
+            ok = mbar_wait(&mbarM, nm & 1u);
+            ++nm;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
+            // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next group
+            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
+                bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
+                          &mbarA);
+                ++nl;
             }
         }
-        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
-        if (ok && tid == 0 && ch + 1 < nch) {
-            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-        }
-    }
-    if (!ok) {
-        if (tid == 0) atomicOr(a.err, 1);
-    } else {
+        if (!ok) break;
         // epilogue 1: only the columns a row uses.  P rows (lane quarters 0, 1;
         // parity par) use fold par of slots 0 and 2 (4 columns each), dP rows
         // (quarters 2, 3) fold 1 - par of slot 1 (4 columns); the two warps of
@@ -514,7 +582,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         double *sd = reinterpret_cast<double *>(sB);   // [128 rows][9]
         const int quarter = warp & 3, g = warp >> 2, par = quarter & 1;
         const int row = quarter * 32 + lane;
-        const int er = a.rexp[((size_t)m * a.ntlA + t) * kTM + row];
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
         if (quarter < 2) {
             const int n0 = acol(par, g == 0 ? 0 : 2, 0, 0);
@@ -529,7 +596,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
                 for (int i = 0; i < 4; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
             for (int i = 0; i < 4; ++i)
-                sd[(size_t)row * 9 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
+                sd[(size_t)row * 9 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n0 + i])));
         } else {
             const int n0 = acol(1 - par, 1, 0, 0) + g * 2;
             long long z[2] = {0, 0};
@@ -543,8 +610,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
                 for (int i = 0; i < 2; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
             for (int i = 0; i < 2; ++i)
-                sd[(size_t)row * 9 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n0 + i])));
+                sd[(size_t)row * 9 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n0 + i])));
         }
+        asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         // epilogue 2: combine P and dP parts; l = m + 64 t + 2 pos + par
         for (int idx = tid; idx < 64 * ncl; idx += kThreads) {
@@ -552,7 +620,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             const int pos = lk >> 1, pr = lk & 1;
             const int k = 64 * t + lk;
             if (k >= K) continue;
-            const AnaCol &q = scol[cc];
+            const AnaCol &q = scol[cb][cc];
             const int l = m + k;
             const double *rp = sd + (size_t)(pr * 32 + pos) * 9;         // slot 0 at [0..4), slot 2 at [4..8)
             const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * 9;   // slot 1 at [0..4)
@@ -570,7 +638,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             if (m == 0) xi = 0.0;
             q.dst[a.moff[m] + k] = make_double2(xr, xi);
         }
+        __syncthreads();   // sd (= sB) and this group's buffers are reused
     }
+    if (!ok && tid == 0) atomicOr(a.err, 1);
+    // a table chunk still in flight must land before the CTA exits (bounded wait)
+    if (tid == 0 && nl > na) (void)mbar_wait(&mbarA, na & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
@@ -579,7 +651,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
 }  // namespace
 
 struct SplitCtx {
-    int T = 0, nh = 0, ntl = 0, ntlA = 0, KpA = 0, S = 7, B = 8;
+    int T = 0, nh = 0, ntl = 0, ntlA = 0, KpA = 0, S = 7, B = 8, nsm = 152;
     __nv_bfloat16 *digS = nullptr, *digA = nullptr;
     long long *sbase = nullptr, *abase = nullptr;
     int *rexpS = nullptr, *rexpA = nullptr, *err = nullptr;
@@ -608,6 +680,11 @@ int split_create(const Geometry &g, const DevTables &t, int /*max_rows*/, SplitC
     SplitCtx *s = new SplitCtx;
     s->T = g.T;
     s->nh = g.nh;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (s->nsm <= 0) s->nsm = 152;
+    }
     const int kmax = std::max(((g.T + 1) + 15) & ~15, (g.nh + 15) & ~15);
     if (kmax <= 126) { s->S = 7; s->B = 8; }
     else if (kmax <= 441) { s->S = 8; s->B = 7; }
@@ -669,7 +746,11 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
     if (p.ncol <= 0) return AEROS_OK;
     SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
                    nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err};
-    dim3 grid(c.T + 1, s->ntl, (p.ncol + kNTs / 2 - 1) / (kNTs / 2));
+    // group slots per (m, latitude tile): about 8 CTAs per SM over the whole grid
+    const int ngrp = (p.ncol + kNTs / 2 - 1) / (kNTs / 2);
+    const int tiles = (c.T + 1) * s->ntl;
+    const int slots = std::max(1, std::min(ngrp, (8 * s->nsm + tiles - 1) / tiles));
+    dim3 grid(c.T + 1, s->ntl, slots);
     if (s->S == 7) k_split_synth<7, 8><<<grid, kThreads, synth_smem<7>(), c.stream>>>(a);
     else k_split_synth<8, 7><<<grid, kThreads, synth_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;
@@ -681,7 +762,12 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, co
     if (ncol <= 0) return AEROS_OK;
     AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
                    c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err};
-    dim3 grid(c.T + 1, s->ntlA, (ncol + kFa - 1) / kFa);
+    // group slots per (m, l tile): about 8 CTAs per SM over the whole grid; each
+    // CTA then loops over ngrp / slots column groups
+    const int ngrp = (ncol + kFa - 1) / kFa;
+    const int tiles = (c.T + 1) * s->ntlA;
+    const int slots = std::max(1, std::min(ngrp, (8 * s->nsm + tiles - 1) / tiles));
+    dim3 grid(c.T + 1, s->ntlA, slots);
     if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
     else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;

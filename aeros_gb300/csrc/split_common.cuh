@@ -194,6 +194,21 @@ __device__ __forceinline__ void put8(const double *x, int e, __nv_bfloat16 *tile
     }
 }
 
+// The same for 4 entries x[0..3] at k0 (k0 % 4 == 0): 8 bytes per slice.
+template <int S, int B>
+__device__ __forceinline__ void put4(const double *x, int e, __nv_bfloat16 *tile, size_t slice_elems, int n, int k0) {
+    uint32_t h[4][S];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Digits<S, B>::cut(fixed55(x[i], e), h[i]);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        uint2 w;
+        w.x = pack_bf16(h[0][s], h[1][s]);
+        w.y = pack_bf16(h[2][s], h[3][s]);
+        *reinterpret_cast<uint2 *>(tile + (size_t)s * slice_elems + swz(n, k0)) = w;
+    }
+}
+
 // Accumulator Y (fp32 holding an exact integer) shifted into the Z window.
 template <int B>
 __device__ __forceinline__ long long zterm(uint32_t y, int q) {

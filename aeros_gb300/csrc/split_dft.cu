@@ -143,8 +143,10 @@ struct DftAnalP {
 };
 
 // ---------------------------------------------------------------- the product
-// CTA (M tile mt, column tile ct): rows mt*128.. of the table times 64 data
-// columns, over the whole contraction in 64-wide chunks.
+// CTA (M tile mt, group slot): rows mt*128.. of the table times column tiles
+// ct = slot, slot + gridDim.y, ... (32 data columns each), over the whole
+// contraction in 32-wide chunks.  TMEM and the barriers are set up once per CTA;
+// the first table chunk of the next tile is fetched during the epilogue.
 template <int S, int B, class P>
 __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch, const __nv_bfloat16 *dig,
                                                             const int *rexp, int *err) {
@@ -161,12 +163,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     __shared__ int cexp[kNT];
     __shared__ int fail;
 
-    const int mt = blockIdx.x, ct = blockIdx.y;
+    const int mt = blockIdx.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Kp = (K + 15) & ~15;
-    const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
-    if (ncl <= 0) return;
-    if (tid < kNT) cexp[tid] = 0;
+    const int nct = (p.ncol() + kNT - 1) / kNT;
+    if ((int)blockIdx.y >= nct) return;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -181,82 +182,94 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     __syncthreads();
     const __nv_bfloat16 *gA = dig + (size_t)mt * nch * S * kTM * kSlice;
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    // phase 1: column scales over the whole contraction, chunk 0 staged
-    const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
-    for (int base = 0; base < ncl * nk8; base += kThreads) {
-        const int task = base + tid;
-        const bool valid = task < ncl * nk8;
-        const int n = valid ? task / nk8 : -1, k0 = valid ? (task - n * nk8) * 8 : 0;
-        double x[8];
-        if (valid) p.bvals8(c0 + n, k0, x);
-        else
-#pragma unroll
-            for (int i = 0; i < 8; ++i) x[i] = 0.0;
-        int be = 0;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) be = max(be, k0 + i < K ? bexp(x[i]) : 0);
-        const unsigned peers = __match_any_sync(0xffffffffu, n);
-        be = __reduce_max_sync(peers, be);
-        if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[n], be);
-        if (valid && k0 < kc0)
-#pragma unroll
-            for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = k0 + i < K ? x[i] : 0.0;
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
+    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+    const int grow = mt * kTM + quarter * 32 + lane;   // this thread's epilogue row
+    const int er = rexp[grow];
+    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
+    uint32_t nl = 1;           // table loads issued (thread 0's count)
     bool ok = true;
-    for (int ch = 0; ch < nch && ok; ++ch) {
-        const int kc = min(kKC, Kp - ch * kKC);
-        for (int task = tid; task < kNT * (kc / 8); task += kThreads) {
-            const int n = task % kNT, k0 = (task / kNT) * 8;
+    const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+
+    for (int ct = blockIdx.y; ct < nct && ok; ct += gridDim.y) {
+        const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
+        if (tid < kNT) cexp[tid] = 0;
+        __syncthreads();
+        // phase 1: column scales over the whole contraction, chunk 0 staged
+        for (int base = 0; base < ncl * nk8; base += kThreads) {
+            const int task = base + tid;
+            const bool valid = task < ncl * nk8;
+            const int n = valid ? task / nk8 : -1, k0 = valid ? (task - n * nk8) * 8 : 0;
             double x[8];
-            if (n < ncl) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
-            } else {
+            if (valid) p.bvals8(c0 + n, k0, x);
+            else
 #pragma unroll
                 for (int i = 0; i < 8; ++i) x[i] = 0.0;
-            }
-            put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNT * kSlice, n, k0);
+            int be = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) be = max(be, k0 + i < K ? bexp(x[i]) : 0);
+            const unsigned peers = __match_any_sync(0xffffffffu, n);
+            be = __reduce_max_sync(peers, be);
+            if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[n], be);
+            if (valid && k0 < kc0)
+#pragma unroll
+                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = k0 + i < K ? x[i] : 0.0;
         }
-        asm volatile("fence.proxy.async.shared::cta;");
         __syncthreads();
-        if (tid == 0) {
-            if (mbar_wait(&mbarA, (uint32_t)(ch & 1))) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                issue_chunk<S>(tmem, sA, sB, kNT, kc, ch == 0);
-                mma_commit(&mbarM);
-            } else {
-                fail = 1;
-                mbar_arrive(&mbarM);
-            }
-        }
-        // the next chunk's data values while the tensor core works on this one
-        if (ch + 1 < nch) {
-            const int kn = min(kKC, Kp - (ch + 1) * kKC);
-            for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
-                const int n = task / (kn / 8), k0 = (task - n * (kn / 8)) * 8;
+        for (int ch = 0; ch < nch && ok; ++ch) {
+            const int kc = min(kKC, Kp - ch * kKC);
+            for (int task = tid; task < kNT * (kc / 8); task += kThreads) {
+                const int n = task % kNT, k0 = (task / kNT) * 8;
                 double x[8];
-                p.bvals8(c0 + n, (ch + 1) * kKC + k0, x);
-                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = (ch + 1) * kKC + k0 + i < K ? x[i] : 0.0;
+                if (n < ncl) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) x[i] = 0.0;
+                }
+                put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNT * kSlice, n, k0);
+            }
+            asm volatile("fence.proxy.async.shared::cta;");
+            __syncthreads();
+            // a one-chunk table stays in shared memory after its first wait
+            const bool needA = nch > 1 || na == 0;
+            if (tid == 0) {
+                if (!needA || mbar_wait(&mbarA, na & 1u)) {
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    issue_chunk<S>(tmem, sA, sB, kNT, kc, ch == 0);
+                    mma_commit(&mbarM);
+                } else {
+                    fail = 1;
+                    mbar_arrive(&mbarM);
+                }
+            }
+            if (needA) ++na;
+            // the next chunk's data values while the tensor core works on this one
+            if (ch + 1 < nch) {
+                const int kn = min(kKC, Kp - (ch + 1) * kKC);
+                for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
+                    const int n = task / (kn / 8), k0 = (task - n * (kn / 8)) * 8;
+                    double x[8];
+                    p.bvals8(c0 + n, (ch + 1) * kKC + k0, x);
+                    for (int i = 0; i < 8; ++i)
+                        stage[n * kSt + k0 + i] = (ch + 1) * kKC + k0 + i < K ? x[i] : 0.0;
+                }
+            }
+            ok = mbar_wait(&mbarM, nm & 1u);
+            ++nm;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
+            // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next tile
+            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || ct + (int)gridDim.y < nct)) {
+                bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
+                          &mbarA);
+                ++nl;
             }
         }
-        ok = mbar_wait(&mbarM, (uint32_t)(ch & 1));
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
-        if (ok && tid == 0 && ch + 1 < nch)
-            bulk_load(sA, gA + (size_t)(ch + 1) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    }
-    if (!ok) {
-        if (tid == 0) atomicOr(err, 1);
-    } else {
+        if (!ok) break;
         // warp w: TMEM lane quarter w % 4 (rows), columns 16 (w / 4) .. +16
-        const int quarter = warp & 3, c16 = (warp >> 2) * 16;
-        const int row = quarter * 32 + lane;
-        const int grow = mt * kTM + row;
-        const int er = rexp[grow];
         for (int h = 0; h < 16; h += 8) {
             uint32_t r[S][8];
 #pragma unroll
@@ -277,7 +290,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                     if (n < ncl) p.store(grow, c0 + n, z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n]))));
                 }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();   // cexp and TMEM are reused by the next tile
     }
+    if (!ok && tid == 0) atomicOr(err, 1);
+    // a table chunk still in flight must land before the CTA exits (bounded wait)
+    if (tid == 0 && nl > na) (void)mbar_wait(&mbarA, na & 1u);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
@@ -296,6 +314,7 @@ struct SplitDft {
     DftPart syn, ana;
     double *msin = nullptr;   // [nlat][ms] m / sin(theta_j)
     int *err = nullptr;
+    int nsm = 152;            // SMs of the device (grid sizing)
 };
 
 namespace {
@@ -358,8 +377,11 @@ void free_part(DftPart &d) {
 }
 
 template <class P>
-void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err) {
-    dim3 grid(d.nmt, (ncol + kNT - 1) / kNT);
+void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, int nsm) {
+    // about 8 CTAs per SM over the grid; each loops over nct / slots column tiles
+    const int nct = (ncol + kNT - 1) / kNT;
+    const int slots = std::max(1, std::min(nct, (8 * nsm + d.nmt - 1) / d.nmt));
+    dim3 grid(d.nmt, slots);
     if (d.S == 7)
         k_split_gemm<7, 8, P><<<grid, kThreads, gemm_smem<7>(), c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
     else
@@ -374,6 +396,11 @@ int split_dft_create(const Geometry &g, SplitDft **out) {
     const char *keep_fft = std::getenv("AEROS_SPLIT_FFT");
     if (keep_fft && keep_fft[0] == '1') return AEROS_OK;
     SplitDft *s = new SplitDft;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (s->nsm <= 0) s->nsm = 152;
+    }
     const int nlon = g.nlon, ms = g.T + 1;
     const long double pi = 3.141592653589793238462643383279502884L;
     const long double nrm = 1.0L / std::sqrt(2.0L * pi), sc = std::sqrt(2.0L * pi) / nlon;
@@ -424,7 +451,7 @@ bool split_dft_has_anal(const SplitDft *s) { return s && s->ana.S > 0; }
 int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     DftSynthP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, s->msin};
-    launch_gemm(s->syn, c, p, nf * c.nlat, s->err);
+    launch_gemm(s->syn, c, p, nf * c.nlat, s->err, s->nsm);
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
 }
@@ -432,7 +459,7 @@ int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, in
 int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     DftAnalP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F};
-    launch_gemm(s->ana, c, p, nf * c.nlat, s->err);
+    launch_gemm(s->ana, c, p, nf * c.nlat, s->err, s->nsm);
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
 }
