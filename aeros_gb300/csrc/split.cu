@@ -130,24 +130,31 @@ struct SynSplitArgs {
 
 // Synthesis smem: A [S][128][64] | B [S][64][64] bf16 | stage [64][65] doubles.
 template <int S>
-constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + (size_t)kNTs * kSt * 8; }
+constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + 2 * (size_t)kNTs * kSt * 8; }
 template <int S>
 constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + 2 * (size_t)kNTa * kSt * 8; }
 
 // One CTA per (m, latitude tile, group slot z): it steps through column groups
 // z, z + gridDim.z, ... (16 complex columns each) with its TMEM, barriers and
-// (for a one-chunk contraction) the table tile kept.
+// (for a one-chunk contraction) the table tile kept.  Software pipeline: the
+// next group's coefficients are gathered (and its column scales formed) into
+// the second stage buffer while the tensor core works on the current group.
 template <int S, int B>
 __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
+    // shared memory: sA | stage 1 | sB | stage 0, so that sB with the stage
+    // buffer of the current group is one contiguous block for the epilogue
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
-    __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
-    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNTs * kKC);   // [kNTs cols][kSt]
+    double *stage1 = reinterpret_cast<double *>(sA + (size_t)S * kTM * kKC);      // [kNTs cols][kSt]
+    __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(stage1 + (size_t)kNTs * kSt);
+    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNTs * kKC);   // [kNTs cols][kSt]
+    static_assert(((size_t)S * kTM * kKC * 2 + (size_t)kNTs * kSt * 8) % 128 == 0, "sB alignment");
+    static_assert(128 * 17 * 8 <= (size_t)kNTs * kSt * 8 + (size_t)S * kNTs * kKC * 2, "epilogue block size");
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
-    __shared__ int cexp[kNTs];
-    __shared__ SynCol scol[kNTs / 2];
-    __shared__ int anyD, fail;
+    __shared__ int cexp[2][kNTs];
+    __shared__ SynCol scol[2][kNTs / 2];
+    __shared__ int anyD[2], fail;
 
     if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
         if (threadIdx.x == 0) atomicOr(a.err, 2);
@@ -159,6 +166,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     const int mo = a.moff[m];
     const int ngrp = (a.ncol + kNTs / 2 - 1) / (kNTs / 2);
     if ((int)blockIdx.z >= ngrp) return;
+    const int gstep = gridDim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -170,39 +178,34 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         mbar_init(&mbarM);
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    __syncthreads();
     const __nv_bfloat16 *gA = a.dig + a.sbase[m] + (size_t)t * nch * S * kTM * kSlice;
-    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tmem = tmem_base;
-    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
-    const int jj = lane, jn = t * 32 + jj, js = a.nlat - 1 - jn;
-    const int *re = a.rexp + ((size_t)m * a.ntl + t) * kTM;
-    const int eRow = re[quarter * 32 + jj];
-    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
-    uint32_t nl = 1;           // table loads issued (thread 0's count)
-    bool ok = true;
 
-    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gridDim.z) {
-        const int c0 = grp * (kNTs / 2);
-        const int ncl = min(kNTs / 2, a.ncol - c0);
-        if (tid < ncl) scol[tid] = a.cols[c0 + tid];
-        if (tid < kNTs) cexp[tid] = 0;
-        if (tid == 0) anyD = 0;
-        __syncthreads();
-        if (tid < ncl && scol[tid].rowD >= 0) anyD = 1;
-        // value k of complex column cc (scaled input coefficient)
-        auto coef = [&](int cc, int k) -> double2 {
-            const SynCol &sc = scol[cc];
-            double2 v = sc.src[mo + k];
-            if (sc.scale) {
-                const double f = a.lfac[sc.scale * a.ms + m + k];
-                v.x *= f;
-                v.y *= f;
-            }
-            return v;
-        };
-        // phase 1: column scales over the full contraction, chunk 0 staged
+    auto set_meta = [&](int grp, int b) {
+        const int c0 = grp * (kNTs / 2), ncl = min(kNTs / 2, a.ncol - c0);
+        if (tid < ncl) scol[b][tid] = a.cols[c0 + tid];
+        if (tid < kNTs) cexp[b][tid] = 0;
+        // a warp-wide vote over the group's columns: any dPbar sum wanted?
+        if (warp == 0) {
+            const bool d = lane < ncl && a.cols[c0 + lane].rowD >= 0;
+            const unsigned v = __ballot_sync(0xffffffffu, d);
+            if (lane == 0) anyD[b] = v != 0;
+        }
+    };
+    // value k of complex column cc (scaled input coefficient), buffer b
+    auto coef = [&](int b, int cc, int k) -> double2 {
+        const SynCol &sc = scol[b][cc];
+        double2 v = sc.src[mo + k];
+        if (sc.scale) {
+            const double f = a.lfac[sc.scale * a.ms + m + k];
+            v.x *= f;
+            v.y *= f;
+        }
+        return v;
+    };
+    // phase 1 of group grp into buffer b: column scales over the full contraction, chunk 0 staged
+    auto gather = [&](int grp, int b) {
+        const int ncl = min(kNTs / 2, a.ncol - grp * (kNTs / 2));
+        double *stage = b ? stage1 : stage0;
         const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
         for (int base = 0; base < ncl * nk8; base += kThreads) {
             const int task = base + tid;
@@ -210,8 +213,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             const int cc = valid ? task / nk8 : -1, k0 = valid ? (task - cc * nk8) * 8 : 0;
             int br = 0, bi = 0;
             double re8[8], im8[8], f[8];
-            const double2 *src = valid ? scol[cc].src + mo + k0 : nullptr;
-            const int sci = valid ? scol[cc].scale : 0;
+            const double2 *src = valid ? scol[b][cc].src + mo + k0 : nullptr;
+            const int sci = valid ? scol[b][cc].scale : 0;
             const double *lf = a.lfac + sci * a.ms + m + k0;
 #pragma unroll
             for (int i = 0; i < 8; ++i) {   // all loads first
@@ -234,8 +237,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             br = __reduce_max_sync(peers, br);
             bi = __reduce_max_sync(peers, bi);
             if (valid && lane == __ffs(peers) - 1) {
-                atomicMax(&cexp[2 * cc], br);
-                atomicMax(&cexp[2 * cc + 1], bi);
+                atomicMax(&cexp[b][2 * cc], br);
+                atomicMax(&cexp[b][2 * cc + 1], bi);
             }
             if (valid && k0 < kc0)
 #pragma unroll
@@ -244,22 +247,43 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
                     stage[(2 * cc + 1) * kSt + k0 + i] = im8[i];
                 }
         }
-        __syncthreads();
+    };
+
+    set_meta(blockIdx.z, 0);
+    __syncthreads();
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    gather(blockIdx.z, 0);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+    const int *rex = a.rexp + ((size_t)m * a.ntl + t) * kTM;
+    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
+    uint32_t nl = 1;           // table loads issued (thread 0's count)
+    bool ok = true;
+
+    int cb = 0;   // buffer of the current group
+    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gstep, cb ^= 1) {
+        const int ncl = min(kNTs / 2, a.ncol - grp * (kNTs / 2));
+        const bool more = grp + gstep < ngrp;
+        double *stage = cb ? stage1 : stage0;
+        if (more) set_meta(grp + gstep, cb ^ 1);   // ordered before its gather by the sync below
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, Kp - ch * kKC);
-            // digits of the data columns (columns of absent fields are zero)
-            // lanes take consecutive tile rows n: 16-byte digit stores fill whole core matrices
-            for (int task = tid; task < kNTs * (kc / 8); task += kThreads) {
-                const int n = task % kNTs, k0 = (task / kNTs) * 8;
-                double x[8];
+            // digits of the data columns (columns of absent fields are zero): all 8 warps,
+            // 4 contraction entries per task, lanes on consecutive tile rows n
+            for (int task = tid; task < kNTs * (kc / 4); task += kThreads) {
+                const int n = task % kNTs, k0 = (task / kNTs) * 4;
+                double x[4];
                 if ((n >> 1) < ncl) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+                    for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) x[i] = 0.0;
+                    for (int i = 0; i < 4; ++i) x[i] = 0.0;
                 }
-                put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNTs * kSlice, n, k0);
+                put4<S, B>(x, scale_exp(cexp[cb][n]), sB, (size_t)kNTs * kSlice, n, k0);
             }
             asm volatile("fence.proxy.async.shared::cta;");
             __syncthreads();
@@ -276,94 +300,92 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
                 }
             }
             if (needA) ++na;
-            // the next chunk's coefficients while the tensor core works on this one
+            // while the tensor core works: the next chunk's coefficients, or the next group's
             if (ch + 1 < nch) {
                 const int kn = min(kKC, Kp - (ch + 1) * kKC);
                 for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
                     const int cc = task / (kn / 8), k0 = (task - cc * (kn / 8)) * 8;
                     for (int i = 0; i < 8; ++i) {
                         const int k = (ch + 1) * kKC + k0 + i;
-                        const double2 v = k < K ? coef(cc, k) : make_double2(0.0, 0.0);
+                        const double2 v = k < K ? coef(cb, cc, k) : make_double2(0.0, 0.0);
                         stage[(2 * cc) * kSt + k0 + i] = v.x;
                         stage[(2 * cc + 1) * kSt + k0 + i] = v.y;
                     }
                 }
+            } else if (more) {
+                gather(grp + gstep, cb ^ 1);
             }
             ok = mbar_wait(&mbarM, nm & 1u);
             ++nm;
             asm volatile("tcgen05.fence::after_thread_sync;");
             ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next group
-            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || grp + (int)gridDim.z < ngrp)) {
+            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
                 bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
                           &mbarA);
                 ++nl;
             }
         }
         if (!ok) break;
-        // epilogue: warp w holds TMEM lane quarter w % 4 (row block P even,
-        // P odd, dP even, dP odd; lane = latitude) for columns 16 (w / 4) .. +16.
-        // The odd blocks go through shared memory (sB + stage, free now) to the
-        // even blocks' warps, which add the hemispheres as integers and store.
-        long long *zodd = reinterpret_cast<long long *>(sB);   // [2 blocks][32 lanes][kNTs + 1]
-        const bool live = quarter < 2 || anyD;
-        // the 8 accumulated columns c16 + h .. + 8 of this warp's lane quarter
-        auto zcols = [&](int h, long long *z) {
-            uint32_t r[S][8];
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-                tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
-            tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 8; ++i) z[i] = 0;
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-#pragma unroll
-                for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
-        };
-        if (live && (quarter & 1))
+        // epilogue, in two rounds of 8 accumulator columns per warp: warp w
+        // reads TMEM lane quarter w % 4 (row block P even, P odd, dP even,
+        // dP odd; lane = latitude), columns 16 (w / 4) + h .. + 8, into
+        // zst[row][8 (w / 4) + i] (sB with this group's stage buffer, both free
+        // now); then every thread takes one (latitude, complex column) and adds
+        // the hemispheres as integers.
+        long long *zst = reinterpret_cast<long long *>(cb ? (void *)stage1 : (void *)sB);   // [128 rows][17]
+        const bool live = quarter < 2 || anyD[cb];
 #pragma unroll 1
-            for (int h = 0; h < 16; h += 8) {
-                long long z[8];
-                zcols(h, z);
+        for (int h = 0; h < 16; h += 8) {
+            if (live) {
+                uint32_t r[S][8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    zodd[((size_t)(quarter >> 1) * 32 + lane) * (kNTs + 1) + c16 + h + i] = z[i];
+                for (int q = 0; q < S; ++q)
+                    tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
+                tmem_wait_ld();
+                long long z[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) z[i] = 0;
+#pragma unroll
+                for (int q = 0; q < S; ++q)
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * 17 + (c16 >> 1) + i] = z[i];
             }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        // tcgen05.ld is warp-collective: the whole warp loads, lanes past the
-        // last latitude only skip the stores
-        if (live && !(quarter & 1)) {
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            const long long *O = zodd + ((size_t)(quarter >> 1) * 32 + lane) * (kNTs + 1) + c16;
-            const bool dP = quarter == 2;
-#pragma unroll 1
-            for (int h = 0; h < 16; h += 8) {
-                if (((c16 + h) >> 1) >= ncl) break;
-                long long z[8];
-                zcols(h, z);
-#pragma unroll
-                for (int i = 0; i < 8; i += 2) {
-                    const int cc = (c16 + h + i) >> 1;
-                    if (cc >= ncl || jn >= a.nh) break;
-                    const SynCol &sc = scol[cc];
-                    const int row = dP ? sc.rowD : sc.rowP;
-                    if (row < 0) continue;
-                    const int ecr = zexp<B>(eRow, scale_exp(cexp[2 * cc]));
-                    const int eci = zexp<B>(eRow, scale_exp(cexp[2 * cc + 1]));
-                    const long long oe = O[h + i], oi = O[h + i + 1];
-                    // P: north E + O, south E - O; dP/dtheta is odd about the equator: south O - E
-                    const double2 nv = make_double2(z_to_f64(z[i] + oe, ecr), z_to_f64(z[i + 1] + oi, eci));
-                    const double2 sv = dP ? make_double2(z_to_f64(oe - z[i], ecr), z_to_f64(oi - z[i + 1], eci))
-                                          : make_double2(z_to_f64(z[i] - oe, ecr), z_to_f64(z[i + 1] - oi, eci));
-                    a.F[((size_t)jn * a.nrow + row) * a.ms + m] = nv;
-                    a.F[((size_t)js * a.nrow + row) * a.ms + m] = sv;
+            __syncthreads();
+            {
+                const int jj = tid >> 3, u = tid & 7;            // latitude, complex column of this round
+                const int ccol = (u >> 2) * 16 + h + 2 * (u & 3); // re column; im = ccol + 1
+                const int cc = ccol >> 1;
+                const int jn = t * 32 + jj;
+                if (cc < ncl && jn < a.nh) {
+                    const int js = a.nlat - 1 - jn;
+                    const SynCol &sc = scol[cb][cc];
+                    const int zc = (u >> 2) * 8 + 2 * (u & 3);
+                    const int ecr = scale_exp(cexp[cb][ccol]), eci = scale_exp(cexp[cb][ccol + 1]);
+                    const long long *E = zst + (size_t)(0 * 32 + jj) * 17 + zc;
+                    const long long *O = zst + (size_t)(1 * 32 + jj) * 17 + zc;
+                    const int eP = rex[jj];
+                    a.F[((size_t)jn * a.nrow + sc.rowP) * a.ms + m] = make_double2(
+                        z_to_f64(E[0] + O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] + O[1], zexp<B>(eP, eci)));
+                    a.F[((size_t)js * a.nrow + sc.rowP) * a.ms + m] = make_double2(
+                        z_to_f64(E[0] - O[0], zexp<B>(eP, ecr)), z_to_f64(E[1] - O[1], zexp<B>(eP, eci)));
+                    if (sc.rowD >= 0) {
+                        // dPbar/dtheta is odd about the equator: south O - E
+                        const long long *dE = zst + (size_t)(2 * 32 + jj) * 17 + zc;
+                        const long long *dO = zst + (size_t)(3 * 32 + jj) * 17 + zc;
+                        const int eD = rex[64 + jj];
+                        a.F[((size_t)jn * a.nrow + sc.rowD) * a.ms + m] = make_double2(
+                            z_to_f64(dE[0] + dO[0], zexp<B>(eD, ecr)), z_to_f64(dE[1] + dO[1], zexp<B>(eD, eci)));
+                        a.F[((size_t)js * a.nrow + sc.rowD) * a.ms + m] = make_double2(
+                            z_to_f64(dO[0] - dE[0], zexp<B>(eD, ecr)), z_to_f64(dO[1] - dE[1], zexp<B>(eD, eci)));
+                    }
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();   // zst is rewritten by the next round / group
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();   // zodd (= sB, stage), scol and cexp are rewritten by the next group
     }
     if (!ok && tid == 0) atomicOr(a.err, 1);
     // a table chunk still in flight must land before the CTA exits (bounded wait)

@@ -33,7 +33,7 @@ namespace {
 constexpr int kNT = kNTile;   // data columns per tile
 
 template <int S>
-constexpr size_t gemm_smem() { return (size_t)S * (kTM + kNT) * kKC * 2 + (size_t)kNT * kSt * 8; }
+constexpr size_t gemm_smem() { return (size_t)S * (kTM + kNT) * kKC * 2 + 2 * (size_t)kNT * kSt * 8; }
 
 // ---------------------------------------------------------------- table digits
 __global__ void k_gemm_prep_exp(const double *__restrict__ T, int Mpad, int K, int *__restrict__ rexp) {
@@ -157,10 +157,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     }
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
     __nv_bfloat16 *sB = sA + (size_t)S * kTM * kSlice;
-    double *stage = reinterpret_cast<double *>(sB + (size_t)S * kNT * kSlice);   // [kNT cols][kSt]
+    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNT * kSlice);   // 2 x [kNT cols][kSt]
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
-    __shared__ int cexp[kNT];
+    __shared__ int cexp[2][kNT];
     __shared__ int fail;
 
     const int mt = blockIdx.x;
@@ -181,22 +181,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     }
     __syncthreads();
     const __nv_bfloat16 *gA = dig + (size_t)mt * nch * S * kTM * kSlice;
-    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tmem = tmem_base;
-    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
-    const int grow = mt * kTM + quarter * 32 + lane;   // this thread's epilogue row
-    const int er = rexp[grow];
-    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
-    uint32_t nl = 1;           // table loads issued (thread 0's count)
-    bool ok = true;
     const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
-
-    for (int ct = blockIdx.y; ct < nct && ok; ct += gridDim.y) {
+    const int gstep = gridDim.y;
+    // phase 1 of column tile ct into buffer b: column scales over the whole contraction, chunk 0 staged
+    auto gather = [&](int ct, int b) {
         const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
-        if (tid < kNT) cexp[tid] = 0;
-        __syncthreads();
-        // phase 1: column scales over the whole contraction, chunk 0 staged
+        double *stage = stage0 + (size_t)b * kNT * kSt;
         for (int base = 0; base < ncl * nk8; base += kThreads) {
             const int task = base + tid;
             const bool valid = task < ncl * nk8;
@@ -211,25 +201,47 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             for (int i = 0; i < 8; ++i) be = max(be, k0 + i < K ? bexp(x[i]) : 0);
             const unsigned peers = __match_any_sync(0xffffffffu, n);
             be = __reduce_max_sync(peers, be);
-            if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[n], be);
+            if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[b][n], be);
             if (valid && k0 < kc0)
 #pragma unroll
                 for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = k0 + i < K ? x[i] : 0.0;
         }
-        __syncthreads();
+    };
+    if (tid < kNT) cexp[0][tid] = 0;
+    __syncthreads();
+    if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
+    gather(blockIdx.y, 0);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    const int quarter = warp & 3, c16 = (warp >> 2) * 16;
+    const int grow = mt * kTM + quarter * 32 + lane;   // this thread's epilogue row
+    const int er = rexp[grow];
+    uint32_t na = 0, nm = 0;   // completed waits on mbarA, mbarM (their phase parities)
+    uint32_t nl = 1;           // table loads issued (thread 0's count)
+    bool ok = true;
+
+    int cb = 0;   // buffer of the current tile
+    for (int ct = blockIdx.y; ct < nct && ok; ct += gstep, cb ^= 1) {
+        const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
+        const bool more = ct + gstep < nct;
+        double *stage = stage0 + (size_t)cb * kNT * kSt;
+        if (more && tid < kNT) cexp[cb ^ 1][tid] = 0;   // ordered before its gather by the sync below
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, Kp - ch * kKC);
-            for (int task = tid; task < kNT * (kc / 8); task += kThreads) {
-                const int n = task % kNT, k0 = (task / kNT) * 8;
-                double x[8];
+            // digits: all 8 warps, 4 contraction entries per task
+            for (int task = tid; task < kNT * (kc / 4); task += kThreads) {
+                const int n = task % kNT, k0 = (task / kNT) * 4;
+                double x[4];
                 if (n < ncl) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) x[i] = stage[n * kSt + k0 + i];
+                    for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) x[i] = 0.0;
+                    for (int i = 0; i < 4; ++i) x[i] = 0.0;
                 }
-                put8<S, B>(x, scale_exp(cexp[n]), sB, (size_t)kNT * kSlice, n, k0);
+                put4<S, B>(x, scale_exp(cexp[cb][n]), sB, (size_t)kNT * kSlice, n, k0);
             }
             asm volatile("fence.proxy.async.shared::cta;");
             __syncthreads();
@@ -246,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                 }
             }
             if (needA) ++na;
-            // the next chunk's data values while the tensor core works on this one
+            // while the tensor core works: the next chunk's data values, or the next tile's
             if (ch + 1 < nch) {
                 const int kn = min(kKC, Kp - (ch + 1) * kKC);
                 for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
@@ -256,13 +268,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                     for (int i = 0; i < 8; ++i)
                         stage[n * kSt + k0 + i] = (ch + 1) * kKC + k0 + i < K ? x[i] : 0.0;
                 }
+            } else if (more) {
+                gather(ct + gstep, cb ^ 1);
             }
             ok = mbar_wait(&mbarM, nm & 1u);
             ++nm;
             asm volatile("tcgen05.fence::after_thread_sync;");
             ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next tile
-            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || ct + (int)gridDim.y < nct)) {
+            if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
                 bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
                           &mbarA);
                 ++nl;
@@ -287,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int n = c16 + h + i;
-                    if (n < ncl) p.store(grow, c0 + n, z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[n]))));
+                    if (n < ncl) p.store(grow, c0 + n, z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n]))));
                 }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
