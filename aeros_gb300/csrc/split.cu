@@ -207,10 +207,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         const int ncl = min(kNTs / 2, a.ncol - grp * (kNTs / 2));
         double *stage = b ? stage1 : stage0;
         const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+        const FastDiv dk8(nk8);
         for (int base = 0; base < ncl * nk8; base += kThreads) {
             const int task = base + tid;
             const bool valid = task < ncl * nk8;
-            const int cc = valid ? task / nk8 : -1, k0 = valid ? (task - cc * nk8) * 8 : 0;
+            const int cq = dk8.div(task);
+            const int cc = valid ? cq : -1, k0 = valid ? (task - cq * nk8) * 8 : 0;
             int br = 0, bi = 0;
             double re8[8], im8[8], f[8];
             const double2 *src = valid ? scol[b][cc].src + mo + k0 : nullptr;
@@ -303,8 +305,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             // while the tensor core works: the next chunk's coefficients, or the next group's
             if (ch + 1 < nch) {
                 const int kn = min(kKC, Kp - (ch + 1) * kKC);
+                static_assert(kKC == 32, "a chunk is 16 or 32 entries");
+                const int sh = kn == kKC ? 2 : 1;   // kn / 8 = 1 << sh
                 for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
-                    const int cc = task / (kn / 8), k0 = (task - cc * (kn / 8)) * 8;
+                    const int cc = task >> sh, k0 = (task & ((1 << sh) - 1)) * 8;
                     for (int i = 0; i < 8; ++i) {
                         const int k = (ch + 1) * kKC + k0 + i;
                         const double2 v = k < K ? coef(cb, cc, k) : make_double2(0.0, 0.0);
@@ -315,10 +319,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             } else if (more) {
                 gather(grp + gstep, cb ^ 1);
             }
-            ok = mbar_wait(&mbarM, nm & 1u);
+            // one thread polls the MMA barrier; the CTA barrier releases the rest
+            const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
             ++nm;
+            ok = __syncthreads_and(okw ? 1 : 0) && !fail;   // one verdict for the whole CTA
             asm volatile("tcgen05.fence::after_thread_sync;");
-            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next group
             if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
                 bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
@@ -500,6 +505,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         }
     };
     // phase 1 of group grp into buffer b: column scales over all latitudes, chunk 0 staged
+    const FastDiv dkp(KpA);
     auto gather = [&](int grp, int b) {
         const int ncl = min(kFa, a.ncol - grp * kFa);
         double *stage = stage0 + (size_t)b * kNTa * kSt;
@@ -507,7 +513,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         for (int base = 0; base < ncl * 3 * KpA; base += kThreads) {
             const int task = base + tid;
             const bool valid = task < ncl * 3 * KpA;
-            const int j = task % KpA, cs = valid ? task / KpA : -1, cc = cs / 3, slot = cs - cc * 3;
+            const int q = dkp.div(task);
+            const int j = task - q * KpA, cs = valid ? q : -1, cc = cs / 3, slot = cs - cc * 3;
             double v[4] = {0.0, 0.0, 0.0, 0.0};
             if (valid) bvals(b, cc, slot, j, v);
             const unsigned peers = __match_any_sync(0xffffffffu, cs);
@@ -575,8 +582,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             // while the tensor core works: the next chunk's grid values, or the next group's
             if (ch + 1 < nch) {
                 const int kn = min(kKC, KpA - (ch + 1) * kKC);
+                const int sh = kn == kKC ? 5 : 4;   // kn = 1 << sh (16 or 32)
                 for (int task = tid; task < ncl * 3 * kn; task += kThreads) {
-                    const int jl = task % kn, cs = task / kn, cc = cs / 3, slot = cs - cc * 3;
+                    const int jl = task & (kn - 1), cs = task >> sh, cc = cs / 3, slot = cs - cc * 3;
                     double v[4];
                     bvals(cb, cc, slot, (ch + 1) * kKC + jl, v);
 #pragma unroll
@@ -585,10 +593,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             } else if (more) {
                 gather(grp + gstep, cb ^ 1);
             }
-            ok = mbar_wait(&mbarM, nm & 1u);
+            // one thread polls the MMA barrier; the CTA barrier releases the rest
+            const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
             ++nm;
+            ok = __syncthreads_and(okw ? 1 : 0) && !fail;   // one verdict for the whole CTA
             asm volatile("tcgen05.fence::after_thread_sync;");
-            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next group
             if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
                 bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
@@ -638,7 +647,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         __syncthreads();
         // epilogue 2: combine P and dP parts; l = m + 64 t + 2 pos + par
         for (int idx = tid; idx < 64 * ncl; idx += kThreads) {
-            const int lk = idx / ncl, cc = idx - lk * ncl;
+            const int lk = ncl == 2 ? idx >> 1 : idx, cc = idx - lk * ncl;   // ncl is 1 or 2
             const int pos = lk >> 1, pr = lk & 1;
             const int k = 64 * t + lk;
             if (k >= K) continue;

@@ -110,6 +110,16 @@ __device__ __forceinline__ void tmem_ld<2>(uint32_t taddr, uint32_t *r) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;"); }
 
+// ------------------------------------------------------------------ division by a launch constant
+// n / d as a multiply-high with m = ceil(2^32 / d): exact while n (m d - 2^32) < 2^32,
+// which holds for n < 2^32 / d (every index here is far below that).
+struct FastDiv {
+    uint32_t d = 1, m = 0;
+    FastDiv() = default;
+    __host__ __device__ explicit FastDiv(int dv) : d((uint32_t)dv), m(dv > 1 ? 0xFFFFFFFFu / (uint32_t)dv + 1u : 0u) {}
+    __device__ __forceinline__ int div(int n) const { return d == 1 ? n : (int)__umulhi((uint32_t)n, m); }
+};
+
 // ------------------------------------------------------------------ integer digit arithmetic
 // Biased exponent field of x (0 for zero and subnormals).
 __device__ __forceinline__ int bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }

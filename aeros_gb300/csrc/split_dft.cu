@@ -72,10 +72,16 @@ struct DftSynthP {
     int nf, nrow, ms, nlat, nlon;
     const double2 *F;
     const double *msin;   // [nlat][ms]: m / sin(theta_j)
+    FastDiv dlat;         // division by nlat
     __device__ int ncol() const { return nf * nlat; }
     __device__ int nrows() const { return nlon; }
+    // output column col = (field, latitude): grid row, indexed by longitude
+    __device__ double *colbase(int col) const {
+        const int f = dlat.div(col), j = col - f * nlat;
+        return fields[f].dst + (size_t)j * nlon;
+    }
     __device__ void bvals8(int col, int k0, double *x) const {
-        const int f = col / nlat, j = col - f * nlat;
+        const int f = dlat.div(col), j = col - f * nlat;
         const FsynField fd = fields[f];
         const double2 *Fr = F + (size_t)j * nrow * ms;
         const double *mb = msin + (size_t)j * ms;
@@ -115,11 +121,6 @@ struct DftSynthP {
             x[2 * t + 1] = xi;
         }
     }
-    __device__ void store(int row, int col, double v) const {
-        if (row >= nlon) return;
-        const int f = col / nlat, j = col - f * nlat;
-        fields[f].dst[(size_t)j * nlon + row] = v;
-    }
 };
 
 // Analysis column (field f, latitude j): the grid row itself.
@@ -127,18 +128,19 @@ struct DftAnalP {
     const FanaField *fields;
     int nf, nrow, ms, nlat, nlon;
     double2 *F;
+    FastDiv dlat;         // division by nlat
     __device__ int ncol() const { return nf * nlat; }
     __device__ int nrows() const { return 2 * ms; }
+    // output column col = (field, latitude): its Fourier row as doubles, indexed by 2 m + (re, im)
+    __device__ double *colbase(int col) const {
+        const int f = dlat.div(col), j = col - f * nlat;
+        return reinterpret_cast<double *>(F) + ((size_t)j * nrow + fields[f].row) * ms * 2;
+    }
     __device__ void bvals8(int col, int k0, double *x) const {
-        const int f = col / nlat, j = col - f * nlat;
+        const int f = dlat.div(col), j = col - f * nlat;
         const double *src = fields[f].src + (size_t)j * nlon;
 #pragma unroll
         for (int i = 0; i < 8; ++i) x[i] = k0 + i < nlon ? src[k0 + i] : 0.0;
-    }
-    __device__ void store(int row, int col, double v) const {
-        if (row >= 2 * ms) return;
-        const int f = col / nlat, j = col - f * nlat, m = row >> 1;
-        reinterpret_cast<double *>(F)[(((size_t)j * nrow + fields[f].row) * ms + m) * 2 + (row & 1)] = v;
     }
 };
 
@@ -161,6 +163,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[2][kNT];
+    __shared__ double *cbase[2][kNT];   // output column bases of the tile
     __shared__ int fail;
 
     const int mt = blockIdx.x;
@@ -184,13 +187,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
     const int gstep = gridDim.y;
     // phase 1 of column tile ct into buffer b: column scales over the whole contraction, chunk 0 staged
+    const FastDiv dk8(nk8);
     auto gather = [&](int ct, int b) {
         const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
         double *stage = stage0 + (size_t)b * kNT * kSt;
+        if (tid < ncl) cbase[b][tid] = p.colbase(c0 + tid);
         for (int base = 0; base < ncl * nk8; base += kThreads) {
             const int task = base + tid;
             const bool valid = task < ncl * nk8;
-            const int n = valid ? task / nk8 : -1, k0 = valid ? (task - n * nk8) * 8 : 0;
+            const int nq = dk8.div(task);
+            const int n = valid ? nq : -1, k0 = valid ? (task - nq * nk8) * 8 : 0;
             double x[8];
             if (valid) p.bvals8(c0 + n, k0, x);
             else
@@ -261,8 +267,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             // while the tensor core works: the next chunk's data values, or the next tile's
             if (ch + 1 < nch) {
                 const int kn = min(kKC, Kp - (ch + 1) * kKC);
+                static_assert(kKC == 32, "a chunk is 16 or 32 entries");
+                const int sh = kn == kKC ? 2 : 1;   // kn / 8 = 1 << sh
                 for (int task = tid; task < ncl * (kn / 8); task += kThreads) {
-                    const int n = task / (kn / 8), k0 = (task - n * (kn / 8)) * 8;
+                    const int n = task >> sh, k0 = (task & ((1 << sh) - 1)) * 8;
                     double x[8];
                     p.bvals8(c0 + n, (ch + 1) * kKC + k0, x);
                     for (int i = 0; i < 8; ++i)
@@ -271,10 +279,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             } else if (more) {
                 gather(ct + gstep, cb ^ 1);
             }
-            ok = mbar_wait(&mbarM, nm & 1u);
+            // one thread polls the MMA barrier; the CTA barrier releases the rest
+            const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
             ++nm;
+            ok = __syncthreads_and(okw ? 1 : 0) && !fail;   // one verdict for the whole CTA
             asm volatile("tcgen05.fence::after_thread_sync;");
-            ok = __syncthreads_and(ok ? 1 : 0) && !fail;   // one verdict for the whole CTA
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next tile
             if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
                 bulk_load(sA, gA + (size_t)((ch + 1) % nch) * S * kTM * kSlice, (uint32_t)(S * kTM * kSlice * 2),
@@ -301,7 +310,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int n = c16 + h + i;
-                    if (n < ncl) p.store(grow, c0 + n, z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n]))));
+                    if (n < ncl) cbase[cb][n][grow] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n])));
                 }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -464,7 +473,7 @@ bool split_dft_has_anal(const SplitDft *s) { return s && s->ana.S > 0; }
 
 int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    DftSynthP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, s->msin};
+    DftSynthP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, s->msin, FastDiv(c.nlat)};
     launch_gemm(s->syn, c, p, nf * c.nlat, s->err, s->nsm);
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -472,7 +481,7 @@ int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, in
 
 int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    DftAnalP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F};
+    DftAnalP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, FastDiv(c.nlat)};
     launch_gemm(s->ana, c, p, nf * c.nlat, s->err, s->nsm);
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
