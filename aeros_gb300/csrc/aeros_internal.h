@@ -114,7 +114,7 @@ struct Tune {
     int fa_lpb = 0, fa_thr = 256;   // Fourier analysis
     int la_ct = 8;                  // FP64 Legendre analysis: output columns (warps) per CTA: 4, 8 or 16
     int col_thr = 64;               // column kernel threads per CTA
-    int col_lanes = 1;              // column kernel lanes per column: 1, 2 or 4
+    int col_lanes = 1;              // column kernel lanes per column: 1, 2, 4, 8 or 16
     int spec_warps = 4;             // spectral kernel warps per CTA
 };
 

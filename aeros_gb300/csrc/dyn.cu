@@ -61,6 +61,11 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
                                                 const double *__restrict__ phis, int hs_on,
                                                 const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
     constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
+    // with up to 8 levels per lane every level loop is unrolled over kChunk with a
+    // guard, so the per-level arrays are indexed by constants and stay in registers
+    constexpr bool kUnroll = kChunk <= 8;
+#define LEVELS_UP(i) for (int i = 0; i < (kUnroll ? kChunk : nk); ++i) if (!kUnroll || i < nk)
+#define LEVELS_DOWN(i) for (int i = (kUnroll ? kChunk : nk) - 1; i >= 0; --i) if (!kUnroll || i < nk)
     const long ng = (long)nlon * nlat;
     const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const long gid = gt / LPC;
@@ -81,7 +86,8 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     // per-level column quantities of this lane's levels; 1/dp replaces the reference's divisions by dp
     double rdp[kChunk], dlnp[kChunk], alpha[kChunk], cfac[kChunk], gc[kChunk], cm[kChunk], scum[kChunk + 1],
         phi[kChunk];
-    for (int i = 0; i < nk; ++i) {
+#pragma unroll
+    LEVELS_UP(i) {
         const int k = k0 + i;
         const LevConst &L = c_lev[k];
         const double ph0 = fma(L.B0, ps, L.A0), ph1 = fma(L.B1, ps, L.A1);
@@ -114,11 +120,18 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
 #pragma unroll
     for (int r = 0; r < LPC; ++r) {
         if (q == r) {
-            for (int i = 0; i < nk; ++i) {
+#pragma unroll
+            LEVELS_UP(i) {
                 scum[i] = sacc;
                 sacc = sacc + cm[i];
             }
-            scum[nk] = sacc;
+            if (kUnroll) {
+#pragma unroll
+                for (int i = 0; i <= kChunk; ++i)
+                    if (i == nk) scum[i] = sacc;
+            } else {
+                scum[nk] = sacc;
+            }
         }
         if (LPC > 1) sacc = __shfl_sync(0xffffffffu, sacc, base + r);
     }
@@ -129,7 +142,8 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
 #pragma unroll
     for (int r = LPC - 1; r >= 0; --r) {
         if (q == r)
-            for (int i = nk - 1; i >= 0; --i) {
+#pragma unroll
+            LEVELS_DOWN(i) {
                 const double rt = kRd * GF(4 * NL + k0 + i);
                 phi[i] = fma(alpha[i], rt, phh);
                 phh = fma(rt, dlnp[i], phh);
@@ -147,7 +161,8 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         psk = exp(kKappa * lnpr);   // (ps/p0)^kappa
         tbase = c_hs.t_eq - dty * x2;
     }
-    for (int i = 0; i < nk; ++i) {
+#pragma unroll
+    LEVELS_UP(i) {
         const int k = k0 + i;
         const LevConst &L = c_lev[k];
         const double uc = GF(k), vc = GF(NL + k), tc = GF(4 * NL + k);
@@ -196,6 +211,8 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     }
 #undef GF
 #undef GO
+#undef LEVELS_UP
+#undef LEVELS_DOWN
 }
 
 // ---------------------------------------------------------------- spectral kernel
@@ -415,13 +432,17 @@ __global__ void k_mass(double2 *__restrict__ lnps, int M, int T, int nlm, int nh
         last = atomicAdd(done + e, 1u) == (unsigned)(nh - 1);
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last) return;
+    // the last block: all its threads fetch the row sums (from L2, past L1), one sums them in order
+    double *rs = reinterpret_cast<double *>(A);   // nlat <= 2 n doubles fit in A
+    for (int j = threadIdx.x; j < nlat; j += blockDim.x) rs[j] = __ldcg(rows + (size_t)e * nlat + j) * w[j];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     done[e] = 0;   // ready for the next launch
     __threadfence();
-    const volatile double *re = rows + (size_t)e * nlat;
     const double dlon = 2.0 * kPi / nlon;
     double t = 0.0;
-    for (int j = 0; j < nlat; ++j) t += w[j] * re[j] * dlon;
+    for (int j = 0; j < nlat; ++j) t += rs[j] * dlon;
     const double mass = t * kA * kA / kGrav;
     if (mode == 0) {
         if (target[e] < 0.0) target[e] = mass;
@@ -958,7 +979,9 @@ int run_tendency(Dyn &d, int hs_on) {
         kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
                                       d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d);
     };
-    if (lpc == 4) go(k_column<4>);
+    if (lpc == 16) go(k_column<16>);
+    else if (lpc == 8) go(k_column<8>);
+    else if (lpc == 4) go(k_column<4>);
     else if (lpc == 2) go(k_column<2>);
     else go(k_column<1>);
     ++d.launches;

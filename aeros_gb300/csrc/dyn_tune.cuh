@@ -137,7 +137,7 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
             for (int ct : {4, 8, 16})
                 if (ct != d.tune.la_ct) { Tune t = d.tune; t.la_ct = ct; trial(t); }
         for (int ct : {32, 64, 128, 256})
-            for (int lp : {1, 2, 4})
+            for (int lp : {1, 2, 4, 8, 16})
                 if (ct != d.tune.col_thr || lp != d.tune.col_lanes) {
                     Tune t = d.tune;
                     t.col_thr = ct;
