@@ -382,14 +382,26 @@ __global__ void k_mass(double2 *__restrict__ lnps, int M, int T, int nlm, int nh
     const int e = blockIdx.y, jn = blockIdx.x, js = nlat - 1 - jn;
     double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * n;
     const double2 *c = lnps + (size_t)e * nlm;
+    // thread per m; the l loop runs in batches of 8 whose loads are all issued
+    // before the sums, which keep the serial order (even/odd l - m alternate)
     for (int m = threadIdx.x; m <= T; m += blockDim.x) {
         double2 ev = make_double2(0, 0), od = make_double2(0, 0);
-        int mo = moff[m];
-        for (int l = m; l <= T; ++l) {
-            double p = Ps[(size_t)(mo + l - m) * nh + jn];
-            double2 v = c[mo + l - m];
-            if ((l - m) & 1) { od.x += p * v.x; od.y += p * v.y; }
-            else { ev.x += p * v.x; ev.y += p * v.y; }
+        const int mo = moff[m], K = T - m + 1;
+        for (int k0 = 0; k0 < K; k0 += 8) {
+            double p[8];
+            double2 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const bool in = k0 + u < K;
+                p[u] = in ? Ps[(size_t)(mo + k0 + u) * nh + jn] : 0.0;
+                v[u] = in ? c[mo + k0 + u] : make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (k0 + u >= K) break;
+                if (u & 1) { od.x += p[u] * v[u].x; od.y += p[u] * v[u].y; }
+                else { ev.x += p[u] * v[u].x; ev.y += p[u] * v[u].y; }
+            }
         }
         Fn[m] = cadd(ev, od);
         Fs[m] = csub(ev, od);
