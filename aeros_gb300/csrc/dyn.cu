@@ -40,12 +40,16 @@ struct LevConst {
     int pure;
     int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
 };
-__constant__ LevConst c_lev[kMaxLev];
 
 struct HsConst {
     double t_eq, t_min, dtheta_z, sigma_b, p0, k_s, k_f, lnp0, rsb;   // rsb = 1/(1 - sigma_b)
 };
-__constant__ HsConst c_hs;
+// Per-handle constants in device memory (handles of different level sets or
+// forcing parameters step side by side, also concurrently inside one group graph).
+struct DynConst {
+    LevConst lev[kMaxLev];
+    HsConst hs;
+};
 
 // ---------------------------------------------------------------- column kernel
 // Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
@@ -59,8 +63,11 @@ template <int LPC>
 __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
                                                 int nlon, int nlat, int M, const double *__restrict__ xlat,
                                                 const double *__restrict__ phis, int hs_on,
-                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka) {
+                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka,
+                                                const DynConst *__restrict__ dc) {
     constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
+    const LevConst *c_lev = dc->lev;
+    const HsConst &c_hs = dc->hs;
     // with up to 8 levels per lane every level loop is unrolled over kChunk with a
     // guard, so the per-level arrays are indexed by constants and stay in registers
     constexpr bool kUnroll = kChunk <= 8;
@@ -476,7 +483,8 @@ __global__ void k_exp_inplace(double *p, size_t n) {
 // D[e][f][j][i]: u_k, v_k, T_k (3 nlev), ps.
 __global__ void k_budget_rows(const double *__restrict__ D, int NL, int nlon, int nlat,
                               const double *__restrict__ phis, const double *__restrict__ xlat,
-                              double *__restrict__ out) {
+                              double *__restrict__ out, const DynConst *__restrict__ dc) {
+    const LevConst *c_lev = dc->lev;
     __shared__ double red[3][128];
     const int e = blockIdx.y, j = blockIdx.x;
     const size_t ng = (size_t)nlon * nlat;
@@ -652,6 +660,7 @@ struct aeros_dyn_s {
     double *xlat_d = nullptr, *phis_d = nullptr;
     bool phis_set = false;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
+    DynConst *dconst = nullptr;                      // level and Held-Suarez constants (device)
     double *mass_rows = nullptr, *mass_tgt = nullptr, *lnr_last = nullptr, *lnr_cum = nullptr;
     unsigned *mass_done = nullptr;                   // per-member block counter of k_mass
     double *bud_rows = nullptr, *bud_res = nullptr, *zm = nullptr;
@@ -920,11 +929,16 @@ int upload_level_consts(Dyn &d) {
             c.hf = std::max(0.0, (bf - d.par.hs_sigma_b) / (1.0 - d.par.hs_sigma_b));
         }
     }
-    AEROS_CUDA(cudaMemcpyToSymbol(c_lev, L.data(), sizeof(LevConst) * n));
     const aeros_params &p = d.par;
-    HsConst h{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
-              std::log(p.hs_p0), 1.0 / (1.0 - p.hs_sigma_b)};
-    AEROS_CUDA(cudaMemcpyToSymbol(c_hs, &h, sizeof(h)));
+    DynConst dc{};
+    for (int k = 0; k < n; ++k) dc.lev[k] = L[k];
+    dc.hs = HsConst{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
+                    std::log(p.hs_p0), 1.0 / (1.0 - p.hs_sigma_b)};
+    if (!d.dconst) {
+        int rc;
+        if ((rc = dalloc(d.dconst, 1))) return rc;
+    }
+    AEROS_CUDA(cudaMemcpy(d.dconst, &dc, sizeof(dc), cudaMemcpyHostToDevice));
     return AEROS_OK;
 }
 
@@ -989,7 +1003,7 @@ int run_tendency(Dyn &d, int hs_on) {
     const unsigned nb = (unsigned)((ncol * lpc + ct - 1) / ct);
     auto go = [&](auto kern) {
         kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
-                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d);
+                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst);
     };
     if (lpc == 16) go(k_column<16>);
     else if (lpc == 8) go(k_column<8>);
@@ -1148,7 +1162,8 @@ void destroy(Dyn *d) {
     void *ps[] = {d->now, d->old, d->tnd, d->FS, d->FA, d->G, d->GA, d->D, d->GT_d, d->TT_d, d->WT_d, d->nu_d,
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
-                  d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done};
+                  d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
+                  d->dconst};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->split) split_destroy(d->split);
@@ -1440,7 +1455,7 @@ int aeros_dyn_budget(aeros_dyn_t h, double *mass, double *energy, double *angmom
     if (rc) return rc;
     k_budget_rows<<<dim3(h->g.nlat, h->M), 128, 0, h->stream>>>(h->D, h->NL, h->g.nlon, h->g.nlat,
                                                                h->phis_set ? h->phis_d : nullptr, h->xlat_d,
-                                                               h->bud_rows);
+                                                               h->bud_rows, h->dconst);
     k_budget_final<<<(h->M + 63) / 64, 64, 0, h->stream>>>(h->bud_rows, h->tab.w, h->g.nlat, h->g.nlon, h->M,
                                                            h->bud_res);
     h->launches += 2;

@@ -1,6 +1,6 @@
 // dyn_adjoint.cuh -- hand-written adjoint of the dry Held-Suarez step and of
-// its transforms (included by dyn.cu: it shares the level constants c_lev,
-// c_hs and the handle internals).
+// its transforms (included by dyn.cu: it shares the per-handle level and
+// Held-Suarez constants and the handle internals).
 //
 // Inner products: grid fields sum_ij f g; spectral fields sum_lm Re(conj(c) d)
 // over all (l, m), m = 0 imaginary parts being no degrees of freedom.  With
@@ -34,7 +34,8 @@ __global__ void k_state_axpy(double2 *__restrict__ y, const double2 *__restrict_
 // J[e] += wgt sum_k int (u^2+v^2)/2 dp_k/g dA.  With seed, also the gradient
 // on the grid, already divided by the Gauss weight: H[e] = (u_b, v_b, lnps_b)/w.
 __global__ void k_ke(const double *__restrict__ D, int NL, int nlon, int nlat, const double *__restrict__ w,
-                     double wgt, double *__restrict__ J, double *__restrict__ H) {
+                     double wgt, double *__restrict__ J, double *__restrict__ H, const DynConst *__restrict__ dc) {
+    const LevConst *c_lev = dc->lev;
     __shared__ double red[128];
     const int e = blockIdx.y, j = blockIdx.x;
     const size_t ng = (size_t)nlon * nlat;
@@ -113,7 +114,10 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
                                                   double *__restrict__ Gb, int NL, int nlon, int nlat, int M,
                                                   const double *__restrict__ xlat, const double *__restrict__ phis,
                                                   int hs_on, const double *__restrict__ hs_dty,
-                                                  const double *__restrict__ hs_ka, double *__restrict__ parb) {
+                                                  const double *__restrict__ hs_ka, double *__restrict__ parb,
+                                                  const DynConst *__restrict__ dc) {
+    const LevConst *c_lev = dc->lev;
+    const HsConst &c_hs = dc->hs;
     const long ng = (long)nlon * nlat;
     const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
     const bool act = gid < ng * M;
@@ -714,7 +718,7 @@ int ke_accumulate(Dyn &d, double wgt, bool seed) {
     int rc;
     if ((rc = diagnose_device(d))) return rc;
     k_ke<<<dim3(d.g.nlat, d.M), 128, 0, d.stream>>>(d.D, NL, d.g.nlon, d.g.nlat, d.tab.w, wgt, a.J,
-                                                    seed ? a.H : nullptr);
+                                                    seed ? a.H : nullptr, d.dconst);
     ++d.launches;
     if (!seed) return AEROS_OK;
     for (int e = 0; e < d.M; ++e) {
@@ -772,7 +776,7 @@ int step_adjoint(Dyn &d, double2 *post, bool capture) {
     const long ncol = (long)d.g.nlon * d.g.nlat * d.M;
     k_column_ad<<<(unsigned)((ncol + 63) / 64), 64, 0, d.stream>>>(
         d.G, a.GAb, a.Gb, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d, d.phis_set ? d.phis_d : nullptr,
-        d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb);
+        d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb, d.dconst);
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     if ((rc = syn_adjoint(d, a.Nb))) return rc;

@@ -291,3 +291,31 @@ def test_hs_perturb_matches_oracle(gpulib):
     o.hs_perturb(1.0)
     for a, b in zip(g.get_state(), o.get_state()):
         assert np.array_equal(a, b)
+
+
+def test_handles_with_different_level_sets(gpulib):
+    """Level and forcing constants belong to the handle: a 16-level handle
+    created before a 20-level one (different sigma levels, different
+    Held-Suarez sigma_b) still steps like its own oracle, and so does the
+    20-level one, stepped alternately."""
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from oracle.pyoracle import OracleDyn
+    pa = held_suarez_params(trunc=21, nlev=16)
+    pb = held_suarez_params(trunc=21, nlev=20)
+    pb.hs_sigma_b = 0.65
+    ga, oa = AerosDyn(pa), OracleDyn(pa)
+    gb, ob = AerosDyn(pb), OracleDyn(pb)
+    for g, o, seed in ((ga, oa, 31), (gb, ob, 32)):
+        st = moving_state(o, seed=seed)
+        o.set_state(*st)
+        g.set_state(*st)
+    for _ in range(3):
+        for g, o in ((ga, oa), (gb, ob)):
+            g.step(1)
+            o.step(1)
+    for g, o in ((ga, oa), (gb, ob)):
+        for a, b in zip(g.get_state(), o.get_state()):
+            assert relerr(a, b) < 1e-11
+        bg, bo = g.budget(), o.budget()
+        assert np.allclose(bg, bo, rtol=1e-12, atol=0)
