@@ -41,6 +41,12 @@ class AerosError(RuntimeError):
 
 _lib = None
 
+
+class AerosRelaxation(ctypes.Structure):
+    """aeros_relaxation: user data of the ready-made aeros_physics_relaxation hook."""
+    _fields_ = [("k_drag", ctypes.c_double), ("k_temp", ctypes.c_double), ("t_ref", ctypes.c_double)]
+
+
 _vp = ctypes.c_void_p
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -85,6 +91,9 @@ _PROTOS = {
     "aeros_dyn_sync": [_vp],
     "aeros_dyn_profile_step": [_vp, _i, _vp, _vp, _i, _ip],
     "aeros_dyn_tendency": [_vp, _vp, _vp, _vp, _vp],
+    "aeros_dyn_tendency_forced": [_vp, _vp, _vp, _vp, _vp],
+    "aeros_dyn_set_physics": [_vp, _vp, _vp],
+    "aeros_physics_relaxation": [_vp, _vp, _vp],
     "aeros_dyn_diagnose": [_vp, _vp, _vp, _vp, _vp],
     "aeros_dyn_budget": [_vp, _vp, _vp, _vp],
     "aeros_dyn_counters": [_vp, _ip, _dp, _dp, _dp],

@@ -365,6 +365,20 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
     }
 }
 
+// The ready-made physics hook: linear relaxation of the winds and temperature
+// on the grid (aeros_physics_relaxation).
+__global__ void k_relaxation(aeros_grid_view v, double k_drag, double k_temp, double t_ref) {
+    const long long per = (long long)v.nlev * v.level_stride, n = (long long)v.nmember * per;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i / per, r = i - e * per;   // r = level * level_stride + point
+        const long long oi = e * v.in_member_stride + r, oo = e * v.out_member_stride + r;
+        v.ae[oo] -= k_drag * v.u[oi];
+        v.an[oo] -= k_drag * v.v[oi];
+        v.dtdt[oo] -= k_temp * (v.temp[oi] - t_ref);
+    }
+}
+
 // Copy X^n into the old slot (start-up step, aeros_timestep.f90:825-828).
 __global__ void k_copy(double2 *dst, const double2 *src, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -661,6 +675,8 @@ struct aeros_dyn_s {
     bool phis_set = false;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
     DynConst *dconst = nullptr;                      // level and Held-Suarez constants (device)
+    aeros_physics_fn phys_fn = nullptr;              // physics hook at the grid seam
+    void *phys_user = nullptr;
     double *mass_rows = nullptr, *mass_tgt = nullptr, *lnr_last = nullptr, *lnr_cum = nullptr;
     unsigned *mass_done = nullptr;                   // per-member block counter of k_mass
     double *bud_rows = nullptr, *bud_res = nullptr, *zm = nullptr;
@@ -982,7 +998,42 @@ int build_step_tables(Dyn &d) {
 }
 
 // ---- launch sequences ----
-int run_tendency(Dyn &d, int hs_on) {
+// The physics hook at the grid seam: view of this handle's grid buffers.
+int run_physics(Dyn &d) {
+    if (!d.phys_fn) return AEROS_OK;
+    const long long ng = (long long)d.g.nlon * d.g.nlat, NL = d.NL;
+    aeros_grid_view v{};
+    v.nmember = d.M;
+    v.nlev = d.NL;
+    v.nlat = d.g.nlat;
+    v.nlon = d.g.nlon;
+    v.level_stride = ng;
+    v.in_member_stride = (7 * NL + 3) * ng;
+    v.out_member_stride = (4 * NL + 1) * ng;
+    v.u = d.G;
+    v.v = d.G + NL * ng;
+    v.vor = d.G + 2 * NL * ng;
+    v.div = d.G + 3 * NL * ng;
+    v.temp = d.G + 4 * NL * ng;
+    v.lnps = d.G + 7 * NL * ng;
+    v.ae = d.GA;
+    v.an = d.GA + NL * ng;
+    v.dtdt = d.GA + 3 * NL * ng;
+    v.dlnpsdt = d.GA + 4 * NL * ng;
+    v.sinlat = d.xlat_d;
+    v.a_half = d.A.data();
+    v.b_half = d.B.data();
+    v.dt = d.par.dt;
+    const int rc = d.phys_fn(d.phys_user, &v, (void *)d.stream);
+    mark(d, "physics");
+    if (rc) {
+        set_error("physics hook returned " + std::to_string(rc));
+        return AEROS_ERR_ARG;
+    }
+    return AEROS_OK;
+}
+
+int run_tendency(Dyn &d, int hs_on, bool physics) {
     Ctx c = d.ctx();
     int rc;
     const int rowsS = d.M * d.nrowS, rowsA = d.M * d.nrowA;
@@ -1013,6 +1064,7 @@ int run_tendency(Dyn &d, int hs_on) {
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "column");
+    if (physics && (rc = run_physics(d))) return rc;
     if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_anal(d.dft))
         rc = split_fourier_anal(d.dft, c, d.faS, d.nfaS, d.FA, rowsA);
     else
@@ -1050,7 +1102,7 @@ int enqueue_step(Dyn &d, bool startup) {
         mark(d, "copy");
         if (d.par.mass_fixer && (rc = run_mass(d, 0))) return rc;
     }
-    if ((rc = run_tendency(d, d.par.held_suarez))) return rc;
+    if ((rc = run_tendency(d, d.par.held_suarez, true))) return rc;
     SpecArgs a{};
     a.vor = d.vor(d.now); a.div = d.div(d.now); a.tmp = d.tmp(d.now); a.lnps = d.lnp(d.now);
     a.vor_o = d.vor(d.old); a.div_o = d.div(d.old); a.tmp_o = d.tmp(d.old); a.lnps_o = d.lnp(d.old);
@@ -1428,9 +1480,35 @@ int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int
 
 int aeros_dyn_tendency(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp, double *dlnps) {
     if (!h) return AEROS_ERR_ARG;
-    int rc = run_tendency(*h, 0);
+    int rc = run_tendency(*h, 0, false);
     if (rc) return rc;
     return get_state(*h, h->tnd, dvor, ddiv, dtemp, dlnps);
+}
+
+int aeros_dyn_tendency_forced(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp, double *dlnps) {
+    if (!h) return AEROS_ERR_ARG;
+    int rc = run_tendency(*h, h->par.held_suarez, true);
+    if (rc) return rc;
+    return get_state(*h, h->tnd, dvor, ddiv, dtemp, dlnps);
+}
+
+int aeros_dyn_set_physics(aeros_dyn_t h, aeros_physics_fn fn, void *user) {
+    if (!h) return AEROS_ERR_ARG;
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    h->phys_fn = fn;
+    h->phys_user = fn ? user : nullptr;
+    for (auto &g : h->graph)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    return capture_graphs(*h);
+}
+
+int aeros_physics_relaxation(void *user, const aeros_grid_view *v, void *stream) {
+    if (!user || !v) return AEROS_ERR_ARG;
+    const aeros_relaxation r = *static_cast<const aeros_relaxation *>(user);
+    const long long n = (long long)v->nmember * v->nlev * v->level_stride;
+    const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 4096);
+    k_relaxation<<<nb, 256, 0, (cudaStream_t)stream>>>(*v, r.k_drag, r.k_temp, r.t_ref);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
 int aeros_dyn_diagnose(aeros_dyn_t h, double *u, double *v, double *temp, double *ps) {

@@ -611,6 +611,10 @@ void adj_free(AdjCtx *a) {
 }
 
 int adj_ensure(Dyn &d) {
+    if (d.phys_fn) {
+        set_error("adjoint: a physics hook is installed (user physics is not differentiated)");
+        return AEROS_ERR_UNSUPPORTED;
+    }
     if (d.adj) return aeros_sht_set_stream(d.adj->sht, d.stream);   // follow aeros_dyn_set_stream
     AdjCtx *a = new AdjCtx;
     d.adj = a;
@@ -930,6 +934,10 @@ int aeros_dyn_window_forward(aeros_dyn_t h, int nsteps, int ckpt_every, double *
 int aeros_dyn_window_backward(aeros_dyn_t h, double *now_ad, double *old_ad, double *ka_ad, double *dty_ad) {
     if (!h) return AEROS_ERR_ARG;
     Dyn &d = *h;
+    if (d.phys_fn) {
+        set_error("adjoint: a physics hook is installed (user physics is not differentiated)");
+        return AEROS_ERR_UNSUPPORTED;
+    }
     if (!d.adj || !d.adj->win_ready) {
         set_error("aeros_dyn_window_backward: no forward window recorded");
         return AEROS_ERR_STATE;

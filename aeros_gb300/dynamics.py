@@ -160,6 +160,35 @@ class AerosDyn:
         _capi.check(_capi.lib().aeros_dyn_tendency(self._h, *[_ptr(x) for x in s]), "aeros_dyn_tendency")
         return self._squeeze(s)
 
+    def tendency_forced(self):
+        """Spectral tendencies with the step's forcing: Held-Suarez (when enabled)
+        and the physics hook, both added on the grid at the seam."""
+        s = self._alloc()
+        _capi.check(_capi.lib().aeros_dyn_tendency_forced(self._h, *[_ptr(x) for x in s]),
+                    "aeros_dyn_tendency_forced")
+        return self._squeeze(s)
+
+    def set_physics(self, fn, user=None):
+        """Install a physics hook at the grid seam (a C function with the
+        aeros_physics_fn signature: an address, or a ctypes function pointer),
+        or remove it with fn=None.  The step graphs are re-captured; the hook
+        enqueues its work when they are.  `user` (a ctypes object, passed by
+        reference) is kept alive by the handle."""
+        if fn is None:
+            self._phys = None
+            _capi.check(_capi.lib().aeros_dyn_set_physics(self._h, None, None), "aeros_dyn_set_physics")
+            return
+        addr = fn if isinstance(fn, int) else ctypes.cast(fn, ctypes.c_void_p).value
+        self._phys = (fn, user)
+        uptr = ctypes.cast(ctypes.byref(user), ctypes.c_void_p) if user is not None else None
+        _capi.check(_capi.lib().aeros_dyn_set_physics(self._h, ctypes.c_void_p(addr), uptr),
+                    "aeros_dyn_set_physics")
+
+    def set_relaxation(self, k_drag, k_temp=0.0, t_ref=0.0):
+        """The ready-made hook aeros_physics_relaxation: ae -= k_drag u,
+        an -= k_drag v, dtdt -= k_temp (T - t_ref) on the grid."""
+        self.set_physics(_capi.lib().aeros_physics_relaxation, _capi.AerosRelaxation(k_drag, k_temp, t_ref))
+
     def diagnose(self):
         shp = (self.nmember, self.nlev, self.nlat, self.nlon)
         u, v, t = np.zeros(shp), np.zeros(shp), np.zeros(shp)

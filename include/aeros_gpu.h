@@ -250,6 +250,61 @@ int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int
 int aeros_dyn_tendency(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp,
                        double *dlnps);
 
+/* Spectral tendencies with the forcing the step applies: Held-Suarez (when
+ * enabled) and the physics hook (aeros_dyn_set_physics), both added on the
+ * grid at the seam of aeros_tendency_grid / aeros_tendency_spectral
+ * (src/dynamics/aeros_tendency.f90:362-388).  Same layout as
+ * aeros_dyn_tendency. */
+int aeros_dyn_tendency_forced(aeros_dyn_t h, double *dvor, double *ddiv, double *dtemp,
+                              double *dlnps);
+
+/* ---- physics seam ---------------------------------------------------------
+ * The grid-space view a physics hook receives at the seam of
+ * src/dynamics/aeros_tendency.f90:362-388: after the adiabatic right-hand
+ * sides (and Held-Suarez forcing, when enabled) are formed on the grid and
+ * before they are transformed back to spectral space, so a hook's
+ * contribution is carried by the same transforms (and a horizontally varying
+ * drag stays exact under the curl).  Device pointers to member 0, level 0;
+ * field f of member e at level k starts at f + e * member_stride +
+ * k * level_stride, each level an (nlon, nlat) grid, longitude fastest,
+ * latitude north to south. */
+typedef struct aeros_grid_view {
+    int nmember, nlev, nlat, nlon;
+    long long level_stride;        /* doubles between levels (nlat * nlon) */
+    long long in_member_stride;    /* doubles between members of u .. lnps */
+    long long out_member_stride;   /* doubles between members of ae .. dlnpsdt */
+    const double *u, *v, *vor, *div, *temp, *lnps;   /* state on the grid (lnps: one level) */
+    double *ae, *an, *dtdt, *dlnpsdt;                /* right-hand sides: add tendencies here */
+    const double *sinlat;          /* (nlat), device */
+    const double *a_half, *b_half; /* (nlev + 1) half-level coefficients, host memory */
+    double dt;                     /* model time step [s] */
+} aeros_grid_view;
+
+/* A physics hook enqueues device work on `stream` (a cudaStream_t) that reads
+ * the view's state and adds to its right-hand sides.  It is called on the
+ * host whenever the handle enqueues its tendency work: when the step graphs
+ * are captured (aeros_dyn_set_physics, aeros_dyn_autotune) and on every direct
+ * launch (aeros_dyn_profile_step, aeros_dyn_tendency_forced); the captured
+ * work is replayed every step.  It must only enqueue stream-ordered work (no
+ * synchronisation, no allocation while capturing) and returns 0, or nonzero
+ * to fail the call that invoked it.  The adjoint entry points refuse a handle
+ * with a hook (they do not differentiate user physics). */
+typedef int (*aeros_physics_fn)(void *user, const aeros_grid_view *view, void *stream);
+
+/* Install (fn != NULL) or remove (fn == NULL) the hook and re-capture the step
+ * graphs.  `user` is passed through unchanged and must outlive the hook. */
+int aeros_dyn_set_physics(aeros_dyn_t h, aeros_physics_fn fn, void *user);
+
+/* A ready-made hook, also the template for user physics: linear relaxation
+ * with `user` pointing to an aeros_relaxation (host memory, read when the hook
+ * runs):  ae -= k_drag u,  an -= k_drag v,  dtdt -= k_temp (T - t_ref). */
+typedef struct aeros_relaxation {
+    double k_drag;   /* [1/s] */
+    double k_temp;   /* [1/s] */
+    double t_ref;    /* [K] */
+} aeros_relaxation;
+int aeros_physics_relaxation(void *user, const aeros_grid_view *view, void *stream);
+
 /* Grid-space fields of the current state: u, v, temp (nlon, nlat, nlev,
  * nmember), ps (nlon, nlat, nmember).  Replaces aeros_timestep_diagnose
  * (src/dynamics/aeros_timestep.f90:1873-1919). */
