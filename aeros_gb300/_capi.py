@@ -98,6 +98,8 @@ _PROTOS = {
     "aeros_dyn_budget": [_vp, _vp, _vp, _vp],
     "aeros_dyn_counters": [_vp, _ip, _dp, _dp, _dp],
     "aeros_dyn_set_mass_target": [_vp, _d],
+    "aeros_dyn_member_counters": [_vp, _i, _dp, _dp, _dp],
+    "aeros_dyn_set_member_counters": [_vp, _i, _d, _d, _d],
     "aeros_dyn_diag_accumulate": [_vp],
     "aeros_dyn_diag_read": [_vp, _i, _vp, _ip],
     "aeros_dyn_gwspeed": [_vp, _dp],

@@ -1558,6 +1558,27 @@ int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target, double *l
     return AEROS_OK;
 }
 
+int aeros_dyn_member_counters(aeros_dyn_t h, int member, double *mass_target, double *lnr_last, double *lnr_cum) {
+    if (!h || member < 0 || member >= h->M) return AEROS_ERR_ARG;
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    if (mass_target) AEROS_CUDA(cudaMemcpy(mass_target, h->mass_tgt + member, 8, cudaMemcpyDeviceToHost));
+    if (lnr_last) AEROS_CUDA(cudaMemcpy(lnr_last, h->lnr_last + member, 8, cudaMemcpyDeviceToHost));
+    if (lnr_cum) AEROS_CUDA(cudaMemcpy(lnr_cum, h->lnr_cum + member, 8, cudaMemcpyDeviceToHost));
+    return AEROS_OK;
+}
+
+int aeros_dyn_set_member_counters(aeros_dyn_t h, int member, double mass_target, double lnr_last, double lnr_cum) {
+    if (!h || member < 0 || member >= h->M || mass_target == 0.0 || !std::isfinite(mass_target) ||
+        !std::isfinite(lnr_last) || !std::isfinite(lnr_cum))
+        return AEROS_ERR_ARG;
+    const double t = mass_target > 0.0 ? mass_target : -1.0;
+    AEROS_CUDA(cudaStreamSynchronize(h->stream));
+    AEROS_CUDA(cudaMemcpy(h->mass_tgt + member, &t, 8, cudaMemcpyHostToDevice));
+    AEROS_CUDA(cudaMemcpy(h->lnr_last + member, &lnr_last, 8, cudaMemcpyHostToDevice));
+    AEROS_CUDA(cudaMemcpy(h->lnr_cum + member, &lnr_cum, 8, cudaMemcpyHostToDevice));
+    return AEROS_OK;
+}
+
 int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass) {
     if (!h || mass == 0.0 || !std::isfinite(mass)) return AEROS_ERR_ARG;
     std::vector<double> t(h->M, mass > 0.0 ? mass : -1.0);   // negative: capture again at the next start-up

@@ -212,6 +212,18 @@ class AerosDyn:
                                                    ctypes.byref(c)), "aeros_dyn_counters")
         return n.value, a.value, b.value, c.value
 
+    def member_counters(self, member=0):
+        """(mass_target, lnr_last, lnr_cum) of one member."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _capi.check(_capi.lib().aeros_dyn_member_counters(self._h, int(member), ctypes.byref(a), ctypes.byref(b),
+                                                          ctypes.byref(c)), "aeros_dyn_member_counters")
+        return a.value, b.value, c.value
+
+    def set_member_counters(self, member, mass_target, lnr_last, lnr_cum):
+        _capi.check(_capi.lib().aeros_dyn_set_member_counters(self._h, int(member), float(mass_target),
+                                                              float(lnr_last), float(lnr_cum)),
+                    "aeros_dyn_set_member_counters")
+
     def set_mass_target(self, mass):
         _capi.check(_capi.lib().aeros_dyn_set_mass_target(self._h, float(mass)), "aeros_dyn_set_mass_target")
 

@@ -322,6 +322,14 @@ int aeros_dyn_counters(aeros_dyn_t h, int *nstep, double *mass_target,
 /* Set every member's target mass [kg]; a negative value clears it, so the
  * next start-up step captures it again (restarting from a new state). */
 int aeros_dyn_set_mass_target(aeros_dyn_t h, double mass);
+/* The mass-fixer scalars of one member, read and restored: the restart
+ * attributes mass_target, lnr_last, lnr_cum of aeros_timestep_write_restart /
+ * _read_restart (src/dynamics/aeros_timestep.f90:1303-1633).  A negative
+ * mass_target clears the member's target (captured again at a start-up step). */
+int aeros_dyn_member_counters(aeros_dyn_t h, int member, double *mass_target, double *lnr_last,
+                              double *lnr_cum);
+int aeros_dyn_set_member_counters(aeros_dyn_t h, int member, double mass_target, double lnr_last,
+                                  double lnr_cum);
 
 /* Zonal-mean statistics (src/aeros_diagnostics.f90:153-276): accumulate one
  * sample of the current state; read the running means of member `member`
