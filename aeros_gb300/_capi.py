@@ -122,6 +122,14 @@ _PROTOS = {
     "aeros_dyn_window_backward": [_vp, _vp, _vp, _vp, _vp],
     "aeros_dyn_autotune": [_vp, _i, _dp, _dp],
     "aeros_dyn_tune_get": [_vp, _vp],
+    "aeros_transport_create": [ctypes.POINTER(_vp), _i, _i, _vp, _vp],
+    "aeros_transport_destroy": [_vp],
+    "aeros_transport_set_stream": [_vp, _vp],
+    "aeros_transport_grid": [_vp, _ip, _ip, _ip],
+    "aeros_transport_set_vert_vanleer": [_vp, _i],
+    "aeros_transport_step": [_vp, _vp, _vp, _vp, _vp, _d],
+    "aeros_transport_last": [_vp, _dp, _ip],
+    "aeros_transport_water": [_vp, _vp, _vp, _dp],
     "aeros_last_error": [],
 }
 _RESTYPE = {"aeros_last_error": ctypes.c_char_p}
