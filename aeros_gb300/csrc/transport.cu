@@ -7,10 +7,10 @@
 // (nsub from the largest total Courant number of the call).  One sub-step:
 //   k_tr_zonal   block per (level, latitude) row, threads over longitude:
 //                periodic van Leer face values, fluxes staged in shared memory
-//   k_tr_merid   thread per (level, longitude) column over latitude: a sliding
-//                window of the row values as they were at the start of the sweep
-//   k_tr_vert    thread per grid column: vertical mass flux from the layer-mass
-//                change of the two sweeps, levels updated top down in place
+//   k_tr_mfaces  thread per (level, face, longitude): meridional face fluxes
+//   k_tr_mupdate thread per cell: the meridional update from its two faces
+//   k_tr_vert    thread per grid column, loaded whole: vertical mass flux from
+//                the layer-mass change of the two sweeps, levels updated top down
 //                (a level's upper-face flux sees the level above already updated,
 //                as the reference's loop does)
 // Grids are (nlev, nlat, nlon) in C order, latitude north to south: the
@@ -131,90 +131,99 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
 }
 
 // Meridional sweep (sweep_merid, :342-386) with the bounded van Leer face
-// value (vl_face_bounded, :413-440); zero flux through the poles.
-__global__ void k_tr_merid(const double *__restrict__ v, double *__restrict__ dp, double *__restrict__ qm,
-                           const double *__restrict__ cosface, const double *__restrict__ dmu, int nlon, int nlat,
-                           int nlev, long ng, double dt) {
+// value (vl_face_bounded, :413-440), as two fully parallel passes over the
+// start-of-sweep state: face fluxes (face f between rows f and f + 1, stored at
+// [k][f][i]; the pole faces 0 and nlat stay zero), then the row updates.
+__global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restrict__ dp,
+                            const double *__restrict__ qm, const double *__restrict__ cosface,
+                            const double *__restrict__ dmu, int nlon, int nlat, int nlev, long ng, double dt,
+                            double *__restrict__ fa, double *__restrict__ fq) {
+    const long nf = (long)(nlat - 1) * nlon;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)nlev * nlon) return;
-    const int k = (int)(t / nlon), i = (int)(t - (long)k * nlon);
+    if (t >= (long)nlev * nf) return;
+    const int k = (int)(t / nf);
+    const long rem = t - (long)k * nf;
+    const int f = 1 + (int)(rem / nlon), i = (int)(rem - (long)(f - 1) * nlon);
     const long base = k * ng + i;
     auto at = [&](int r) { return base + (long)(r - 1) * nlon; };   // Fortran row r = 1..nlat
-    // window of the start-of-sweep values: q at rows r-1 .. r+2, dp at r, r+1
-    double qm1 = 0.0, q0, q1, q2, d0, d1;
-    d0 = dp[at(1)];
-    q0 = qm[at(1)] / d0;
-    if (nlat > 1) { d1 = dp[at(2)]; q1 = qm[at(2)] / d1; } else { d1 = d0; q1 = q0; }
-    q2 = nlat > 2 ? qm[at(3)] / dp[at(3)] : 0.0;
-    double fa_prev = 0.0, fq_prev = 0.0;   // north pole face
-    for (int r = 1; r <= nlat; ++r) {
-        double fa = 0.0, fq = 0.0;          // face r + 1/2 (south pole face: 0)
-        if (r < nlat) {
-            const double vf = 0.5 * (v[at(r)] + v[at(r + 1)]);
-            const double dy = kA * dmu[r - 1] / fmax(cosface[r], 1.0e-6);
-            const double cour = fabs(vf) * dt / dy;
-            double qf;
-            if (vf >= 0.0) {
-                // upwind row r, neighbours r - 1 and r + 1
-                qf = (r <= 1 || r >= nlat) ? q0 : q0 + 0.5 * (1.0 - cour) * vanleer(q0 - qm1, q1 - q0);
-                fa = d0 * vf * cosface[r];
-            } else {
-                // upwind row r + 1, neighbours r + 2 and r
-                qf = (r + 1 <= 1 || r + 1 >= nlat) ? q1 : q1 + 0.5 * (1.0 - cour) * vanleer(q1 - q2, q0 - q1);
-                fa = d1 * vf * cosface[r];
-            }
-            fq = qf * fa;
-        }
-        const double den = kA * dmu[r - 1];
-        dp[at(r)] = d0 - dt * (fa - fa_prev) / den;
-        qm[at(r)] = qm[at(r)] - dt * (fq - fq_prev) / den;
-        fa_prev = fa;
-        fq_prev = fq;
-        // shift the window one row south
-        qm1 = q0;
-        q0 = q1;
-        d0 = d1;
-        q1 = q2;
-        if (r + 2 <= nlat) d1 = dp[at(r + 2)];   // rows below r are not updated yet
-        q2 = r + 3 <= nlat ? qm[at(r + 3)] / dp[at(r + 3)] : 0.0;
+    auto qa = [&](int r) { return qm[at(r)] / dp[at(r)]; };
+    const double vf = 0.5 * (v[at(f)] + v[at(f + 1)]);
+    const double dy = kA * dmu[f - 1] / fmax(cosface[f], 1.0e-6);
+    const double cour = fabs(vf) * dt / dy;
+    double qf, a;
+    if (vf >= 0.0) {
+        const double q0 = qa(f);
+        qf = (f <= 1 || f >= nlat) ? q0 : q0 + 0.5 * (1.0 - cour) * vanleer(q0 - qa(f - 1), qa(f + 1) - q0);
+        a = dp[at(f)] * vf * cosface[f];
+    } else {
+        const double q1 = qa(f + 1);
+        qf = (f + 1 <= 1 || f + 1 >= nlat) ? q1 : q1 + 0.5 * (1.0 - cour) * vanleer(q1 - qa(f + 2), qa(f) - q1);
+        a = dp[at(f + 1)] * vf * cosface[f];
     }
+    const long o = (long)k * (nlat + 1) * nlon + (long)f * nlon + i;
+    fa[o] = a;
+    fq[o] = qf * a;
+}
+
+__global__ void k_tr_mupdate(double *__restrict__ dp, double *__restrict__ qm, const double *__restrict__ fa,
+                             const double *__restrict__ fq, const double *__restrict__ dmu, int nlon, int nlat,
+                             int nlev, long ng, double dt) {
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)nlev * ng) return;
+    const int k = (int)(t / ng);
+    const long c = t - (long)k * ng;
+    const int j = (int)(c / nlon), i = (int)(c - (long)j * nlon);   // Fortran row j + 1: faces j + 1 and j
+    const long fo = (long)k * (nlat + 1) * nlon + (long)j * nlon + i;
+    const double den = kA * dmu[j];
+    dp[t] = dp[t] - dt * (fa[fo + nlon] - fa[fo]) / den;
+    qm[t] = qm[t] - dt * (fq[fo + nlon] - fq[fo]) / den;
 }
 
 // Vertical mass flux and the top-down update (transport_substep, :238-297;
-// vflux_q :491-513, vflux_q_vl :515-553).
+// vflux_q :491-513, vflux_q_vl :515-553).  The column is loaded first; the
+// update runs on the loaded copy and is written back.
 __global__ void k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
                           const double *__restrict__ B, int nlev, long ng, double dt, int vl) {
     const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (c >= ng) return;
-    double scum[kTrMaxLev + 1], mfl[kTrMaxLev + 1];
+    double d[kTrMaxLev], m[kTrMaxLev], mfl[kTrMaxLev + 1];
+    for (int k = 0; k < nlev; ++k) {
+        d[k] = dp[k * ng + c];
+        m[k] = qm[k * ng + c];
+    }
+    // scum(k) = scum(k-1) + (dp0(k) - dp(k)) / dt; mfl(k) = B(k) scum(nlev) - scum(k)
+    double scum[kTrMaxLev + 1];
     scum[0] = 0.0;
-    for (int k = 1; k <= nlev; ++k) scum[k] = scum[k - 1] + (dp0[(k - 1) * ng + c] - dp[(k - 1) * ng + c]) / dt;
+    for (int k = 1; k <= nlev; ++k) scum[k] = scum[k - 1] + (dp0[(k - 1) * ng + c] - d[k - 1]) / dt;
     for (int k = 0; k <= nlev; ++k) mfl[k] = B[k] * scum[nlev] - scum[k];
-    auto qa = [&](int kk) { return qm[(kk - 1) * ng + c] / dp[(kk - 1) * ng + c]; };   // Fortran level kk
-    // flux through face kf (between levels kf and kf + 1) with mass flux m
-    auto flux = [&](int kf, double m) -> double {
+    auto qa = [&](int kk) { return m[kk - 1] / d[kk - 1]; };   // Fortran level kk
+    // flux through face kf (between levels kf and kf + 1) with mass flux mm
+    auto flux = [&](int kf, double mm) -> double {
         if (kf <= 0 || kf >= nlev) return 0.0;
-        if (!vl) return (m >= 0.0 ? qa(kf) : qa(kf + 1)) * m;
-        const int kd = m >= 0.0 ? kf : kf + 1;
+        if (!vl) return (mm >= 0.0 ? qa(kf) : qa(kf + 1)) * mm;
+        const int kd = mm >= 0.0 ? kf : kf + 1;
         const double qd = qa(kd);
-        const double cour = fabs(m) * dt / dp[(kd - 1) * ng + c];
-        if (kd - 1 < 1 || kd + 1 > nlev) return qd * m;
+        const double cour = fabs(mm) * dt / d[kd - 1];
+        if (kd - 1 < 1 || kd + 1 > nlev) return qd * mm;
         double sm, sp;
-        if (m >= 0.0) {
+        if (mm >= 0.0) {
             sm = qd - qa(kd - 1);
             sp = qa(kd + 1) - qd;
         } else {
             sm = qd - qa(kd + 1);
             sp = qa(kd - 1) - qd;
         }
-        return (qd + 0.5 * (1.0 - cour) * vanleer(sm, sp)) * m;
+        return (qd + 0.5 * (1.0 - cour) * vanleer(sm, sp)) * mm;
     };
     for (int k = 1; k <= nlev; ++k) {
         const double da = mfl[k] - mfl[k - 1];
         const double dq = flux(k, mfl[k]) - flux(k - 1, mfl[k - 1]);
-        const long o = (k - 1) * ng + c;
-        dp[o] = dp[o] - dt * da;
-        qm[o] = qm[o] - dt * dq;
+        d[k - 1] = d[k - 1] - dt * da;
+        m[k - 1] = m[k - 1] - dt * dq;
+    }
+    for (int k = 0; k < nlev; ++k) {
+        dp[k * ng + c] = d[k];
+        qm[k * ng + c] = m[k];
     }
 }
 
@@ -270,6 +279,7 @@ struct aeros_transport_s {
     std::vector<double> w;                                       // Gauss weights (host)
     double *A = nullptr, *B = nullptr, *dmu = nullptr, *coslat = nullptr, *cosface = nullptr;
     double *dp = nullptr, *qm = nullptr, *dp0 = nullptr;         // (nlev, nlat, nlon)
+    double *mfa = nullptr, *mfq = nullptr;                       // meridional face fluxes (nlev, nlat + 1, nlon)
     double *su = nullptr, *sv = nullptr, *sq = nullptr, *sl = nullptr, *rows = nullptr;   // staging
     unsigned long long *cmax = nullptr;
     cudaStream_t stream = nullptr;
@@ -283,7 +293,7 @@ namespace {
 
 void tr_free(aeros_transport_s *h) {
     double *ps[] = {h->A, h->B, h->dmu, h->coslat, h->cosface, h->dp, h->qm, h->dp0, h->su, h->sv, h->sq, h->sl,
-                    h->rows};
+                    h->rows, h->mfa, h->mfq};
     for (double *p : ps)
         if (p) cudaFree(p);
     if (h->cmax) cudaFree(h->cmax);
@@ -344,7 +354,9 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
         (rc = tr_alloc(h->coslat, g.nlat)) || (rc = tr_alloc(h->cosface, g.nlat + 1)) || (rc = tr_alloc(h->dp, n3)) ||
         (rc = tr_alloc(h->qm, n3)) || (rc = tr_alloc(h->dp0, n3)) || (rc = tr_alloc(h->su, n3)) ||
         (rc = tr_alloc(h->sv, n3)) || (rc = tr_alloc(h->sq, n3)) || (rc = tr_alloc(h->sl, (size_t)h->ng)) ||
-        (rc = tr_alloc(h->rows, g.nlat)) || (rc = tr_alloc(h->cmax, 1))) {
+        (rc = tr_alloc(h->rows, g.nlat)) || (rc = tr_alloc(h->cmax, 1)) ||
+        (rc = tr_alloc(h->mfa, (size_t)nlev * (g.nlat + 1) * g.nlon)) ||
+        (rc = tr_alloc(h->mfq, (size_t)nlev * (g.nlat + 1) * g.nlon))) {
         tr_free(h);
         return rc;
     }
@@ -353,6 +365,8 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
               cudaMemcpy(h->dmu, g.w.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemcpy(h->coslat, cl.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemcpy(h->cosface, cf.data(), 8 * (g.nlat + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemset(h->mfa, 0, 8 * (size_t)nlev * (g.nlat + 1) * g.nlon) == cudaSuccess &&   // pole faces stay 0
+              cudaMemset(h->mfq, 0, 8 * (size_t)nlev * (g.nlat + 1) * g.nlon) == cudaSuccess &&
               cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -428,12 +442,16 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
     const int zthr = (h->nlon + 31) / 32 * 32;
     if (zthr > 1024) { set_error("transport: nlon above 1024"); return AEROS_ERR_UNSUPPORTED; }
     const size_t zsm = (size_t)4 * h->nlon * sizeof(double);
-    const unsigned nbm = (unsigned)(((long)h->nlev * h->nlon + 127) / 128);
+    const unsigned nbf = (unsigned)(((long)h->nlev * (h->nlat - 1) * h->nlon + 255) / 256);
+    const unsigned nbu = (unsigned)(((long)h->nlev * ng + 255) / 256);
     for (int s = 0; s < nsub; ++s) {
         k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(ud, h->dp, h->qm, h->dp0, h->coslat, h->nlon,
                                                                      h->nlat, ng, h->dlam, dts);
-        k_tr_merid<<<nbm, 128, 0, h->stream>>>(vd, h->dp, h->qm, h->cosface, h->dmu, h->nlon, h->nlat, h->nlev, ng,
-                                               dts);
+        if (h->nlat > 1)
+            k_tr_mfaces<<<nbf, 256, 0, h->stream>>>(vd, h->dp, h->qm, h->cosface, h->dmu, h->nlon, h->nlat, h->nlev,
+                                                    ng, dts, h->mfa, h->mfq);
+        k_tr_mupdate<<<nbu, 256, 0, h->stream>>>(h->dp, h->qm, h->mfa, h->mfq, h->dmu, h->nlon, h->nlat, h->nlev,
+                                                 ng, dts);
         k_tr_vert<<<nbc, 128, 0, h->stream>>>(h->dp0, h->dp, h->qm, h->B, h->nlev, ng, dts, h->vert_vanleer);
     }
     AEROS_CUDA(cudaGetLastError());

@@ -21,7 +21,11 @@ def main(argv=None):
     ap.add_argument("--members", type=int, default=16)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--transport", action="store_true",
+                    help="run `steps` tracer-transport calls (one member's grid) instead of dynamics steps")
     a = ap.parse_args(argv)
+    if a.transport:
+        return transport_case(a)
     from .params import held_suarez_params, PREC_FP64, PREC_SPLIT
     from .dynamics import AerosDyn
     from .spectral import AerosSHT
@@ -40,6 +44,36 @@ def main(argv=None):
     for _ in range(a.steps):
         ks = dyn.profile_step()
     print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
+    return 0
+
+
+def transport_case(a):
+    """The bench's transport workload: winds of a 35 m/s solid-body rotation
+    plus a divergent part and 2 m/s seeded noise, the wavenumber-1 surface
+    pressure of the reference's transport test, q = 0.01, dt = 1800 s, device
+    arrays; `steps` calls of AerosTransport.step."""
+    import torch
+    from .params import held_suarez_params
+    from .dynamics import AerosDyn
+    from .transport import AerosTransport
+    d = AerosDyn(held_suarez_params(trunc=a.trunc, nlev=a.nlev))
+    nlev, nlat, nlon = d.nlev, d.nlat, d.nlon
+    lon = 2.0 * np.pi * np.arange(nlon) / nlon
+    lat = np.arcsin(d.sinlat)
+    rng = np.random.default_rng(7)
+    k = (np.arange(1, nlev + 1) / nlev)[:, None, None]
+    u = (35.0 * np.cos(lat)[None, :, None] + 35.0 * np.sin(lon)[None, None, :] * np.cos(lat)[None, :, None] * k
+         + rng.normal(0.0, 2.0, (nlev, nlat, nlon)))
+    v = 17.5 * np.cos(lon)[None, None, :] + rng.normal(0.0, 2.0, (nlev, nlat, nlon))
+    lnps = np.log(1.0e5 * (1.0 + 0.05 * np.sin(lon)[None, :] * np.cos(lat)[:, None]))
+    q = np.full((nlev, nlat, nlon), 0.01)
+    g = AerosTransport(a.trunc, d.A, d.B)
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (u, v, lnps, q)]
+    for _ in range(a.steps):
+        g.step(*dev, 1800.0)
+    torch.cuda.synchronize()
+    cfl, nsub = g.last()
+    print(f"transport calls={a.steps} max_courant={cfl:.3f} substeps={nsub}")
     return 0
 
 

@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the T85/T170/T341 transform sweep")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner of the batched form")
+    ap.add_argument("--no-transport", action="store_true", help="skip the tracer-transport measurement")
     return ap.parse_args()
 
 
@@ -339,6 +340,60 @@ def adjoint_form(args):
             "fd_rel_err_ka": abs(fd - ka_b[0]) / abs(ka_b[0])}
 
 
+def transport_form(args, torch):
+    """Tracer transport (the grid tracer of the moist model) at T42L20, dt 1800 s:
+    winds of a 35 m/s solid-body rotation plus a divergent part and 2 m/s seeded
+    noise, the wavenumber-1 surface pressure and a blob tracer of the
+    reference's transport test; device-resident arrays, one synchronised call
+    per sample (the call reads the Courant number back to size its sub-steps).
+    The numpy oracle's time for the same call is the CPU line beside it."""
+    import numpy as np
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.transport import AerosTransport
+    d = AerosDyn(held_suarez_params(trunc=args.trunc, nlev=args.nlev))
+    s = AerosSHT(args.trunc, batch_max=1)
+    nlev, nlat, nlon = d.nlev, d.nlat, d.nlon
+    lon = 2.0 * np.pi * np.arange(nlon) / nlon
+    lat = np.arcsin(np.asarray(s.sinlat))
+    rng = np.random.default_rng(7)
+    k = (np.arange(1, nlev + 1) / nlev)[:, None, None]
+    u = (35.0 * np.cos(lat)[None, :, None] + 35.0 * np.sin(lon)[None, None, :] * np.cos(lat)[None, :, None] * k
+         + rng.normal(0.0, 2.0, (nlev, nlat, nlon)))
+    v = 17.5 * np.cos(lon)[None, None, :] + rng.normal(0.0, 2.0, (nlev, nlat, nlon))
+    lnps = np.log(1.0e5 * (1.0 + 0.05 * np.sin(lon)[None, :] * np.cos(lat)[:, None]))
+    r2 = (lon[None, :] - np.pi) ** 2 + 4.0 * lat[:, None] ** 2
+    q = np.broadcast_to(0.002 + 0.015 * np.exp(-6.0 * r2), (nlev, nlat, nlon)).copy()
+    A, B = d.A, d.B
+    g = AerosTransport(args.trunc, A, B)
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (u, v, lnps, q)]
+    for _ in range(3):
+        g.step(*dev, 1800.0)
+    torch.cuda.synchronize()
+    n = 20
+    t0 = time.perf_counter()
+    for _ in range(n):
+        g.step(*dev, 1800.0)
+    torch.cuda.synchronize()
+    t_gpu = (time.perf_counter() - t0) / n
+    cfl, nsub = g.last()
+    from oracle.transport_oracle import OracleTransport
+    o = OracleTransport(np.asarray(s.sinlat), np.asarray(s.gauss_w), nlon, A, B)
+    o.transport(u, v, lnps, q, 1800.0)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        o.transport(u, v, lnps, q, 1800.0)
+    t_cpu = (time.perf_counter() - t0) / 3
+    cells = nlev * nlat * nlon
+    # algorithmic bytes of one sub-step: zonal 6, meridional 5, vertical 6 doubles per cell
+    sub_bytes = 17 * 8 * cells
+    return {"workload": f"T{args.trunc}L{nlev} grid {nlon}x{nlat}, dt 1800 s, device arrays", "ms_per_call": t_gpu * 1e3,
+            "max_courant": cfl, "substeps": nsub, "cell_substeps_per_s": cells * nsub / t_gpu,
+            "achieved_GBs": sub_bytes * nsub / t_gpu / 1e9, "bytes_per_substep": sub_bytes,
+            "cpu_oracle_ms_per_call": t_cpu * 1e3, "cpu_oracle": "numpy restatement, 1 core"}
+
+
 def batched_form(args, torch):
     """Config of 96 uneven members: 32 x T21L16 + 32 x T31L20 + 32 x T42L20,
     each member with its own seed and equator-pole contrast dT_y ~ U(40, 80) K,
@@ -586,6 +641,9 @@ def run_gpu(args, rank, world, local):
     sweep = None
     if not args.no_sweep and rank == 0:
         sweep = transform_sweep(args, torch)
+    transport = None
+    if not args.no_transport and rank == 0:
+        transport = transport_form(args, torch)
 
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1) else None
     if rank == 0:
@@ -601,6 +659,7 @@ def run_gpu(args, rank, world, local):
                 "sypd_l2_resident": sypd(t_warm) * world,
                 "e2e": e2e, "roofline": roof, "kernels_ms": prof, "cpu_baseline": cpu,
                 "split_precision": split, "batched": batched, "adjoint": adjoint, "transform_sweep": sweep,
+                "transport": transport,
                 "clocks": clk, "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     if world > 1:
