@@ -37,6 +37,7 @@ struct LevConst {
     double lnbf, bfk;             // ln(bf), bf^kappa with p_full = bf ps (pure)
     double rdB;                   // 1 / (B1 - B0) (pure): 1/dp = rdB / ps
     double hf;                    // Held-Suarez max(0, (sigma - sigma_b)/(1 - sigma_b)) (pure)
+    double kfhf;                  // Held-Suarez drag rate k_f hf (pure)
     int pure;
     int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
 };
@@ -160,31 +161,45 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     if (!act) return;
     const double f = 2.0 * kOmega * xlat[j];
     const double x2 = xlat[j] * xlat[j], c2 = 1.0 - x2, c4 = c2 * c2;
-    double dty = 0, ka = 0, psk = 0, lnpr = 0, tbase = 0;
+    // Held-Suarez per column: T_eq numerator tbase - dtheta_z c2 ln(p/p0) = T0 - Gc ln(bf)
+    // on a pure level, and k_T = k_a + hf K4
+    double ka = 0, psk = 0, lnpr = 0, tbase = 0, Gc = 0, T0 = 0, K4 = 0;
     if (hs_on) {
-        dty = hs_dty[e];
+        const double dty = hs_dty[e];
         ka = hs_ka[e];
         lnpr = lnps - c_hs.lnp0;
         psk = exp(kKappa * lnpr);   // (ps/p0)^kappa
         tbase = c_hs.t_eq - dty * x2;
+        Gc = c_hs.dtheta_z * c2;
+        T0 = tbase - Gc * lnpr;
+        K4 = (c_hs.k_s - ka) * c4;
     }
+    // x_k - x_{k-1} of u, v, T: the difference below a level is the one above the next
+    double dua = 0.0, dva = 0.0, dta = 0.0;
 #pragma unroll
     LEVELS_UP(i) {
         const int k = k0 + i;
         const LevConst &L = c_lev[k];
         const double uc = GF(k), vc = GF(NL + k), tc = GF(4 * NL + k);
-        const double up = k > 0 ? GF(k - 1) : 0.0, vp = k > 0 ? GF(NL + k - 1) : 0.0,
-                     tp = k > 0 ? GF(4 * NL + k - 1) : 0.0;
-        const double un = k + 1 < NL ? GF(k + 1) : 0.0, vn = k + 1 < NL ? GF(NL + k + 1) : 0.0,
-                     tn = k + 1 < NL ? GF(4 * NL + k + 1) : 0.0;
+        if (i == 0 && k > 0) {
+            dua = uc - GF(k - 1);
+            dva = vc - GF(NL + k - 1);
+            dta = tc - GF(4 * NL + k - 1);
+        }
+        const bool below = k + 1 < NL;
+        const double dub = below ? GF(k + 1) - uc : 0.0, dvb = below ? GF(NL + k + 1) - vc : 0.0,
+                     dtb = below ? GF(4 * NL + k + 1) - tc : 0.0;
         const double r = rdp[i];
         const double omega = cfac[i] * gc[i] - (scum[i] * dlnp[i] + alpha[i] * cm[i]) * r;
         const double mup = L.B0 * SN - scum[i];        // M at half level k (above)
         const double mlo = L.B1 * SN - scum[i + 1];    // M at half level k+1 (below)
         const double hr = 0.5 * r;
-        const double vu = hr * (((k < NL - 1) ? mlo * (un - uc) : 0.0) + ((k > 0) ? mup * (uc - up) : 0.0));
-        const double vv = hr * (((k < NL - 1) ? mlo * (vn - vc) : 0.0) + ((k > 0) ? mup * (vc - vp) : 0.0));
-        const double vt = hr * (((k < NL - 1) ? mlo * (tn - tc) : 0.0) + ((k > 0) ? mup * (tc - tp) : 0.0));
+        const double vu = hr * (mlo * dub + mup * dua);
+        const double vv = hr * (mlo * dvb + mup * dva);
+        const double vt = hr * (mlo * dtb + mup * dta);
+        dua = dub;
+        dva = dvb;
+        dta = dtb;
         const double zf = GF(2 * NL + k) + f;
         const double pgf = kRd * tc * cfac[i];
         double ae = zf * vc - vu - pgf * dpx;
@@ -193,21 +208,23 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         double dtdt = -(uc * GF(5 * NL + k) + vc * GF(6 * NL + k)) - vt + kKappa * tc * omega;
         if (hs_on) {
             // src/physics/aeros_held_suarez.f90:177-293
-            double lnpf, pfk, hf;
+            double teqn, pfk, hf, kv;
             if (L.pure) {
-                lnpf = L.lnbf + lnpr;
+                teqn = fma(-Gc, L.lnbf, T0);
                 pfk = L.bfk * psk;
                 hf = L.hf;
+                kv = L.kfhf;
             } else {
                 const double pf = 0.5 * (fma(L.B0, ps, L.A0) + fma(L.B1, ps, L.A1));
-                lnpf = log(pf / c_hs.p0);
+                const double lnpf = log(pf / c_hs.p0);
+                teqn = tbase - Gc * lnpf;
                 pfk = exp(kKappa * lnpf);
                 hf = fmax(0.0, (pf / ps - c_hs.sigma_b) * c_hs.rsb);
+                kv = c_hs.k_f * hf;
             }
-            const double teq = fmax(c_hs.t_min, (tbase - c_hs.dtheta_z * lnpf * c2) * pfk);
-            const double kt = ka + (c_hs.k_s - ka) * hf * c4;
+            const double teq = fmax(c_hs.t_min, teqn * pfk);
+            const double kt = fma(hf, K4, ka);
             dtdt -= kt * (tc - teq);
-            const double kv = c_hs.k_f * hf;
             ae -= kv * uc;
             an -= kv * vc;
         }
@@ -943,6 +960,7 @@ int upload_level_consts(Dyn &d) {
             c.lnbf = std::log(bf);
             c.bfk = std::pow(bf, kKappa);
             c.hf = std::max(0.0, (bf - d.par.hs_sigma_b) / (1.0 - d.par.hs_sigma_b));
+            c.kfhf = d.par.hs_k_f * c.hf;
         }
     }
     const aeros_params &p = d.par;
