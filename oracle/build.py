@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 Compiles oracle/aeros_oracle.cpp into oracle/_build/libaeros_oracle.so with the
-host compiler.  Portable flags only (the library is rebuilt on the Arm GPU machine):
+host compiler.  Portable flags only (the library is rebuilt on every machine, x86-64 and aarch64):
 no -march=native, no ISA intrinsics.  -ffp-contract=off keeps the arithmetic
 free of fused multiply-adds on both x86-64 and aarch64.
 """
