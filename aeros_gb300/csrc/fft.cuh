@@ -66,18 +66,27 @@ __device__ __forceinline__ void dft_small(double2 *v) {
     }
 }
 
+// n / d for a divisor fixed per stage: multiply-high by m = ceil(2^32 / d), exact
+// for n < 2^32 / d (every index here is far below that)
+struct StageDiv {
+    unsigned d, m;
+    __device__ __forceinline__ explicit StageDiv(int dv) : d((unsigned)dv), m(dv > 1 ? 0xFFFFFFFFu / (unsigned)dv + 1u : 0u) {}
+    __device__ __forceinline__ int div(int n) const { return d == 1 ? n : (int)__umulhi((unsigned)n, m); }
+};
+
 template <int R, bool INV>
 __device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int nrows, int stride, int n, int Ns,
                                           const double2 *__restrict__ tw, int tid, int nthr) {
     const int nb = n / R;
     const int tstep = n / (Ns * R);
     const int total = nrows * nb;
+    const StageDiv dnb(nb), dns(Ns);
     for (int idx = tid; idx < total; idx += nthr) {
-        int row = idx / nb;
+        int row = dnb.div(idx);
         int j = idx - row * nb;
         const double2 *x = src + row * stride;
         double2 *y = dst + row * stride;
-        int k = j % Ns;
+        int k = j - dns.div(j) * Ns;
         double2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = x[j + r * nb];

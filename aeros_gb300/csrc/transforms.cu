@@ -31,10 +31,11 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
     const int nr = min(lpb, nlat - j0);
     double2 *A = sm, *B = sm + (size_t)lpb * n, *X = sm + (size_t)2 * lpb * n;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const StageDiv dms(ms), dn(n), dnlon(nlon);
 
     // X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m], m = 0..T (imag of X_0 dropped)
     for (int idx = tid; idx < nr * ms; idx += nthr) {
-        const int r = idx / ms, m = idx - r * ms;
+        const int r = dms.div(idx), m = idx - r * ms;
         const int j = j0 + r;
         const double bs = m * isin[j];
         const double2 *Fr = F + (size_t)j * nrow * ms;
@@ -57,7 +58,7 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
     __syncthreads();
     // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O
     for (int idx = tid; idx < nr * n; idx += nthr) {
-        const int r = idx / n, k = idx - r * n;
+        const int r = dn.div(idx), k = idx - r * n;
         const int kc = n - k;
         const double2 xk = k <= T ? X[(size_t)r * ms + k] : make_double2(0.0, 0.0);
         const double2 xc = (kc <= T && kc < n) ? X[(size_t)r * ms + kc] : make_double2(0.0, 0.0);
@@ -70,7 +71,7 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
     double2 *res = fft_rows<true>(A, B, nr, n, plan, tw, tid, nthr);
     const double *rr = reinterpret_cast<const double *>(res);
     for (int idx = tid; idx < nr * nlon; idx += nthr) {
-        int r = idx / nlon, i = idx - r * nlon;
+        int r = dnlon.div(idx), i = idx - r * nlon;
         fd.dst[(size_t)(j0 + r) * nlon + i] = rr[(size_t)r * 2 * n + i];
     }
 }
@@ -87,18 +88,20 @@ __global__ void k_fourier_anal(const FanaField *__restrict__ fields, double2 *__
     const int nr = min(lpb, nlat - j0);
     double2 *A = sm, *B = sm + (size_t)lpb * n;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    const StageDiv dms(ms), dnlon(nlon);
     double *Ar = reinterpret_cast<double *>(A);
     for (int idx = tid; idx < nr * nlon; idx += nthr) {
-        int r = idx / nlon, i = idx - r * nlon;
+        int r = dnlon.div(idx), i = idx - r * nlon;
         Ar[(size_t)r * 2 * n + i] = fd.src[(size_t)(j0 + r) * nlon + i];
     }
     __syncthreads();
     double2 *Z = fft_rows<false>(A, B, nr, n, plan, tw, tid, nthr);
     const double sc = kSq2Pi / nlon;
     for (int idx = tid; idx < nr * ms; idx += nthr) {
-        int r = idx / ms, m = idx - r * ms;
-        double2 a = Z[(size_t)r * n + (m % n)];
-        double2 b = Z[(size_t)r * n + ((n - m) % n)];
+        int r = dms.div(idx), m = idx - r * ms;
+        // m <= T < n, so m % n = m and (n - m) % n = (m == 0 ? 0 : n - m)
+        double2 a = Z[(size_t)r * n + m];
+        double2 b = Z[(size_t)r * n + (m == 0 ? 0 : n - m)];
         // E = (a + conj b)/2, O = -i/2 (a - conj b),  X = E + e^{-2 pi i m/N} O
         double2 E = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
         double2 O = make_double2(0.5 * (a.y + b.y), -0.5 * (a.x - b.x));
