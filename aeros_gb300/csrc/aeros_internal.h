@@ -113,6 +113,7 @@ struct Tune {
     int fs_lpb = 0, fs_thr = 256;   // Fourier synthesis: latitudes per CTA, threads
     int fa_lpb = 0, fa_thr = 256;   // Fourier analysis
     int la_ct = 8;                  // FP64 Legendre analysis: output columns (warps) per CTA: 4, 8 or 16
+    int ls_jt = 32;                 // FP64 Legendre synthesis: latitudes per CTA: 8, 16 or 32
     int col_thr = 64;               // column kernel threads per CTA
     int col_lanes = 1;              // column kernel lanes per column: 1, 2, 4, 8 or 16
     int spec_warps = 4;             // spectral kernel warps per CTA

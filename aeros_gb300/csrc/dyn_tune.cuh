@@ -58,7 +58,7 @@ bool tune_load(Dyn &d) {
         std::string k;
         Tune t;
         if (!(in >> k >> t.fs_lpb >> t.fs_thr >> t.fa_lpb >> t.fa_thr >> t.la_ct >> t.col_thr >> t.spec_warps >>
-              t.col_lanes))
+              t.col_lanes >> t.ls_jt))
             continue;
         if (k != key) continue;
         d.tune = t;
@@ -73,7 +73,7 @@ void tune_store(Dyn &d) {
     std::ofstream f(path, std::ios::app);
     const Tune &t = d.tune;
     f << tune_key(d) << " " << t.fs_lpb << " " << t.fs_thr << " " << t.fa_lpb << " " << t.fa_thr << " " << t.la_ct
-      << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << "\n";
+      << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << " " << t.ls_jt << "\n";
 }
 
 int recapture(Dyn &d) {
@@ -133,9 +133,12 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
                 t.fa_thr = thr;
                 trial(t);
             }
-        if (d.par.precision == AEROS_PREC_FP64)
+        if (d.par.precision == AEROS_PREC_FP64) {
             for (int ct : {4, 8, 16})
                 if (ct != d.tune.la_ct) { Tune t = d.tune; t.la_ct = ct; trial(t); }
+            for (int jt : {8, 16, 32})
+                if (jt != d.tune.ls_jt) { Tune t = d.tune; t.ls_jt = jt; trial(t); }
+        }
         for (int ct : {32, 64, 128, 256})
             for (int lp : {1, 2, 4, 8, 16})
                 if (ct != d.tune.col_thr || lp != d.tune.col_lanes) {
@@ -164,12 +167,12 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
     return AEROS_OK;
 }
 
-// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes.
-int aeros_dyn_tune_get(aeros_dyn_t h, int *shape8) {
-    if (!h || !shape8) return AEROS_ERR_ARG;
+// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes, ls_jt.
+int aeros_dyn_tune_get(aeros_dyn_t h, int *shape9) {
+    if (!h || !shape9) return AEROS_ERR_ARG;
     const Tune &t = h->tune;
-    const int v[8] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr, t.spec_warps, t.col_lanes};
-    std::memcpy(shape8, v, sizeof(v));
+    const int v[9] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr, t.spec_warps, t.col_lanes, t.ls_jt};
+    std::memcpy(shape9, v, sizeof(v));
     return AEROS_OK;
 }
 

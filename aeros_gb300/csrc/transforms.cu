@@ -157,16 +157,18 @@ int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2
 // even and odd (l - m) parts of sum_l c_lm Pbar_lm(x_j) [and dPbar], which
 // fold into the north row (E + O) and the south row (E - O; O - E for dPbar,
 // whose parity is opposite).
-constexpr int kSynJT = 32;   // latitudes per tile
+// kSynJT (latitudes per tile: 32, 16 or 8) trades work per CTA for CTAs:
+// the m = 0 tiles carry the longest contraction and bound one member's step.
 constexpr int kSynCT = 16;   // columns per tile
 constexpr int kSynKC = 16;   // degrees per smem chunk (even)
 constexpr int kSynThreads = 128;
-constexpr int kSynQ = kSynJT * kSynCT / kSynThreads;
 
+template <int kSynJT>
 __global__ void __launch_bounds__(kSynThreads) k_leg_synth_fp64(
     const SynCol *__restrict__ cols, int ncol, int ncolD_first, const int *__restrict__ tile_first,
     const double *__restrict__ Ps, const double *__restrict__ dPs, const double *__restrict__ lfac,
     const int *__restrict__ moff, double2 *__restrict__ F, int nrow, int ms, int T, int nh, int nlat) {
+    constexpr int kSynQ = kSynJT * kSynCT / kSynThreads;
     __shared__ double sP[kSynKC][kSynJT];
     __shared__ double sD[kSynKC][kSynJT];
     __shared__ double2 sC[kSynKC][kSynCT];
@@ -290,10 +292,15 @@ void free_syn_plan(SynPlan &p) {
 
 int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) {
     if (p.ncol <= 0) return AEROS_OK;
-    dim3 grid(c.T + 1, p.ntile, (c.nh + kSynJT - 1) / kSynJT);
-    k_leg_synth_fp64<<<grid, kSynThreads, 0, c.stream>>>(p.cols_d, p.ncol, p.ncolD_first, p.tiles_d, c.tab->Ps,
-                                                         c.tab->dPs, c.tab->lfac, c.tab->moff, F, nrow, c.ms, c.T,
-                                                         c.nh, c.nlat);
+    const int jt = c.tune ? c.tune->ls_jt : 32;
+    auto go = [&](auto kern, int JT) {
+        dim3 grid(c.T + 1, p.ntile, (c.nh + JT - 1) / JT);
+        kern<<<grid, kSynThreads, 0, c.stream>>>(p.cols_d, p.ncol, p.ncolD_first, p.tiles_d, c.tab->Ps, c.tab->dPs,
+                                                 c.tab->lfac, c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+    };
+    if (jt == 8) go(k_leg_synth_fp64<8>, 8);
+    else if (jt == 16) go(k_leg_synth_fp64<16>, 16);
+    else go(k_leg_synth_fp64<32>, 32);
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;

@@ -258,7 +258,7 @@ class AerosDyn:
         return c.value
 
     # ------------------------------------------------------------------ autotuner
-    TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps", "col_lanes")
+    TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps", "col_lanes", "ls_jt")
 
     def autotune(self, reps=3):
         """Choose launch shapes by timing whole steps; returns (ms before, ms after, shapes)."""
@@ -268,7 +268,7 @@ class AerosDyn:
         return b.value, a.value, self.tune_shapes()
 
     def tune_shapes(self):
-        v = np.zeros(8, np.int32)
+        v = np.zeros(len(self.TUNE_KEYS), np.int32)
         _capi.check(_capi.lib().aeros_dyn_tune_get(self._h, _ptr(v)), "aeros_dyn_tune_get")
         return dict(zip(self.TUNE_KEYS, (int(x) for x in v)))
 

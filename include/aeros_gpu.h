@@ -380,16 +380,17 @@ int aeros_dyn_launch_count(aeros_dyn_t h, long long *count);
 
 /* Launch-shape autotuner (no reference counterpart): times whole steps for
  * each candidate shape of the longitude FFTs (latitudes and threads per CTA),
- * the FP64 Legendre analysis (columns per CTA), the column kernel (threads per
- * CTA, lanes per column) and the spectral kernel (warps per CTA), keeps the fastest, restores the state and re-captures the step
- * graphs.  ms_before / ms_after: step time with the old and the chosen shapes.
+ * the FP64 Legendre analysis (columns per CTA) and synthesis (latitudes per
+ * CTA), the column kernel (threads per CTA, lanes per column) and the
+ * spectral kernel (warps per CTA), keeps the fastest, restores the state and
+ * re-captures the step graphs.  ms_before / ms_after: step time with the old and the chosen shapes.
  * With AEROS_TUNE_CACHE set to a file name, results are appended there and new
  * handles of the same GPU, grid, levels, ensemble size and precision start
  * from them.  Tune member handles before grouping them. */
 int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_after);
 /* The shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr,
- * spec_warps, col_lanes (0 = heuristic). */
-int aeros_dyn_tune_get(aeros_dyn_t h, int *shape8);
+ * spec_warps, col_lanes, ls_jt (0 = heuristic); shape9 holds 9 ints. */
+int aeros_dyn_tune_get(aeros_dyn_t h, int *shape9);
 
 /* ======================================================================== */
 /* Ensemble groups: several dyn handles (e.g. members of different          */
