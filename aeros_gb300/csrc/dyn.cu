@@ -420,27 +420,35 @@ __global__ void k_mass(double2 *__restrict__ lnps, int M, int T, int nlm, int nh
     const int e = blockIdx.y, jn = blockIdx.x, js = nlat - 1 - jn;
     double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * n;
     const double2 *c = lnps + (size_t)e * nlm;
-    // thread per m; the l loop runs in batches of 8 whose loads are all issued
-    // before the sums, which keep the serial order (even/odd l - m alternate)
-    for (int m = threadIdx.x; m <= T; m += blockDim.x) {
-        double2 ev = make_double2(0, 0), od = make_double2(0, 0);
+    // thread per (m, parity of l - m): each sums its parity in the serial order,
+    // in batches of 16 degrees whose loads are all issued before the sums
+    double2 *Eo = A;   // even / odd parts [2][ms], combined below (A is free until the FFT prep)
+    for (int t = threadIdx.x; t < 2 * ms; t += blockDim.x) {
+        const int m = t >> 1, par = t & 1;
+        double2 acc = make_double2(0, 0);
         const int mo = moff[m], K = T - m + 1;
-        for (int k0 = 0; k0 < K; k0 += 8) {
-            double p[8];
-            double2 v[8];
+        for (int k0 = par; k0 < K; k0 += 32) {
+            double p[16];
+            double2 v[16];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const bool in = k0 + u < K;
-                p[u] = in ? Ps[(size_t)(mo + k0 + u) * nh + jn] : 0.0;
-                v[u] = in ? c[mo + k0 + u] : make_double2(0.0, 0.0);
+            for (int u = 0; u < 16; ++u) {
+                const int k = k0 + 2 * u;
+                const bool in = k < K;
+                p[u] = in ? Ps[(size_t)(mo + k) * nh + jn] : 0.0;
+                v[u] = in ? c[mo + k] : make_double2(0.0, 0.0);
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (k0 + u >= K) break;
-                if (u & 1) { od.x += p[u] * v[u].x; od.y += p[u] * v[u].y; }
-                else { ev.x += p[u] * v[u].x; ev.y += p[u] * v[u].y; }
+            for (int u = 0; u < 16; ++u) {
+                if (k0 + 2 * u >= K) break;
+                acc.x += p[u] * v[u].x;
+                acc.y += p[u] * v[u].y;
             }
         }
+        Eo[par * ms + m] = acc;
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m <= T; m += blockDim.x) {
+        const double2 ev = Eo[m], od = Eo[ms + m];
         Fn[m] = cadd(ev, od);
         Fs[m] = csub(ev, od);
     }
