@@ -88,6 +88,7 @@ _PROTOS = {
     "aeros_dyn_hs_perturb": [_vp, _d],
     "aeros_dyn_step": [_vp, _i],
     "aeros_dyn_step_async": [_vp, _i],
+    "aeros_dyn_step_packed": [_vp, _vp, _vp, _i, _i, _vp],
     "aeros_dyn_sync": [_vp],
     "aeros_dyn_profile_step": [_vp, _i, _vp, _vp, _i, _ip],
     "aeros_dyn_tendency": [_vp, _vp, _vp, _vp, _vp],

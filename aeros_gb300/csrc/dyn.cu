@@ -1447,6 +1447,21 @@ int aeros_dyn_step(aeros_dyn_t h, int nsteps) {
     return aeros_dyn_sync(h);
 }
 
+int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,
+                          double *now_out) {
+    if (!h || !now_in || !old_in || nstep < 0 || nsteps < 0) return AEROS_ERR_ARG;
+    const size_t bytes = h->nstate() * sizeof(double2);
+    // the packed order vor | div | temp | lnps (all members each) is the device layout of a time level
+    AEROS_CUDA(cudaMemcpyAsync(h->now, now_in, bytes, cudaMemcpyDefault, h->stream));
+    AEROS_CUDA(cudaMemcpyAsync(h->old, old_in, bytes, cudaMemcpyDefault, h->stream));
+    AEROS_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+    h->nstep = nstep;
+    int rc = aeros_dyn_step_async(h, nsteps);
+    if (rc) return rc;
+    if (now_out) AEROS_CUDA(cudaMemcpyAsync(now_out, h->now, bytes, cudaMemcpyDefault, h->stream));
+    return aeros_dyn_sync(h);
+}
+
 int aeros_dyn_step_async(aeros_dyn_t h, int nsteps) {
     if (!h || nsteps < 0) return AEROS_ERR_ARG;
     for (int i = 0; i < nsteps; ++i) {

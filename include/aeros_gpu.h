@@ -238,6 +238,15 @@ int aeros_dyn_step(aeros_dyn_t h, int nsteps);
  * graphs; no host synchronization).  aeros_dyn_sync waits for them and
  * reports AEROS_ERR_NONFINITE if any step produced a NaN/Inf. */
 int aeros_dyn_step_async(aeros_dyn_t h, int nsteps);
+/* A caller that keeps the state on the host, in one call: X^n (now_in) and
+ * X^(n-1) (old_in) with its step count nstep in, nsteps steps, the new X^n out
+ * (now_out, may be NULL).  Each array is one time level packed vor | div |
+ * temp | lnps (all members each, aeros_dyn_state_size complex values), host or
+ * device: the same as aeros_dyn_set_state + aeros_dyn_set_old_state +
+ * aeros_dyn_step + aeros_dyn_get_state with three copies and one
+ * synchronisation. */
+int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,
+                          double *now_out);
 int aeros_dyn_sync(aeros_dyn_t h);
 
 /* Run one step with a CUDA event after every kernel (no graph) and return the

@@ -342,3 +342,21 @@ def test_restart_file_resumes_bitwise(gpulib, tmp_path):
     for x, y in zip(a.get_state(), b.get_state()):
         assert np.array_equal(x, y)
     assert a.counters() == b.counters()
+
+
+def test_step_packed_equals_the_four_calls(gpulib):
+    """aeros_dyn_step_packed == set_state + set_old_state(nstep) + step + get_state, bitwise."""
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    p = held_suarez_params(trunc=21, nlev=12)
+    a = AerosDyn(p)
+    a.set_isothermal(264.0, 1.0e5)
+    a.hs_perturb(1.0)
+    a.step(5)
+    now, old, n = a.pack(*a.get_state()), a.pack(*a.get_old_state()), a.counters()[0]
+    b = AerosDyn(p)
+    b.set_mass_target(a.member_counters(0)[0])
+    out = b.step_packed(now, old, n, nsteps=3)
+    a.step(3)
+    assert np.array_equal(out, a.pack(*a.get_state()))
+    assert b.counters()[0] == n + 3
