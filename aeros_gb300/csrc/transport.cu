@@ -9,8 +9,9 @@
 //                periodic van Leer face values, fluxes staged in shared memory
 //   k_tr_mfaces  thread per (level, face, longitude): meridional face fluxes
 //   k_tr_mupdate thread per cell: the meridional update from its two faces
-//   k_tr_vert    thread per grid column, loaded whole: vertical mass flux from
-//                the layer-mass change of the two sweeps, levels updated top down
+//   k_tr_vert    thread per grid column, streamed down the column: vertical mass
+//                flux from the layer-mass change of the two sweeps, levels updated
+//                top down
 //                (a level's upper-face flux sees the level above already updated,
 //                as the reference's loop does)
 // Grids are (nlev, nlat, nlon) in C order, latitude north to south: the
@@ -180,50 +181,59 @@ __global__ void k_tr_mupdate(double *__restrict__ dp, double *__restrict__ qm, c
 }
 
 // Vertical mass flux and the top-down update (transport_substep, :238-297;
-// vflux_q :491-513, vflux_q_vl :515-553).  The column is loaded first; the
-// update runs on the loaded copy and is written back.
+// vflux_q :491-513, vflux_q_vl :515-553), streamed over the column: a first
+// pass forms the column sum of the layer-mass change, a second recomputes the
+// running sums in the same order while it walks down, holding only the levels
+// around the one being updated (two above, updated; two below, not yet).
 __global__ void k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
                           const double *__restrict__ B, int nlev, long ng, double dt, int vl) {
     const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (c >= ng) return;
-    double d[kTrMaxLev], m[kTrMaxLev], mfl[kTrMaxLev + 1];
-    for (int k = 0; k < nlev; ++k) {
-        d[k] = dp[k * ng + c];
-        m[k] = qm[k * ng + c];
-    }
-    // scum(k) = scum(k-1) + (dp0(k) - dp(k)) / dt; mfl(k) = B(k) scum(nlev) - scum(k)
-    double scum[kTrMaxLev + 1];
-    scum[0] = 0.0;
-    for (int k = 1; k <= nlev; ++k) scum[k] = scum[k - 1] + (dp0[(k - 1) * ng + c] - d[k - 1]) / dt;
-    for (int k = 0; k <= nlev; ++k) mfl[k] = B[k] * scum[nlev] - scum[k];
-    auto qa = [&](int kk) { return m[kk - 1] / d[kk - 1]; };   // Fortran level kk
-    // flux through face kf (between levels kf and kf + 1) with mass flux mm
-    auto flux = [&](int kf, double mm) -> double {
+    auto at = [&](int kk) { return (long)(kk - 1) * ng + c; };   // Fortran level kk
+    double SN = 0.0;                                             // scum(nlev)
+    for (int kk = 1; kk <= nlev; ++kk) SN = SN + (dp0[at(kk)] - dp[at(kk)]) / dt;
+    // flux through face kf (between levels kf and kf + 1) with mass flux mm, from the ratios of
+    // levels kf - 1 .. kf + 2 and the thicknesses of levels kf, kf + 1 as the loop sees them
+    auto flux = [&](int kf, double mm, double qa_m1, double qa_0, double qa_p1, double qa_p2, double d0,
+                    double d1) -> double {
         if (kf <= 0 || kf >= nlev) return 0.0;
-        if (!vl) return (mm >= 0.0 ? qa(kf) : qa(kf + 1)) * mm;
-        const int kd = mm >= 0.0 ? kf : kf + 1;
-        const double qd = qa(kd);
-        const double cour = fabs(mm) * dt / d[kd - 1];
+        if (!vl) return (mm >= 0.0 ? qa_0 : qa_p1) * mm;
+        const bool down = mm >= 0.0;
+        const int kd = down ? kf : kf + 1;
+        const double qd = down ? qa_0 : qa_p1;
+        const double cour = fabs(mm) * dt / (down ? d0 : d1);
         if (kd - 1 < 1 || kd + 1 > nlev) return qd * mm;
-        double sm, sp;
-        if (mm >= 0.0) {
-            sm = qd - qa(kd - 1);
-            sp = qa(kd + 1) - qd;
-        } else {
-            sm = qd - qa(kd + 1);
-            sp = qa(kd - 1) - qd;
-        }
+        const double sm = down ? qd - qa_m1 : qd - qa_p2;
+        const double sp = down ? qa_p1 - qd : qa_0 - qd;
         return (qd + 0.5 * (1.0 - cour) * vanleer(sm, sp)) * mm;
     };
+    double m0 = qm[at(1)], d0 = dp[at(1)];                                      // level k, not yet updated
+    double m1 = nlev > 1 ? qm[at(2)] : 0.0, d1 = nlev > 1 ? dp[at(2)] : 1.0;    // level k + 1
+    double q2 = nlev > 2 ? qm[at(3)] / dp[at(3)] : 0.0;                         // ratio of level k + 2
+    double qu1 = 0.0, qu2 = 0.0, du1 = 1.0;   // updated ratios of levels k - 1, k - 2; thickness of k - 1
+    double scum_prev = 0.0, mfl_prev = B[0] * SN;   // scum(0) = 0, mfl(0)
     for (int k = 1; k <= nlev; ++k) {
-        const double da = mfl[k] - mfl[k - 1];
-        const double dq = flux(k, mfl[k]) - flux(k - 1, mfl[k - 1]);
-        d[k - 1] = d[k - 1] - dt * da;
-        m[k - 1] = m[k - 1] - dt * dq;
-    }
-    for (int k = 0; k < nlev; ++k) {
-        dp[k * ng + c] = d[k];
-        qm[k * ng + c] = m[k];
+        const double scum = scum_prev + (dp0[at(k)] - d0) / dt;
+        const double mfl = B[k] * SN - scum;
+        const double q0 = m0 / d0, q1 = m1 / d1;
+        const double da = mfl - mfl_prev;
+        const double dq = flux(k, mfl, qu1, q0, q1, q2, d0, d1) - flux(k - 1, mfl_prev, qu2, qu1, q0, q1, du1, d0);
+        const double dn = d0 - dt * da, mn = m0 - dt * dq;
+        dp[at(k)] = dn;
+        qm[at(k)] = mn;
+        // slide one level down
+        qu2 = qu1;
+        qu1 = mn / dn;
+        du1 = dn;
+        m0 = m1;
+        d0 = d1;
+        if (k + 2 <= nlev) {
+            m1 = qm[at(k + 2)];
+            d1 = dp[at(k + 2)];
+        }
+        q2 = k + 3 <= nlev ? qm[at(k + 3)] / dp[at(k + 3)] : 0.0;
+        scum_prev = scum;
+        mfl_prev = mfl;
     }
 }
 
