@@ -440,6 +440,13 @@ def batched_form(args, torch):
     return out
 
 
+def arm_config(args, nlon, nlat, world):
+    """The workload both arms report (the reference arm runs the same configuration on the host)."""
+    return {"workload": f"held_suarez_T{args.trunc}L{args.nlev}_dt1800_fp64", "members_per_gpu": 1,
+            "grid": f"{nlon}x{nlat}", "l2": "flushed (256 MB write) before every timed step",
+            "precision": "fp64", "parallelism": f"replicas x{world}"}
+
+
 # ---------------------------------------------------------------- reference arm
 def run_reference(args, rank, world):
     if rank != 0:
@@ -465,8 +472,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "SYPD", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"held_suarez_T{args.trunc}L{args.nlev}_dt1800", "members": 1,
-                       "grid": f"{o.nlon}x{o.nlat}"},
+            "config": arm_config(args, o.nlon, o.nlat, world),
             "cpu_baseline": {"value": v, "unit": "SYPD", "cores": cores, "kind": "port",
                              "sample": f"{args.steps} oracle steps after {args.warmup} warm-up, OpenMP over levels"},
             "e2e": {"value": v, "unit": "SYPD", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -648,9 +654,7 @@ def run_gpu(args, rank, world, local):
         line = {"metric": METRIC, "value": sypd(t_gpu) * world, "unit": "SYPD", "n_gpus": world, "steps": K,
                 "warmup": args.warmup, "ms_per_step": t_gpu * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"held_suarez_T{args.trunc}L{args.nlev}_dt1800_fp64", "members_per_gpu": 1,
-                           "grid": f"{dyn.nlon}x{dyn.nlat}", "l2": "flushed (256 MB write) before every timed step",
-                           "precision": "fp64", "parallelism": f"replicas x{world}"},
+                "config": arm_config(args, dyn.nlon, dyn.nlat, world),
                 "ms_per_step_l2_resident": t_warm * 1e3,
                 "launch_shapes": None if tune is None else {"ms_before": tune[0], "ms_after": tune[1],
                                                             "shapes": tune[2]},
