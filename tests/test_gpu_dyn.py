@@ -360,3 +360,21 @@ def test_step_packed_equals_the_four_calls(gpulib):
     a.step(3)
     assert np.array_equal(out, a.pack(*a.get_state()))
     assert b.counters()[0] == n + 3
+
+
+@pytest.mark.parametrize("trunc", [21, 42])
+def test_forced_tendency_matches_oracle(gpulib, trunc):
+    """aeros_dyn_tendency_forced: the adiabatic tendencies plus the Held-Suarez forcing
+    added on the grid at the seam, against the oracle's forced tendency."""
+    g, o, s = make_pair(trunc, 20)
+    st = moving_state(o, seed=8)
+    o.set_state(*st)
+    g.set_state(*st)
+    tg = g.tendency_forced()
+    to = o.tendency(forced=True)
+    assert relerr(tg[0], to[0]) < 1e-12
+    assert relerr(tg[2], to[2]) < 1e-12
+    assert relerr(tg[3], to[3]) < 1e-12
+    assert relerr(tg[1], to[1]) < max(1e-12, 20 * oracle_floor(o, st, 1))
+    ta = g.tendency()
+    assert relerr(ta[2], tg[2]) > 1e-8    # the forcing is in the forced tendency

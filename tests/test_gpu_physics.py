@@ -73,3 +73,19 @@ def test_adjoint_refuses_a_hook(gpulib):
     with pytest.raises(AerosError) as ei:
         g.window_forward(4, 2)
     assert ei.value.code == ERR_UNSUPPORTED
+
+
+def test_hook_inside_an_ensemble_group(gpulib):
+    """A handle's hook is part of its step graph, so a group that contains it steps
+    bit-identically to the handle stepped alone."""
+    from aeros_gb300.dynamics import AerosGroup
+    a, _ = _dyn()
+    b, _ = _dyn()
+    c, _ = _dyn(trunc=31)
+    for h in (a, b):
+        h.set_relaxation(1.0 / 86400.0, 1.0 / (4 * 86400.0), 250.0)
+    g = AerosGroup([a, c])
+    g.step(3)
+    b.step(3)
+    for x, y in zip(a.get_state(), b.get_state()):
+        assert np.array_equal(x, y)
