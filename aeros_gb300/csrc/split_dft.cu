@@ -32,8 +32,12 @@ namespace {
 
 constexpr int kNT = kNTile;   // data columns per tile
 
-template <int S>
-constexpr size_t gemm_smem() { return (size_t)S * (kTM + kNT) * kKC * 2 + 2 * (size_t)kNT * kSt * 8; }
+// Shared memory: the table chunk, the data digits and the stage: two chunk-wide
+// buffers, or (FULL) one buffer holding every contraction entry of a tile.
+template <int S, bool FULL>
+size_t gemm_smem(int Kp) {
+    return (size_t)S * (kTM + kNT) * kKC * 2 + (FULL ? (size_t)kNT * (Kp + 1) * 8 : 2 * (size_t)kNT * kSt * 8);
+}
 
 // ---------------------------------------------------------------- table digits
 __global__ void k_gemm_prep_exp(const double *__restrict__ T, int Mpad, int K, int *__restrict__ rexp) {
@@ -149,7 +153,11 @@ struct DftAnalP {
 // ct = slot, slot + gridDim.y, ... (32 data columns each), over the whole
 // contraction in 32-wide chunks.  TMEM and the barriers are set up once per CTA;
 // the first table chunk of the next tile is fetched during the epilogue.
-template <int S, int B, class P>
+// FULL: the gather of a tile stages every contraction entry (each data value is
+// formed once; the synthesis columns' wind combinations cost FP64), otherwise
+// chunk 0 is staged and later chunks are formed again while the previous
+// chunk's MMA runs.
+template <int S, int B, class P, bool FULL>
 __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch, const __nv_bfloat16 *dig,
                                                             const int *rexp, int *err) {
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     }
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
     __nv_bfloat16 *sB = sA + (size_t)S * kTM * kSlice;
-    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNT * kSlice);   // 2 x [kNT cols][kSt]
+    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNT * kSlice);   // see gemm_smem
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[2][kNT];
@@ -185,12 +193,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     __syncthreads();
     const __nv_bfloat16 *gA = dig + (size_t)mt * nch * S * kTM * kSlice;
     const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
+    const int Kst = FULL ? Kp + 1 : kSt;   // stage row stride (odd: conflict-free)
     const int gstep = gridDim.y;
     // phase 1 of column tile ct into buffer b: column scales over the whole contraction, chunk 0 staged
     const FastDiv dk8(nk8);
     auto gather = [&](int ct, int b) {
         const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
-        double *stage = stage0 + (size_t)b * kNT * kSt;
+        double *stage = FULL ? stage0 : stage0 + (size_t)b * kNT * kSt;
         if (tid < ncl) cbase[b][tid] = p.colbase(c0 + tid);
         for (int base = 0; base < ncl * nk8; base += kThreads) {
             const int task = base + tid;
@@ -208,9 +217,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             const unsigned peers = __match_any_sync(0xffffffffu, n);
             be = __reduce_max_sync(peers, be);
             if (valid && lane == __ffs(peers) - 1) atomicMax(&cexp[b][n], be);
-            if (valid && k0 < kc0)
+            if (valid && (FULL || k0 < kc0))
 #pragma unroll
-                for (int i = 0; i < 8; ++i) stage[n * kSt + k0 + i] = k0 + i < K ? x[i] : 0.0;
+                for (int i = 0; i < 8; ++i) stage[n * Kst + k0 + i] = k0 + i < K ? x[i] : 0.0;
         }
     };
     if (tid < kNT) cexp[0][tid] = 0;
@@ -232,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     for (int ct = blockIdx.y; ct < nct && ok; ct += gstep, cb ^= 1) {
         const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
         const bool more = ct + gstep < nct;
-        double *stage = stage0 + (size_t)cb * kNT * kSt;
+        double *stage = FULL ? stage0 : stage0 + (size_t)cb * kNT * kSt;
         if (more && tid < kNT) cexp[cb ^ 1][tid] = 0;   // ordered before its gather by the sync below
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, Kp - ch * kKC);
@@ -241,8 +250,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                 const int n = task % kNT, k0 = (task / kNT) * 4;
                 double x[4];
                 if (n < ncl) {
+                    const double *sr = stage + n * Kst + (FULL ? ch * kKC : 0) + k0;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
+                    for (int i = 0; i < 4; ++i) x[i] = sr[i];
                 } else {
 #pragma unroll
                     for (int i = 0; i < 4; ++i) x[i] = 0.0;
@@ -265,7 +275,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             }
             if (needA) ++na;
             // while the tensor core works: the next chunk's data values, or the next tile's
-            if (ch + 1 < nch) {
+            if (!FULL && ch + 1 < nch) {
                 const int kn = min(kKC, Kp - (ch + 1) * kKC);
                 static_assert(kKC == 32, "a chunk is 16 or 32 entries");
                 const int sh = kn == kKC ? 2 : 1;   // kn / 8 = 1 << sh
@@ -276,8 +286,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
                     for (int i = 0; i < 8; ++i)
                         stage[n * kSt + k0 + i] = (ch + 1) * kKC + k0 + i < K ? x[i] : 0.0;
                 }
-            } else if (more) {
-                gather(ct + gstep, cb ^ 1);
+            } else if (ch + 1 == nch && more) {
+                gather(ct + gstep, cb ^ 1);   // FULL: the stage is free once the last chunk's digits are cut
             }
             // one thread polls the MMA barrier; the CTA barrier releases the rest
             const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
@@ -378,18 +388,22 @@ int build_part(DftPart &d, const std::vector<double> &T, int M, int K) {
     if (rc == AEROS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = AEROS_ERR_CUDA;
     cudaFree(Td);
     if (rc) return rc;
-    if (d.S == 7)
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)gemm_smem<7>()));
-    else
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)gemm_smem<8>()));
-    if (d.S == 7)
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftAnalP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)gemm_smem<7>()));
-    else
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftAnalP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)gemm_smem<8>()));
+    const int Kp = (K + 15) & ~15;
+    if (d.S == 7) {
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, false>(Kp)));
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, true>(Kp)));
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftAnalP, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, false>(Kp)));
+    } else {
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, false>(Kp)));
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, true>(Kp)));
+        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftAnalP, false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, false>(Kp)));
+    }
     return AEROS_OK;
 }
 
@@ -399,16 +413,29 @@ void free_part(DftPart &d) {
     d = DftPart{};
 }
 
+// Whole-contraction staging for the synthesis columns (their wind and gradient
+// combinations are formed once), where it keeps two CTAs per SM.
+template <class P> constexpr bool kWantFull = false;
+template <> constexpr bool kWantFull<DftSynthP> = true;
+constexpr size_t kTwoPerSm = 110 * 1024;
+
 template <class P>
 void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, int nsm) {
     // about 8 CTAs per SM over the grid; each loops over nct / slots column tiles
     const int nct = (ncol + kNT - 1) / kNT;
     const int slots = std::max(1, std::min(nct, (8 * nsm + d.nmt - 1) / d.nmt));
+    const int Kp = (d.K + 15) & ~15;
     dim3 grid(d.nmt, slots);
-    if (d.S == 7)
-        k_split_gemm<7, 8, P><<<grid, kThreads, gemm_smem<7>(), c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
-    else
-        k_split_gemm<8, 7, P><<<grid, kThreads, gemm_smem<8>(), c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
+    auto go = [&](auto kern, size_t smem) {
+        kern<<<grid, kThreads, smem, c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
+    };
+    if (d.S == 7) {
+        if (kWantFull<P> && gemm_smem<7, true>(Kp) <= kTwoPerSm) go(k_split_gemm<7, 8, P, kWantFull<P>>, gemm_smem<7, true>(Kp));
+        else go(k_split_gemm<7, 8, P, false>, gemm_smem<7, false>(Kp));
+    } else {
+        if (kWantFull<P> && gemm_smem<8, true>(Kp) <= kTwoPerSm) go(k_split_gemm<8, 7, P, kWantFull<P>>, gemm_smem<8, true>(Kp));
+        else go(k_split_gemm<8, 7, P, false>, gemm_smem<8, false>(Kp));
+    }
     if (c.launches) ++*c.launches;
 }
 
