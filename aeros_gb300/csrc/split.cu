@@ -126,6 +126,7 @@ struct SynSplitArgs {
     double2 *F;
     int nrow, ms, T, nh, nlat, ntl;
     int *err;
+    int smajor;   // grid (slot, m, tile) instead of (m, tile, slot)
 };
 
 // Synthesis smem: A [S][128][64] | B [S][64][64] bf16 | stage [64][65] doubles.
@@ -134,8 +135,8 @@ constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + 2 * 
 template <int S>
 constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + 2 * (size_t)kNTa * kSt * 8; }
 
-// One CTA per (m, latitude tile, group slot z): it steps through column groups
-// z, z + gridDim.z, ... (16 complex columns each) with its TMEM, barriers and
+// One CTA per (group slot z, m, latitude tile): it steps through column groups
+// z, z + (number of slots), ... (16 complex columns each) with its TMEM, barriers and
 // (for a one-chunk contraction) the table tile kept.  Software pipeline: the
 // next group's coefficients are gathered (and its column scales formed) into
 // the second stage buffer while the tensor core works on the current group.
@@ -160,13 +161,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int m = blockIdx.x, t = blockIdx.y;
+    const int slot = a.smajor ? blockIdx.x : blockIdx.z, m = a.smajor ? blockIdx.y : blockIdx.x,
+              t = a.smajor ? blockIdx.z : blockIdx.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = a.T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
     const int mo = a.moff[m];
     const int ngrp = (a.ncol + kNTs / 2 - 1) / (kNTs / 2);
-    if ((int)blockIdx.z >= ngrp) return;
-    const int gstep = gridDim.z;
+    if (slot >= ngrp) return;
+    const int gstep = a.smajor ? gridDim.x : gridDim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -251,10 +253,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         }
     };
 
-    set_meta(blockIdx.z, 0);
+    set_meta(slot, 0);
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    gather(blockIdx.z, 0);
+    gather(slot, 0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -266,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     bool ok = true;
 
     int cb = 0;   // buffer of the current group
-    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gstep, cb ^= 1) {
+    for (int grp = slot; grp < ngrp && ok; grp += gstep, cb ^= 1) {
         const int ncl = min(kNTs / 2, a.ncol - grp * (kNTs / 2));
         const bool more = grp + gstep < ngrp;
         double *stage = cb ? stage1 : stage0;
@@ -412,6 +414,7 @@ struct AnaSplitArgs {
     const double2 *F;
     int nrow, ms, T, nh, nlat, ntlA, KpA;
     int *err;
+    int smajor;   // grid (slot, m, tile) instead of (m, tile, slot)
 };
 
 // B column of (fold, slot, field cc, comp): fold 0 = north + south, 1 = north - south;
@@ -420,8 +423,8 @@ __host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
     return fold * 12 + slot * 4 + cc * 2 + comp;
 }
 
-// One CTA per (m, l tile, group slot z): it steps through column groups
-// z, z + gridDim.z, ... with its TMEM, barriers and (for a one-chunk
+// One CTA per (group slot z, m, l tile): it steps through column groups
+// z, z + (number of slots), ... with its TMEM, barriers and (for a one-chunk
 // contraction) the table tile kept.  Software pipeline: the next group's grid
 // values are gathered (and its column scales formed) into the second stage
 // buffer while the tensor core works on the current group.
@@ -443,13 +446,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int m = blockIdx.x, t = blockIdx.y;
+    const int slot = a.smajor ? blockIdx.x : blockIdx.z, m = a.smajor ? blockIdx.y : blockIdx.x,
+              t = a.smajor ? blockIdx.z : blockIdx.y;
     const int K = a.T - m + 1;
     const int ngrp = (a.ncol + kFa - 1) / kFa;
-    if (64 * t >= K || (int)blockIdx.z >= ngrp) return;
+    if (64 * t >= K || slot >= ngrp) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
-    const int gstep = gridDim.z;
+    const int gstep = a.smajor ? gridDim.x : gridDim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -529,10 +533,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         }
     };
 
-    set_meta(blockIdx.z, 0);
+    set_meta(slot, 0);
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    gather(blockIdx.z, 0);
+    gather(slot, 0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -543,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     bool ok = true;
 
     int cb = 0;   // buffer of the current group
-    for (int grp = blockIdx.z; grp < ngrp && ok; grp += gstep, cb ^= 1) {
+    for (int grp = slot; grp < ngrp && ok; grp += gstep, cb ^= 1) {
         const int ncl = min(kFa, a.ncol - grp * kFa);
         const bool more = grp + gstep < ngrp;
         double *stage = stage0 + (size_t)cb * kNTa * kSt;
@@ -773,15 +777,28 @@ void split_destroy(SplitCtx *s) {
     delete s;
 }
 
+// Group slots per (m, tile): about 8 CTAs per SM over the grid.  Where the tiles
+// alone give two CTAs per SM (long truncations, multi-chunk tables read once per group)
+// there are at least 4 slots and the slot is the fastest grid index, so the CTAs
+// sharing an (m, tile) table run together and read its chunks from L2; otherwise
+// m is the fastest index, which spreads the long and short contractions.
+static int split_slots(int ngrp, int tiles, int nsm, bool *smajor) {
+    *smajor = tiles >= 2 * nsm;
+    return std::max(1, std::min(ngrp, std::max(*smajor ? 4 : 1, (8 * nsm + tiles - 1) / tiles)));
+}
+static dim3 split_grid(int slots, int ms, int ntile, bool smajor) {
+    return smajor ? dim3(slots, ms, ntile) : dim3(ms, ntile, slots);
+}
+
 int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int nrow) {
     if (p.ncol <= 0) return AEROS_OK;
-    SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
-                   nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err};
-    // group slots per (m, latitude tile): about 8 CTAs per SM over the whole grid
     const int ngrp = (p.ncol + kNTs / 2 - 1) / (kNTs / 2);
     const int tiles = (c.T + 1) * s->ntl;
-    const int slots = std::max(1, std::min(ngrp, (8 * s->nsm + tiles - 1) / tiles));
-    dim3 grid(c.T + 1, s->ntl, slots);
+    bool smajor;
+    const int slots = split_slots(ngrp, tiles, s->nsm, &smajor);
+    SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
+                   nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err, smajor ? 1 : 0};
+    const dim3 grid = split_grid(slots, c.T + 1, s->ntl, smajor);
     if (s->S == 7) k_split_synth<7, 8><<<grid, kThreads, synth_smem<7>(), c.stream>>>(a);
     else k_split_synth<8, 7><<<grid, kThreads, synth_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;
@@ -791,14 +808,13 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
 
 int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
     if (ncol <= 0) return AEROS_OK;
-    AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
-                   c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err};
-    // group slots per (m, l tile): about 8 CTAs per SM over the whole grid; each
-    // CTA then loops over ngrp / slots column groups
     const int ngrp = (ncol + kFa - 1) / kFa;
     const int tiles = (c.T + 1) * s->ntlA;
-    const int slots = std::max(1, std::min(ngrp, (8 * s->nsm + tiles - 1) / tiles));
-    dim3 grid(c.T + 1, s->ntlA, slots);
+    bool smajor;
+    const int slots = split_slots(ngrp, tiles, s->nsm, &smajor);
+    AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
+                   c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err, smajor ? 1 : 0};
+    const dim3 grid = split_grid(slots, c.T + 1, s->ntlA, smajor);
     if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
     else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);
     if (c.launches) ++*c.launches;
