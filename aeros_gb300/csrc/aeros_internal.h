@@ -129,6 +129,10 @@ struct Ctx {
 };
 // Largest latitude count per Fourier CTA that fits `smem_per_lat` bytes in 200 KB.
 int fourier_lpb_limit(size_t smem_per_lat);
+// Raise (never lower) a kernel's dynamic shared-memory limit to `bytes`: the
+// limit is per function, shared by every handle and by step graphs captured
+// earlier with larger launches.
+int raise_smem_limit(const void *func, size_t bytes);
 
 // ---------------------------------------------------------------- kernels
 // Legendre synthesis plan: columns [0, ncolD_first) produce Pbar sums only,

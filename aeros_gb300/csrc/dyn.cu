@@ -1108,6 +1108,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
 int run_mass(Dyn &d, int mode) {
     const int n = d.g.nlon / 2;
     size_t smem = (size_t)(2 * d.g.ms + 4 * n) * sizeof(double2);
+    if (int rc = raise_smem_limit((const void *)k_mass, smem)) return rc;
     k_mass<<<dim3(d.g.nh, d.M), 128, smem, d.stream>>>(d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat,
                                                        d.g.nlon, d.tab.Ps, d.tab.moff, d.tab.plan, d.tab.tw,
                                                        d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt,

@@ -701,10 +701,8 @@ int prep_tables(SplitCtx *s, const Geometry &g, const DevTables &t, int nchS) {
     k_prep_anal_dig<S, B><<<dim3(g.T + 1, s->ntlA, (s->KpA + kKC - 1) / kKC), 256>>>(
         t.PaT, t.dPaT, t.moff, s->abase, g.T, g.nh, s->ntlA, s->KpA, s->rexpA, s->digA);
     AEROS_CUDA(cudaGetLastError());
-    AEROS_CUDA(cudaFuncSetAttribute(k_split_synth<S, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)synth_smem<S>()));
-    AEROS_CUDA(cudaFuncSetAttribute(k_split_anal<S, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)anal_smem<S>()));
+    if (int rc = raise_smem_limit((const void *)k_split_synth<S, B>, synth_smem<S>())) return rc;
+    if (int rc = raise_smem_limit((const void *)k_split_anal<S, B>, anal_smem<S>())) return rc;
     return AEROS_OK;
 }
 

@@ -389,21 +389,23 @@ int build_part(DftPart &d, const std::vector<double> &T, int M, int K) {
     cudaFree(Td);
     if (rc) return rc;
     const int Kp = (K + 15) & ~15;
+    const void *fn[3];
+    size_t sz[3];
     if (d.S == 7) {
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP, false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, false>(Kp)));
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftSynthP, true>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, true>(Kp)));
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<7, 8, DftAnalP, false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<7, false>(Kp)));
+        fn[0] = (const void *)k_split_gemm<7, 8, DftSynthP, false>;
+        fn[1] = (const void *)k_split_gemm<7, 8, DftSynthP, true>;
+        fn[2] = (const void *)k_split_gemm<7, 8, DftAnalP, false>;
+        sz[0] = sz[2] = gemm_smem<7, false>(Kp);
+        sz[1] = gemm_smem<7, true>(Kp);
     } else {
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP, false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, false>(Kp)));
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftSynthP, true>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, true>(Kp)));
-        AEROS_CUDA(cudaFuncSetAttribute(k_split_gemm<8, 7, DftAnalP, false>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem<8, false>(Kp)));
+        fn[0] = (const void *)k_split_gemm<8, 7, DftSynthP, false>;
+        fn[1] = (const void *)k_split_gemm<8, 7, DftSynthP, true>;
+        fn[2] = (const void *)k_split_gemm<8, 7, DftAnalP, false>;
+        sz[0] = sz[2] = gemm_smem<8, false>(Kp);
+        sz[1] = gemm_smem<8, true>(Kp);
     }
+    for (int i = 0; i < 3; ++i)
+        if (int e = raise_smem_limit(fn[i], sz[i])) return e;
     return AEROS_OK;
 }
 

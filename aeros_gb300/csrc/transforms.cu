@@ -1,4 +1,6 @@
 #include <algorithm>
+#include <map>
+#include <mutex>
 // transforms.cu -- FP64 spherical-harmonic transform kernels for sm_103a.
 //
 // A synthesis is two launches: the per-m Legendre contraction (spectral ->
@@ -122,6 +124,17 @@ static int fourier_lpb(int nlon) {
 
 int fourier_lpb_limit(size_t smem_per_lat) { return (int)std::max<size_t>(1, (200 * 1024) / smem_per_lat); }
 
+int raise_smem_limit(const void *func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<const void *, size_t> cur;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &c = cur[func];
+    if (bytes <= c || bytes <= 48 * 1024) return AEROS_OK;
+    AEROS_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    c = bytes;
+    return AEROS_OK;
+}
+
 int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     const size_t per_lat = (size_t)(2 * (c.nlon / 2) + c.ms) * sizeof(double2);
@@ -129,7 +142,7 @@ int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const 
     const int thr = c.tune ? c.tune->fs_thr : 256;
     size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
-    if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = raise_smem_limit((const void *)k_fourier_synth, smem)) return rc;
     k_fourier_synth<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
                                                    c.tab->tw, c.tab->twN, c.tab->sint);
     if (c.launches) ++*c.launches;
@@ -144,7 +157,7 @@ int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2
     const int thr = c.tune ? c.tune->fa_thr : 256;
     size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
-    if (smem > 48 * 1024) AEROS_CUDA(cudaFuncSetAttribute(k_fourier_anal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = raise_smem_limit((const void *)k_fourier_anal, smem)) return rc;
     k_fourier_anal<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
                                                   c.tab->tw, c.tab->twN);
     if (c.launches) ++*c.launches;

@@ -37,3 +37,16 @@ def test_group_matches_individual_handles(gpulib, precision):
             assert np.array_equal(x, y)
         assert a.counters()[0] == b.counters()[0] == 4
     assert g.launch_count() > 0
+
+
+def test_smaller_handle_created_later_keeps_larger_launches(gpulib):
+    """A kernel's shared-memory limit is per function: creating a smaller split
+    handle after a larger one must not shrink what the larger one launches with."""
+    big, _ = _make(42, 20, 1, 500, precision=1)
+    ref, _ = _make(42, 20, 1, 500, precision=1)
+    ref.step(2)
+    small, _ = _make(21, 16, 1, 600, precision=1)
+    small.step(1)
+    big.step(2)
+    for x, y in zip(big.get_state(), ref.get_state()):
+        assert np.array_equal(x, y)
