@@ -19,7 +19,8 @@
 
 namespace aeros {
 
-static std::string g_last_error;
+// one message per thread, like errno: handles on different threads do not race on it
+static thread_local std::string g_last_error;
 void set_error(const std::string &s) { g_last_error = s; }
 const char *last_error() { return g_last_error.c_str(); }
 

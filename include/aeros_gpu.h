@@ -461,7 +461,8 @@ int aeros_dyn_window_forward(aeros_dyn_t h, int nsteps, int ckpt_every, double *
  * recomputed from the checkpoints; the handle is left at the end of the window. */
 int aeros_dyn_window_backward(aeros_dyn_t h, double *now_ad, double *old_ad, double *ka_ad, double *dty_ad);
 
-/* Last CUDA error string for diagnostics (static storage). */
+/* Message of the last failed call on the calling thread (thread-local storage,
+ * valid until that thread's next failing call). */
 const char *aeros_last_error(void);
 
 #ifdef __cplusplus
