@@ -330,7 +330,9 @@ typedef struct aeros_grid_view {
 typedef int (*aeros_physics_fn)(void *user, const aeros_grid_view *view, void *stream);
 
 /* Install (fn != NULL) or remove (fn == NULL) the hook and re-capture the step
- * graphs.  `user` is passed through unchanged and must outlive the hook. */
+ * graphs.  `user` is passed through unchanged and must outlive the hook.  An
+ * ensemble group copies its members' step graphs when it is created: install
+ * hooks before grouping. */
 int aeros_dyn_set_physics(aeros_dyn_t h, aeros_physics_fn fn, void *user);
 
 /* A ready-made hook, also the template for user physics: linear relaxation
