@@ -23,9 +23,13 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--transport", action="store_true",
                     help="run `steps` tracer-transport calls (one member's grid) instead of dynamics steps")
+    ap.add_argument("--sht-batch", type=int, default=0,
+                    help="run `steps` scalar synthesis + analysis pairs of this many fields at --trunc instead")
     a = ap.parse_args(argv)
     if a.transport:
         return transport_case(a)
+    if a.sht_batch > 0:
+        return sht_case(a)
     from .params import held_suarez_params, PREC_FP64, PREC_SPLIT
     from .dynamics import AerosDyn
     from .spectral import AerosSHT
@@ -44,6 +48,28 @@ def main(argv=None):
     for _ in range(a.steps):
         ks = dyn.profile_step()
     print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
+    return 0
+
+
+def sht_case(a):
+    """Scalar transforms of seeded red-spectrum fields (Var ~ (l+1)^-3, seed 1) on
+    device arrays, in the chosen precision: `steps` synthesis + analysis pairs."""
+    import torch
+    from .spectral import AerosSHT
+    from .params import PREC_SPLIT, PREC_FP64
+    s = AerosSHT(a.trunc, batch_max=a.sht_batch)
+    s.set_precision(PREC_SPLIT if a.precision == "split" else PREC_FP64)
+    L = np.asarray(s.l_of_lm, float)
+    M = np.asarray(s.m_of_lm)
+    rng = np.random.default_rng(1)
+    c = (rng.standard_normal((a.sht_batch, s.nlm)) + 1j * rng.standard_normal((a.sht_batch, s.nlm))) * (L + 1) ** -1.5
+    c[:, M == 0] = c[:, M == 0].real
+    cd = torch.from_numpy(c).cuda()
+    for _ in range(a.steps):
+        g = s.synthesis(cd)
+        s.analysis(g)
+    torch.cuda.synchronize()
+    print(f"sht T{a.trunc} batch={a.sht_batch} pairs={a.steps} precision={a.precision}")
     return 0
 
 
