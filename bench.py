@@ -400,7 +400,9 @@ def batched_form(args, torch):
     stepped by one CUDA graph launch per step; FP64 and split precision.
     Each member handle's launch shapes are chosen by the autotuner before the
     group is built (outside the timed region).  Working set > L2, so no flush
-    is needed."""
+    is needed.  Beside it: the same members stepped one by one through the
+    single-member FP64 path (32 x the step time of one member of each
+    configuration)."""
     import numpy as np
     from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
     from aeros_gb300.dynamics import AerosDyn, AerosGroup
@@ -436,7 +438,27 @@ def batched_form(args, torch):
         out[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3,
                      "gpu_launches_per_step": (g.launch_count() - n0) / args.batched_steps}
         del g, hs
-    # the same 32 T42L20 members one by one through the single-member FP64 path
+    # the same 96 members one by one through the single-member FP64 path: one handle per
+    # configuration (autotuned), its step time x 32 members, summed over the configurations
+    seq = 0.0
+    per = {}
+    for T, L in cfg:
+        d = AerosDyn(held_suarez_params(trunc=T, nlev=L))
+        d.set_isothermal(264.0, 1.0e5)
+        d.hs_perturb(1.0)
+        if not args.no_tune:
+            d.autotune(reps=3)
+        s = torch.cuda.Stream()
+        d.set_stream(s.cuda_stream)
+        d.step_async(3)
+        d.sync()
+        t1 = time_steps(d, s, args.batched_steps, torch)
+        per[f"T{T}L{L}"] = t1 * 1e3
+        seq += 32 * t1
+        del d
+    out["one_by_one_fp64"] = {"sypd": 96 * sypd(seq), "ms_per_step": seq * 1e3, "ms_per_member_step": per}
+    for name in ("fp64", "split"):
+        out[name]["vs_one_by_one_fp64"] = out[name]["sypd"] / out["one_by_one_fp64"]["sypd"]
     return out
 
 
