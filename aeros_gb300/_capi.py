@@ -122,7 +122,8 @@ _PROTOS = {
     "aeros_dyn_window_forward": [_vp, _i, _i, _vp],
     "aeros_dyn_window_backward": [_vp, _vp, _vp, _vp, _vp],
     "aeros_dyn_autotune": [_vp, _i, _dp, _dp],
-    "aeros_dyn_tune_get": [_vp, _vp],
+    "aeros_dyn_tune_get": [_vp, _vp, _i],
+    "aeros_dyn_tune_set": [_vp, _vp, _i],
     "aeros_transport_create": [ctypes.POINTER(_vp), _i, _i, _vp, _vp],
     "aeros_transport_destroy": [_vp],
     "aeros_transport_set_stream": [_vp, _vp],

@@ -117,6 +117,7 @@ struct Tune {
     int col_thr = 64;               // column kernel threads per CTA
     int col_lanes = 1;              // column kernel lanes per column: 1, 2, 4, 8 or 16
     int spec_warps = 4;             // spectral kernel warps per CTA
+    int spec_cols = 0;              // spectral kernel layout: 0 a warp per coefficient, 1 a thread per real column
 };
 
 // Launch context for the transform kernels.

@@ -255,7 +255,7 @@ struct SpecArgs {
     const double *MinvT;                      // [l][j][k]
     const double *dfac;                       // (T+1) diffusion factor for this h
     const int *l_of_lm;
-    int nlm, NL, M;
+    int nlm, NL, M, T;
     double h, a1, astep, hh_old;
     double half_nu, raw_alpha, raw_beta;
     int semi_implicit, raw_on;
@@ -380,6 +380,183 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
         a.lnps_o[op] = pnow;
         a.lnps[op] = pnew;
     }
+}
+
+// The same update in the column layout: a thread per real column (member e,
+// coefficient lm, real or imaginary part) with all NLT levels in registers;
+// warps are grouped by degree l (wtab[w] = (l, first column of the warp among
+// the 2 M (l + 1) columns of degree l)), so the inverse of degree l is read at
+// one address per warp.  Every lane does useful FP64 work -- the warp per
+// coefficient leaves 32 - nlev lanes idle -- at the price of serial level
+// products per thread, which pays once an ensemble has enough columns to fill
+// the SMs.  The arithmetic and its order are those of k_spectral: the level
+// products run j = 0 .. nlev-1 from zero, the nu . e sum is the warp
+// butterfly's tree.
+template <int NLT>
+__global__ void __launch_bounds__(256) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
+    __shared__ double sG[NLT * NLT], sT[NLT * NLT], sW[NLT * NLT];
+    __shared__ double sNu[NLT], sPc[NLT];
+    for (int i = threadIdx.x; i < NLT * NLT; i += blockDim.x) {
+        sG[i] = a.GT[i];
+        sT[i] = a.TT[i];
+        sW[i] = a.WT[i];
+    }
+    for (int i = threadIdx.x; i < NLT; i += blockDim.x) {
+        sNu[i] = a.nu[i];
+        sPc[i] = a.pcoef[i];
+    }
+    __syncthreads();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= nwarp) return;
+    const int2 wl = wtab[warp];
+    const int l = wl.x, idx = wl.y + (threadIdx.x & 31);
+    if (idx >= 2 * a.M * (l + 1)) return;
+    const int comp = idx & 1, r = idx >> 1, e = r / (l + 1), m = r - e * (l + 1);
+    const int lm = m * (2 * a.T + 1 - m) / 2 + l;
+    const size_t ls = (size_t)2 * a.nlm;                              // level stride (doubles)
+    const size_t o0 = ((size_t)e * NLT * a.nlm + lm) * 2 + comp;      // level 0 of this column
+    const size_t op = ((size_t)e * a.nlm + lm) * 2 + comp;
+    double *vor = reinterpret_cast<double *>(a.vor), *vor_o = reinterpret_cast<double *>(a.vor_o);
+    double *dv = reinterpret_cast<double *>(a.div), *dv_o = reinterpret_cast<double *>(a.div_o);
+    double *tm = reinterpret_cast<double *>(a.tmp), *tm_o = reinterpret_cast<double *>(a.tmp_o);
+    const double *tv = reinterpret_cast<const double *>(a.tv), *td = reinterpret_cast<const double *>(a.td);
+    const double *tt = reinterpret_cast<const double *>(a.tt);
+    const double h = a.h, fd = a.dfac[l];
+    const bool raw = a.raw_on;
+    auto filt = [&](double xo, double &xn, double &xw) {
+        double dx = a.half_nu * (xo - 2.0 * xn + xw);
+        xn += a.raw_alpha * dx;
+        xw -= a.raw_beta * dx;
+    };
+    bool bad = false;
+    // vorticity: leapfrog, diffusion, RAW
+#pragma unroll
+    for (int k = 0; k < NLT; ++k) {
+        const size_t o = o0 + k * ls;
+        const double vo = vor_o[o];
+        double vn = vor[o], vw = vo + h * tv[o];
+        vw = vw * fd;
+        if (raw) filt(vo, vn, vw);
+        bad |= !isfinite(vw);
+        vor_o[o] = vn;
+        vor[o] = vw;
+    }
+    const double pold = reinterpret_cast<const double *>(a.lnps_o)[op];
+    double pnow = reinterpret_cast<const double *>(a.lnps)[op];
+    const double rp = reinterpret_cast<const double *>(a.tp)[op];
+    double pnew;
+    if (a.semi_implicit) {
+        const double lam = (double)l * (l + 1) / (kA * kA);
+        const double pz = pold - pnow + a.astep * rp;
+        const double ha = h * a.astep, hl = h * lam;
+        double y[NLT], g[NLT];
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            const size_t o = o0 + k * ls;
+            y[k] = tm_o[o] - tm[o] + a.astep * tt[o];
+        }
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < NLT; ++j) s += sG[j * NLT + k] * y[j];
+            g[k] = s;
+        }
+        double *x = y;   // y is dead from here
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            const size_t o = o0 + k * ls;
+            x[k] = ha * dv[o] - a.hh_old * dv_o[o];
+        }
+        // g becomes the right-hand side
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            double wx = 0.0;
+#pragma unroll
+            for (int j = 0; j < NLT; ++j) wx += sW[j * NLT + k] * x[j];
+            const size_t o = o0 + k * ls;
+            const double pc = sPc[k];
+            g[k] = dv_o[o] + h * td[o] + hl * (g[k] + pc * pz) + lam * wx;
+        }
+        const double *Mi = a.MinvT + (size_t)l * NLT * NLT;
+        double dn[NLT];
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < NLT; ++j) s += Mi[j * NLT + k] * g[j];
+            dn[k] = s;
+        }
+        double *ed = g;   // the right-hand side is dead from here
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            const size_t o = o0 + k * ls;
+            const double dold = dv_o[o];
+            double dnow = dv[o];
+            const double db = a.a1 * dn[k] + (1.0 - a.a1) * dold;
+            ed[k] = db - dnow;
+            double dw = dn[k] * fd;
+            if (raw) filt(dold, dnow, dw);
+            bad |= !isfinite(dw);
+            dv_o[o] = dnow;
+            dv[o] = dw;
+        }
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            double te = 0.0;
+#pragma unroll
+            for (int j = 0; j < NLT; ++j) te += sT[j * NLT + k] * ed[j];
+            const size_t o = o0 + k * ls;
+            const double told = tm_o[o];
+            double tnow = tm[o], tw = told + h * (tt[o] - te);
+            tw = tw * fd;
+            if (raw) filt(told, tnow, tw);
+            bad |= !isfinite(tw);
+            tm_o[o] = tnow;
+            tm[o] = tw;
+        }
+        double sum[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) sum[i] = i < NLT ? __dmul_rn(sNu[i], ed[i]) : 0.0;
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1)
+#pragma unroll
+            for (int i = 0; i < w; ++i) sum[i] = sum[i] + sum[i + w];
+        pnew = pold + h * (rp - sum[0]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) {
+            const size_t o = o0 + k * ls;
+            const double dold = dv_o[o], told = tm_o[o];
+            double dnow = dv[o], tnow = tm[o];
+            double dw = dold + h * td[o], tw = told + h * tt[o];
+            dw = dw * fd;
+            tw = tw * fd;
+            if (raw) {
+                filt(dold, dnow, dw);
+                filt(told, tnow, tw);
+            }
+            bad |= !(isfinite(dw) && isfinite(tw));
+            dv_o[o] = dnow;
+            dv[o] = dw;
+            tm_o[o] = tnow;
+            tm[o] = tw;
+        }
+        pnew = pold + h * rp;
+    }
+    if (raw) filt(pold, pnow, pnew);
+    bad |= !isfinite(pnew);
+    if (bad) atomicOr(a.flag, 1);
+    reinterpret_cast<double *>(a.lnps_o)[op] = pnow;
+    reinterpret_cast<double *>(a.lnps)[op] = pnew;
+}
+
+// Level counts with a column-layout instantiation.
+constexpr int kSpecColLevels[] = {16, 20};
+bool spec_cols_available(int nlev) {
+    for (int n : kSpecColLevels)
+        if (n == nlev) return true;
+    return false;
 }
 
 // The ready-made physics hook: linear relaxation of the winds and temperature
@@ -696,6 +873,8 @@ struct aeros_dyn_s {
     double *GT_d = nullptr, *TT_d = nullptr, *WT_d = nullptr, *nu_d = nullptr, *pc_d = nullptr;
     double *Minv_d[2] = {nullptr, nullptr};                    // h = dt, 2 dt
     double *dfac_d[2] = {nullptr, nullptr};
+    int2 *spec_wt = nullptr;                                   // column-layout spectral warps: (l, first column)
+    int spec_nw = 0;
     double *xlat_d = nullptr, *phis_d = nullptr;
     bool phis_set = false;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
@@ -1020,6 +1199,12 @@ int build_step_tables(Dyn &d) {
     if ((rc = dput(d.GT_d, GT)) || (rc = dput(d.TT_d, TT)) || (rc = dput(d.WT_d, WT)) || (rc = dput(d.nu_d, d.nu)) ||
         (rc = dput(d.pc_d, d.pcoef)))
         return rc;
+    // warps of the column-layout spectral kernel: the 2 M (l + 1) real columns of degree l, 32 per warp
+    std::vector<int2> wt;
+    for (int l = 0; l <= T; ++l)
+        for (int c = 0; c < 2 * d.M * (l + 1); c += 32) wt.push_back(make_int2(l, c));
+    d.spec_nw = (int)wt.size();
+    if ((rc = dput(d.spec_wt, wt))) return rc;
     return AEROS_OK;
 }
 
@@ -1139,7 +1324,7 @@ int enqueue_step(Dyn &d, bool startup) {
     a.MinvT = d.Minv_d[s];
     a.dfac = d.dfac_d[s];
     a.l_of_lm = d.tab.l_of_lm;
-    a.nlm = d.g.nlm; a.NL = d.NL; a.M = d.M;
+    a.nlm = d.g.nlm; a.NL = d.NL; a.M = d.M; a.T = d.g.T;
     a.h = d.par.dt * (startup ? 1.0 : 2.0);
     a.a1 = d.par.si_alpha;
     a.astep = a.a1 * a.h;
@@ -1150,9 +1335,15 @@ int enqueue_step(Dyn &d, bool startup) {
     a.semi_implicit = d.par.semi_implicit;
     a.raw_on = (!startup && d.par.eps_filter > 0.0) ? 1 : 0;
     a.flag = d.flag;
-    long nw = (long)d.g.nlm * d.M;
     const int sw = d.tune.spec_warps;
-    k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
+    if (d.tune.spec_cols && spec_cols_available(d.NL)) {
+        const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
+        if (d.NL == 16) k_spectral_cols<16><<<nb, 32 * sw, 0, d.stream>>>(a, d.spec_wt, d.spec_nw);
+        else k_spectral_cols<20><<<nb, 32 * sw, 0, d.stream>>>(a, d.spec_wt, d.spec_nw);
+    } else {
+        long nw = (long)d.g.nlm * d.M;
+        k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
+    }
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "spectral");
@@ -1242,7 +1433,7 @@ void destroy(Dyn *d) {
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
                   d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
-                  d->dconst};
+                  d->dconst, d->spec_wt};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->split) split_destroy(d->split);

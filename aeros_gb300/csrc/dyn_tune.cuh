@@ -2,8 +2,8 @@
 //
 // The shapes that matter differ with truncation, level count and ensemble
 // size: latitudes and threads per CTA of the longitude FFTs, output columns
-// per CTA of the FP64 Legendre analysis, and the CTA sizes of the column and
-// spectral kernels.  aeros_dyn_autotune times whole steps (direct launches,
+// per CTA of the FP64 Legendre analysis, the CTA sizes of the column and
+// spectral kernels and the spectral kernel's layout.  aeros_dyn_autotune times whole steps (direct launches,
 // CUDA events on the handle's stream) for each candidate of one shape at a
 // time, keeps the fastest (coordinate descent, two sweeps), restores the
 // state and re-captures the step graphs.  With AEROS_TUNE_CACHE naming a file,
@@ -11,6 +11,7 @@
 // handle with a matching key starts from them without timing.
 #include <cstdio>
 #include <fstream>
+#include <initializer_list>
 #include <sstream>
 #include <string>
 
@@ -58,7 +59,7 @@ bool tune_load(Dyn &d) {
         std::string k;
         Tune t;
         if (!(in >> k >> t.fs_lpb >> t.fs_thr >> t.fa_lpb >> t.fa_thr >> t.la_ct >> t.col_thr >> t.spec_warps >>
-              t.col_lanes >> t.ls_jt))
+              t.col_lanes >> t.ls_jt >> t.spec_cols))
             continue;
         if (k != key) continue;
         d.tune = t;
@@ -73,7 +74,8 @@ void tune_store(Dyn &d) {
     std::ofstream f(path, std::ios::app);
     const Tune &t = d.tune;
     f << tune_key(d) << " " << t.fs_lpb << " " << t.fs_thr << " " << t.fa_lpb << " " << t.fa_thr << " " << t.la_ct
-      << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << " " << t.ls_jt << "\n";
+      << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << " " << t.ls_jt << " " << t.spec_cols
+      << "\n";
 }
 
 int recapture(Dyn &d) {
@@ -147,8 +149,14 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
                     t.col_lanes = lp;
                     trial(t);
                 }
-        for (int sw : {1, 2, 4, 8})
-            if (sw != d.tune.spec_warps) { Tune t = d.tune; t.spec_warps = sw; trial(t); }
+        for (int sc : {0, 1})
+            for (int sw : {1, 2, 4, 8}) {
+                if ((sc && !spec_cols_available(d.NL)) || (sc == d.tune.spec_cols && sw == d.tune.spec_warps)) continue;
+                Tune t = d.tune;
+                t.spec_cols = sc;
+                t.spec_warps = sw;
+                trial(t);
+            }
     }
     // restore
     AEROS_CUDA(cudaMemcpyAsync(d.old, sv, nst * sizeof(double2), cudaMemcpyDeviceToDevice, d.stream));
@@ -167,13 +175,44 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
     return AEROS_OK;
 }
 
-// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes, ls_jt.
-int aeros_dyn_tune_get(aeros_dyn_t h, int *shape9) {
-    if (!h || !shape9) return AEROS_ERR_ARG;
+// The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes, ls_jt,
+// spec_cols; the first n of them (n <= 10).
+int aeros_dyn_tune_get(aeros_dyn_t h, int *shape, int n) {
+    if (!h || !shape || n < 0 || n > 10) return AEROS_ERR_ARG;
     const Tune &t = h->tune;
-    const int v[9] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr, t.spec_warps, t.col_lanes, t.ls_jt};
-    std::memcpy(shape9, v, sizeof(v));
+    const int v[10] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct,
+                       t.col_thr, t.spec_warps, t.col_lanes, t.ls_jt, t.spec_cols};
+    std::memcpy(shape, v, sizeof(int) * n);
     return AEROS_OK;
+}
+
+// Set the launch shapes explicitly (same order as aeros_dyn_tune_get, all 10);
+// each must be one the autotuner would try.  Re-captures the step graphs.
+int aeros_dyn_tune_set(aeros_dyn_t h, const int *shape, int n) {
+    if (!h || !shape || n != 10) return AEROS_ERR_ARG;
+    Dyn &d = *h;
+    auto in = [](int v, std::initializer_list<int> ok) {
+        for (int x : ok)
+            if (v == x) return true;
+        return false;
+    };
+    const size_t fs_lat = (size_t)(2 * (d.g.nlon / 2) + d.g.ms) * sizeof(double2);
+    const size_t fa_lat = (size_t)2 * (d.g.nlon / 2) * sizeof(double2);
+    Tune t;
+    t.fs_lpb = shape[0]; t.fs_thr = shape[1]; t.fa_lpb = shape[2]; t.fa_thr = shape[3]; t.la_ct = shape[4];
+    t.col_thr = shape[5]; t.spec_warps = shape[6]; t.col_lanes = shape[7]; t.ls_jt = shape[8]; t.spec_cols = shape[9];
+    const bool good = (t.fs_lpb == 0 || (in(t.fs_lpb, {1, 2, 4, 8, 16}) && t.fs_lpb <= fourier_lpb_limit(fs_lat))) &&
+                      (t.fa_lpb == 0 || (in(t.fa_lpb, {1, 2, 4, 8, 16}) && t.fa_lpb <= fourier_lpb_limit(fa_lat))) &&
+                      in(t.fs_thr, {64, 128, 256, 512}) && in(t.fa_thr, {64, 128, 256, 512}) &&
+                      in(t.la_ct, {4, 8, 16}) && in(t.col_thr, {32, 64, 128, 256}) &&
+                      in(t.spec_warps, {1, 2, 4, 8}) && in(t.col_lanes, {1, 2, 4, 8, 16}) &&
+                      in(t.ls_jt, {8, 16, 32}) && (t.spec_cols == 0 || (t.spec_cols == 1 && spec_cols_available(d.NL)));
+    if (!good) {
+        set_error("aeros_dyn_tune_set: a launch shape outside the autotuner's candidates");
+        return AEROS_ERR_ARG;
+    }
+    d.tune = t;
+    return recapture(d);
 }
 
 }  // extern "C"

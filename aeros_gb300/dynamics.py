@@ -272,7 +272,8 @@ class AerosDyn:
         return c.value
 
     # ------------------------------------------------------------------ autotuner
-    TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps", "col_lanes", "ls_jt")
+    TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps", "col_lanes", "ls_jt",
+                 "spec_cols")
 
     def autotune(self, reps=3):
         """Choose launch shapes by timing whole steps; returns (ms before, ms after, shapes)."""
@@ -283,8 +284,19 @@ class AerosDyn:
 
     def tune_shapes(self):
         v = np.zeros(len(self.TUNE_KEYS), np.int32)
-        _capi.check(_capi.lib().aeros_dyn_tune_get(self._h, _ptr(v)), "aeros_dyn_tune_get")
+        _capi.check(_capi.lib().aeros_dyn_tune_get(self._h, _ptr(v), len(v)), "aeros_dyn_tune_get")
         return dict(zip(self.TUNE_KEYS, (int(x) for x in v)))
+
+    def set_tune_shapes(self, **shapes):
+        """Set launch shapes by name (the others keep their values); each must
+        be one the autotuner would try.  Re-captures the step graphs."""
+        cur = self.tune_shapes()
+        unknown = set(shapes) - set(cur)
+        if unknown:
+            raise KeyError(f"unknown launch shapes {sorted(unknown)}")
+        cur.update(shapes)
+        v = np.array([cur[k] for k in self.TUNE_KEYS], np.int32)
+        _capi.check(_capi.lib().aeros_dyn_tune_set(self._h, _ptr(v), len(v)), "aeros_dyn_tune_set")
 
     # ------------------------------------------------------------------ adjoint
     # Packed state: vor (M, nlev, nlm) | div | temp | lnps (M, nlm), complex128.

@@ -42,3 +42,40 @@ def test_autotune_results_unchanged(gpulib, tmp_path, monkeypatch, prec):
         assert np.array_equal(a, b)
     fresh = AerosDyn(p)
     assert fresh.tune_shapes() == shapes
+
+
+@pytest.mark.parametrize("nlev,prec,si", [(20, 0, 1), (16, 1, 1), (20, 0, 0)])
+def test_spectral_column_layout_same_results(gpulib, nlev, prec, si):
+    """The thread-per-column spectral kernel computes every update with the
+    arithmetic, in the order, of the warp-per-coefficient kernel."""
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    p = held_suarez_params(trunc=31, nlev=nlev, nmember=3, precision=prec, semi_implicit=si)
+    ref, cols = AerosDyn(p), AerosDyn(p)
+    st = _state(ref)
+    ref.set_state(*st)
+    cols.set_state(*st)
+    cols.set_tune_shapes(spec_cols=1, spec_warps=2)
+    assert cols.tune_shapes()["spec_cols"] == 1 and ref.tune_shapes()["spec_cols"] == 0
+    ref.step(6)
+    cols.step(6)
+    for a, b in zip(ref.get_state(), cols.get_state()):
+        rel = np.max(np.abs(a - b)) / np.max(np.abs(a))
+        assert np.array_equal(a, b), f"largest relative difference {rel:.3e}"
+
+
+def test_tune_set_rejects_shapes_outside_the_candidates(gpulib):
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from aeros_gb300._capi import AerosError
+    d = AerosDyn(held_suarez_params(trunc=21, nlev=12))
+    before = d.tune_shapes()
+    with pytest.raises(AerosError):
+        d.set_tune_shapes(spec_cols=1)      # no column-layout kernel for 12 levels
+    with pytest.raises(AerosError):
+        d.set_tune_shapes(spec_warps=3)
+    with pytest.raises(KeyError):
+        d.set_tune_shapes(warps=2)
+    assert d.tune_shapes() == before
+    d.set_tune_shapes(col_thr=128, col_lanes=4)
+    assert d.tune_shapes()["col_lanes"] == 4
