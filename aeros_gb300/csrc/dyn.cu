@@ -383,30 +383,38 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
 }
 
 // The same update in the column layout: a thread per real column (member e,
-// coefficient lm, real or imaginary part) with all NLT levels in registers;
-// warps are grouped by degree l (wtab[w] = (l, first column of the warp among
-// the 2 M (l + 1) columns of degree l)), so the inverse of degree l is read at
-// one address per warp.  Every lane does useful FP64 work -- the warp per
-// coefficient leaves 32 - nlev lanes idle -- at the price of serial level
-// products per thread, which pays once an ensemble has enough columns to fill
-// the SMs.  The arithmetic and its order are those of k_spectral: the level
-// products run j = 0 .. nlev-1 from zero, the nu . e sum is the warp
-// butterfly's tree.
+// coefficient lm, real or imaginary part); warps are grouped by degree l
+// (wtab[w] = (l, first column of the warp among the 2 M (l + 1) columns of
+// degree l)), so the inverse of degree l is read at one address per warp.
+// Every lane does useful FP64 work -- the warp per coefficient leaves
+// 32 - nlev lanes idle -- at the price of serial level products per thread,
+// which pays once an ensemble has enough columns to fill the SMs.  The
+// thread's level vectors live in shared memory ([level][thread], two slots),
+// the products' NLT accumulators in registers, so 16 warps fit on an SM.  The
+// arithmetic and its order are those of k_spectral: every level product runs
+// j = 0 .. nlev-1 from zero, the nu . e sum is the warp butterfly's tree.
 template <int NLT>
-__global__ void __launch_bounds__(256) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
-    __shared__ double sG[NLT * NLT], sT[NLT * NLT], sW[NLT * NLT];
-    __shared__ double sNu[NLT], sPc[NLT];
-    for (int i = threadIdx.x; i < NLT * NLT; i += blockDim.x) {
+__host__ __device__ constexpr size_t spec_cols_smem(int threads) {
+    return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads);
+}
+
+template <int NLT>
+__global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
+    extern __shared__ double sm_cols[];
+    double *sG = sm_cols, *sT = sG + NLT * NLT, *sW = sT + NLT * NLT, *sNu = sW + NLT * NLT, *sPc = sNu + NLT;
+    double *v1 = sPc + NLT + threadIdx.x, *v2 = v1 + NLT * blockDim.x;   // slot k at [k * blockDim.x]
+    const int nt = blockDim.x;
+    for (int i = threadIdx.x; i < NLT * NLT; i += nt) {
         sG[i] = a.GT[i];
         sT[i] = a.TT[i];
         sW[i] = a.WT[i];
     }
-    for (int i = threadIdx.x; i < NLT; i += blockDim.x) {
+    for (int i = threadIdx.x; i < NLT; i += nt) {
         sNu[i] = a.nu[i];
         sPc[i] = a.pcoef[i];
     }
     __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warp = (blockIdx.x * nt + threadIdx.x) >> 5;
     if (warp >= nwarp) return;
     const int2 wl = wtab[warp];
     const int l = wl.x, idx = wl.y + (threadIdx.x & 31);
@@ -428,9 +436,20 @@ __global__ void __launch_bounds__(256) k_spectral_cols(SpecArgs a, const int2 *_
         xn += a.raw_alpha * dx;
         xw -= a.raw_beta * dx;
     };
+    // acc[k] = sum_j P[k][j] v[j], j ascending; P[k][j] at P[j * NLT + k]
+    auto product = [&](const double *P, const double *v, double *acc) {
+#pragma unroll
+        for (int k = 0; k < NLT; ++k) acc[k] = 0.0;
+#pragma unroll
+        for (int j = 0; j < NLT; ++j) {
+            const double vj = v[j * nt];
+#pragma unroll
+            for (int k = 0; k < NLT; ++k) acc[k] += P[j * NLT + k] * vj;
+        }
+    };
     bool bad = false;
     // vorticity: leapfrog, diffusion, RAW
-#pragma unroll
+#pragma unroll 4
     for (int k = 0; k < NLT; ++k) {
         const size_t o = o0 + k * ls;
         const double vo = vor_o[o];
@@ -449,66 +468,47 @@ __global__ void __launch_bounds__(256) k_spectral_cols(SpecArgs a, const int2 *_
         const double lam = (double)l * (l + 1) / (kA * kA);
         const double pz = pold - pnow + a.astep * rp;
         const double ha = h * a.astep, hl = h * lam;
-        double y[NLT], g[NLT];
-#pragma unroll
-        for (int k = 0; k < NLT; ++k) {
+        double acc[NLT];
+#pragma unroll 4
+        for (int k = 0; k < NLT; ++k) {   // v1 = y
             const size_t o = o0 + k * ls;
-            y[k] = tm_o[o] - tm[o] + a.astep * tt[o];
+            v1[k * nt] = tm_o[o] - tm[o] + a.astep * tt[o];
         }
+        product(sG, v1, acc);             // G y
 #pragma unroll
-        for (int k = 0; k < NLT; ++k) {
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < NLT; ++j) s += sG[j * NLT + k] * y[j];
-            g[k] = s;
-        }
-        double *x = y;   // y is dead from here
-#pragma unroll
-        for (int k = 0; k < NLT; ++k) {
+        for (int k = 0; k < NLT; ++k) v2[k * nt] = acc[k];
+#pragma unroll 4
+        for (int k = 0; k < NLT; ++k) {   // v1 = x
             const size_t o = o0 + k * ls;
-            x[k] = ha * dv[o] - a.hh_old * dv_o[o];
+            v1[k * nt] = ha * dv[o] - a.hh_old * dv_o[o];
         }
-        // g becomes the right-hand side
+        product(sW, v1, acc);             // W x; v2 becomes the right-hand side
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
-            double wx = 0.0;
-#pragma unroll
-            for (int j = 0; j < NLT; ++j) wx += sW[j * NLT + k] * x[j];
             const size_t o = o0 + k * ls;
             const double pc = sPc[k];
-            g[k] = dv_o[o] + h * td[o] + hl * (g[k] + pc * pz) + lam * wx;
+            v2[k * nt] = dv_o[o] + h * td[o] + hl * (v2[k * nt] + pc * pz) + lam * acc[k];
         }
-        const double *Mi = a.MinvT + (size_t)l * NLT * NLT;
-        double dn[NLT];
+        product(a.MinvT + (size_t)l * NLT * NLT, v2, acc);   // D^(n+1)
 #pragma unroll
-        for (int k = 0; k < NLT; ++k) {
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < NLT; ++j) s += Mi[j * NLT + k] * g[j];
-            dn[k] = s;
-        }
-        double *ed = g;   // the right-hand side is dead from here
-#pragma unroll
-        for (int k = 0; k < NLT; ++k) {
+        for (int k = 0; k < NLT; ++k) {   // v1 = e = D-bar - D^n
             const size_t o = o0 + k * ls;
             const double dold = dv_o[o];
             double dnow = dv[o];
-            const double db = a.a1 * dn[k] + (1.0 - a.a1) * dold;
-            ed[k] = db - dnow;
-            double dw = dn[k] * fd;
+            const double db = a.a1 * acc[k] + (1.0 - a.a1) * dold;
+            v1[k * nt] = db - dnow;
+            double dw = acc[k] * fd;
             if (raw) filt(dold, dnow, dw);
             bad |= !isfinite(dw);
             dv_o[o] = dnow;
             dv[o] = dw;
         }
+        product(sT, v1, acc);             // tau e
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
-            double te = 0.0;
-#pragma unroll
-            for (int j = 0; j < NLT; ++j) te += sT[j * NLT + k] * ed[j];
             const size_t o = o0 + k * ls;
             const double told = tm_o[o];
-            double tnow = tm[o], tw = told + h * (tt[o] - te);
+            double tnow = tm[o], tw = told + h * (tt[o] - acc[k]);
             tw = tw * fd;
             if (raw) filt(told, tnow, tw);
             bad |= !isfinite(tw);
@@ -517,14 +517,14 @@ __global__ void __launch_bounds__(256) k_spectral_cols(SpecArgs a, const int2 *_
         }
         double sum[32];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) sum[i] = i < NLT ? __dmul_rn(sNu[i], ed[i]) : 0.0;
+        for (int i = 0; i < 32; ++i) sum[i] = i < NLT ? __dmul_rn(sNu[i], v1[i * nt]) : 0.0;
 #pragma unroll
         for (int w = 16; w > 0; w >>= 1)
 #pragma unroll
             for (int i = 0; i < w; ++i) sum[i] = sum[i] + sum[i + w];
         pnew = pold + h * (rp - sum[0]);
     } else {
-#pragma unroll
+#pragma unroll 4
         for (int k = 0; k < NLT; ++k) {
             const size_t o = o0 + k * ls;
             const double dold = dv_o[o], told = tm_o[o];
@@ -1205,6 +1205,9 @@ int build_step_tables(Dyn &d) {
         for (int c = 0; c < 2 * d.M * (l + 1); c += 32) wt.push_back(make_int2(l, c));
     d.spec_nw = (int)wt.size();
     if ((rc = dput(d.spec_wt, wt))) return rc;
+    if (d.NL == 16) rc = raise_smem_limit((const void *)k_spectral_cols<16>, spec_cols_smem<16>(256));
+    if (d.NL == 20) rc = raise_smem_limit((const void *)k_spectral_cols<20>, spec_cols_smem<20>(256));
+    if (rc) return rc;
     return AEROS_OK;
 }
 
@@ -1338,8 +1341,10 @@ int enqueue_step(Dyn &d, bool startup) {
     const int sw = d.tune.spec_warps;
     if (d.tune.spec_cols && spec_cols_available(d.NL)) {
         const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
-        if (d.NL == 16) k_spectral_cols<16><<<nb, 32 * sw, 0, d.stream>>>(a, d.spec_wt, d.spec_nw);
-        else k_spectral_cols<20><<<nb, 32 * sw, 0, d.stream>>>(a, d.spec_wt, d.spec_nw);
+        if (d.NL == 16)
+            k_spectral_cols<16><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        else
+            k_spectral_cols<20><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
     } else {
         long nw = (long)d.g.nlm * d.M;
         k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
@@ -1517,6 +1522,11 @@ int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_ha
         int rows = (int)(M * std::max(8 * NL + 2, 4 * NL + 1));
         if ((rc = split_create(d->g, d->tab, rows, &d->split))) { destroy(d); return rc; }
         if ((rc = split_dft_create(d->g, &d->dft))) { destroy(d); return rc; }
+    }
+    // spectral kernel: the column layout once there are ~16k real columns (measured crossover on GB300)
+    if (spec_cols_available(NL) && 2LL * M * d->g.nlm >= 16384) {
+        d->tune.spec_cols = 1;
+        d->tune.spec_warps = 2;
     }
     tune_load(*d);   // launch shapes of an earlier aeros_dyn_autotune (AEROS_TUNE_CACHE)
     if ((rc = capture_graphs(*d))) { destroy(d); return rc; }

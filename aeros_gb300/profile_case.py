@@ -1,6 +1,7 @@
 """A fixed step workload for profiling one kernel under ncu.
 
   python -m aeros_gb300.profile_case --trunc 42 --nlev 20 --members 16 --steps 3 [--precision fp64|split]
+                                    [--shapes spec_cols=1,spec_warps=2]
 
 Builds an ensemble of Held-Suarez members (rest + 0.1 K noise, one seed per
 member) and runs `steps` steps with direct launches (no graph), so that an
@@ -23,6 +24,8 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--transport", action="store_true",
                     help="run `steps` tracer-transport calls (one member's grid) instead of dynamics steps")
+    ap.add_argument("--shapes", default="",
+                    help="launch shapes to set before stepping, e.g. spec_cols=1,spec_warps=2 (AerosDyn.TUNE_KEYS)")
     ap.add_argument("--sht-batch", type=int, default=0,
                     help="run `steps` scalar synthesis + analysis pairs of this many fields at --trunc instead")
     a = ap.parse_args(argv)
@@ -36,6 +39,8 @@ def main(argv=None):
     p = held_suarez_params(trunc=a.trunc, nlev=a.nlev, nmember=a.members,
                            precision=PREC_SPLIT if a.precision == "split" else PREC_FP64)
     dyn = AerosDyn(p)
+    if a.shapes:
+        dyn.set_tune_shapes(**{k: int(v) for k, v in (kv.split("=") for kv in a.shapes.split(","))})
     sht = AerosSHT(a.trunc, batch_max=a.nlev)
     dyn.set_isothermal(264.0, 1.0e5)
     vor, div, t, lnps = dyn.get_state(squeeze=False)
