@@ -886,6 +886,7 @@ struct aeros_dyn_s {
     double *bud_rows = nullptr, *bud_res = nullptr, *zm = nullptr;
     int nsample = 0;
     int *flag = nullptr;
+    int *hflag = nullptr;                            // pinned host copies of the error words (3)
     double c00 = 0;
     int nrowS = 0, nrowA = 0;
     SynPlan synS, synD;
@@ -1441,6 +1442,7 @@ void destroy(Dyn *d) {
                   d->dconst, d->spec_wt};
     for (void *p : ps)
         if (p) cudaFree(p);
+    if (d->hflag) cudaFreeHost(d->hflag);
     if (d->split) split_destroy(d->split);
     if (d->dft) split_dft_destroy(d->dft);
     if (d->adj) adj_release(d->adj);
@@ -1487,6 +1489,7 @@ int aeros_dyn_create(aeros_dyn_t *out, const aeros_params *p, const double *a_ha
     if ((rc = upload_tables(d->g, d->tab))) { destroy(d); return rc; }
     if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess) { destroy(d); return AEROS_ERR_CUDA; }
     d->own_stream = true;
+    if (cudaMallocHost(&d->hflag, 3 * sizeof(int)) != cudaSuccess) { destroy(d); return AEROS_ERR_CUDA; }
     const size_t ng = (size_t)d->g.nlon * d->g.nlat, M = d->M, NL = d->NL;
     const size_t nst = d->nstate();
     if ((rc = dalloc(d->now, nst)) || (rc = dalloc(d->old, nst)) || (rc = dalloc(d->tnd, nst)) ||
@@ -1677,15 +1680,20 @@ int aeros_dyn_step_async(aeros_dyn_t h, int nsteps) {
 
 int aeros_dyn_sync(aeros_dyn_t h) {
     if (!h) return AEROS_ERR_ARG;
-    int flag = 0;
-    AEROS_CUDA(cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    // the error words, copied into pinned memory behind the stream's work: one synchronisation
+    int *hf = h->hflag;
+    hf[0] = hf[1] = hf[2] = 0;
+    const int *w1 = split_err_word(h->split), *w2 = split_dft_err_word(h->dft);
+    AEROS_CUDA(cudaMemcpyAsync(hf, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (w1) AEROS_CUDA(cudaMemcpyAsync(hf + 1, w1, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (w2) AEROS_CUDA(cudaMemcpyAsync(hf + 2, w2, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     AEROS_CUDA(cudaStreamSynchronize(h->stream));
-    if (flag) {
+    if (hf[0]) {
         set_error("non-finite value in the spectral state");
         return AEROS_ERR_NONFINITE;
     }
-    int rc = split_check(h->split);
-    return rc ? rc : split_dft_check(h->dft);
+    int rc = split_flag_status(hf[1]);
+    return rc ? rc : split_dft_flag_status(hf[2]);
 }
 
 int aeros_dyn_profile_step(aeros_dyn_t h, int maxk, double *ms, char *names, int name_len, int *nk) {

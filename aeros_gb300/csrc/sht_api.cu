@@ -46,6 +46,7 @@ struct aeros_sht_s {
     std::map<DescKey, DescSet> cache;
     SplitCtx *split = nullptr;
     SplitDft *dft = nullptr;              // split form's longitude DFT products
+    int *hflag = nullptr;                 // pinned host copies of the split error words (2)
 
     Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches}; }
 };
@@ -249,9 +250,14 @@ int dispatch(aeros_sht_t h, int op, bool in_spec, int nin, int nout, const doubl
     if (!dev) {
         AEROS_CUDA(cudaMemcpyAsync(out0, do0, nO * 8, cudaMemcpyDefault, h->stream));
         if (nout > 1) AEROS_CUDA(cudaMemcpyAsync(out1, do1, nO * 8, cudaMemcpyDefault, h->stream));
+        // the split error words ride behind the copies: one synchronisation
+        const int *w1 = split_err_word(h->split), *w2 = split_dft_err_word(h->dft);
+        h->hflag[0] = h->hflag[1] = 0;
+        if (w1) AEROS_CUDA(cudaMemcpyAsync(h->hflag, w1, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        if (w2) AEROS_CUDA(cudaMemcpyAsync(h->hflag + 1, w2, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
         AEROS_CUDA(cudaStreamSynchronize(h->stream));
-        if ((rc = split_check(h->split))) return rc;
-        return split_dft_check(h->dft);
+        if ((rc = split_flag_status(h->hflag[0]))) return rc;
+        return split_dft_flag_status(h->hflag[1]);
     }
     return AEROS_OK;
 }
@@ -304,12 +310,16 @@ int aeros_sht_create(aeros_sht_t *out, int trunc, int nlon, int nlat, int batch_
         return AEROS_ERR_NOMEM;
     }
     if (cudaMalloc(&h->partial, sizeof(double) * h->g.nlat * batch_max) != cudaSuccess ||
-        cudaMalloc(&h->totals, sizeof(double) * batch_max) != cudaSuccess) {
+        cudaMalloc(&h->totals, sizeof(double) * batch_max) != cudaSuccess ||
+        cudaMallocHost(&h->hflag, 2 * sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
+        aeros_sht_destroy(h);
+        set_error("transform workspace allocation failed");
         return AEROS_ERR_NOMEM;
     }
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
+        aeros_sht_destroy(h);
         return AEROS_ERR_CUDA;
     }
     h->own_stream = true;
@@ -330,6 +340,7 @@ int aeros_sht_destroy(aeros_sht_t h) {
     if (h->adbuf) cudaFree(h->adbuf);
     if (h->partial) cudaFree(h->partial);
     if (h->totals) cudaFree(h->totals);
+    if (h->hflag) cudaFreeHost(h->hflag);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AEROS_OK;

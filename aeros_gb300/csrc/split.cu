@@ -824,10 +824,16 @@ int split_error(SplitCtx *s, int *flag) {
     return cudaMemcpy(flag, s->err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess ? AEROS_OK : AEROS_ERR_CUDA;
 }
 
+const int *split_err_word(const SplitCtx *s) { return s ? s->err : nullptr; }
+
 int split_check(SplitCtx *s) {
     if (!s) return AEROS_OK;
     int flag = 0;
     if (split_error(s, &flag) != AEROS_OK) return AEROS_ERR_CUDA;
+    return split_flag_status(flag);
+}
+
+int split_flag_status(int flag) {
     if (flag) {
         set_error(flag & 2 ? "split path: shared memory not 1024-byte aligned"
                            : "split path: tensor-core wait gave up (bounded mbarrier wait)");

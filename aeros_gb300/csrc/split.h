@@ -18,6 +18,10 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, co
 int split_error(SplitCtx *s, int *flag);
 // AEROS_OK, or AEROS_ERR_CUDA with the last-error text set when the flag is up.
 int split_check(SplitCtx *s);
+// The same check split in two, for a caller that reads several flags with one
+// synchronisation: the device word (nullptr for a null context), then its status.
+const int *split_err_word(const SplitCtx *s);
+int split_flag_status(int flag);
 
 // Longitude transforms of the split form as exact-digit DFT products on the
 // tensor cores (split_dft.cu).  Same contracts as launch_fourier_synth /
@@ -32,5 +36,7 @@ bool split_dft_has_anal(const SplitDft *s);
 int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow);
 int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow);
 int split_dft_check(SplitDft *s);
+const int *split_dft_err_word(const SplitDft *s);
+int split_dft_flag_status(int flag);
 
 }  // namespace aeros

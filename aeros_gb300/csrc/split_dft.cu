@@ -516,10 +516,16 @@ int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int
     return AEROS_OK;
 }
 
+const int *split_dft_err_word(const SplitDft *s) { return s ? s->err : nullptr; }
+
 int split_dft_check(SplitDft *s) {
     if (!s) return AEROS_OK;
     int flag = 0;
     if (cudaMemcpy(&flag, s->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return AEROS_ERR_CUDA;
+    return split_dft_flag_status(flag);
+}
+
+int split_dft_flag_status(int flag) {
     if (flag) {
         set_error(flag & 2 ? "split DFT: shared memory not 1024-byte aligned"
                            : "split DFT: tensor-core wait gave up (bounded mbarrier wait)");
