@@ -244,9 +244,17 @@ int aeros_dyn_step_async(aeros_dyn_t h, int nsteps);
  * temp | lnps (all members each, aeros_dyn_state_size complex values), host or
  * device: the same as aeros_dyn_set_state + aeros_dyn_set_old_state +
  * aeros_dyn_step + aeros_dyn_get_state with three copies and one
- * synchronisation. */
+ * synchronisation.  With nsteps = 1 and every array device memory or pinned
+ * host memory (aeros_host_register), the copies, the step and the error-word
+ * reads are one CUDA graph launch, built for the call's pointers and reused
+ * while they stay the same. */
 int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,
                           double *now_out);
+/* Page-lock (cudaHostRegister) or release a host array so that copies from and
+ * to it run at full speed and aeros_dyn_step_packed takes its one-graph form;
+ * for a Fortran host's state arrays. */
+int aeros_host_register(void *ptr, size_t bytes);
+int aeros_host_unregister(void *ptr);
 int aeros_dyn_sync(aeros_dyn_t h);
 
 /* Run one step with a CUDA event after every kernel (no graph) and return the

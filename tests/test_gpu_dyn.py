@@ -362,6 +362,61 @@ def test_step_packed_equals_the_four_calls(gpulib):
     assert b.counters()[0] == n + 3
 
 
+@pytest.mark.parametrize("kind", ["pinned", "registered", "device"])
+def test_step_packed_one_graph_form(gpulib, kind):
+    """One step between pinned, registered or device buffers runs as one graph
+    launch: bitwise the four-call result, through the start-up step and the
+    regular one, and rebuilt when the buffers change."""
+    import ctypes
+    import torch
+    from aeros_gb300 import _capi
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    p = held_suarez_params(trunc=21, nlev=12, nmember=2)
+    a = AerosDyn(p)
+    a.set_isothermal(264.0, 1.0e5)
+    a.hs_perturb(1.0)
+    n0 = a.pack(*a.get_state())
+    lib = _capi.lib()
+    keep = []
+
+    def buf(x):
+        if kind == "device":
+            t = torch.from_numpy(np.array(x)).cuda()
+            keep.append(t)
+            return t
+        if kind == "pinned":
+            t = torch.empty(x.shape, dtype=torch.complex128, pin_memory=True)
+            t.numpy()[...] = x
+            keep.append(t)
+            return t.numpy()
+        h = np.array(x)
+        _capi.check(lib.aeros_host_register(h.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(h.nbytes)),
+                    "aeros_host_register")
+        keep.append(h)
+        return h
+
+    def host(x):
+        return x.cpu().numpy() if kind == "device" else np.array(x)
+
+    b = AerosDyn(p)
+    nw, od, out = buf(n0), buf(n0), buf(np.zeros_like(n0))
+    b.step_packed(nw, od, 0, nsteps=1, now_out=out)           # start-up step: X^(n-1) = X^n on entry
+    a.step(1)
+    assert np.array_equal(host(out), a.pack(*a.get_state()))
+    cur, prev = a.pack(*a.get_state()), a.pack(*a.get_old_state())
+    for it in range(3):                                         # regular steps, two alternating buffer sets
+        nw2, od2, out2 = buf(cur), buf(prev), buf(np.zeros_like(n0))
+        b.step_packed(nw2, od2, 1 + it, nsteps=1, now_out=out2)
+        a.step(1)
+        assert np.array_equal(host(out2), a.pack(*a.get_state()))
+        cur, prev = a.pack(*a.get_state()), a.pack(*a.get_old_state())
+    assert b.counters()[0] == 4
+    if kind == "registered":
+        for h in keep:
+            _capi.check(lib.aeros_host_unregister(h.ctypes.data_as(ctypes.c_void_p)), "aeros_host_unregister")
+
+
 @pytest.mark.parametrize("trunc", [21, 42])
 def test_forced_tendency_matches_oracle(gpulib, trunc):
     """aeros_dyn_tendency_forced: the adiabatic tendencies plus the Held-Suarez forcing
