@@ -911,14 +911,16 @@ struct aeros_dyn_s {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // start-up, regular
     cudaGraph_t graph_src[2] = {nullptr, nullptr};   // kept for ensemble groups and the packed step
     long long graph_gen = 0;                         // bumped by every capture of the step graphs
-    struct {                                         // aeros_dyn_step_packed's one-graph form, for its last pointers
+    struct PackedGraph {                             // aeros_dyn_step_packed's one-graph form for a pointer set
         const void *now_in = nullptr, *old_in = nullptr;
-        void *now_out = nullptr;
+        void *now_out = nullptr, *old_out = nullptr;
         int s = -1;
         long long gen = -1;
         int copy_kernels = 0;                        // kernel launches of the graph besides the step's
         cudaGraphExec_t exec = nullptr;
-    } packed;
+    };
+    PackedGraph packed[4];                           // the last pointer sets (a ping-pong loop uses two)
+    int packed_next = 0;                             // the entry replaced next
     long long graph_kernels[2] = {0, 0};
     int nstep = 0;
     std::vector<cudaEvent_t> *prof = nullptr;        // events recorded after each launch
@@ -1411,14 +1413,19 @@ int flag_status(Dyn &d) {
 }
 
 // One step of aeros_dyn_step_packed as one graph: the two time levels in, the
-// flag reset, the step (a child copy of its captured graph), X^n out and the
-// error words to pinned host memory.  Built for the call's pointers and kept
-// until they or the step graphs change.
-int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now_out, int s, size_t bytes) {
-    auto &pk = d.packed;
-    if (pk.exec && pk.now_in == now_in && pk.old_in == old_in && pk.now_out == now_out && pk.s == s &&
-        pk.gen == d.graph_gen)
-        return AEROS_OK;
+// flag reset, the step (a child copy of its captured graph), the two new time
+// levels out and the error words to pinned host memory.  Built for the call's
+// pointers and kept until they or the step graphs change.
+int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now_out, double *old_out, int s,
+                 size_t bytes, Dyn::PackedGraph **out) {
+    for (auto &pk : d.packed)
+        if (pk.exec && pk.now_in == now_in && pk.old_in == old_in && pk.now_out == now_out &&
+            pk.old_out == old_out && pk.s == s && pk.gen == d.graph_gen) {
+            *out = &pk;
+            return AEROS_OK;
+        }
+    auto &pk = d.packed[d.packed_next];
+    d.packed_next = (d.packed_next + 1) % 4;
     if (pk.exec) cudaGraphExecDestroy(pk.exec);
     pk.exec = nullptr;
     cudaGraph_t g;
@@ -1432,8 +1439,11 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
         }
         return a.devicePointer;
     };
-    const void *dn = dev_addr(now_in), *dold = dev_addr(old_in), *dout = now_out ? dev_addr(now_out) : nullptr;
-    const bool mapped = dn && dold && (!now_out || dout);   // copy kernels: ~20 us less than copy-engine copies
+    const void *dn = dev_addr(now_in), *dold = dev_addr(old_in);
+    void *dout = now_out ? const_cast<void *>(dev_addr(now_out)) : nullptr;
+    void *dold_out = old_out ? const_cast<void *>(dev_addr(old_out)) : nullptr;
+    // copy kernels: ~20 us less than copy-engine copies
+    const bool mapped = dn && dold && (!now_out || dout) && (!old_out || dold_out);
     auto build = [&]() -> int {
         cudaGraphNode_t n_now, n_old, n_set, n_step, n_out, n_f;
         size_t n2 = bytes / sizeof(double2);
@@ -1463,9 +1473,19 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
         const cudaGraphNode_t before[3] = {n_now, n_old, n_set};
         AEROS_CUDA(cudaGraphAddChildGraphNode(&n_step, g, mapped ? before + 1 : before, mapped ? 2 : 3,
                                               d.graph_src[s]));
-        if (now_out && mapped) {
-            double2 *o = static_cast<double2 *>(const_cast<void *>(dout));
-            const double2 *src = d.now;
+        if (mapped && now_out && old_out) {
+            double2 *o0 = static_cast<double2 *>(dout), *o1 = static_cast<double2 *>(dold_out);
+            const double2 *s0 = d.now, *s1 = d.old;
+            void *args[] = {&o0, &s0, &o1, &s1, &n2};
+            cudaKernelNodeParams kp{};
+            kp.func = (void *)k_copy_pair;
+            kp.gridDim = dim3(nblk);
+            kp.blockDim = dim3(256);
+            kp.kernelParams = args;
+            AEROS_CUDA(cudaGraphAddKernelNode(&n_out, g, &n_step, 1, &kp));
+        } else if (mapped && (now_out || old_out)) {
+            double2 *o = static_cast<double2 *>(now_out ? dout : dold_out);
+            const double2 *src = now_out ? d.now : d.old;
             void *args[] = {&o, &src, &n2};
             cudaKernelNodeParams kp{};
             kp.func = (void *)k_copy;
@@ -1473,8 +1493,11 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
             kp.blockDim = dim3(256);
             kp.kernelParams = args;
             AEROS_CUDA(cudaGraphAddKernelNode(&n_out, g, &n_step, 1, &kp));
-        } else if (now_out) {
-            AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_out, g, &n_step, 1, now_out, d.now, bytes, cudaMemcpyDefault));
+        } else {
+            if (now_out)
+                AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_out, g, &n_step, 1, now_out, d.now, bytes, cudaMemcpyDefault));
+            if (old_out)
+                AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_out, g, &n_step, 1, old_out, d.old, bytes, cudaMemcpyDefault));
         }
         const int *words[3] = {d.flag, split_err_word(d.split), split_dft_err_word(d.dft)};
         for (int i = 0; i < 3; ++i)
@@ -1493,9 +1516,11 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
     pk.now_in = now_in;
     pk.old_in = old_in;
     pk.now_out = now_out;
+    pk.old_out = old_out;
     pk.s = s;
     pk.gen = d.graph_gen;
-    pk.copy_kernels = mapped ? (now_out ? 2 : 1) : 0;
+    pk.copy_kernels = mapped ? ((now_out || old_out) ? 2 : 1) : 0;
+    *out = &pk;
     return AEROS_OK;
 }
 
@@ -1554,7 +1579,8 @@ void destroy(Dyn *d) {
         if (g) cudaGraphExecDestroy(g);
     for (auto &g : d->graph_src)
         if (g) cudaGraphDestroy(g);
-    if (d->packed.exec) cudaGraphExecDestroy(d->packed.exec);
+    for (auto &pk : d->packed)
+        if (pk.exec) cudaGraphExecDestroy(pk.exec);
     free_syn_plan(d->synS);
     free_syn_plan(d->synD);
     void *ps[] = {d->now, d->old, d->tnd, d->FS, d->FA, d->G, d->GA, d->D, d->GT_d, d->TT_d, d->WT_d, d->nu_d,
@@ -1775,16 +1801,18 @@ int aeros_dyn_step(aeros_dyn_t h, int nsteps) {
 }
 
 int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,
-                          double *now_out) {
+                          double *now_out, double *old_out) {
     if (!h || !now_in || !old_in || nstep < 0 || nsteps < 0) return AEROS_ERR_ARG;
     const size_t bytes = h->nstate() * sizeof(double2);
     // one step between pinned (or device) buffers: a single graph launch and one synchronisation
-    if (nsteps == 1 && graph_copyable(now_in) && graph_copyable(old_in) && (!now_out || graph_copyable(now_out))) {
+    if (nsteps == 1 && graph_copyable(now_in) && graph_copyable(old_in) && (!now_out || graph_copyable(now_out)) &&
+        (!old_out || graph_copyable(old_out))) {
         const int s = nstep == 0 ? 0 : 1;
-        if (int rc = packed_graph(*h, now_in, old_in, now_out, s, bytes)) return rc;
+        Dyn::PackedGraph *pk = nullptr;
+        if (int rc = packed_graph(*h, now_in, old_in, now_out, old_out, s, bytes, &pk)) return rc;
         h->hflag[0] = h->hflag[1] = h->hflag[2] = 0;
-        AEROS_CUDA(cudaGraphLaunch(h->packed.exec, h->stream));
-        h->launches += h->graph_kernels[s] + h->packed.copy_kernels;
+        AEROS_CUDA(cudaGraphLaunch(pk->exec, h->stream));
+        h->launches += h->graph_kernels[s] + pk->copy_kernels;
         h->nstep = nstep + 1;
         AEROS_CUDA(cudaStreamSynchronize(h->stream));
         return flag_status(*h);
@@ -1797,6 +1825,7 @@ int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old
     int rc = aeros_dyn_step_async(h, nsteps);
     if (rc) return rc;
     if (now_out) AEROS_CUDA(cudaMemcpyAsync(now_out, h->now, bytes, cudaMemcpyDefault, h->stream));
+    if (old_out) AEROS_CUDA(cudaMemcpyAsync(old_out, h->old, bytes, cudaMemcpyDefault, h->stream));
     return aeros_dyn_sync(h);
 }
 

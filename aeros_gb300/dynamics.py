@@ -212,18 +212,20 @@ class AerosDyn:
                                                    ctypes.byref(c)), "aeros_dyn_counters")
         return n.value, a.value, b.value, c.value
 
-    def step_packed(self, now_in, old_in, nstep, nsteps=1, now_out=None):
+    def step_packed(self, now_in, old_in, nstep, nsteps=1, now_out=None, old_out=None):
         """aeros_dyn_step_packed: packed complex128 time levels (vor | div | temp | lnps,
         state_size() values each, host or CUDA) in, nsteps steps, the new X^n into
-        now_out (allocated when None); returns now_out."""
+        now_out (allocated when None) and, when given, the new X^(n-1) (the
+        filtered previous level) into old_out; returns now_out."""
         n = self.state_size()
         if now_out is None:
             now_out = np.empty(n, np.complex128)
-        for a in (now_in, old_in, now_out):
+        for a in (now_in, old_in, now_out) + (() if old_out is None else (old_out,)):
             if a.shape != (n,) or (not _is_torch(a) and (a.dtype != np.complex128 or not a.flags.c_contiguous)):
                 raise ValueError(f"packed states are contiguous complex128 arrays of {n} values")
         _capi.check(_capi.lib().aeros_dyn_step_packed(self._h, _ptr(now_in), _ptr(old_in), int(nstep), int(nsteps),
-                                                      _ptr(now_out)), "aeros_dyn_step_packed")
+                                                      _ptr(now_out), None if old_out is None else _ptr(old_out)),
+                    "aeros_dyn_step_packed")
         return now_out
 
     def member_counters(self, member=0):

@@ -239,17 +239,19 @@ int aeros_dyn_step(aeros_dyn_t h, int nsteps);
  * reports AEROS_ERR_NONFINITE if any step produced a NaN/Inf. */
 int aeros_dyn_step_async(aeros_dyn_t h, int nsteps);
 /* A caller that keeps the state on the host, in one call: X^n (now_in) and
- * X^(n-1) (old_in) with its step count nstep in, nsteps steps, the new X^n out
- * (now_out, may be NULL).  Each array is one time level packed vor | div |
- * temp | lnps (all members each, aeros_dyn_state_size complex values), host or
- * device: the same as aeros_dyn_set_state + aeros_dyn_set_old_state +
- * aeros_dyn_step + aeros_dyn_get_state with three copies and one
+ * X^(n-1) (old_in) with its step count nstep in, nsteps steps, the new X^n
+ * (now_out) and the new X^(n-1) (old_out: the RAW-filtered previous level,
+ * which the next call takes as old_in) out; either output may be NULL.  Each
+ * array is one time level packed vor | div | temp | lnps (all members each,
+ * aeros_dyn_state_size complex values), host or device: the same as
+ * aeros_dyn_set_state + aeros_dyn_set_old_state + aeros_dyn_step +
+ * aeros_dyn_get_state + aeros_dyn_get_old_state with four copies and one
  * synchronisation.  With nsteps = 1 and every array device memory or pinned
  * host memory (aeros_host_register), the copies, the step and the error-word
  * reads are one CUDA graph launch, built for the call's pointers and reused
  * while they stay the same. */
 int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,
-                          double *now_out);
+                          double *now_out, double *old_out);
 /* Page-lock (cudaHostRegister) or release a host array so that copies from and
  * to it run at full speed and aeros_dyn_step_packed takes its one-graph form;
  * for a Fortran host's state arrays. */

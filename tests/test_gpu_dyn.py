@@ -356,9 +356,11 @@ def test_step_packed_equals_the_four_calls(gpulib):
     now, old, n = a.pack(*a.get_state()), a.pack(*a.get_old_state()), a.counters()[0]
     b = AerosDyn(p)
     b.set_mass_target(a.member_counters(0)[0])
-    out = b.step_packed(now, old, n, nsteps=3)
+    old_out = np.empty_like(now)
+    out = b.step_packed(now, old, n, nsteps=3, old_out=old_out)
     a.step(3)
     assert np.array_equal(out, a.pack(*a.get_state()))
+    assert np.array_equal(old_out, a.pack(*a.get_old_state()))
     assert b.counters()[0] == n + 3
 
 
@@ -404,14 +406,20 @@ def test_step_packed_one_graph_form(gpulib, kind):
     b.step_packed(nw, od, 0, nsteps=1, now_out=out)           # start-up step: X^(n-1) = X^n on entry
     a.step(1)
     assert np.array_equal(host(out), a.pack(*a.get_state()))
-    cur, prev = a.pack(*a.get_state()), a.pack(*a.get_old_state())
-    for it in range(3):                                         # regular steps, two alternating buffer sets
-        nw2, od2, out2 = buf(cur), buf(prev), buf(np.zeros_like(n0))
-        b.step_packed(nw2, od2, 1 + it, nsteps=1, now_out=out2)
+    cur, prev = host(out), a.pack(*a.get_old_state())
+    for it in range(4):                                         # regular steps: the outputs feed the next call
+        nw2, od2, out2, old2 = buf(cur), buf(prev), buf(np.zeros_like(n0)), buf(np.zeros_like(n0))
+        if it == 3:
+            b.step_packed(nw2, od2, 1 + it, nsteps=1, now_out=out2)   # X^n only: another graph
+            old2 = None
+        else:
+            b.step_packed(nw2, od2, 1 + it, nsteps=1, now_out=out2, old_out=old2)
         a.step(1)
         assert np.array_equal(host(out2), a.pack(*a.get_state()))
-        cur, prev = a.pack(*a.get_state()), a.pack(*a.get_old_state())
-    assert b.counters()[0] == 4
+        if old2 is not None:
+            assert np.array_equal(host(old2), a.pack(*a.get_old_state()))
+            cur, prev = host(out2), host(old2)
+    assert b.counters()[0] == 5
     if kind == "registered":
         for h in keep:
             _capi.check(lib.aeros_host_unregister(h.ctypes.data_as(ctypes.c_void_p)), "aeros_host_unregister")
