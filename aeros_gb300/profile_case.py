@@ -24,6 +24,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--transport", action="store_true",
                     help="run `steps` tracer-transport calls (one member's grid) instead of dynamics steps")
+    ap.add_argument("--tune", action="store_true", help="run the launch-shape autotuner before stepping")
     ap.add_argument("--shapes", default="",
                     help="launch shapes to set before stepping, e.g. spec_cols=1,spec_warps=2 (AerosDyn.TUNE_KEYS)")
     ap.add_argument("--sht-batch", type=int, default=0,
@@ -50,6 +51,9 @@ def main(argv=None):
         tg = sht.synthesis(t[e]) + rng.normal(0.0, 0.1, (a.nlev, dyn.nlat, dyn.nlon))
         t[e] = sht.analysis(tg)
     dyn.set_state(vor, div, t, lnps)
+    if a.tune:
+        before, after, shapes = dyn.autotune(reps=3)
+        print(f"autotune: {before:.4f} -> {after:.4f} ms/step with {shapes}")
     for _ in range(a.steps):
         ks = dyn.profile_step()
     print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
