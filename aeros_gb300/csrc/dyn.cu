@@ -908,6 +908,8 @@ struct aeros_dyn_s {
     int nfaS = 0;
     AnaCol *acS = nullptr;
     int nacS = 0;
+    int *agS = nullptr;                              // split analysis column groups of acS (starts)
+    int nagS = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // start-up, regular
     cudaGraph_t graph_src[2] = {nullptr, nullptr};   // kept for ensemble groups and the packed step
     long long graph_gen = 0;                         // bumped by every capture of the step graphs
@@ -1120,6 +1122,11 @@ int build_descriptors(Dyn &d) {
     if ((rc = dput(d.fsS, fs))) return rc;
     if ((rc = dput(d.faS, fa))) return rc;
     if ((rc = dput(d.acS, ac))) return rc;
+    {
+        const std::vector<int> gs = split_anal_groups(ac);
+        if ((rc = dput(d.agS, gs))) return rc;
+        d.nagS = (int)gs.size() - 1;
+    }
     d.nfsS = (int)fs.size();
     d.nfaS = (int)fa.size();
     d.nacS = (int)ac.size();
@@ -1310,7 +1317,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     if (rc) return rc;
     mark(d, "fourier_anal");
     if (d.par.precision == AEROS_PREC_SPLIT && d.split)
-        rc = split_leg_anal(d.split, c, d.acS, d.nacS, d.FA, rowsA);
+        rc = split_leg_anal(d.split, c, d.acS, d.agS, d.nagS, d.FA, rowsA);
     else
         rc = launch_leg_anal_fp64(c, d.acS, d.nacS, d.FA, rowsA);
     mark(d, "legendre_anal");
@@ -1587,7 +1594,7 @@ void destroy(Dyn *d) {
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
                   d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
-                  d->dconst, d->spec_wt};
+                  d->dconst, d->spec_wt, d->agS};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->hflag) cudaFreeHost(d->hflag);

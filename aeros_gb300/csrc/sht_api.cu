@@ -22,6 +22,8 @@ struct DescSet {
     int nfana = 0;
     AnaCol *ana = nullptr;
     int nana = 0;
+    int *agrp = nullptr;   // split analysis column groups of ana (starts)
+    int nagrp = 0;
     int nrow = 0;
 };
 
@@ -58,6 +60,7 @@ void free_desc(DescSet &d) {
     if (d.fsyn) cudaFree(d.fsyn);
     if (d.fana) cudaFree(d.fana);
     if (d.ana) cudaFree(d.ana);
+    if (d.agrp) cudaFree(d.agrp);
     d = DescSet{};
 }
 
@@ -186,6 +189,11 @@ int get_desc(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, vo
     if ((rc = upload_vec(d.fsyn, fs))) return rc;
     if ((rc = upload_vec(d.fana, fa))) return rc;
     if ((rc = upload_vec(d.ana, ac))) return rc;
+    {
+        const std::vector<int> gs = split_anal_groups(ac);
+        if ((rc = upload_vec(d.agrp, gs))) return rc;
+        d.nagrp = (int)gs.size() - 1;
+    }
     d.nfsyn = (int)fs.size();
     d.nfana = (int)fa.size();
     d.nana = (int)ac.size();
@@ -220,7 +228,7 @@ int run_anal(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, vo
         rc = launch_fourier_anal(c, d->fana, d->nfana, h->F, d->nrow);
     if (rc) return rc;
     if (h->precision == AEROS_PREC_SPLIT && h->split)
-        return split_leg_anal(h->split, c, d->ana, d->nana, h->F, d->nrow);
+        return split_leg_anal(h->split, c, d->ana, d->agrp, d->nagrp, h->F, d->nrow);
     return launch_leg_anal_fp64(c, d->ana, d->nana, h->F, d->nrow);
 }
 

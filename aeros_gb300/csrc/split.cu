@@ -36,8 +36,11 @@ namespace aeros {
 namespace {
 
 constexpr int kNTs = kNTile;   // synthesis tile columns: 16 complex fields x (re, im)
-constexpr int kNTa = kNTile;   // analysis tile columns: 2 folds x 3 slots x 2 fields x (re, im), 24 used
-constexpr int kFa = 2;         // analysis fields per tile
+constexpr int kNTa = kNTile;   // analysis tile columns: up to 8 sources x 2 folds x (re, im)
+constexpr int kFaSlots = kNTa / 4;   // sources (used AnaCol slots) per analysis column group
+constexpr int kFaCols = 8;           // AnaCols per analysis column group
+constexpr int kSdStride = 17;        // doubles per row of the analysis epilogue's row table (16 values)
+constexpr int kStagePad = 9216;      // analysis stage buffer 1 (kNTa x kSt doubles) padded to 1024 bytes
 
 // ------------------------------------------------------------------ table prep
 // Synthesis tables: tile image (m, lat tile t, chunk ch): rows r = blk*32 + jj
@@ -132,8 +135,12 @@ struct SynSplitArgs {
 // Synthesis smem: A [S][128][64] | B [S][64][64] bf16 | stage [64][65] doubles.
 template <int S>
 constexpr size_t synth_smem() { return (size_t)S * (kTM + kNTs) * kKC * 2 + 2 * (size_t)kNTs * kSt * 8; }
+// Analysis smem: A | stage 1 (padded) | B | stage 0; the epilogue row table
+// [128][kSdStride] doubles reuses B with the current group's stage buffer.
 template <int S>
-constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + 2 * (size_t)kNTa * kSt * 8; }
+constexpr size_t anal_smem() { return (size_t)S * (kTM + kNTa) * kKC * 2 + kStagePad + (size_t)kNTa * kSt * 8; }
+static_assert(kStagePad >= kNTa * kSt * 8 && kStagePad % 1024 == 0, "analysis stage padding");
+static_assert((size_t)7 * kNTa * kKC * 2 + kNTa * kSt * 8 >= 128 * kSdStride * 8, "analysis row table fits");
 
 // One CTA per (group slot z, m, latitude tile): it steps through column groups
 // z, z + (number of slots), ... (16 complex columns each) with its TMEM, barriers and
@@ -405,7 +412,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
 // ------------------------------------------------------------------ analysis kernel
 struct AnaSplitArgs {
     const AnaCol *cols;
-    int ncol;
+    const int *gstart;   // column groups: AnaCols [gstart[g], gstart[g + 1])
+    int ngrp;
     const double *lfac, *isin;
     const int *moff;
     const long long *abase;
@@ -417,11 +425,18 @@ struct AnaSplitArgs {
     int smajor;   // grid (slot, m, tile) instead of (m, tile, slot)
 };
 
-// B column of (fold, slot, field cc, comp): fold 0 = north + south, 1 = north - south;
-// slot s scales Fourier row s of the field by (a_s + i b_s m / sin) (slots 0, 1).
-__host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
-    return fold * 12 + slot * 4 + cc * 2 + comp;
-}
+// Sources of a column group: every used slot of its AnaCols is one source, a
+// Fourier row with its scaling, contracted with the Pbar rows (slots 1 and 3:
+// "P sources") or the dPbar rows (slot 2: "D sources").  A source owns four B
+// columns (hemisphere folds north +- south x re, im): P source i at
+// fold * 2 nP + 2 i + comp, D source i at 4 nP + fold * 2 nD + 2 i + comp.
+struct AnaMeta {
+    int nc, nsrc, nP, nD;                 // AnaCols, sources, P and D sources
+    int p0[kFaCols], p2[kFaCols], d1[kFaCols];   // source of slot 1, 3 (P) and 2 (D) of an AnaCol, -1 unused
+    int row[kFaSlots], kind[kFaSlots];    // Fourier row; scaling 0 real, 1 imaginary, 2 general, 3 none
+    int col[kFaSlots], fstride[kFaSlots]; // B column of fold 0 (re); fold stride
+    double a[kFaSlots], bm[kFaSlots];     // scaling a + i b m / sin
+};
 
 // One CTA per (group slot z, m, l tile): it steps through column groups
 // z, z + (number of slots), ... with its TMEM, barriers and (for a one-chunk
@@ -430,16 +445,18 @@ __host__ __device__ constexpr int acol(int fold, int slot, int cc, int comp) {
 // buffer while the tensor core works on the current group.
 template <int S, int B>
 __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
+    // shared memory: sA | stage 1 | sB | stage 0; the epilogue's row table
+    // takes sB with the current group's stage buffer (contiguous either way)
     extern __shared__ __align__(1024) unsigned char smraw[];
     __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smraw);
-    __nv_bfloat16 *sB = sA + (size_t)S * kTM * kKC;
-    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);   // 2 x [kNTa cols][kSt]
+    double *stage1 = reinterpret_cast<double *>(sA + (size_t)S * kTM * kKC);
+    __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(stage1) + kStagePad);
+    double *stage0 = reinterpret_cast<double *>(sB + (size_t)S * kNTa * kKC);
     __shared__ __align__(8) uint64_t mbarA, mbarM;
     __shared__ uint32_t tmem_base;
     __shared__ int cexp[2][kNTa];
-    __shared__ AnaCol scol[2][kFa];
-    __shared__ int skind[2][kFa][2];   // slot scaling: 0 real (b = 0), 1 imaginary (a = 0), 2 general
-    __shared__ double sbm[2][kFa][2];  // b m of the slot
+    __shared__ AnaCol scol[2][kFaCols];
+    __shared__ AnaMeta meta[2];
     __shared__ int fail;
 
     if (smem_u32(smraw) & 1023u) {   // swizzled tiles need 1024-byte alignment
@@ -449,7 +466,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     const int slot = a.smajor ? blockIdx.x : blockIdx.z, m = a.smajor ? blockIdx.y : blockIdx.x,
               t = a.smajor ? blockIdx.z : blockIdx.y;
     const int K = a.T - m + 1;
-    const int ngrp = (a.ncol + kFa - 1) / kFa;
+    const int ngrp = a.ngrp;
     if (64 * t >= K || slot >= ngrp) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
@@ -466,66 +483,112 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     const __nv_bfloat16 *gA = a.dig + a.abase[m] + (size_t)t * nch * S * kTM * kSlice;
+    auto stage_of = [&](int b) { return b == 0 ? stage0 : stage1; };
 
-    // group metadata into buffer b (scale classes of the two slots)
+    // group metadata into buffer b: the AnaCols, their sources and the B
+    // columns, by warp 0 (lane i: AnaCol i; source offsets by warp scans)
     auto set_meta = [&](int grp, int b) {
-        const int c0 = grp * kFa, ncl = min(kFa, a.ncol - c0);
-        if (tid < ncl) scol[b][tid] = a.cols[c0 + tid];
         if (tid < kNTa) cexp[b][tid] = 0;
-        if (tid < 2 * ncl) {
-            const AnaCol q = a.cols[c0 + (tid >> 1)];
-            const int sl = tid & 1;
-            const double aa = sl == 0 ? q.a1 : q.a2, bb = sl == 0 ? q.b1 : q.b2;
-            skind[b][tid >> 1][sl] =
-                (__double_as_longlong(bb) << 1) == 0 ? 0 : ((__double_as_longlong(aa) << 1) == 0 ? 1 : 2);
-            sbm[b][tid >> 1][sl] = bb * m;
+        if (warp != 0) return;
+        const int c0 = a.gstart[grp], nc = a.gstart[grp + 1] - c0;
+        AnaMeta &g = meta[b];
+        const bool act = lane < nc;
+        AnaCol q{};
+        if (act) {
+            q = a.cols[c0 + lane];
+            scol[b][lane] = q;
+        }
+        const int np = act ? (q.row1 >= 0) + (q.row3 >= 0) : 0, nd = act ? (q.row2 >= 0) : 0;
+        int sp = np, sq = nd;   // inclusive scans over the lanes (nc <= kFaCols = 8)
+#pragma unroll
+        for (int o = 1; o < kFaCols; o <<= 1) {
+            const int x = __shfl_up_sync(0xffffffffu, sp, o), y = __shfl_up_sync(0xffffffffu, sq, o);
+            if (lane >= o) {
+                sp += x;
+                sq += y;
+            }
+        }
+        const int nP = __shfl_sync(0xffffffffu, sp, kFaCols - 1), nD = __shfl_sync(0xffffffffu, sq, kFaCols - 1);
+        if (lane == 0) {
+            g.nc = nc;
+            g.nP = nP;
+            g.nD = nD;
+            g.nsrc = nP + nD;
+        }
+        if (!act) return;
+        // P sources are 0 .. nP-1 (in AnaCol order, slot 1 before slot 3), D sources nP .. nP+nD-1
+        auto put = [&](int s, int row, double aa, double bb, int kind, int col, int fstride) {
+            g.row[s] = row;
+            g.a[s] = aa;
+            g.bm[s] = bb * m;
+            g.kind[s] = kind;
+            g.col[s] = col;
+            g.fstride[s] = fstride;
+        };
+        auto kind_of = [](double aa, double bb) {
+            return (__double_as_longlong(bb) << 1) == 0 ? 0 : ((__double_as_longlong(aa) << 1) == 0 ? 1 : 2);
+        };
+        int ip = sp - np;
+        const int id = sq - nd;
+        g.p0[lane] = g.p2[lane] = g.d1[lane] = -1;
+        if (q.row1 >= 0) {
+            put(ip, q.row1, q.a1, q.b1, kind_of(q.a1, q.b1), 2 * ip, 2 * nP);
+            g.p0[lane] = ip++;
+        }
+        if (q.row3 >= 0) {
+            put(ip, q.row3, 1.0, 0.0, 3, 2 * ip, 2 * nP);
+            g.p2[lane] = ip;
+        }
+        if (q.row2 >= 0) {
+            put(nP + id, q.row2, q.a2, q.b2, kind_of(q.a2, q.b2), 4 * nP + 2 * id, 2 * nD);
+            g.d1[lane] = id;
         }
     };
-    // the four B values (fold x comp) of field cc, slot s at north latitude j (buffer b)
-    auto bvals = [&](int b, int cc, int slot, int j, double *v) {
-        const AnaCol &q = scol[b][cc];
-        const int row = slot == 0 ? q.row1 : (slot == 1 ? q.row2 : q.row3);
-        if (row < 0 || j >= a.nh) { v[0] = v[1] = v[2] = v[3] = 0.0; return; }
+    // the four B values (fold x comp) of source s at north latitude j (buffer b)
+    auto bvals = [&](int b, int s, int j, double *v) {
+        const AnaMeta &g = meta[b];
+        if (j >= a.nh) { v[0] = v[1] = v[2] = v[3] = 0.0; return; }
+        const int row = g.row[s];
         const double2 fn = a.F[((size_t)j * a.nrow + row) * a.ms + m];
         const double2 fs = a.F[((size_t)(a.nlat - 1 - j) * a.nrow + row) * a.ms + m];
         // fold first (the scaling is linear), then scale by (a + i b m / sin)
         const double er = fn.x + fs.x, ei = fn.y + fs.y, orr = fn.x - fs.x, oi = fn.y - fs.y;
-        if (slot < 2) {
-            const int kd = skind[b][cc][slot];
-            const double aa = slot == 0 ? q.a1 : q.a2;
-            if (kd == 0) {
-                v[0] = aa * er; v[1] = aa * ei; v[2] = aa * orr; v[3] = aa * oi;
-            } else {
-                const double bb = sbm[b][cc][slot] * a.isin[j];
-                if (kd == 1) {
-                    v[0] = -bb * ei; v[1] = bb * er; v[2] = -bb * oi; v[3] = bb * orr;
-                } else {
-                    v[0] = fma(aa, er, -bb * ei); v[1] = fma(aa, ei, bb * er);
-                    v[2] = fma(aa, orr, -bb * oi); v[3] = fma(aa, oi, bb * orr);
-                }
-            }
-        } else {
+        const int kd = g.kind[s];
+        if (kd == 3) {
             v[0] = er; v[1] = ei; v[2] = orr; v[3] = oi;
+        } else if (kd == 0) {
+            const double aa = g.a[s];
+            v[0] = aa * er; v[1] = aa * ei; v[2] = aa * orr; v[3] = aa * oi;
+        } else {
+            const double bb = g.bm[s] * a.isin[j];
+            if (kd == 1) {
+                v[0] = -bb * ei; v[1] = bb * er; v[2] = -bb * oi; v[3] = bb * orr;
+            } else {
+                const double aa = g.a[s];
+                v[0] = fma(aa, er, -bb * ei); v[1] = fma(aa, ei, bb * er);
+                v[2] = fma(aa, orr, -bb * oi); v[3] = fma(aa, oi, bb * orr);
+            }
         }
     };
     // phase 1 of group grp into buffer b: column scales over all latitudes, chunk 0 staged
     const FastDiv dkp(KpA);
-    auto gather = [&](int grp, int b) {
-        const int ncl = min(kFa, a.ncol - grp * kFa);
-        double *stage = stage0 + (size_t)b * kNTa * kSt;
+    auto gather = [&](int b) {
+        const AnaMeta &g = meta[b];
+        double *stage = stage_of(b);
         const int kc0 = min(kKC, KpA);
-        for (int base = 0; base < ncl * 3 * KpA; base += kThreads) {
+        for (int base = 0; base < g.nsrc * KpA; base += kThreads) {
             const int task = base + tid;
-            const bool valid = task < ncl * 3 * KpA;
+            const bool valid = task < g.nsrc * KpA;
             const int q = dkp.div(task);
-            const int j = task - q * KpA, cs = valid ? q : -1, cc = cs / 3, slot = cs - cc * 3;
+            const int j = task - q * KpA, s = valid ? q : -1;
             double v[4] = {0.0, 0.0, 0.0, 0.0};
-            if (valid) bvals(b, cc, slot, j, v);
-            const unsigned peers = __match_any_sync(0xffffffffu, cs);
+            if (valid) bvals(b, s, j, v);
+            const unsigned peers = __match_any_sync(0xffffffffu, s);
             const bool leader = valid && lane == __ffs(peers) - 1;
+            const int c0 = valid ? g.col[s] : 0, fs = valid ? g.fstride[s] : 0;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                const int n = acol(f >> 1, slot, cc, f & 1);
+                const int n = c0 + (f >> 1) * fs + (f & 1);
                 const int be = __reduce_max_sync(peers, bexp(v[f]));
                 if (leader) atomicMax(&cexp[b][n], be);
                 if (valid && j < kc0) stage[n * kSt + j] = v[f];
@@ -536,7 +599,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     set_meta(slot, 0);
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    gather(slot, 0);
+    gather(0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -548,24 +611,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
 
     int cb = 0;   // buffer of the current group
     for (int grp = slot; grp < ngrp && ok; grp += gstep, cb ^= 1) {
-        const int ncl = min(kFa, a.ncol - grp * kFa);
+        const AnaMeta &g = meta[cb];
+        const int ncu = 4 * g.nsrc;   // B columns in use
         const bool more = grp + gstep < ngrp;
-        double *stage = stage0 + (size_t)cb * kNTa * kSt;
+        double *stage = stage_of(cb);
         if (more) set_meta(grp + gstep, cb ^ 1);   // ordered before its gather by the sync below
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, KpA - ch * kKC);
-            // digits: all 8 warps, 4 contraction entries per task
-            for (int task = tid; task < kNTa * (kc / 4); task += kThreads) {
-                const int n = task % kNTa, k0 = (task / kNTa) * 4;
-                const int cc = (n % 4) >> 1;
+            // digits of the columns in use (the others' accumulators are never read):
+            // all 8 warps, 4 contraction entries per task
+            for (int task = tid; task < ncu * (kc / 4); task += kThreads) {
+                const int k0 = (task / ncu) * 4, n = task - (k0 / 4) * ncu;
                 double x[4];
-                if (n < 24 && cc < ncl) {
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
-                } else {
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) x[i] = 0.0;
-                }
+                for (int i = 0; i < 4; ++i) x[i] = stage[n * kSt + k0 + i];
                 put4<S, B>(x, scale_exp(cexp[cb][n]), sB, (size_t)kNTa * kSlice, n, k0);
             }
             asm volatile("fence.proxy.async.shared::cta;");
@@ -587,15 +646,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             if (ch + 1 < nch) {
                 const int kn = min(kKC, KpA - (ch + 1) * kKC);
                 const int sh = kn == kKC ? 5 : 4;   // kn = 1 << sh (16 or 32)
-                for (int task = tid; task < ncl * 3 * kn; task += kThreads) {
-                    const int jl = task & (kn - 1), cs = task >> sh, cc = cs / 3, slot = cs - cc * 3;
+                for (int task = tid; task < g.nsrc * kn; task += kThreads) {
+                    const int jl = task & (kn - 1), s = task >> sh;
                     double v[4];
-                    bvals(cb, cc, slot, (ch + 1) * kKC + jl, v);
+                    bvals(cb, s, (ch + 1) * kKC + jl, v);
 #pragma unroll
-                    for (int f = 0; f < 4; ++f) stage[acol(f >> 1, slot, cc, f & 1) * kSt + jl] = v[f];
+                    for (int f = 0; f < 4; ++f) stage[(g.col[s] + (f >> 1) * g.fstride[s] + (f & 1)) * kSt + jl] = v[f];
                 }
             } else if (more) {
-                gather(grp + gstep, cb ^ 1);
+                gather(cb ^ 1);
             }
             // one thread polls the MMA barrier; the CTA barrier releases the rest
             const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
@@ -610,34 +669,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
             }
         }
         if (!ok) break;
-        // epilogue 1: only the columns a row uses.  P rows (lane quarters 0, 1;
-        // parity par) use fold par of slots 0 and 2 (4 columns each), dP rows
-        // (quarters 2, 3) fold 1 - par of slot 1 (4 columns); the two warps of
-        // a quarter split them.
-        double *sd = reinterpret_cast<double *>(sB);   // [128 rows][9]
-        const int quarter = warp & 3, g = warp >> 2, par = quarter & 1;
+        // epilogue 1: P rows (lane quarters 0, 1; parity par) take fold par of
+        // the P sources, dP rows (quarters 2, 3) fold 1 - par of the D sources;
+        // the two warps of a quarter split the columns, two at a time
+        double *sd = cb == 0 ? reinterpret_cast<double *>(sB) : stage1;   // [128 rows][kSdStride]
+        const int quarter = warp & 3, gw = warp >> 2, par = quarter & 1;
         const int row = quarter * 32 + lane;
         const uint32_t tl = tmem + ((uint32_t)(quarter * 32) << 16);
-        if (quarter < 2) {
-            const int n0 = acol(par, g == 0 ? 0 : 2, 0, 0);
-            long long z[4] = {0, 0, 0, 0};
-            uint32_t r[S][4];
-#pragma unroll
-            for (int q = 0; q < S; ++q) tmem_ld<4>(tl + (uint32_t)(q * kNTa + n0), r[q]);
-            tmem_wait_ld();
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-#pragma unroll
-                for (int i = 0; i < 4; ++i) z[i] += zterm<B>(r[q][i], q);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                sd[(size_t)row * 9 + g * 4 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n0 + i])));
-        } else {
-            const int n0 = acol(1 - par, 1, 0, 0) + g * 2;
+        const int nv = quarter < 2 ? 2 * g.nP : 2 * g.nD;                       // values of this row
+        const int cbase = quarter < 2 ? par * 2 * g.nP : 4 * g.nP + (1 - par) * 2 * g.nD;
+        const int half = ((nv / 2 + 1) / 2) * 2;                                // warp 0's share (even)
+        const int v0 = gw == 0 ? 0 : half, v1 = gw == 0 ? half : nv;
+        for (int c = v0; c < v1; c += 2) {   // warp-uniform bounds
             long long z[2] = {0, 0};
             uint32_t r[S][2];
 #pragma unroll
-            for (int q = 0; q < S; ++q) tmem_ld<2>(tl + (uint32_t)(q * kNTa + n0), r[q]);
+            for (int q = 0; q < S; ++q) tmem_ld<2>(tl + (uint32_t)(q * kNTa + cbase + c), r[q]);
             tmem_wait_ld();
 #pragma unroll
             for (int q = 0; q < S; ++q)
@@ -645,35 +692,37 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
                 for (int i = 0; i < 2; ++i) z[i] += zterm<B>(r[q][i], q);
 #pragma unroll
             for (int i = 0; i < 2; ++i)
-                sd[(size_t)row * 9 + g * 2 + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][n0 + i])));
+                sd[(size_t)row * kSdStride + c + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][cbase + c + i])));
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
-        // epilogue 2: combine P and dP parts; l = m + 64 t + 2 pos + par
-        for (int idx = tid; idx < 64 * ncl; idx += kThreads) {
-            const int lk = ncl == 2 ? idx >> 1 : idx, cc = idx - lk * ncl;   // ncl is 1 or 2
+        // epilogue 2: combine the P and dP parts; l = m + 64 t + 2 pos + par
+        const int nc = g.nc;
+        for (int idx = tid; idx < 64 * nc; idx += kThreads) {
+            const int lk = idx / nc, cc = idx - lk * nc;
             const int pos = lk >> 1, pr = lk & 1;
             const int k = 64 * t + lk;
             if (k >= K) continue;
             const AnaCol &q = scol[cb][cc];
             const int l = m + k;
-            const double *rp = sd + (size_t)(pr * 32 + pos) * 9;         // slot 0 at [0..4), slot 2 at [4..8)
-            const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * 9;   // slot 1 at [0..4)
+            const double *rp = sd + (size_t)(pr * 32 + pos) * kSdStride;
+            const double *rd = sd + (size_t)((2 + pr) * 32 + pos) * kSdStride;
+            const int p0 = g.p0[cc], d1 = g.d1[cc], p2 = g.p2[cc];
             double xr = 0.0, xi = 0.0;
-            if (q.row1 >= 0) { xr += rp[cc * 2]; xi += rp[cc * 2 + 1]; }
-            if (q.row2 >= 0) { xr += rd[cc * 2]; xi += rd[cc * 2 + 1]; }
+            if (p0 >= 0) { xr += rp[2 * p0]; xi += rp[2 * p0 + 1]; }
+            if (d1 >= 0) { xr += rd[2 * d1]; xi += rd[2 * d1 + 1]; }
             const double post = a.lfac[q.post * a.ms + l];
             xr *= post;
             xi *= post;
-            if (q.row3 >= 0) {
+            if (p2 >= 0) {
                 const double f3 = a.lfac[q.lf3 * a.ms + l];
-                xr += f3 * rp[4 + cc * 2];
-                xi += f3 * rp[4 + cc * 2 + 1];
+                xr += f3 * rp[2 * p2];
+                xi += f3 * rp[2 * p2 + 1];
             }
             if (m == 0) xi = 0.0;
             q.dst[a.moff[m] + k] = make_double2(xr, xi);
         }
-        __syncthreads();   // sd (= sB) and this group's buffers are reused
+        __syncthreads();   // the row table and this group's buffers are reused
     }
     if (!ok && tid == 0) atomicOr(a.err, 1);
     // a table chunk still in flight must land before the CTA exits (bounded wait)
@@ -804,14 +853,32 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
     return AEROS_OK;
 }
 
-int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
-    if (ncol <= 0) return AEROS_OK;
-    const int ngrp = (ncol + kFa - 1) / kFa;
+std::vector<int> split_anal_groups(const std::vector<AnaCol> &cols) {
+    std::vector<int> start;
+    int used = kFaSlots, nc = kFaCols;
+    for (int i = 0; i < (int)cols.size(); ++i) {
+        const AnaCol &q = cols[i];
+        const int n = (q.row1 >= 0) + (q.row2 >= 0) + (q.row3 >= 0);
+        if (used + n > kFaSlots || nc == kFaCols) {
+            start.push_back(i);
+            used = 0;
+            nc = 0;
+        }
+        used += n;
+        ++nc;
+    }
+    start.push_back((int)cols.size());
+    return start;
+}
+
+int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, const int *gstart_d, int ngrp, const double2 *F,
+                   int nrow) {
+    if (ngrp <= 0) return AEROS_OK;
     const int tiles = (c.T + 1) * s->ntlA;
     bool smajor;
     const int slots = split_slots(ngrp, tiles, s->nsm, &smajor);
-    AnaSplitArgs a{cols_d, ncol, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F, nrow, c.ms,
-                   c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err, smajor ? 1 : 0};
+    AnaSplitArgs a{cols_d, gstart_d, ngrp, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F,
+                   nrow, c.ms, c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err, smajor ? 1 : 0};
     const dim3 grid = split_grid(slots, c.T + 1, s->ntlA, smajor);
     if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
     else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);

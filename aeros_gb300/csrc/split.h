@@ -12,7 +12,12 @@ int split_create(const Geometry &g, const DevTables &t, int max_rows, SplitCtx *
 void split_destroy(SplitCtx *s);
 // Same contract as launch_leg_synth_fp64 / launch_leg_anal_fp64.
 int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int nrow);
-int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
+// The analysis runs on column groups of AnaCols (split_anal_groups: group g
+// is [start[g], start[g + 1]), packed by used slots); gstart_d holds the
+// ngrp + 1 starts on the device.
+int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, const int *gstart_d, int ngrp, const double2 *F,
+                   int nrow);
+std::vector<int> split_anal_groups(const std::vector<AnaCol> &cols);
 // Sticky device error flag of the split kernels (1: an mbarrier wait gave up,
 // 2: misaligned shared memory); read after the stream has synchronised.
 int split_error(SplitCtx *s, int *flag);
