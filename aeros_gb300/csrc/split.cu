@@ -189,16 +189,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
     }
     const __nv_bfloat16 *gA = a.dig + a.sbase[m] + (size_t)t * nch * S * kTM * kSlice;
 
-    auto set_meta = [&](int grp, int b) {
-        const int c0 = grp * (kNTs / 2), ncl = min(kNTs / 2, a.ncol - c0);
-        if (tid < ncl) scol[b][tid] = a.cols[c0 + tid];
+    // Warp 0 fetches a group's columns into registers one group ahead of
+    // set_meta, so the global loads never hold up the CTA's barriers.
+    SynCol pre{};
+    int pre_ncl = 0;
+    auto prefetch = [&](int grp) {
+        if (warp != 0 || grp >= ngrp) return;
+        const int c0 = grp * (kNTs / 2);
+        pre_ncl = min(kNTs / 2, a.ncol - c0);
+        if (lane < pre_ncl) pre = a.cols[c0 + lane];
+    };
+    auto set_meta = [&](int b) {
         if (tid < kNTs) cexp[b][tid] = 0;
+        if (warp != 0) return;
+        if (lane < pre_ncl) scol[b][lane] = pre;
         // a warp-wide vote over the group's columns: any dPbar sum wanted?
-        if (warp == 0) {
-            const bool d = lane < ncl && a.cols[c0 + lane].rowD >= 0;
-            const unsigned v = __ballot_sync(0xffffffffu, d);
-            if (lane == 0) anyD[b] = v != 0;
-        }
+        const unsigned v = __ballot_sync(0xffffffffu, lane < pre_ncl && pre.rowD >= 0);
+        if (lane == 0) anyD[b] = v != 0;
     };
     // value k of complex column cc (scaled input coefficient), buffer b
     auto coef = [&](int b, int cc, int k) -> double2 {
@@ -260,7 +267,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         }
     };
 
-    set_meta(slot, 0);
+    prefetch(slot);
+    set_meta(0);
+    prefetch(slot + gstep);
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
     gather(slot, 0);
@@ -279,7 +288,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         const int ncl = min(kNTs / 2, a.ncol - grp * (kNTs / 2));
         const bool more = grp + gstep < ngrp;
         double *stage = cb ? stage1 : stage0;
-        if (more) set_meta(grp + gstep, cb ^ 1);   // ordered before its gather by the sync below
+        if (more) {
+            set_meta(cb ^ 1);           // group grp + gstep; ordered before its gather by the sync below
+            prefetch(grp + 2 * gstep);
+        }
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, Kp - ch * kKC);
             // digits of the data columns (columns of absent fields are zero): all 8 warps,
@@ -485,19 +497,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
     const __nv_bfloat16 *gA = a.dig + a.abase[m] + (size_t)t * nch * S * kTM * kSlice;
     auto stage_of = [&](int b) { return b == 0 ? stage0 : stage1; };
 
-    // group metadata into buffer b: the AnaCols, their sources and the B
-    // columns, by warp 0 (lane i: AnaCol i; source offsets by warp scans)
-    auto set_meta = [&](int grp, int b) {
+    // Warp 0 fetches a group's AnaCols into registers one group ahead of
+    // set_meta, so the global loads never hold up the CTA's barriers.
+    AnaCol pre{};
+    int pre_nc = 0;
+    auto prefetch = [&](int grp) {
+        if (warp != 0 || grp >= ngrp) return;
+        const int c0 = a.gstart[grp];
+        pre_nc = a.gstart[grp + 1] - c0;
+        if (lane < pre_nc) pre = a.cols[c0 + lane];
+    };
+    // group metadata into buffer b from the prefetched AnaCols: their sources
+    // and the B columns, by warp 0 (lane i: AnaCol i; source offsets by warp scans)
+    auto set_meta = [&](int b) {
         if (tid < kNTa) cexp[b][tid] = 0;
         if (warp != 0) return;
-        const int c0 = a.gstart[grp], nc = a.gstart[grp + 1] - c0;
+        const int nc = pre_nc;
         AnaMeta &g = meta[b];
         const bool act = lane < nc;
-        AnaCol q{};
-        if (act) {
-            q = a.cols[c0 + lane];
-            scol[b][lane] = q;
-        }
+        const AnaCol q = pre;
+        if (act) scol[b][lane] = q;
         const int np = act ? (q.row1 >= 0) + (q.row3 >= 0) : 0, nd = act ? (q.row2 >= 0) : 0;
         int sp = np, sq = nd;   // inclusive scans over the lanes (nc <= kFaCols = 8)
 #pragma unroll
@@ -596,7 +615,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         }
     };
 
-    set_meta(slot, 0);
+    prefetch(slot);
+    set_meta(0);
+    prefetch(slot + gstep);
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
     gather(0);
@@ -615,7 +636,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         const int ncu = 4 * g.nsrc;   // B columns in use
         const bool more = grp + gstep < ngrp;
         double *stage = stage_of(cb);
-        if (more) set_meta(grp + gstep, cb ^ 1);   // ordered before its gather by the sync below
+        if (more) {
+            set_meta(cb ^ 1);           // group grp + gstep; ordered before its gather by the sync below
+            prefetch(grp + 2 * gstep);
+        }
         for (int ch = 0; ch < nch && ok; ++ch) {
             const int kc = min(kKC, KpA - ch * kKC);
             // digits of the columns in use (the others' accumulators are never read):

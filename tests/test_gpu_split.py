@@ -116,3 +116,33 @@ def test_transform_sweep_vs_oracle(gpulib, T, B):
         es, ea = relerr(g.synthesis(c), fo), relerr(g.analysis(fo), co)
         print(f"T{T} B={B} precision {prec}: synthesis {es:.2e} analysis {ea:.2e}")
         assert es < tol and ea < tol
+
+
+@pytest.mark.parametrize("T", [42, 85])
+def test_split_analysis_groups_are_per_column(gpulib, T):
+    """The analysis packs outputs into column groups of up to 8 sources; every
+    output is computed from its own columns, so a batch's analyses equal the
+    same fields analysed one at a time, bitwise, across group boundaries."""
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import PREC_SPLIT
+    from oracle.pyoracle import OracleSHT
+    o = OracleSHT(T)
+    g = AerosSHT(T, batch_max=13, precision=PREC_SPLIT)
+    rng = np.random.default_rng(77)
+    c = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (13,))
+    f = o.synthesis(c)
+    batch = g.analysis(f)                       # 13 one-slot outputs: groups of 8 and 5
+    for i in (0, 7, 8, 12):
+        assert np.array_equal(batch[i], g.analysis(f[i:i + 1])[0])
+    assert relerr(batch, o.analysis(f)) < TOL
+    s = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (5,))
+    t = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (5,))
+    s[:, 0] = 0
+    t[:, 0] = 0
+    vth, vph = o.synthesis_vec(s, t)
+    S, Tt = g.analysis_vec(vth, vph)            # 10 two-slot outputs: groups of 4, 4 and 2
+    for i in (0, 2, 4):
+        S1, T1 = g.analysis_vec(vth[i:i + 1], vph[i:i + 1])
+        assert np.array_equal(S[i], S1[0]) and np.array_equal(Tt[i], T1[0])
+    so, to = o.analysis_vec(vth, vph)
+    assert relerr(S, so) < TOL and relerr(Tt, to) < TOL
