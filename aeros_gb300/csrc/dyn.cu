@@ -579,14 +579,32 @@ __global__ void k_copy(double2 *dst, const double2 *src, size_t n) {
         dst[i] = src[i];
 }
 
-// Two time levels in at once (the packed step's inputs, read straight from
-// mapped host memory over the chip-to-chip link, or from device memory).
-__global__ void k_copy_pair(double2 *d0, const double2 *__restrict__ s0, double2 *d1, const double2 *__restrict__ s1,
-                            size_t n) {
+// The packed step's inputs: both time levels in at once (read straight from
+// mapped host memory over the chip-to-chip link, or from device memory), and
+// the non-finite flag cleared.
+__global__ void k_packed_in(double2 *now, const double2 *__restrict__ now_src, double2 *old,
+                           const double2 *__restrict__ old_src, size_t n, int *flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *flag = 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double2 a = s0[i], b = s1[i];
-        d0[i] = a;
-        d1[i] = b;
+        const double2 a = now_src[i], b = old_src[i];
+        now[i] = a;
+        old[i] = b;
+    }
+}
+
+// The packed step's outputs: the new time levels out (a null destination is
+// skipped) and the three error words to the caller-visible pinned words.
+__global__ void k_packed_out(double2 *now_dst, const double2 *__restrict__ now, double2 *old_dst,
+                            const double2 *__restrict__ old, size_t n, int *words, const int *w0, const int *w1,
+                            const int *w2) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        words[0] = *w0;
+        words[1] = w1 ? *w1 : 0;
+        words[2] = w2 ? *w2 : 0;
+    }
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (now_dst) now_dst[i] = now[i];
+        if (old_dst) old_dst[i] = old[i];
     }
 }
 
@@ -1421,8 +1439,10 @@ int flag_status(Dyn &d) {
 
 // One step of aeros_dyn_step_packed as one graph: the two time levels in, the
 // flag reset, the step (a child copy of its captured graph), the two new time
-// levels out and the error words to pinned host memory.  Built for the call's
-// pointers and kept until they or the step graphs change.
+// levels out and the error words to pinned host memory.  With mapped arrays
+// (pinned host or device memory) that is three nodes, two of them kernels that
+// read and write the arrays directly; otherwise copy-engine copies.  Built for
+// the call's pointers and kept until they or the step graphs change.
 int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now_out, double *old_out, int s,
                  size_t bytes, Dyn::PackedGraph **out) {
     for (auto &pk : d.packed)
@@ -1450,67 +1470,57 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
     void *dout = now_out ? const_cast<void *>(dev_addr(now_out)) : nullptr;
     void *dold_out = old_out ? const_cast<void *>(dev_addr(old_out)) : nullptr;
     // copy kernels: ~20 us less than copy-engine copies
-    const bool mapped = dn && dold && (!now_out || dout) && (!old_out || dold_out);
+    const void *dwords = dev_addr(d.hflag);   // pinned error words, mapped
+    const bool mapped = dn && dold && (!now_out || dout) && (!old_out || dold_out) && dwords;
     auto build = [&]() -> int {
-        cudaGraphNode_t n_now, n_old, n_set, n_step, n_out, n_f;
         size_t n2 = bytes / sizeof(double2);
         const unsigned nblk = (unsigned)std::min<size_t>((n2 + 255) / 256, 1024);
+        const int *words[3] = {d.flag, split_err_word(d.split), split_dft_err_word(d.dft)};
+        cudaGraphNode_t n_in, n_step, n_out;
         if (mapped) {
+            // three nodes: copies in (and the flag cleared), the step, copies and error words out
             double2 *a0 = d.now, *a1 = d.old;
             const double2 *b0 = static_cast<const double2 *>(dn), *b1 = static_cast<const double2 *>(dold);
-            void *args[] = {&a0, &b0, &a1, &b1, &n2};
+            int *fl = d.flag;
+            void *args_in[] = {&a0, &b0, &a1, &b1, &n2, &fl};
             cudaKernelNodeParams kp{};
-            kp.func = (void *)k_copy_pair;
+            kp.func = (void *)k_packed_in;
             kp.gridDim = dim3(nblk);
             kp.blockDim = dim3(256);
-            kp.kernelParams = args;
-            AEROS_CUDA(cudaGraphAddKernelNode(&n_now, g, nullptr, 0, &kp));
-            n_old = n_now;
-        } else {
-            AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_now, g, nullptr, 0, d.now, now_in, bytes, cudaMemcpyDefault));
-            AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_old, g, nullptr, 0, d.old, old_in, bytes, cudaMemcpyDefault));
-        }
-        cudaMemsetParams mp{};
-        mp.dst = d.flag;
-        mp.value = 0;
-        mp.elementSize = sizeof(int);
-        mp.width = 1;
-        mp.height = 1;
-        AEROS_CUDA(cudaGraphAddMemsetNode(&n_set, g, nullptr, 0, &mp));
-        const cudaGraphNode_t before[3] = {n_now, n_old, n_set};
-        AEROS_CUDA(cudaGraphAddChildGraphNode(&n_step, g, mapped ? before + 1 : before, mapped ? 2 : 3,
-                                              d.graph_src[s]));
-        if (mapped && now_out && old_out) {
-            double2 *o0 = static_cast<double2 *>(dout), *o1 = static_cast<double2 *>(dold_out);
+            kp.kernelParams = args_in;
+            AEROS_CUDA(cudaGraphAddKernelNode(&n_in, g, nullptr, 0, &kp));
+            AEROS_CUDA(cudaGraphAddChildGraphNode(&n_step, g, &n_in, 1, d.graph_src[s]));
+            double2 *o0 = static_cast<double2 *>(const_cast<void *>(dout)), *o1 = static_cast<double2 *>(const_cast<void *>(dold_out));
             const double2 *s0 = d.now, *s1 = d.old;
-            void *args[] = {&o0, &s0, &o1, &s1, &n2};
-            cudaKernelNodeParams kp{};
-            kp.func = (void *)k_copy_pair;
-            kp.gridDim = dim3(nblk);
-            kp.blockDim = dim3(256);
-            kp.kernelParams = args;
-            AEROS_CUDA(cudaGraphAddKernelNode(&n_out, g, &n_step, 1, &kp));
-        } else if (mapped && (now_out || old_out)) {
-            double2 *o = static_cast<double2 *>(now_out ? dout : dold_out);
-            const double2 *src = now_out ? d.now : d.old;
-            void *args[] = {&o, &src, &n2};
-            cudaKernelNodeParams kp{};
-            kp.func = (void *)k_copy;
-            kp.gridDim = dim3(nblk);
-            kp.blockDim = dim3(256);
-            kp.kernelParams = args;
+            int *wd = static_cast<int *>(const_cast<void *>(dwords));
+            const int *w0 = words[0], *w1 = words[1], *w2 = words[2];
+            void *args_out[] = {&o0, &s0, &o1, &s1, &n2, &wd, &w0, &w1, &w2};
+            kp.func = (void *)k_packed_out;
+            kp.gridDim = dim3((now_out || old_out) ? nblk : 1);
+            kp.kernelParams = args_out;
             AEROS_CUDA(cudaGraphAddKernelNode(&n_out, g, &n_step, 1, &kp));
         } else {
+            cudaGraphNode_t n_old, n_set, n_f;
+            AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_in, g, nullptr, 0, d.now, now_in, bytes, cudaMemcpyDefault));
+            AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_old, g, nullptr, 0, d.old, old_in, bytes, cudaMemcpyDefault));
+            cudaMemsetParams mp{};
+            mp.dst = d.flag;
+            mp.value = 0;
+            mp.elementSize = sizeof(int);
+            mp.width = 1;
+            mp.height = 1;
+            AEROS_CUDA(cudaGraphAddMemsetNode(&n_set, g, nullptr, 0, &mp));
+            const cudaGraphNode_t before[3] = {n_in, n_old, n_set};
+            AEROS_CUDA(cudaGraphAddChildGraphNode(&n_step, g, before, 3, d.graph_src[s]));
             if (now_out)
                 AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_out, g, &n_step, 1, now_out, d.now, bytes, cudaMemcpyDefault));
             if (old_out)
                 AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_out, g, &n_step, 1, old_out, d.old, bytes, cudaMemcpyDefault));
+            for (int i = 0; i < 3; ++i)
+                if (words[i])
+                    AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_f, g, &n_step, 1, d.hflag + i, words[i], sizeof(int),
+                                                        cudaMemcpyDeviceToHost));
         }
-        const int *words[3] = {d.flag, split_err_word(d.split), split_dft_err_word(d.dft)};
-        for (int i = 0; i < 3; ++i)
-            if (words[i])
-                AEROS_CUDA(cudaGraphAddMemcpyNode1D(&n_f, g, &n_step, 1, d.hflag + i, words[i], sizeof(int),
-                                                    cudaMemcpyDeviceToHost));
         AEROS_CUDA(cudaGraphInstantiate(&pk.exec, g, 0));
         return AEROS_OK;
     };
@@ -1526,7 +1536,7 @@ int packed_graph(Dyn &d, const double *now_in, const double *old_in, double *now
     pk.old_out = old_out;
     pk.s = s;
     pk.gen = d.graph_gen;
-    pk.copy_kernels = mapped ? ((now_out || old_out) ? 2 : 1) : 0;
+    pk.copy_kernels = mapped ? 2 : 0;
     *out = &pk;
     return AEROS_OK;
 }

@@ -425,6 +425,38 @@ def test_step_packed_one_graph_form(gpulib, kind):
             _capi.check(lib.aeros_host_unregister(h.ctypes.data_as(ctypes.c_void_p)), "aeros_host_unregister")
 
 
+@pytest.mark.parametrize("kind", ["pinned", "host"])
+def test_step_packed_reports_nonfinite(gpulib, kind):
+    """A NaN in the packed input comes back as AEROS_ERR_NONFINITE from the
+    one-graph form (pinned arrays) and the copy form (pageable arrays); the next
+    clean call succeeds (the flag is cleared on entry)."""
+    import torch
+    from aeros_gb300._capi import AerosError, ERR_NONFINITE
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    d = AerosDyn(held_suarez_params(trunc=21, nlev=12, mass_fixer=0))
+    d.set_isothermal(264.0, 1.0e5)
+    d.step(2)
+    now, old = d.pack(*d.get_state()), d.pack(*d.get_old_state())
+
+    def buf(x):
+        if kind == "host":
+            return np.array(x)
+        t = torch.empty(x.shape, dtype=torch.complex128, pin_memory=True)
+        t.numpy()[...] = x
+        return t.numpy()
+
+    bad = now.copy()
+    bad[d.nlev * d.nlm + 7] = np.nan          # a divergence coefficient
+    nw, od, out, out_old = buf(bad), buf(old), buf(np.zeros_like(now)), buf(np.zeros_like(now))
+    with pytest.raises(AerosError) as ei:
+        d.step_packed(nw, od, 2, 1, out, out_old)
+    assert ei.value.code == ERR_NONFINITE
+    nw[...] = now
+    d.step_packed(nw, od, 2, 1, out, out_old)
+    assert np.all(np.isfinite(out))
+
+
 @pytest.mark.parametrize("trunc", [21, 42])
 def test_forced_tendency_matches_oracle(gpulib, trunc):
     """aeros_dyn_tendency_forced: the adiabatic tendencies plus the Held-Suarez forcing
