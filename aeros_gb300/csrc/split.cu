@@ -855,7 +855,9 @@ void split_destroy(SplitCtx *s) {
 // m is the fastest index, which spreads the long and short contractions.
 static int split_slots(int ngrp, int tiles, int nsm, bool *smajor) {
     *smajor = tiles >= 2 * nsm;
-    return std::max(1, std::min(ngrp, std::max(*smajor ? 4 : 1, (8 * nsm + tiles - 1) / tiles)));
+    // at most four full waves of two CTAs per SM: a grid just above a whole number
+    // of waves would leave a last wave of a few CTAs running alone
+    return std::max(1, std::min(ngrp, std::max(*smajor ? 4 : 1, 8 * nsm / tiles)));
 }
 static dim3 split_grid(int slots, int ms, int ntile, bool smajor) {
     return smajor ? dim3(slots, ms, ntile) : dim3(ms, ntile, slots);
