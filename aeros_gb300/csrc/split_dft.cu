@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
             // one thread polls the MMA barrier; the CTA barrier releases the rest
             const bool okw = tid == 0 ? mbar_wait(&mbarM, nm & 1u) : true;
             ++nm;
-            ok = __syncthreads_and(okw ? 1 : 0) && !fail;   // one verdict for the whole CTA
+            ok = __syncthreads_and(okw ? 1 : 0) && !fail;   // one outcome for the whole CTA
             asm volatile("tcgen05.fence::after_thread_sync;");
             // the table chunk the next MMA needs: the next chunk, or chunk 0 of the next tile
             if (ok && tid == 0 && nch > 1 && (ch + 1 < nch || more)) {
