@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             }
         }
         if (!ok) break;
-        // epilogue, in two rounds of 8 accumulator columns per warp: warp w
+        // epilogue, in two passes of 8 accumulator columns per warp: warp w
         // reads TMEM lane quarter w % 4 (row block P even, P odd, dP even,
         // dP odd; lane = latitude), columns 16 (w / 4) + h .. + 8, into
         // zst[row][8 (w / 4) + i] (sB with this group's stage buffer, both free
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
             }
             __syncthreads();
             {
-                const int jj = tid >> 3, u = tid & 7;            // latitude, complex column of this round
+                const int jj = tid >> 3, u = tid & 7;            // latitude, complex column of this pass
                 const int ccol = (u >> 2) * 16 + h + 2 * (u & 3); // re column; im = ccol + 1
                 const int cc = ccol >> 1;
                 const int jn = t * 32 + jj;
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncthreads();   // zst is rewritten by the next round / group
+            __syncthreads();   // zst is rewritten by the next pass / group
         }
     }
     if (!ok && tid == 0) atomicOr(a.err, 1);
