@@ -131,3 +131,39 @@ def test_device_pointers(pair):
     cb = g.analysis(fd)
     torch.cuda.synchronize()
     assert relerr(cb.cpu().numpy(), c) < 1e-13
+
+
+def test_call_argument_errors(gpulib):
+    """Per-call argument errors (batch outside 1..batch_max, null arrays, (l, m)
+    outside the truncation, packed states of the wrong count) come back as
+    status codes without device work, and the handles stay usable."""
+    import ctypes
+    from aeros_gb300 import _capi
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    L = _capi.lib()
+    s = AerosSHT(21, batch_max=2)
+    c = np.zeros((3, s.nlm), np.complex128)
+    f = np.zeros((3, s.nlat, s.nlon))
+
+    def p(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    assert L.aeros_sht_synthesis(s._h, p(c), p(f), 3) == _capi.ERR_ARG
+    assert L.aeros_sht_synthesis(s._h, p(c), p(f), 0) == _capi.ERR_ARG
+    assert L.aeros_sht_synthesis(s._h, None, p(f), 1) == _capi.ERR_ARG
+    assert L.aeros_sht_analysis(s._h, p(f), None, 1) == _capi.ERR_ARG
+    assert L.aeros_sht_lm(s._h, 0, 0) == 1
+    assert L.aeros_sht_lm(s._h, 3, 4) == -1 and L.aeros_sht_lm(s._h, 22, 0) == -1
+    c[0, 1] = 1.0
+    assert L.aeros_sht_synthesis(s._h, p(c), p(f), 1) == _capi.OK
+    assert np.abs(f[0]).max() > 0.0
+    d = AerosDyn(held_suarez_params(trunc=21, nlev=12))
+    x = np.zeros(d.state_size(), np.complex128)
+    assert L.aeros_dyn_step_packed(d._h, None, p(x), 0, 1, None, None) == _capi.ERR_ARG
+    assert L.aeros_dyn_step_packed(d._h, p(x), p(x), -1, 1, None, None) == _capi.ERR_ARG
+    with pytest.raises(ValueError):
+        d.step_packed(x[:-1], x, 0)
+    d.set_isothermal(264.0, 1.0e5)
+    d.step(1)
