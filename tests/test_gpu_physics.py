@@ -89,3 +89,26 @@ def test_hook_inside_an_ensemble_group(gpulib):
     b.step(3)
     for x, y in zip(a.get_state(), b.get_state()):
         assert np.array_equal(x, y)
+
+
+def test_hook_in_the_packed_step(gpulib):
+    """aeros_dyn_step_packed runs the hook too: between pinned arrays (one graph)
+    its two new time levels equal set_state + step + get_state, bitwise."""
+    import torch
+    ga, st = _dyn()
+    gb, _ = _dyn()
+    for g in (ga, gb):
+        g.set_relaxation(1.0 / 86400.0, 1.0 / (4 * 86400.0), 250.0)
+        g.step(2)
+    now, old, n = ga.pack(*ga.get_state()), ga.pack(*ga.get_old_state()), ga.counters()[0]
+
+    def pinned(x):
+        t = torch.empty(x.shape, dtype=torch.complex128, pin_memory=True)
+        t.numpy()[...] = x
+        return t.numpy()
+
+    hn, ho, out, out_old = pinned(now), pinned(old), pinned(np.zeros_like(now)), pinned(np.zeros_like(now))
+    gb.step_packed(hn, ho, n, 1, out, out_old)
+    ga.step(1)
+    assert np.array_equal(out, ga.pack(*ga.get_state()))
+    assert np.array_equal(out_old, ga.pack(*ga.get_old_state()))
