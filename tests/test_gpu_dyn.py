@@ -364,8 +364,9 @@ def test_step_packed_equals_the_four_calls(gpulib):
     assert b.counters()[0] == n + 3
 
 
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("kind", ["pinned", "registered", "device"])
-def test_step_packed_one_graph_form(gpulib, kind):
+def test_step_packed_one_graph_form(gpulib, kind, prec):
     """One step between pinned, registered or device buffers runs as one graph
     launch: bitwise the four-call result, through the start-up step and the
     regular one, and rebuilt when the buffers change."""
@@ -374,7 +375,7 @@ def test_step_packed_one_graph_form(gpulib, kind):
     from aeros_gb300 import _capi
     from aeros_gb300.params import held_suarez_params
     from aeros_gb300.dynamics import AerosDyn
-    p = held_suarez_params(trunc=21, nlev=12, nmember=2)
+    p = held_suarez_params(trunc=21, nlev=12, nmember=2, precision=prec)
     a = AerosDyn(p)
     a.set_isothermal(264.0, 1.0e5)
     a.hs_perturb(1.0)
