@@ -87,6 +87,9 @@ _PROTOS = {
     "aeros_dyn_set_phis": [_vp, _vp],
     "aeros_dyn_hs_perturb": [_vp, _d],
     "aeros_dyn_step": [_vp, _i],
+    "aeros_dyn_set_time": [_vp, _d],
+    "aeros_dyn_update": [_vp, _d],
+    "aeros_dyn_get_time": [_vp, _vp, _vp],
     "aeros_dyn_step_async": [_vp, _i],
     "aeros_dyn_step_packed": [_vp, _vp, _vp, _i, _i, _vp, _vp],
     "aeros_host_register": [_vp, ctypes.c_size_t],

@@ -24,6 +24,7 @@ constexpr double kGrav = 9.80665;      // :85
 constexpr double kRd = 287.05;         // :88
 constexpr double kCp = 1004.64;        // :90
 constexpr double kKappa = kRd / kCp;   // :92
+constexpr double kYearSeconds = 365.25 * 86400.0;   // year_seconds, :100
 
 void set_error(const std::string &s);
 
@@ -163,5 +164,16 @@ void launch_spec_axpy(cudaStream_t st, double2 *y, const double2 *x, int nf, con
 void launch_grid_wscale(cudaStream_t st, double *g, int nf, const Ctx &c, double f, int wp);
 int launch_laplacian(const Ctx &c, double2 *coeffs, int inverse, int nbatch);
 int launch_surface_integral(const Ctx &c, const double *field, double *partial, double *total, int nbatch);
+
+// Read-only view of a transform handle for the other translation units.
+struct ShtView {
+    const Geometry *g;
+    const DevTables *tab;
+    cudaStream_t stream;
+    long long *launches;
+    int device;      // the device current when the handle was created (its tables live there)
+    int precision;   // AEROS_PREC_*
+};
+int sht_view(aeros_sht_t h, ShtView &v);
 
 }  // namespace aeros

@@ -943,6 +943,10 @@ struct aeros_dyn_s {
     int packed_next = 0;                             // the entry replaced next
     long long graph_kernels[2] = {0, 0};
     int nstep = 0;
+    // facade clock of aeros_update (src/aeros.f90:202-241): model time [yr], the
+    // time at initialisation, and the steps taken through aeros_dyn_update
+    double time = 0.0, time_init = 0.0;
+    int facade_nstep = 0;
     std::vector<cudaEvent_t> *prof = nullptr;        // events recorded after each launch
     std::vector<std::string> *prof_names = nullptr;
     double2 *stage = nullptr;                        // host transfer staging
@@ -1815,6 +1819,45 @@ int aeros_dyn_step(aeros_dyn_t h, int nsteps) {
     int rc = aeros_dyn_step_async(h, nsteps);
     if (rc) return rc;
     return aeros_dyn_sync(h);
+}
+
+int aeros_dyn_set_time(aeros_dyn_t h, double time_init) {
+    if (!h || !std::isfinite(time_init)) return AEROS_ERR_ARG;
+    h->time_init = h->time = time_init;
+    h->facade_nstep = 0;
+    return AEROS_OK;
+}
+
+int aeros_dyn_get_time(aeros_dyn_t h, double *time, int *nstep) {
+    if (!h) return AEROS_ERR_ARG;
+    if (time) *time = h->time;
+    if (nstep) *nstep = h->facade_nstep;
+    return AEROS_OK;
+}
+
+int aeros_dyn_update(aeros_dyn_t h, double time) {
+    if (!h || !std::isfinite(time)) return AEROS_ERR_ARG;
+    if (time < h->time) {
+        set_error("aeros_dyn_update: cannot step backwards");
+        return AEROS_ERR_ARG;
+    }
+    // target step count from the absolute elapsed time, rounded half away from
+    // zero (Fortran nint), so rounding errors do not accumulate over calls
+    const double x = (time - h->time_init) * kYearSeconds / h->par.dt;
+    const double r = std::round(x);
+    if (!(std::fabs(r) < 2147483647.0)) {
+        set_error("aeros_dyn_update: step count out of range");
+        return AEROS_ERR_ARG;
+    }
+    const int target = (int)r;
+    const int ndo = target - h->facade_nstep;
+    if (ndo > 0) {
+        int rc = aeros_dyn_step(h, ndo);
+        if (rc) return rc;
+    }
+    h->facade_nstep = std::max(target, h->facade_nstep);
+    h->time = time;
+    return AEROS_OK;
 }
 
 int aeros_dyn_step_packed(aeros_dyn_t h, const double *now_in, const double *old_in, int nstep, int nsteps,

@@ -21,21 +21,16 @@
 // Set-up: the first call on a device, with that device current, resolves the
 // arrays' device addresses with cudaGetSymbolAddress (host code cannot use the
 // array names as device addresses).  Make that first call before any stream
-// capture.
+// capture.  The handle's device must be the current device at every call (the
+// addresses resolved are the current device's copies of the arrays); a call
+// made with another device current is rejected with AEROS_ERR_ARG.
+//
+// The computation is the FP64 Legendre synthesis and FFT whatever the handle's
+// precision mode: on an FP64 handle the result is aeros_sht_synthesis's.
 #include <cuda_runtime.h>
 #include <mutex>
 #include <vector>
 #include "aeros_internal.h"
-
-namespace aeros {
-struct ShtView {
-    const Geometry *g;
-    const DevTables *tab;
-    cudaStream_t stream;
-    long long *launches;
-};
-int sht_view(aeros_sht_t h, ShtView &v);
-}  // namespace aeros
 
 using namespace aeros;
 
@@ -104,6 +99,10 @@ extern "C" int aeros_sht_synthesis_noalloc(aeros_sht_t h, const double *coeffs, 
     }
     int dev = 0;
     AEROS_CUDA(cudaGetDevice(&dev));
+    if (dev != v.device) {
+        set_error("aeros_sht_synthesis_noalloc: the current device is not the handle's device");
+        return AEROS_ERR_ARG;
+    }
     Addr *a = nullptr;
     int rc = resolve(dev, a);
     if (rc) return rc;

@@ -49,6 +49,7 @@ struct aeros_sht_s {
     SplitCtx *split = nullptr;
     SplitDft *dft = nullptr;              // split form's longitude DFT products
     int *hflag = nullptr;                 // pinned host copies of the split error words (2)
+    int device = 0;                       // device current at creation: the tables live there
 
     Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches}; }
 };
@@ -275,19 +276,14 @@ int dispatch(aeros_sht_t h, int op, bool in_spec, int nin, int nout, const doubl
 namespace aeros {
 const char *last_error();
 
-// Read-only view of a handle for the other translation units of the library.
-struct ShtView {
-    const Geometry *g;
-    const DevTables *tab;
-    cudaStream_t stream;
-    long long *launches;
-};
 int sht_view(aeros_sht_t h, ShtView &v) {
     if (!h) return AEROS_ERR_ARG;
     v.g = &h->g;
     v.tab = &h->tab;
     v.stream = h->stream;
     v.launches = &h->launches;
+    v.device = h->device;
+    v.precision = h->precision;
     return AEROS_OK;
 }
 }  // namespace aeros
@@ -305,6 +301,12 @@ int aeros_sht_create(aeros_sht_t *out, int trunc, int nlon, int nlat, int batch_
     if (!out || trunc < 1 || batch_max < 1) return AEROS_ERR_ARG;
     *out = nullptr;
     aeros_sht_s *h = new aeros_sht_s;
+    if (cudaGetDevice(&h->device) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        set_error("aeros_sht_create: no CUDA device");
+        return AEROS_ERR_CUDA;
+    }
     int rc = build_geometry(h->g, trunc, nlon, nlat);
     if (rc) { delete h; return rc; }
     if ((rc = upload_tables(h->g, h->tab))) { free_tables(h->tab); delete h; return rc; }

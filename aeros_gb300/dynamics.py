@@ -41,8 +41,6 @@ class AerosDyn:
         self.gauss_w = np.zeros(self.nlat)
         L.aeros_dyn_info(h, None, None, None, None, _ptr(self.A), _ptr(self.B), _ptr(self.sigma_full),
                          _ptr(self.sinlat), _ptr(self.gauss_w))
-        self.time = 0.0
-        self.time_init = 0.0
 
     def close(self):
         if getattr(self, "_h", None):
@@ -143,17 +141,32 @@ class AerosDyn:
             out.append((nm, float(ms[i])))
         return out
 
+    @property
+    def time(self):
+        """Facade clock [yr]: the time of the last aeros_dyn_update (or set_time)."""
+        return self.facade_clock()[0]
+
+    @time.setter
+    def time(self, t):
+        self.set_time(t)
+
+    def set_time(self, time_init):
+        """Model time at initialisation [yr] (aeros_init's time_init,
+        src/aeros.f90:121-124); clears the facade's step count."""
+        _capi.check(_capi.lib().aeros_dyn_set_time(self._h, float(time_init)), "aeros_dyn_set_time")
+
+    def facade_clock(self):
+        """(time [yr], steps taken through update)."""
+        t, n = ctypes.c_double(), ctypes.c_int()
+        _capi.check(_capi.lib().aeros_dyn_get_time(self._h, ctypes.byref(t), ctypes.byref(n)), "aeros_dyn_get_time")
+        return t.value, n.value
+
     def update(self, time_years):
         """Advance to `time_years` with the step-count rule of aeros_update
-        (src/aeros.f90:202-241): n_target = nint((t - t0) yr / dt)."""
-        if time_years < self.time:
-            raise ValueError("cannot step backwards")
-        nstep = self.counters()[0]
-        x = (time_years - self.time_init) * YEAR_SECONDS / self.params.dt
-        target = int(np.sign(x) * np.floor(abs(x) + 0.5))   # Fortran nint: halves away from zero
-        if target > nstep:
-            self.step(target - nstep)
-        self.time = time_years
+        (src/aeros.f90:202-241): n_target = nint((t - t0) yr / dt), halves away
+        from zero; an earlier time raises (the reference's "cannot step
+        backwards" stop)."""
+        _capi.check(_capi.lib().aeros_dyn_update(self._h, float(time_years)), "aeros_dyn_update")
 
     def tendency(self):
         s = self._alloc()

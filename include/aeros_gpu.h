@@ -2,8 +2,9 @@
  * aeros_gpu.h -- C-ABI of the GB300 (sm_103a) spectral dynamics path.
  *
  * This is the drop-in boundary for aeros' spectral transform module and its
- * dry time step.  A Fortran host binds it with iso_c_binding (interfaces are
- * given in INTEGRATION.md); Python binds it with ctypes (aeros_gb300/_capi.py).
+ * dry time step.  A Fortran host binds it with iso_c_binding through bind(C)
+ * interfaces of these prototypes; Python binds it with ctypes
+ * (aeros_gb300/_capi.py).
  *
  * Conventions (identical to the reference arrays, so a Fortran caller passes
  * its arrays straight through):
@@ -138,13 +139,16 @@ int aeros_sht_launch_count(aeros_sht_t h, long long *count);
 /* Scalar synthesis that allocates nothing, for callers that cannot call
  * cudaMalloc (device memory owned by another allocator or reserved up front,
  * or a loop whose memory must not change once it runs).  No counterpart in
- * the reference.  Same result as aeros_sht_synthesis; coeffs and field must
- * be device pointers.  Its Fourier-row scratch (2^19 complex = 8 MiB) and
- * descriptors live in static device arrays that every GPU loading the library
- * holds until exit: nbatch <= 256 and nlat * nbatch * (T+1) <= 2^19, else
- * AEROS_ERR_ARG.  All calls share those arrays, so calls that overlap on the
- * GPU race.  The first call on a device resolves the arrays' addresses; make
- * it before any stream capture.  Synchronous. */
+ * the reference.  It always computes in FP64 (the handle's precision mode is
+ * not used): on an FP64 handle the result is aeros_sht_synthesis's.  coeffs
+ * and field must be device pointers, and the handle's device (the one current
+ * at aeros_sht_create) must be the current device, else AEROS_ERR_ARG.  Its
+ * Fourier-row scratch (2^19 complex = 8 MiB) and descriptors live in static
+ * device arrays that every GPU loading the library holds until exit:
+ * nbatch <= 256 and nlat * nbatch * (T+1) <= 2^19, else AEROS_ERR_ARG.  All
+ * calls share those arrays, so calls that overlap on the GPU race.  The first
+ * call on a device resolves the arrays' addresses; make it before any stream
+ * capture.  Synchronous. */
 int aeros_sht_synthesis_noalloc(aeros_sht_t h, const double *coeffs, double *field, int nbatch);
 
 /* ======================================================================== */
@@ -233,6 +237,20 @@ int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis);
 /* Advance every member by nsteps dynamics steps.  Replaces nsteps calls of
  * aeros_timestep_step (src/dynamics/aeros_timestep.f90:776-1137), dry path. */
 int aeros_dyn_step(aeros_dyn_t h, int nsteps);
+
+/* Facade clock (src/aeros.f90:60-124,202-241).  aeros_dyn_set_time sets the
+ * model time at initialisation [yr] (aeros_init's optional time_init; 0 at
+ * creation) and clears the facade's step count.  aeros_dyn_update advances to
+ * `time` [yr] with the reference's rule: target = nint((time - time_init) *
+ * year_seconds / dt) (halves rounded away from zero, year_seconds = 365.25 d),
+ * take target - nstep steps when positive, then nstep = max(target, nstep) and
+ * the clock reads `time`.  A time earlier than the clock is AEROS_ERR_ARG
+ * ("cannot step backwards", the reference's stop 1) and steps nothing.  Grid
+ * fields are read with aeros_dyn_diagnose, which always sees the current
+ * state.  aeros_dyn_get_time returns the clock and the facade's step count. */
+int aeros_dyn_set_time(aeros_dyn_t h, double time_init);
+int aeros_dyn_update(aeros_dyn_t h, double time);
+int aeros_dyn_get_time(aeros_dyn_t h, double *time, int *nstep);
 
 /* Enqueue nsteps steps on the handle's stream and return at once (CUDA
  * graphs; no host synchronization).  aeros_dyn_sync waits for them and

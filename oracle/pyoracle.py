@@ -79,6 +79,31 @@ def grid_size(trunc):
     return a.value, b.value
 
 
+YEAR_SECONDS = 365.25 * 86400.0   # year_seconds, src/aeros_defs.f90:100
+
+
+class OracleClock:
+    """The facade's clock of src/aeros.f90:60-124,202-241 (aeros_init's
+    time/time_init/nstep and aeros_update's step-count rule)."""
+
+    def __init__(self, dt, time_init=0.0):
+        self.dt = float(dt)
+        self.time_init = self.time = float(time_init)   # :121-123
+        self.nstep = 0                                   # :124
+
+    def update(self, time):
+        """Steps aeros_update takes to reach `time` [yr]; raises ValueError for
+        an earlier time (:212-216, "cannot step backwards", stop 1)."""
+        if time < self.time:
+            raise ValueError("cannot step backwards")
+        x = (float(time) - self.time_init) * YEAR_SECONDS / self.dt     # :220-221
+        target = int(np.sign(x) * np.floor(abs(x) + 0.5))              # nint: halves away from zero
+        ndo = target - self.nstep                                       # :222
+        self.nstep = max(target, self.nstep)                            # :228
+        self.time = float(time)                                         # :229
+        return max(ndo, 0)
+
+
 class OracleSHT:
     """CPU restatement of aeros_sht_class + the transforms of aeros_spectral."""
 

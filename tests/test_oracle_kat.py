@@ -416,3 +416,35 @@ def test_hs_perturb_formula():
                 lm = m * (2 * T + 1 - m) // 2 + l
                 exp[k - 1, lm] += amp * np.cos(3 * l + 5 * m + k) + 1j * amp * np.sin(7 * l + 2 * m + 3 * k)
     assert np.array_equal(t1, exp)
+
+
+def _exact_half_time(time_init, k, dt):
+    """A time t [yr] with (t - time_init) * year_seconds / dt == k + 0.5 exactly."""
+    from oracle.pyoracle import YEAR_SECONDS
+    t = time_init + (k + 0.5) * dt / YEAR_SECONDS
+    for _ in range(64):
+        x = (t - time_init) * YEAR_SECONDS / dt
+        if x == k + 0.5:
+            return t
+        t = np.nextafter(t, np.inf if x < k + 0.5 else -np.inf)
+    raise AssertionError("no exactly-half time found")
+
+
+def test_update_step_count_rule():
+    """aeros_update (src/aeros.f90:202-241): n_target = nint((t - t0) yr / dt),
+    halves away from zero, steps only forward, refuses an earlier time."""
+    from oracle.pyoracle import OracleClock, YEAR_SECONDS
+    dt = 1800.0
+    step = dt / YEAR_SECONDS
+    c = OracleClock(dt, time_init=0.0)
+    assert c.update(0.0) == 0 and c.nstep == 0
+    assert c.update(2.49 * step) == 2 and c.nstep == 2
+    t_half = _exact_half_time(0.0, 2, dt)
+    assert c.update(t_half) == 1 and c.nstep == 3          # 2.5 -> 3
+    assert c.update(3.49 * step) == 0 and c.nstep == 3
+    assert c.update(10.0 * step) == 7 and c.nstep == 10
+    with pytest.raises(ValueError):
+        c.update(0.0)
+    assert c.nstep == 10
+    c = OracleClock(dt, time_init=0.25)                       # aeros_init's time_init
+    assert c.update(0.25 + 1.2 * step) == 1 and c.nstep == 1
