@@ -27,6 +27,7 @@ namespace {
 
 constexpr int kMaxLev = 32;   // warp-per-coefficient solve: one lane per level
 constexpr double kNrmD = 0.39894228040143267794;   // 1/sqrt(2 pi)
+constexpr double kRsqrt4Pi = 0.28209479177387814347;   // 1/sqrt(4 pi): field mean per (0,0) coefficient
 
 // Per-level constants of the vertical coordinate (src/dynamics/aeros_vertical.f90).
 // A level is "pure" when both bounding half levels have A = 0 and the upper one
@@ -38,6 +39,7 @@ struct LevConst {
     double rdB;                   // 1 / (B1 - B0) (pure): 1/dp = rdB / ps
     double hf;                    // Held-Suarez max(0, (sigma - sigma_b)/(1 - sigma_b)) (pure)
     double kfhf;                  // Held-Suarez drag rate k_f hf (pure)
+    double dlnp_ref, alpha_ref;   // ln(p_k+1/2 / p_k-1/2) and alpha at ps = ps_ref (= dlnp, alpha when pure)
     int pure;
     int topzero;                  // p_half(k) == 0 at every ps (zero-pressure top)
 };
@@ -50,6 +52,7 @@ struct HsConst {
 struct DynConst {
     LevConst lev[kMaxLev];
     HsConst hs;
+    double phis_mean;             // mean surface geopotential (0 without one)
 };
 
 // ---------------------------------------------------------------- column kernel
@@ -65,7 +68,8 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
                                                 int nlon, int nlat, int M, const double *__restrict__ xlat,
                                                 const double *__restrict__ phis, int hs_on,
                                                 const double *__restrict__ hs_dty, const double *__restrict__ hs_ka,
-                                                const DynConst *__restrict__ dc) {
+                                                const DynConst *__restrict__ dc, const double2 *__restrict__ tspec,
+                                                int nlm) {
     constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
     const LevConst *c_lev = dc->lev;
     const HsConst &c_hs = dc->hs;
@@ -145,18 +149,31 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     }
     const double SN = sacc;
     if (act && q == 0) GO(4 * NL) = -SN / ps;
-    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474), lane by lane from the surface
+    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474), lane by lane from the surface.
+    // Beside it, the same integral of a horizontally uniform column: the level's global-mean temperature
+    // (its (0,0) coefficient / sqrt(4 pi)) over the reference pressures, from the mean surface geopotential.
+    // Phi - Phi_ref differs from Phi by a constant per level, which only the l = 0 coefficient of the
+    // (Phi + K) analysis sees and the Laplacian multiplies by zero: the divergence tendency is unchanged,
+    // but the analysis no longer carries the round-off of a 1e5 m2/s2 mean into every coefficient.
     double phh = (act && phis) ? phis[c] : 0.0;
+    double phr = phis ? dc->phis_mean : 0.0;
+    const double2 *tsp = tspec + (size_t)e * NL * nlm;
 #pragma unroll
     for (int r = LPC - 1; r >= 0; --r) {
         if (q == r)
 #pragma unroll
             LEVELS_DOWN(i) {
+                const LevConst &L = c_lev[k0 + i];
                 const double rt = kRd * GF(4 * NL + k0 + i);
-                phi[i] = fma(alpha[i], rt, phh);
+                const double rtb = kRd * (tsp[(size_t)(k0 + i) * nlm].x * kRsqrt4Pi);
+                phi[i] = fma(alpha[i], rt, phh) - fma(L.alpha_ref, rtb, phr);
                 phh = fma(rt, dlnp[i], phh);
+                phr = fma(rtb, L.dlnp_ref, phr);
             }
-        if (LPC > 1) phh = __shfl_sync(0xffffffffu, phh, base + r);
+        if (LPC > 1) {
+            phh = __shfl_sync(0xffffffffu, phh, base + r);
+            phr = __shfl_sync(0xffffffffu, phr, base + r);
+        }
     }
     if (!act) return;
     const double f = 2.0 * kOmega * xlat[j];
@@ -907,6 +924,7 @@ struct aeros_dyn_s {
     int spec_nw = 0;
     double *xlat_d = nullptr, *phis_d = nullptr;
     bool phis_set = false;
+    double phis_mean = 0.0;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
     DynConst *dconst = nullptr;                      // level and Held-Suarez constants (device)
     aeros_physics_fn phys_fn = nullptr;              // physics hook at the grid seam
@@ -1201,10 +1219,22 @@ int upload_level_consts(Dyn &d) {
             c.bfk = std::pow(bf, kKappa);
             c.hf = std::max(0.0, (bf - d.par.hs_sigma_b) / (1.0 - d.par.hs_sigma_b));
             c.kfhf = d.par.hs_k_f * c.hf;
+            c.dlnp_ref = c.dlnp;
+            c.alpha_ref = c.alpha;
+        } else {
+            const double p0 = c.A0 + c.B0 * d.ps_ref, p1 = c.A1 + c.B1 * d.ps_ref;
+            if (p0 <= 0.0) {
+                c.dlnp_ref = 0.0;
+                c.alpha_ref = std::log(2.0);
+            } else {
+                c.dlnp_ref = std::log(p1 / p0);
+                c.alpha_ref = 1.0 - (p0 / (p1 - p0)) * c.dlnp_ref;
+            }
         }
     }
     const aeros_params &p = d.par;
     DynConst dc{};
+    dc.phis_mean = d.phis_mean;
     for (int k = 0; k < n; ++k) dc.lev[k] = L[k];
     dc.hs = HsConst{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
                     std::log(p.hs_p0), 1.0 / (1.0 - p.hs_sigma_b)};
@@ -1321,7 +1351,8 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     const unsigned nb = (unsigned)((ncol * lpc + ct - 1) / ct);
     auto go = [&](auto kern) {
         kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
-                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst);
+                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
+                                      d.tmp(d.now), d.g.nlm);
     };
     if (lpc == 16) go(k_column<16>);
     else if (lpc == 8) go(k_column<8>);
@@ -1800,7 +1831,17 @@ int aeros_dyn_hs_perturb(aeros_dyn_t h, double amp) {
 
 int aeros_dyn_set_phis(aeros_dyn_t h, const double *phis) {
     if (!h || !phis) return AEROS_ERR_ARG;
-    AEROS_CUDA(cudaMemcpy(h->phis_d, phis, sizeof(double) * h->g.nlon * h->g.nlat, cudaMemcpyDefault));
+    const size_t ng = (size_t)h->g.nlon * h->g.nlat;
+    AEROS_CUDA(cudaMemcpy(h->phis_d, phis, sizeof(double) * ng, cudaMemcpyDefault));
+    {
+        std::vector<double> hp(ng);
+        AEROS_CUDA(cudaMemcpy(hp.data(), h->phis_d, sizeof(double) * ng, cudaMemcpyDeviceToHost));
+        double s = 0.0;
+        for (double v : hp) s += v;
+        h->phis_mean = s / (double)ng;
+        int rc = upload_level_consts(*h);
+        if (rc) return rc;
+    }
     if (!h->phis_set) {
         // the graphs were captured without the surface geopotential
         h->phis_set = true;

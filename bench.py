@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--t42-handles", type=int, default=3, choices=[1, 2, 3, 4, 6, 8, 12],
+                    help="handles the 96 T42L20 members are split into")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the T85/T170/T341 transform sweep")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner of the batched form")
@@ -394,55 +396,87 @@ def transport_form(args, torch):
             "cpu_oracle_ms_per_call": t_cpu * 1e3, "cpu_oracle": "numpy restatement, 1 core"}
 
 
-def batched_form(args, torch):
-    """Config of 96 uneven members: 32 x T21L16 + 32 x T31L20 + 32 x T42L20,
-    each member with its own seed and equator-pole contrast dT_y ~ U(40, 80) K,
-    stepped by one CUDA graph launch per step; FP64 and split precision.
-    Each member handle's launch shapes are chosen by the autotuner before the
-    group is built (outside the timed region).  Working set > L2, so no flush
-    is needed.  Beside it: the same members stepped one by one through the
-    single-member FP64 path (32 x the step time of one member of each
-    configuration)."""
+def build_members(cfg, prec, seed_base, tune, autotune_log):
+    """Ensemble handles: one per (T, L, n) of cfg, n members each, every member
+    with its own seed (rest, 264 K, 1000 hPa, N(0, 0.1^2) K grid noise) and
+    equator-pole contrast dT_y ~ U(40, 80) K; launch shapes autotuned outside
+    any timed region."""
     import numpy as np
-    from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
-    from aeros_gb300.dynamics import AerosDyn, AerosGroup
+    from aeros_gb300.params import held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
     from aeros_gb300.spectral import AerosSHT
-    out = {"members": "32 x T21L16 + 32 x T31L20 + 32 x T42L20", "steps": args.batched_steps}
-    cfg = [(21, 16), (31, 20), (42, 20)]
+    rng = np.random.default_rng(seed_base)
+    hs, seed = [], seed_base
+    for T, L, n in cfg:
+        d = AerosDyn(held_suarez_params(trunc=T, nlev=L, nmember=n, precision=prec))
+        sht = AerosSHT(T, batch_max=L)
+        d.set_isothermal(264.0, 1.0e5)
+        vor, div, t, lnps = d.get_state(squeeze=False)
+        t = t.copy()
+        for e in range(n):
+            r = np.random.default_rng(seed)
+            seed += 1
+            t[e] = sht.analysis(sht.synthesis(t[e]) + r.normal(0.0, 0.1, (L, d.nlat, d.nlon)))
+            d.set_member_forcing(e, rng.uniform(40.0, 80.0), 1.0 / (40.0 * 86400.0))
+        d.set_state(vor, div, t, lnps)
+        if tune:
+            b0, b1, shp = d.autotune(reps=3)
+            autotune_log[f"T{T}L{L}x{n}"] = {"ms_before": b0, "ms_after": b1, "shapes": shp}
+        hs.append(d)
+    return hs
+
+
+def time_group(hs, steps, torch):
+    from aeros_gb300.dynamics import AerosGroup
+    g = AerosGroup(hs)
+    s = torch.cuda.Stream()
+    g.set_stream(s.cuda_stream)
+    g.step_async(3)
+    g.sync()
+    n0 = g.launch_count()
+    t = time_steps(g, s, steps, torch)
+    launches = (g.launch_count() - n0) / steps
+    del g
+    return t, launches
+
+
+def batched_form(args, torch, t_single):
+    """The batching form.  (1) T42L20 ensembles: 96 members of the headline
+    configuration (each its own seed and dT_y), one CUDA graph launch per step,
+    FP64 and split precision; their aggregate SYPD over the single-member FP64
+    path's is the ratio the >= 20x target is stated for.  (2) The mixed
+    configuration of 96 uneven members, 32 x T21L16 + 32 x T31L20 + 32 x
+    T42L20, FP64 and split, beside the same members stepped one by one through
+    the single-member FP64 path (32 x the step time of one member of each
+    configuration).  Working sets > L2, so no flush is needed."""
+    from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
+    from aeros_gb300.dynamics import AerosDyn
+    out = {"steps": args.batched_steps}
+    tunelog = {}
+    # (1) T42L20 ensembles
+    nh = args.t42_handles
+    per = 96 // nh
+    t42 = {"members": f"96 x T42L20 ({nh} handles of {per})"}
     for name, prec in (("fp64", PREC_FP64), ("split", PREC_SPLIT)):
-        rng = np.random.default_rng(1000)
-        hs = []
-        for T, L in cfg:
-            d = AerosDyn(held_suarez_params(trunc=T, nlev=L, nmember=32, precision=prec))
-            sht = AerosSHT(T, batch_max=L)
-            d.set_isothermal(264.0, 1.0e5)
-            vor, div, t, lnps = d.get_state(squeeze=False)
-            t = t.copy()
-            for e in range(32):
-                r = np.random.default_rng(1000 + len(hs) * 32 + e)
-                t[e] = sht.analysis(sht.synthesis(t[e]) + r.normal(0.0, 0.1, (L, d.nlat, d.nlon)))
-                d.set_member_forcing(e, rng.uniform(40.0, 80.0), 1.0 / (40.0 * 86400.0))
-            d.set_state(vor, div, t, lnps)
-            if not args.no_tune:
-                b0, b1, shp = d.autotune(reps=3)
-                out.setdefault("autotune", {}).setdefault(name, {})[f"T{T}L{L}x32"] = {
-                    "ms_before": b0, "ms_after": b1, "shapes": shp}
-            hs.append(d)
-        g = AerosGroup(hs)
-        s = torch.cuda.Stream()
-        g.set_stream(s.cuda_stream)
-        g.step_async(3)
-        g.sync()
-        n0 = g.launch_count()
-        t = time_steps(g, s, args.batched_steps, torch)
-        out[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3,
-                     "gpu_launches_per_step": (g.launch_count() - n0) / args.batched_steps}
-        del g, hs
-    # the same 96 members one by one through the single-member FP64 path: one handle per
-    # configuration (autotuned), its step time x 32 members, summed over the configurations
+        hs = build_members([(42, 20, per)] * nh, prec, 5000, not args.no_tune, tunelog.setdefault("t42_" + name, {}))
+        t, nl = time_group(hs, args.batched_steps, torch)
+        del hs
+        t42[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "us_per_member_step": t * 1e6 / 96,
+                     "gpu_launches_per_step": nl, "vs_fp64_single": 96 * sypd(t) / sypd(t_single)}
+    out["t42l20"] = t42
+    out["vs_fp64_single_T42L20"] = t42["split"]["vs_fp64_single"]
+    # (2) the mixed configuration
+    cfg = [(21, 16, 32), (31, 20, 32), (42, 20, 32)]
+    mixed = {"members": "32 x T21L16 + 32 x T31L20 + 32 x T42L20"}
+    for name, prec in (("fp64", PREC_FP64), ("split", PREC_SPLIT)):
+        hs = build_members(cfg, prec, 1000, not args.no_tune, tunelog.setdefault("mixed_" + name, {}))
+        t, nl = time_group(hs, args.batched_steps, torch)
+        del hs
+        mixed[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "gpu_launches_per_step": nl,
+                       "vs_fp64_single_mixed": 96 * sypd(t) / sypd(t_single)}
     seq = 0.0
-    per = {}
-    for T, L in cfg:
+    perm = {}
+    for T, L, n in cfg:
         d = AerosDyn(held_suarez_params(trunc=T, nlev=L))
         d.set_isothermal(264.0, 1.0e5)
         d.hs_perturb(1.0)
@@ -453,12 +487,14 @@ def batched_form(args, torch):
         d.step_async(3)
         d.sync()
         t1 = time_steps(d, s, args.batched_steps, torch)
-        per[f"T{T}L{L}"] = t1 * 1e3
-        seq += 32 * t1
+        perm[f"T{T}L{L}"] = t1 * 1e3
+        seq += n * t1
         del d
-    out["one_by_one_fp64"] = {"sypd": 96 * sypd(seq), "ms_per_step": seq * 1e3, "ms_per_member_step": per}
+    mixed["one_by_one_fp64"] = {"sypd": 96 * sypd(seq), "ms_per_step": seq * 1e3, "ms_per_member_step": perm}
     for name in ("fp64", "split"):
-        out[name]["vs_one_by_one_fp64"] = out[name]["sypd"] / out["one_by_one_fp64"]["sypd"]
+        mixed[name]["vs_one_by_one_fp64"] = mixed[name]["sypd"] / mixed["one_by_one_fp64"]["sypd"]
+    out["mixed"] = mixed
+    out["autotune"] = tunelog
     return out
 
 
@@ -474,13 +510,14 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     import numpy as np
-    from oracle.pyoracle import OracleDyn, OracleSHT, set_threads
+    import oracle.pyoracle as po
     from aeros_gb300.params import held_suarez_params
-    cores = os.cpu_count() or 1
-    set_threads(cores)
+    cores, model = host_cpu()
+    po.use_variant("fast")
+    po.set_threads(cores)
     p = held_suarez_params(trunc=args.trunc, nlev=args.nlev)
-    o = OracleDyn(p, nthreads=cores)
-    s = OracleSHT(args.trunc)
+    o = po.OracleDyn(p, nthreads=cores)
+    s = po.OracleSHT(args.trunc)
     o.set_isothermal(264.0, 1.0e5)
     vor, div, t, lnps = o.get_state()
     rng = np.random.default_rng(0)
@@ -495,36 +532,66 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": arm_config(args, o.nlon, o.nlat, world),
-            "cpu_baseline": {"value": v, "unit": "SYPD", "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} oracle steps after {args.warmup} warm-up, OpenMP over levels"},
+            "cpu_baseline": {"value": v, "unit": "SYPD", "cores": cores, "kind": "port", "cpu_model": model,
+                             "build": "oracle/aeros_oracle.cpp, g++ -O3 -ffp-contract=fast -funroll-loops -fopenmp",
+                             "sample": f"{args.steps} oracle steps after {args.warmup} warm-up, OpenMP over "
+                                       f"levels and columns"},
             "e2e": {"value": v, "unit": "SYPD", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def cpu_baseline_sample(args):
-    """The oracle (CPU restatement) timed on this host's cores, bounded sample."""
+def host_cpu():
+    """Host core count and CPU model (lscpu), for the CPU-baseline record."""
+    import subprocess
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return os.cpu_count() or 1, model
+
+
+def oracle_step_time(args, threads, nsteps):
+    """Seconds per Held-Suarez step of the CPU oracle's timing build on `threads`
+    OpenMP threads, from the config's initial state after 3 warm-up steps."""
     import numpy as np
-    from oracle.pyoracle import OracleDyn, OracleSHT, set_threads
+    import oracle.pyoracle as po
     from aeros_gb300.params import held_suarez_params
-    cores = os.cpu_count() or 1
-    set_threads(cores)
+    po.use_variant("fast")
+    po.set_threads(threads)
     p = held_suarez_params(trunc=args.trunc, nlev=args.nlev)
-    o = OracleDyn(p, nthreads=cores)
-    s = OracleSHT(args.trunc)
+    o = po.OracleDyn(p, nthreads=threads)
+    s = po.OracleSHT(args.trunc)
     o.set_isothermal(264.0, 1.0e5)
     vor, div, t, lnps = o.get_state()
     rng = np.random.default_rng(0)
     o.set_state(vor, div, s.analysis(s.synthesis(t) + rng.normal(0, 0.1, (o.nlev, o.nlat, o.nlon))), lnps)
     o.step(3)
-    n = args.cpu_steps
     t0 = time.perf_counter()
-    o.step(n)
-    dt = (time.perf_counter() - t0) / n
-    return {"value": sypd(dt), "unit": "SYPD", "cores": cores, "kind": "port",
+    o.step(nsteps)
+    return (time.perf_counter() - t0) / nsteps
+
+
+def cpu_baseline_sample(args):
+    """The oracle (CPU restatement of the reference's algorithm, timing build:
+    -O3, fused multiply-adds, per-thread column scratch) timed on this host's
+    cores at all threads and at one thread, bounded samples."""
+    cores, model = host_cpu()
+    n = args.cpu_steps
+    dt = oracle_step_time(args, cores, n)
+    n1 = max(3, n // 6)
+    dt1 = oracle_step_time(args, 1, n1)
+    return {"value": sypd(dt), "unit": "SYPD", "cores": cores, "kind": "port", "cpu_model": model,
             "ms_per_step": dt * 1e3,
-            "sample": f"{n} Held-Suarez T{args.trunc}L{args.nlev} steps of the CPU oracle after 3 warm-up, "
-                      f"{cores} OpenMP threads"}
+            "one_thread": {"value": sypd(dt1), "unit": "SYPD", "ms_per_step": dt1 * 1e3, "steps": n1},
+            "build": "oracle/aeros_oracle.cpp, g++ -O3 -ffp-contract=fast -funroll-loops -fopenmp",
+            "sample": f"{n} Held-Suarez T{args.trunc}L{args.nlev} steps of the CPU oracle after 3 warm-up on "
+                      f"{cores} OpenMP threads (levels and columns), and {n1} steps on one thread"}
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -657,11 +724,7 @@ def run_gpu(args, rank, world, local):
         split = split_form(args, sht, dyn, flush, torch)
     batched = None
     if not args.no_batched:
-        batched = batched_form(args, torch)
-        if batched is not None:
-            for k in list(batched):
-                if isinstance(batched[k], dict) and "sypd" in batched[k]:
-                    batched[k]["vs_fp64_single"] = batched[k]["sypd"] / sypd(t_gpu)
+        batched = batched_form(args, torch, t_gpu)
 
     adjoint = None
     if not args.no_adjoint and rank == 0:

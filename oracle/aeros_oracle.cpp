@@ -551,10 +551,11 @@ inline void vgrid_alpha(const VGrid &vg, const double *ph, double *alpha, double
     }
 }
 
-inline void hydrostatic(const VGrid &vg, double phis, const double *temp, const double *ph, double *phi_full) {
+// alpha: caller's scratch of nlev entries
+inline void hydrostatic(const VGrid &vg, double phis, const double *temp, const double *ph, double *phi_full,
+                        double *alpha) {
     int n = vg.nlev;
-    std::vector<double> alpha(n);
-    vgrid_alpha(vg, ph, alpha.data(), nullptr);
+    vgrid_alpha(vg, ph, alpha, nullptr);
     double phh = phis;
     for (int k = n - 1; k >= 0; --k) {
         phi_full[k] = phh + alpha[k] * R_D * temp[k];
@@ -798,11 +799,14 @@ void tendency_grid(Dyn &d, const Spec &st) {
     const int n = d.nlev;
     bool ztop = (vg.A[0] <= 0.0 && vg.B[0] <= 0.0);
     const size_t ng = (size_t)d.nlon * d.nlat;
-#pragma omp parallel for schedule(static) num_threads(d.nthreads)
+#pragma omp parallel num_threads(d.nthreads)
+    {
+    // per-thread column scratch, every entry rewritten for each column
+    std::vector<double> ph(n + 1), pf(n), dpl(n), alpha(n), dlnp(n), cfac(n), uc(n), vc(n), tc(n), dc(n), gc(n),
+        cmass(n), scum(n + 1), mflux(n + 1), omga(n), phi(n), hal(n);
+#pragma omp for schedule(static)
     for (long c = 0; c < (long)ng; ++c) {
         int j = (int)(c / d.nlon);
-        std::vector<double> ph(n + 1), pf(n), dpl(n), alpha(n), dlnp(n), cfac(n), uc(n), vc(n), tc(n), dc(n), gc(n),
-            cmass(n), scum(n + 1), mflux(n + 1), omga(n), phi(n);
         double ps = std::exp(d.lnps_g[c]);
         vgrid_pressure(vg, ps, ph.data(), pf.data(), dpl.data());
         vgrid_alpha(vg, ph.data(), alpha.data(), dlnp.data());
@@ -826,7 +830,7 @@ void tendency_grid(Dyn &d, const Spec &st) {
         for (int k = 0; k <= n; ++k) mflux[k] = vg.B[k] * scum[n] - scum[k];
         for (int k = 0; k < n; ++k)
             omga[k] = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cmass[k]) / dpl[k];
-        hydrostatic(vg, d.phis[c], tc.data(), ph.data(), phi.data());
+        hydrostatic(vg, d.phis[c], tc.data(), ph.data(), phi.data(), hal.data());
         auto vadv = [&](const std::vector<double> &x, int k) {
             // 0-based k; mflux index k+1 is the half level below full level k.
             double lower = 0.0, upper = 0.0;
@@ -846,6 +850,7 @@ void tendency_grid(Dyn &d, const Spec &st) {
             d.dtdt[o] = -(uc[k] * d.dtdx[o] + vc[k] * d.dtdy[o]) - vt + KAPPA * tc[k] * omga[k];
         }
     }
+    }
 }
 
 // src/physics/aeros_held_suarez.f90:177-293
@@ -854,10 +859,12 @@ void hs_apply(Dyn &d) {
     const aeros_params &p = d.par;
     const int n = d.nlev;
     const size_t ng = (size_t)d.nlon * d.nlat;
-#pragma omp parallel for schedule(static) num_threads(d.nthreads)
+#pragma omp parallel num_threads(d.nthreads)
+    {
+    std::vector<double> ph(n + 1), pf(n);   // per-thread column scratch
+#pragma omp for schedule(static)
     for (long c = 0; c < (long)ng; ++c) {
         int j = (int)(c / d.nlon);
-        std::vector<double> ph(n + 1), pf(n);
         double ps = std::exp(d.lnps_g[c]);
         vgrid_pressure(vg, ps, ph.data(), pf.data(), nullptr);
         for (int k = 0; k < n; ++k) {
@@ -874,6 +881,7 @@ void hs_apply(Dyn &d) {
             d.ae[o] -= kv * d.u[o];
             d.an[o] -= kv * d.v[o];
         }
+    }
     }
 }
 

@@ -28,3 +28,10 @@ def relerr(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def truth(o, st, forced=False):
+    """Spectral tendencies of state `st` evaluated in long double by
+    oracle/truth.cpp, with oracle handle o's parameters and vertical grid."""
+    from oracle.pyoracle import truth_tendency
+    return truth_tendency(o.params, o.nlon, o.nlat, o.A, o.B, st, forced=forced)

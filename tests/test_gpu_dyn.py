@@ -1,23 +1,25 @@
 """GPU dynamics parity: the dry Held-Suarez step on the GPU (C-ABI) against
-the CPU oracle on the same seeded inputs.
+the CPU oracle on the same seeded inputs, and its tendencies against the
+same chain evaluated in long double (oracle/truth.cpp, "truth").
 
-Bars (max |gpu - oracle| / scale):
-  tendencies of vorticity, temperature, ln ps    1e-12 of max |tendency|
-  divergence tendency                            max(1e-12, 20 x the oracle's own
-      change under 1-ulp input perturbations, measured in the test): dD/dt is
-      the small residual of the Coriolis, pressure-gradient and geopotential
-      terms, so any two FP64 implementations that sum in a different order
-      differ by ~eps x that cancellation ratio relative to dD/dt itself
-      (measured: 2e-13 at T21, 7e-13 at T42 for the oracle against itself)
+Bars (max |a - b| / max |b|):
+  tendencies, GPU against truth                  1e-12 for every field
+  divergence tendency, GPU against truth         also no further from truth than
+      the FP64 oracle is: dD/dt = div(A) - lap(Phi + K) cancels several digits,
+      and the oracle (the reference's algorithm in FP64) lies 3e-12 - 1.4e-11
+      from truth; the GPU analyses Phi + K less a per-level constant, which
+      only the l = 0 coefficient sees (multiplied by zero in the Laplacian)
+  tendencies of vorticity, temperature, ln ps,   1e-12 of max |tendency|
+      GPU against oracle
   state after one step (moving state)            1e-12 for vor, T, ln ps;
-                                                 1e-11 for D (carries h dD/dt)
+                                                 1e-10 for D (carries the oracle's h dD/dt error)
   state after 10 steps                           1e-10
   mass fixer                                     target 1e-13 rel, ln r 1e-14 abs
 """
 import numpy as np
 import pytest
 
-from tests._helpers import red_spectrum, relerr
+from tests._helpers import red_spectrum, relerr, truth
 
 pytestmark = pytest.mark.gpu
 
@@ -55,32 +57,27 @@ def make_pair(trunc, nlev, **kw):
     return AerosDyn(p), OracleDyn(p), OracleSHT(trunc)
 
 
-def oracle_floor(o, st, which, reps=3):
-    """Relative change of the oracle's tendency field `which` when the input
-    state is perturbed at the last bit (its rounding sensitivity)."""
-    o.set_state(*st)
-    t0 = o.tendency()[which]
-    rng = np.random.default_rng(99)
-    worst = 0.0
-    for _ in range(reps):
-        o.set_state(*[x * (1 + 2.2e-16 * rng.standard_normal(x.shape)) for x in st])
-        worst = max(worst, relerr(o.tendency()[which], t0))
-    o.set_state(*st)
-    return worst
+def check_against_truth(tg, to, tt, label):
+    """GPU (tg) and oracle (to) tendencies against truth (tt): every GPU field
+    within 1e-12 of truth, the GPU's divergence no further from truth than the
+    oracle's, and vor, T, ln ps within 1e-12 of the oracle."""
+    eg = [relerr(a, b) for a, b in zip(tg, tt)]
+    eo = [relerr(a, b) for a, b in zip(to, tt)]
+    print(f"{label}: GPU-truth", ["%.1e" % x for x in eg], " oracle-truth", ["%.1e" % x for x in eo])
+    for i in range(4):
+        assert eg[i] < 1e-12, (label, i, eg[i])
+    assert eg[1] <= eo[1], (label, eg[1], eo[1])
+    for i in (0, 2, 3):
+        assert relerr(tg[i], to[i]) < 1e-12
 
 
-@pytest.mark.parametrize("trunc,nlev", [(21, 12), (42, 20)])
+@pytest.mark.parametrize("trunc,nlev", [(21, 12), (31, 20), (42, 20)])
 def test_adiabatic_tendency(gpulib, trunc, nlev):
     g, o, s = make_pair(trunc, nlev)
     st = moving_state(o)
     o.set_state(*st)
     g.set_state(*st)
-    tg = g.tendency()
-    to = o.tendency()
-    assert relerr(tg[0], to[0]) < 1e-12
-    assert relerr(tg[2], to[2]) < 1e-12
-    assert relerr(tg[3], to[3]) < 1e-12
-    assert relerr(tg[1], to[1]) < max(1e-12, 20 * oracle_floor(o, st, 1))
+    check_against_truth(g.tendency(), o.tendency(), truth(o, st), f"T{trunc}L{nlev} adiabatic")
 
 
 def test_rest_state_tendency(gpulib):
@@ -104,7 +101,7 @@ def test_hs_steps_match_oracle(gpulib, trunc):
     g.step(1)
     sg, so = g.get_state(), o.get_state()
     assert relerr(sg[0], so[0]) < 1e-12
-    assert relerr(sg[1], so[1]) < 1e-11
+    assert relerr(sg[1], so[1]) < 1e-10
     assert relerr(sg[2], so[2]) < 1e-12
     assert relerr(sg[3], so[3]) < 1e-12
     o.step(9)
@@ -267,11 +264,13 @@ def test_config_T31L20_480_steps(gpulib):
     g.set_state(vor, div, t, lnps)
     o.set_state(vor, div, t, lnps)
     tg, to = g.tendency(), o.tendency()
+    tt = truth(o, (vor, div, t, lnps))
     assert np.max(np.abs(tg[0] - to[0])) < 1e-20
-    e_div = relerr(tg[1], to[1])
+    e_div, o_div = relerr(tg[1], tt[1]), relerr(to[1], tt[1])
     e_t, e_p = relerr(tg[2], to[2]), relerr(tg[3], to[3])
-    print(f"T31L20 step-1 tendencies: div {e_div:.1e}  T {e_t:.1e}  lnps {e_p:.1e}")
-    assert e_t < 1e-12 and e_p < 1e-12 and e_div < 1e-11
+    print(f"T31L20 step-1 tendencies: div {e_div:.1e} from truth (oracle {o_div:.1e})  T {e_t:.1e}  lnps {e_p:.1e}")
+    assert e_t < 1e-12 and e_p < 1e-12 and e_div < 1e-12 and e_div <= o_div
+    assert relerr(tg[2], tt[2]) < 1e-12 and relerr(tg[3], tt[3]) < 1e-12
     daily = []
     for day in range(10):
         g.step(48)
@@ -468,9 +467,6 @@ def test_forced_tendency_matches_oracle(gpulib, trunc):
     g.set_state(*st)
     tg = g.tendency_forced()
     to = o.tendency(forced=True)
-    assert relerr(tg[0], to[0]) < 1e-12
-    assert relerr(tg[2], to[2]) < 1e-12
-    assert relerr(tg[3], to[3]) < 1e-12
-    assert relerr(tg[1], to[1]) < max(1e-12, 20 * oracle_floor(o, st, 1))
+    check_against_truth(tg, to, truth(o, st, forced=True), f"T{trunc}L20 forced")
     ta = g.tendency()
     assert relerr(ta[2], tg[2]) > 1e-8    # the forcing is in the forced tendency

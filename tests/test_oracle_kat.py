@@ -448,3 +448,56 @@ def test_update_step_count_rule():
     assert c.nstep == 10
     c = OracleClock(dt, time_init=0.25)                       # aeros_init's time_init
     assert c.update(0.25 + 1.2 * step) == 1 and c.nstep == 1
+
+
+def test_timing_build_matches_parity_build():
+    """The CPU baseline times the oracle's -ffp-contract=fast build; it computes
+    the same steps as the parity build (fused multiply-adds change the last bits
+    only)."""
+    import oracle.pyoracle as po
+    from aeros_gb300.params import held_suarez_params
+    p = held_suarez_params(trunc=21, nlev=8)
+    out = []
+    for variant in ("fast", "parity"):
+        po.use_variant(variant)
+        o = po.OracleDyn(p)
+        o.set_isothermal(264.0, 1.0e5)
+        o.hs_perturb(1.0)
+        o.step(4)
+        out.append(o.get_state())
+    po.use_variant("parity")
+    for a, b in zip(*out):
+        assert np.max(np.abs(a - b)) <= 1e-11 * np.max(np.abs(b))
+
+
+def test_truth_chain_is_the_oracle_chain():
+    """oracle/truth.cpp restates the tendency chain independently; in double it
+    agrees with the oracle to round-off, and the oracle lies within the FP64
+    round-off of the long double evaluation (1e-12 except the divergence, whose
+    cancellation leaves the oracle ~1e-11 from it at T42L20)."""
+    from oracle.pyoracle import OracleDyn, OracleSHT, truth_tendency
+    from aeros_gb300.params import held_suarez_params
+    for T, nl in ((21, 12), (42, 20)):
+        p = held_suarez_params(trunc=T, nlev=nl)
+        o, s = OracleDyn(p), OracleSHT(T)
+        rng = np.random.default_rng(5)
+        L, M = s.l_of_lm.astype(float), s.m_of_lm
+
+        def red(shape, amp):
+            x = (rng.standard_normal(shape + (len(L),)) + 1j * rng.standard_normal(shape + (len(L),))) * amp / (L + 1)
+            x[..., M == 0] = x[..., M == 0].real
+            return x
+        o.set_isothermal(264.0, 1.0e5)
+        _, _, t, lnps = o.get_state()
+        vor, div = red((nl,), 1e-5), red((nl,), 2e-6)
+        vor[:, 0] = div[:, 0] = 0
+        st = (vor, div, t + red((nl,), 1.0), lnps + red((), 0.01))
+        o.set_state(*st)
+        for forced in (False, True):
+            to = o.tendency(forced=forced)
+            td = truth_tendency(p, s.nlon, s.nlat, o.A, o.B, st, forced=forced, wide=False)
+            tw = truth_tendency(p, s.nlon, s.nlat, o.A, o.B, st, forced=forced, wide=True)
+            for i in range(4):
+                bar = 5e-11 if i == 1 else 1e-12
+                assert relerr(to[i], tw[i]) < bar, (T, forced, i)
+                assert relerr(td[i], tw[i]) < bar, (T, forced, i)
