@@ -81,7 +81,8 @@ struct AnaCol {
 };
 
 // per-l factor tables (device, each T+1 long)
-enum LFac { LF_ONE = 0, LF_INV_LL1 = 1, LF_LL1_A2 = 2, LF_F = 3, LF_G = 4, LF_COUNT = 5 };
+// LF_NO0: 1 except 0 at l = 0 (a field less its global mean, the (0,0) term)
+enum LFac { LF_ONE = 0, LF_INV_LL1 = 1, LF_LL1_A2 = 2, LF_F = 3, LF_G = 4, LF_NO0 = 5, LF_COUNT = 6 };
 
 // ---------------------------------------------------------------- geometry
 struct Geometry {

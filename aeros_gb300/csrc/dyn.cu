@@ -20,6 +20,7 @@
 #include "aeros_internal.h"
 #include "fft.cuh"
 #include "split.h"
+#include "df.cuh"
 
 using namespace aeros;
 
@@ -56,8 +57,10 @@ struct DynConst {
 };
 
 // ---------------------------------------------------------------- column kernel
-// Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T_k,
-// dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy.  Outputs GA[e][f][j][i]:
+// Grid fields of member e: G[e][f][j][i] with f = u_k, v_k, vor_k, div_k, T'_k,
+// dTdx_k, dTdy_k (7 nlev), lnps, dlnpsdx, dlnpsdy; T'_k = T_k - Tb_k is the
+// temperature less its level mean Tb_k = T_00,k / sqrt(4 pi) (tspec: the
+// member's spectral temperature).  Outputs GA[e][f][j][i]:
 // ae_k, an_k, ek_k, dtdt_k (4 nlev), dlnpsdt.
 // LPC lanes (adjacent in a warp) share a column, each owning a contiguous chunk
 // of levels.  The two vertical sums (mass flux from the top, geopotential from
@@ -149,31 +152,36 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     }
     const double SN = sacc;
     if (act && q == 0) GO(4 * NL) = -SN / ps;
-    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474), lane by lane from the surface.
-    // Beside it, the same integral of a horizontally uniform column: the level's global-mean temperature
-    // (its (0,0) coefficient / sqrt(4 pi)) over the reference pressures, from the mean surface geopotential.
-    // Phi - Phi_ref differs from Phi by a constant per level, which only the l = 0 coefficient of the
-    // (Phi + K) analysis sees and the Laplacian multiplies by zero: the divergence tendency is unchanged,
-    // but the analysis no longer carries the round-off of a 1e5 m2/s2 mean into every coefficient.
-    double phh = (act && phis) ? phis[c] : 0.0;
-    double phr = phis ? dc->phis_mean : 0.0;
+    // hydrostatic integral, upward (src/dynamics/aeros_vertical.f90:428-474), lane by lane from the surface,
+    // of the deviation from a horizontally uniform reference column: the level's global-mean temperature
+    // Tb_k (its (0,0) coefficient / sqrt(4 pi)) over the reference pressures p = A + B ps_ref, standing on
+    // the mean surface geopotential.  Phi'_k = Phi_k - Phi_ref,k is summed from R (T - Tb) (plus
+    // R Tb (dlnp - dlnp_ref) on levels whose dlnp depends on ps), so it carries the round-off of its own
+    // size, not that of a 1e5 m2/s2 geopotential.  Phi' differs from Phi by a constant per level, which
+    // only the l = 0 coefficient of the (Phi + K) analysis sees and the Laplacian multiplies by zero:
+    // the divergence tendency is that of Phi, with far less cancellation.
+    double phh = (act && phis) ? phis[c] - dc->phis_mean : 0.0;
     const double2 *tsp = tspec + (size_t)e * NL * nlm;
+#define TB(k) (tsp[(size_t)(k) * nlm].x * kRsqrt4Pi)
+#define TF(k) (GF(4 * NL + (k)) + TB(k))
 #pragma unroll
     for (int r = LPC - 1; r >= 0; --r) {
         if (q == r)
 #pragma unroll
             LEVELS_DOWN(i) {
                 const LevConst &L = c_lev[k0 + i];
-                const double rt = kRd * GF(4 * NL + k0 + i);
-                const double rtb = kRd * (tsp[(size_t)(k0 + i) * nlm].x * kRsqrt4Pi);
-                phi[i] = fma(alpha[i], rt, phh) - fma(L.alpha_ref, rtb, phr);
-                phh = fma(rt, dlnp[i], phh);
-                phr = fma(rtb, L.dlnp_ref, phr);
+                const double tb = TB(k0 + i);
+                const double rtd = kRd * GF(4 * NL + k0 + i);
+                if (L.pure) {
+                    phi[i] = fma(alpha[i], rtd, phh);
+                    phh = fma(rtd, dlnp[i], phh);
+                } else {
+                    const double rtb = kRd * tb;
+                    phi[i] = fma(alpha[i], rtd, phh) + rtb * (alpha[i] - L.alpha_ref);
+                    phh = fma(rtd, dlnp[i], phh) + rtb * (dlnp[i] - L.dlnp_ref);
+                }
             }
-        if (LPC > 1) {
-            phh = __shfl_sync(0xffffffffu, phh, base + r);
-            phr = __shfl_sync(0xffffffffu, phr, base + r);
-        }
+        if (LPC > 1) phh = __shfl_sync(0xffffffffu, phh, base + r);
     }
     if (!act) return;
     const double f = 2.0 * kOmega * xlat[j];
@@ -197,15 +205,15 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     LEVELS_UP(i) {
         const int k = k0 + i;
         const LevConst &L = c_lev[k];
-        const double uc = GF(k), vc = GF(NL + k), tc = GF(4 * NL + k);
+        const double uc = GF(k), vc = GF(NL + k), tc = TF(k);
         if (i == 0 && k > 0) {
             dua = uc - GF(k - 1);
             dva = vc - GF(NL + k - 1);
-            dta = tc - GF(4 * NL + k - 1);
+            dta = tc - TF(k - 1);
         }
         const bool below = k + 1 < NL;
         const double dub = below ? GF(k + 1) - uc : 0.0, dvb = below ? GF(NL + k + 1) - vc : 0.0,
-                     dtb = below ? GF(4 * NL + k + 1) - tc : 0.0;
+                     dtb = below ? TF(k + 1) - tc : 0.0;
         const double r = rdp[i];
         const double omega = cfac[i] * gc[i] - (scum[i] * dlnp[i] + alpha[i] * cm[i]) * r;
         const double mup = L.B0 * SN - scum[i];        // M at half level k (above)
@@ -252,9 +260,13 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
     }
 #undef GF
 #undef GO
+#undef TB
+#undef TF
 #undef LEVELS_UP
 #undef LEVELS_DOWN
 }
+
+#include "column_df.cuh"
 
 // ---------------------------------------------------------------- spectral kernel
 // Warp per (member, lm); lane k = level.  Semi-implicit correction form of
@@ -578,6 +590,17 @@ bool spec_cols_available(int nlev) {
 
 // The ready-made physics hook: linear relaxation of the winds and temperature
 // on the grid (aeros_physics_relaxation).
+// G's temperature slots hold T' = T - Tb; add Tb = T_00 / sqrt(4 pi) back (before a physics hook).
+__global__ void k_add_level_mean(double *__restrict__ G, const double2 *__restrict__ tspec, int NL, int M, long ng,
+                                 int nlm) {
+    const size_t n = (size_t)M * NL * ng;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t ek = i / ng, c = i - ek * ng;
+        const int e = (int)(ek / NL), k = (int)(ek - (size_t)e * NL);
+        G[((size_t)e * (7 * NL + 3) + 4 * NL + k) * ng + c] += tspec[((size_t)e * NL + k) * nlm].x * kRsqrt4Pi;
+    }
+}
+
 __global__ void k_relaxation(aeros_grid_view v, double k_drag, double k_temp, double t_ref) {
     const long long per = (long long)v.nlev * v.level_stride, n = (long long)v.nmember * per;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -927,6 +950,7 @@ struct aeros_dyn_s {
     double phis_mean = 0.0;
     double *hs_dty_d = nullptr, *hs_ka_d = nullptr;
     DynConst *dconst = nullptr;                      // level and Held-Suarez constants (device)
+    LevConstDF *ldf = nullptr;                       // the level constants as double-floats (device)
     aeros_physics_fn phys_fn = nullptr;              // physics hook at the grid seam
     void *phys_user = nullptr;
     double *mass_rows = nullptr, *mass_tgt = nullptr, *lnr_last = nullptr, *lnr_cum = nullptr;
@@ -1111,7 +1135,10 @@ int build_descriptors(Dyn &d) {
         for (int k = 0; k < NL; ++k) sp.push_back(SynCol{Dv(k), LF_ONE, R + NL + k, -1, 0});
         for (int k = 0; k < NL; ++k) spd.push_back(SynCol{V(k), LF_G, R + 2 * NL + k, R + 5 * NL + 1 + k, 0});
         for (int k = 0; k < NL; ++k) spd.push_back(SynCol{Dv(k), LF_F, R + 3 * NL + k, R + 6 * NL + 1 + k, 0});
-        for (int k = 0; k < NL; ++k) spd.push_back(SynCol{Tv(k), LF_ONE, R + 4 * NL + k, R + 7 * NL + 1 + k, 0});
+        // T less its level mean (the (0,0) term): the grid holds the deviation T' = T - Tb, which FP64
+        // represents to the round-off of the deviation, not of a 264 K temperature; the column kernels
+        // add Tb = T_00 / sqrt(4 pi) back where they need T (dT/dtheta is the same either way)
+        for (int k = 0; k < NL; ++k) spd.push_back(SynCol{Tv(k), LF_NO0, R + 4 * NL + k, R + 7 * NL + 1 + k, 0});
         spd.push_back(SynCol{Pv, LF_ONE, R + 5 * NL, R + 8 * NL + 1, 0});
         double *Ge = d.G + (size_t)e * (7 * NL + 3) * ng;
         auto GF = [&](int f) { return Ge + (size_t)f * ng; };
@@ -1243,6 +1270,31 @@ int upload_level_consts(Dyn &d) {
         if ((rc = dalloc(d.dconst, 1))) return rc;
     }
     AEROS_CUDA(cudaMemcpy(d.dconst, &dc, sizeof(dc), cudaMemcpyHostToDevice));
+    std::vector<LevConstDF> ld(n);
+    for (int k = 0; k < n; ++k) {
+        const LevConst &c = L[k];
+        LevConstDF &x = ld[k];
+        x.dB = df_host(c.dB);
+        x.B0 = df_host(c.B0);
+        x.B1 = df_host(c.B1);
+        x.alpha_ref = df_host(c.alpha_ref);
+        x.dlnp_ref = df_host(c.dlnp_ref);
+        if (c.pure) {
+            x.rdB = df_host(c.rdB);
+            x.dlnp = df_host(c.dlnp);
+            x.alpha = df_host(c.alpha);
+            x.cfac = df_host(c.cfac);
+            x.lnbf = df_host(c.lnbf);
+            x.bfk = df_host(c.bfk);
+            x.hf = df_host(c.hf);
+            x.kfhf = df_host(c.kfhf);
+        }
+    }
+    if (!d.ldf) {
+        int rc;
+        if ((rc = dalloc(d.ldf, n))) return rc;
+    }
+    AEROS_CUDA(cudaMemcpy(d.ldf, ld.data(), sizeof(LevConstDF) * n, cudaMemcpyHostToDevice));
     return AEROS_OK;
 }
 
@@ -1299,6 +1351,14 @@ int build_step_tables(Dyn &d) {
 int run_physics(Dyn &d) {
     if (!d.phys_fn) return AEROS_OK;
     const long long ng = (long long)d.g.nlon * d.g.nlat, NL = d.NL;
+    // the hook sees the temperature itself: add the level means back to the grid's T'
+    {
+        const size_t n = (size_t)d.M * NL * ng;
+        k_add_level_mean<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, d.stream>>>(
+            d.G, d.tmp(d.now), d.NL, d.M, ng, d.g.nlm);
+        ++d.launches;
+        AEROS_CUDA(cudaGetLastError());
+    }
     aeros_grid_view v{};
     v.nmember = d.M;
     v.nlev = d.NL;
@@ -1354,7 +1414,19 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
                                       d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
                                       d.tmp(d.now), d.g.nlm);
     };
-    if (lpc == 16) go(k_column<16>);
+    auto go_df = [&](auto kern) {
+        kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
+                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
+                                      d.ldf, d.tmp(d.now), d.g.nlm);
+    };
+    if (d.par.precision == AEROS_PREC_SPLIT) {
+        // split form: the column terms in double-float on the FP32/INT32 pipes
+        if (lpc == 16) go_df(k_column_df<16>);
+        else if (lpc == 8) go_df(k_column_df<8>);
+        else if (lpc == 4) go_df(k_column_df<4>);
+        else if (lpc == 2) go_df(k_column_df<2>);
+        else go_df(k_column_df<1>);
+    } else if (lpc == 16) go(k_column<16>);
     else if (lpc == 8) go(k_column<8>);
     else if (lpc == 4) go(k_column<4>);
     else if (lpc == 2) go(k_column<2>);
@@ -1639,7 +1711,7 @@ void destroy(Dyn *d) {
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
                   d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
-                  d->dconst, d->spec_wt, d->agS};
+                  d->dconst, d->ldf, d->spec_wt, d->agS};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->hflag) cudaFreeHost(d->hflag);

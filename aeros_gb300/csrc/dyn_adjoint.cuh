@@ -115,7 +115,8 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
                                                   const double *__restrict__ xlat, const double *__restrict__ phis,
                                                   int hs_on, const double *__restrict__ hs_dty,
                                                   const double *__restrict__ hs_ka, double *__restrict__ parb,
-                                                  const DynConst *__restrict__ dc) {
+                                                  const DynConst *__restrict__ dc, const double2 *__restrict__ tspec,
+                                                  int nlm) {
     const LevConst *c_lev = dc->lev;
     const HsConst &c_hs = dc->hs;
     const long ng = (long)nlon * nlat;
@@ -132,6 +133,8 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
 #define GF(f) Gf[(size_t)(f) * ng]
 #define AB(f) Ab[(size_t)(f) * ng]
 #define GB(f) Bo[(size_t)(f) * ng]
+        // G's temperature slots hold T' = T - T_00 / sqrt(4 pi) (k_column); the column is linearised about T
+#define TF(k) (GF(4 * NL + (k)) + tspec[((size_t)e * NL + (k)) * nlm].x * kRsqrt4Pi)
         const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
         const double ps = exp(lnps), rps = 1.0 / ps;
         // ---- forward recomputation (k_column)
@@ -192,11 +195,11 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
         // ---- reverse of the output loop
         for (int k = 0; k < NL; ++k) {
             const LevConst &L = c_lev[k];
-            const double uc = GF(k), vc = GF(NL + k), tc = GF(4 * NL + k);
+            const double uc = GF(k), vc = GF(NL + k), tc = TF(k);
             const double up = k > 0 ? GF(k - 1) : 0.0, vp = k > 0 ? GF(NL + k - 1) : 0.0,
-                         tp = k > 0 ? GF(4 * NL + k - 1) : 0.0;
+                         tp = k > 0 ? TF(k - 1) : 0.0;
             const double un = k + 1 < NL ? GF(k + 1) : 0.0, vn = k + 1 < NL ? GF(NL + k + 1) : 0.0,
-                         tn = k + 1 < NL ? GF(4 * NL + k + 1) : 0.0;
+                         tn = k + 1 < NL ? TF(k + 1) : 0.0;
             const double r = rdp[k];
             const double omega = cfac[k] * gc[k] - (scum[k] * dlnp[k] + alpha[k] * cm[k]) * r;
             const double mup = L.B0 * SN - scum[k], mlo = L.B1 * SN - scum[k + 1];
@@ -311,7 +314,7 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
         {
             double Pb = 0.0;
             for (int k = 0; k < NL; ++k) {
-                const double rt = kRd * GF(4 * NL + k);
+                const double rt = kRd * TF(k);
                 const double rtb = dlnp[k] * Pb + alpha[k] * phib[k];
                 dlnpb[k] += rt * Pb;
                 alphab[k] += rt * phib[k];
@@ -382,6 +385,7 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
 #undef GF
 #undef AB
 #undef GB
+#undef TF
     }
     // parameter adjoints: a 64-column block spans at most two members when the
     // grid has >= 64 points; reduce in shared memory, then one atomic each
@@ -780,7 +784,7 @@ int step_adjoint(Dyn &d, double2 *post, bool capture) {
     const long ncol = (long)d.g.nlon * d.g.nlat * d.M;
     k_column_ad<<<(unsigned)((ncol + 63) / 64), 64, 0, d.stream>>>(
         d.G, a.GAb, a.Gb, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d, d.phis_set ? d.phis_d : nullptr,
-        d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb, d.dconst);
+        d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb, d.dconst, d.tmp(d.now), d.g.nlm);
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     if ((rc = syn_adjoint(d, a.Nb))) return rc;

@@ -192,6 +192,7 @@ int upload_tables(const Geometry &g, DevTables &t) {
         lf[LF_LL1_A2 * ms + l] = ll / (kA * kA);
         lf[LF_F * ms + l] = l ? -kA / ll : 0.0;
         lf[LF_G * ms + l] = l ? kA / ll : 0.0;
+        lf[LF_NO0 * ms + l] = l ? 1.0 : 0.0;
     }
     if ((rc = upload(t.lfac, lf.data(), lf.size()))) return rc;
     const int n = g.nlon / 2;
