@@ -1,30 +1,33 @@
 // column_df.cuh -- the column kernel of the split-precision form in
-// double-float arithmetic (included by dyn.cu after k_column).
+// double-float arithmetic (included by dyn.cu, inside its unnamed namespace,
+// after k_column and df.cuh).
 //
 // The same column terms as k_column (src/dynamics/aeros_tendency.f90:475-600,
 // aeros_vertical.f90:344-474) and Held-Suarez forcing
-// (src/physics/aeros_held_suarez.f90:177-293), per grid point and level
-// evaluated with FP32-pair operations (df.cuh) on the FP32/INT32 pipes
-// instead of ~56 FP64 operations on GB300's narrow FP64 pipe.  Inputs and
-// outputs stay FP64 (converted with integer operations).  FP64 remains for
-// what is once per column (exp of ln ps, 1/ps, the Held-Suarez column
-// factors) and for levels whose pressure thickness is not a fixed fraction of
-// ps (a non-zero A: the model top), where logs of pressure ratios are taken.
-// Relative error per output ~1e-14 (48-bit significands); the tendencies stay
-// within 1e-10 of the FP64 oracle, the split form's bar.
-// Included inside dyn.cu's unnamed namespace, after df.cuh.
+// (src/physics/aeros_held_suarez.f90:177-293), evaluated with FP32-pair
+// operations (df.cuh) on the FP32/INT32 pipes instead of ~56 FP64 operations
+// per grid point and level on GB300's narrow FP64 pipe.  Inputs and outputs
+// stay FP64, converted with integer operations; the per-column exponentials,
+// logarithms and reciprocals are double-float too, so the kernel issues no
+// FP64 instruction.  Relative error per output ~1e-14 (48-bit significands);
+// the tendencies stay within 1e-10 of the FP64 oracle, the split form's bar.
 #pragma once
 
-// Per-level constants of a pure (A = 0) level as double-floats, and those every level needs.
+// Per-level constants as double-floats (the pure-level ones valid when the level is pure).
 struct LevConstDF {
-    df2 dB, B0, B1, rdB, dlnp, alpha, cfac, lnbf, bfk, hf, kfhf, alpha_ref, dlnp_ref;
+    df2 dB, A0, A1, B0, B1, rdB, dlnp, alpha, cfac, lnbf, bfk, hf, kfhf, alpha_ref, dlnp_ref;
 };
 
 __device__ __forceinline__ df2 df_shfl(df2 v, int src) {
     return df2{__shfl_sync(0xffffffffu, v.h, src), __shfl_sync(0xffffffffu, v.l, src)};
 }
 
-template <int LPC>
+// A thread per column, two passes down the column and no per-level arrays
+// (arrays of every level would live in local memory and, for a 32-member
+// ensemble, be evicted to DRAM): pass 1 sums the mass-flux divergence SN and
+// the hydrostatic sum H = sum_k R T'_k dlnp_k over the column; pass 2 carries
+// the partial sums from the top, so the flux above a level is its running sum
+// and the geopotential below it H less the running sum.
 __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G, double *__restrict__ GA, int NL,
                                                    int nlon, int nlat, int M, const double *__restrict__ xlat,
                                                    const double *__restrict__ phis, int hs_on,
@@ -32,201 +35,146 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
                                                    const double *__restrict__ hs_ka, const DynConst *__restrict__ dc,
                                                    const LevConstDF *__restrict__ ldf,
                                                    const double2 *__restrict__ tspec, int nlm) {
-    constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
     const LevConst *c_lev = dc->lev;
-    const HsConst &c_hs = dc->hs;
-    constexpr bool kUnroll = kChunk <= 8;
-#define LEVELS_UP(i) for (int i = 0; i < (kUnroll ? kChunk : nk); ++i) if (!kUnroll || i < nk)
-#define LEVELS_DOWN(i) for (int i = (kUnroll ? kChunk : nk) - 1; i >= 0; --i) if (!kUnroll || i < nk)
+    const ColConstDF &K = dc->cdf;
     const long ng = (long)nlon * nlat;
-    const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    const long gid = gt / LPC;
-    const int q = (int)(gt % LPC);
-    const int base = (threadIdx.x & 31) - q;
-    const bool act = gid < ng * M;
-    const int e = act ? (int)(gid / ng) : 0;
-    const long c = act ? gid - (long)e * ng : 0;
+    const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (gid >= ng * M) return;
+    const int e = (int)(gid / ng);
+    const long c = gid - (long)e * ng;
     const int j = (int)(c / nlon);
     const double *Gf = G + (size_t)e * (7 * NL + 3) * ng + c;
     double *Go = GA + (size_t)e * (4 * NL + 1) * ng + c;
+    const df2 z{0.0f, 0.0f};
 #define GF(f) Gf[(size_t)(f) * ng]
 #define GO(f) Go[(size_t)(f) * ng]
-#define GD(f) (act ? d2df(GF(f)) : df2{0.0f, 0.0f})
-    const int C = (NL + LPC - 1) / LPC;
-    const int k0 = min(NL, q * C), k1 = min(NL, k0 + C), nk = k1 - k0;
-    const double lnps = act ? GF(7 * NL) : 0.0;
-    const double ps = exp(lnps), rps = 1.0 / ps;
-    const df2 psd = d2df(ps), rpsd = d2df(rps), dpx = GD(7 * NL + 1), dpy = GD(7 * NL + 2);
-    df2 rdp[kChunk], dlnp[kChunk], alpha[kChunk], cfac[kChunk], gc[kChunk], cm[kChunk], scum[kChunk + 1],
-        phi[kChunk];
-#pragma unroll
-    LEVELS_UP(i) {
-        const int k = k0 + i;
-        const LevConst &L = c_lev[k];
-        const LevConstDF &Ld = ldf[k];
-        df2 d;
-        if (L.pure) {
-            d = df_mul(Ld.dB, psd);
-            rdp[i] = df_mul(Ld.rdB, rpsd);
-            dlnp[i] = Ld.dlnp;
-            alpha[i] = Ld.alpha;
-            cfac[i] = Ld.cfac;
-        } else {
-            // pressure-dependent logs in FP64, as k_column
-            const double ph0 = fma(L.B0, ps, L.A0), ph1 = fma(L.B1, ps, L.A1);
-            const double d8 = ph1 - ph0, r8 = 1.0 / d8;
-            double dl, al;
-            if (ph0 <= 0.0) {
-                al = 0.69314718055994530942;
-                dl = 0.0;
-            } else {
-                dl = log(ph1 / ph0);
-                al = 1.0 - (ph0 * r8) * dl;
-            }
-            d = d2df(d8);
-            rdp[i] = d2df(r8);
-            dlnp[i] = d2df(dl);
-            alpha[i] = d2df(al);
-            cfac[i] = d2df((ps * r8) * (L.B0 * dl + L.dB * al));
-        }
-        const df2 g = df_add(df_mul(GD(k), dpx), df_mul(GD(NL + k), dpy));
-        gc[i] = g;
-        // cm = dp D + dB ps g (on a pure level dB ps = dp)
-        cm[i] = L.pure ? df_mul(d, df_add(GD(3 * NL + k), g))
-                       : df_add(df_mul(d, GD(3 * NL + k)), df_mul(df_mul(Ld.dB, psd), g));
-    }
-    // mass flux sum from the top, lane by lane in level order
-    df2 sacc{0.0f, 0.0f};
-#pragma unroll
-    for (int r = 0; r < LPC; ++r) {
-        if (q == r) {
-#pragma unroll
-            LEVELS_UP(i) {
-                scum[i] = sacc;
-                sacc = df_add(sacc, cm[i]);
-            }
-            if (kUnroll) {
-#pragma unroll
-                for (int i = 0; i <= kChunk; ++i)
-                    if (i == nk) scum[i] = sacc;
-            } else {
-                scum[nk] = sacc;
-            }
-        }
-        if (LPC > 1) sacc = df_shfl(sacc, base + r);
-    }
-    const df2 SN = sacc;
-    if (act && q == 0) GO(4 * NL) = df2d(df_neg(df_mul(SN, rpsd)));
-    // hydrostatic integral of the deviation from the reference column (see k_column): G holds
-    // T' = T - Tb, Tb = T_00 / sqrt(4 pi) the level mean
-    df2 phh = (act && phis) ? d2df(phis[c] - dc->phis_mean) : df2{0.0f, 0.0f};
+#define GD(f) d2df(GF(f))
+    const df2 lnps = GD(7 * NL);
+    const df2 ps = df_exp(lnps), rps = df_recip(ps), dpx = GD(7 * NL + 1), dpy = GD(7 * NL + 2);
     const double2 *tsp = tspec + (size_t)e * NL * nlm;
-#define TBD(k) d2df(tsp[(size_t)(k) * nlm].x * kRsqrt4Pi)
-    const df2 kRdD = d2df(kRd);
-#pragma unroll
-    for (int r = LPC - 1; r >= 0; --r) {
-        if (q == r)
-#pragma unroll
-            LEVELS_DOWN(i) {
-                const LevConst &L = c_lev[k0 + i];
-                const LevConstDF &Ld = ldf[k0 + i];
-                const df2 rtd = df_mul(kRdD, GD(4 * NL + k0 + i));
-                phi[i] = df_fma(alpha[i], rtd, phh);
-                phh = df_fma(rtd, dlnp[i], phh);
-                if (!L.pure) {
-                    const df2 rtb = df_mul(kRdD, TBD(k0 + i));
-                    phi[i] = df_fma(rtb, df_sub(alpha[i], Ld.alpha_ref), phi[i]);
-                    phh = df_fma(rtb, df_sub(dlnp[i], Ld.dlnp_ref), phh);
-                }
-            }
-        if (LPC > 1) phh = df_shfl(phh, base + r);
-    }
-    if (!act) return;
-    // per column, FP64
-    const double x = xlat[j];
-    const df2 f = d2df(2.0 * kOmega * x);
-    const double x2 = x * x, c2 = 1.0 - x2, c4 = c2 * c2;
-    df2 kaD{0, 0}, pskD{0, 0}, GcD{0, 0}, T0D{0, 0}, K4D{0, 0};
-    double ka = 0, tbase = 0, Gc = 0, K4 = 0;
-    if (hs_on) {
-        const double dty = hs_dty[e];
-        ka = hs_ka[e];
-        const double lnpr = lnps - c_hs.lnp0;
-        tbase = c_hs.t_eq - dty * x2;
-        Gc = c_hs.dtheta_z * c2;
-        K4 = (c_hs.k_s - ka) * c4;
-        kaD = d2df(ka);
-        pskD = d2df(exp(kKappa * lnpr));   // (ps/p0)^kappa
-        GcD = d2df(Gc);
-        T0D = d2df(tbase - Gc * lnpr);
-        K4D = d2df(K4);
-    }
-    const df2 kKappaD = d2df(kKappa), tminD = d2df(c_hs.t_min);
-    // u, v, T of the current level and the next one, carried down the column
-    const df2 z{0.0f, 0.0f};
-    df2 dua = z, dva = z, dta = z;
-    df2 un = z, vn = z, tn = z;
-    if (nk > 0) {
-        un = GD(k0);
-        vn = GD(NL + k0);
-        tn = df_add(GD(4 * NL + k0), TBD(k0));
-        if (k0 > 0) {
-            dua = df_sub(un, GD(k0 - 1));
-            dva = df_sub(vn, GD(NL + k0 - 1));
-            dta = df_sub(tn, df_add(GD(4 * NL + k0 - 1), TBD(k0 - 1)));
-        }
-    }
-#pragma unroll
-    LEVELS_UP(i) {
-        const int k = k0 + i;
-        const LevConst &L = c_lev[k];
+    const df2 rs4pi = df_make(0x1.20dd76p-2f, -0x1.f7ac92p-27f);   // 1 / sqrt(4 pi)
+#define TBD(k) df_mul(d2df(tsp[(size_t)(k) * nlm].x), rs4pi)
+    // pressure geometry of level k: thickness d, 1/d, dlnp, alpha, cfac (logs only on levels with A != 0)
+    auto geom = [&](int k, df2 &d, df2 &r, df2 &dl, df2 &al, df2 &cf) {
         const LevConstDF &Ld = ldf[k];
-        const df2 uc = un, vc = vn, tc = tn;
+        if (c_lev[k].pure) {
+            d = df_mul(Ld.dB, ps);
+            r = df_mul(Ld.rdB, rps);
+            dl = Ld.dlnp;
+            al = Ld.alpha;
+            cf = Ld.cfac;
+        } else {
+            const df2 ph0 = df_add(df_mul(Ld.B0, ps), Ld.A0), ph1 = df_add(df_mul(Ld.B1, ps), Ld.A1);
+            d = df_sub(ph1, ph0);
+            r = df_recip(d);
+            if (ph0.h <= 0.0f) {
+                al = K.ln2;
+                dl = z;
+            } else {
+                dl = df_log(df_mul(ph1, df_recip(ph0)));
+                al = df_sub(df2{1.0f, 0.0f}, df_mul(df_mul(ph0, r), dl));
+            }
+            cf = df_mul(df_mul(ps, r), df_add(df_mul(Ld.B0, dl), df_mul(Ld.dB, al)));
+        }
+    };
+    // cm = dp D + dB ps g (on a pure level dB ps = dp), g = v . grad ln ps
+    auto mass = [&](int k, df2 d, df2 uc, df2 vc, df2 &g) {
+        g = df_add(df_mul(uc, dpx), df_mul(vc, dpy));
+        return c_lev[k].pure ? df_mul(d, df_add(GD(3 * NL + k), g))
+                             : df_add(df_mul(d, GD(3 * NL + k)), df_mul(df_mul(ldf[k].dB, ps), g));
+    };
+    // R T' dlnp (+ R Tb (dlnp - dlnp_ref) where dlnp depends on ps): level k's share of the
+    // hydrostatic integral of the deviation from the reference column (see k_column)
+    auto hstep = [&](int k, df2 rtd, df2 dl) {
+        df2 h = df_mul(rtd, dl);
+        if (!c_lev[k].pure) h = df_fma(df_mul(K.kRd, TBD(k)), df_sub(dl, ldf[k].dlnp_ref), h);
+        return h;
+    };
+    // pass 1: column totals
+    df2 SN = z, H = z;
+    for (int k = 0; k < NL; ++k) {
+        df2 d, r, dl, al, cf, g;
+        geom(k, d, r, dl, al, cf);
+        SN = df_add(SN, mass(k, d, GD(k), GD(NL + k), g));
+        H = df_add(H, hstep(k, df_mul(K.kRd, GD(4 * NL + k)), dl));
+    }
+    GO(4 * NL) = df2d(df_neg(df_mul(SN, rps)));
+    const df2 phs = phis ? d2df(phis[c] - dc->phis_mean) : z;
+    // per column
+    const df2 x = d2df(xlat[j]);
+    const df2 f = df_mul(K.two_omega, x);
+    const df2 x2 = df_mul(x, x), c2 = df_sub(df2{1.0f, 0.0f}, x2), c4 = df_mul(c2, c2);
+    df2 ka = z, psk = z, Gc = z, T0 = z, K4 = z, tbase = z;
+    if (hs_on) {
+        ka = d2df(hs_ka[e]);
+        const df2 lnpr = df_sub(lnps, K.lnp0);
+        tbase = df_sub(K.t_eq, df_mul(d2df(hs_dty[e]), x2));
+        Gc = df_mul(K.dtheta_z, c2);
+        K4 = df_mul(df_sub(K.k_s, ka), c4);
+        psk = df_exp(df_mul(K.kappa, lnpr));   // (ps/p0)^kappa
+        T0 = df_sub(tbase, df_mul(Gc, lnpr));
+    }
+    // pass 2, from the top: u, v, T' of the current level and the next one carried down
+    df2 scum = z, hrun = z, dua = z, dva = z, dta = z;
+    df2 un = GD(0), vn = GD(NL), tpn = GD(4 * NL), tbn = TBD(0);
+    for (int k = 0; k < NL; ++k) {
+        const LevConstDF &Ld = ldf[k];
+        const df2 uc = un, vc = vn, tp = tpn, tc = df_add(tpn, tbn);
         const bool below = k + 1 < NL;
         if (below) {
             un = GD(k + 1);
             vn = GD(NL + k + 1);
-            tn = df_add(GD(4 * NL + k + 1), TBD(k + 1));
+            tpn = GD(4 * NL + k + 1);
+            tbn = TBD(k + 1);
         }
         const df2 dub = below ? df_sub(un, uc) : z, dvb = below ? df_sub(vn, vc) : z,
-                  dtb = below ? df_sub(tn, tc) : z;
-        const df2 r = rdp[i];
-        const df2 omega = df_sub(df_mul(cfac[i], gc[i]),
-                                 df_mul(df_add(df_mul(scum[i], dlnp[i]), df_mul(alpha[i], cm[i])), r));
-        const df2 mup = df_sub(df_mul(Ld.B0, SN), scum[i]);
-        const df2 mlo = df_sub(df_mul(Ld.B1, SN), scum[i + 1]);
+                  dtb = below ? df_sub(df_add(tpn, tbn), tc) : z;
+        df2 d, r, dl, al, cf, g;
+        geom(k, d, r, dl, al, cf);
+        const df2 cm = mass(k, d, uc, vc, g);
+        // geopotential deviation: the sum below this level plus its own half layer
+        const df2 rtd = df_mul(K.kRd, tp);
+        hrun = df_add(hrun, hstep(k, rtd, dl));
+        df2 phi = df_add(df_add(phs, df_sub(H, hrun)), df_mul(al, rtd));
+        if (!c_lev[k].pure) phi = df_fma(df_mul(K.kRd, TBD(k)), df_sub(al, Ld.alpha_ref), phi);
+        const df2 scum1 = df_add(scum, cm);
+        const df2 omega = df_sub(df_mul(cf, g), df_mul(df_add(df_mul(scum, dl), df_mul(al, cm)), r));
         const df2 hr = df_scale(r, 0.5f);
-        const df2 vu = df_mul(hr, df_add(df_mul(mlo, dub), df_mul(mup, dua)));
-        const df2 vv = df_mul(hr, df_add(df_mul(mlo, dvb), df_mul(mup, dva)));
-        const df2 vt = df_mul(hr, df_add(df_mul(mlo, dtb), df_mul(mup, dta)));
+        const df2 mup = df_mul(hr, df_sub(df_mul(Ld.B0, SN), scum));    // M above / (2 dp)
+        const df2 mlo = df_mul(hr, df_sub(df_mul(Ld.B1, SN), scum1));   // M below / (2 dp)
+        scum = scum1;
+        const df2 vu = df_add(df_mul(mlo, dub), df_mul(mup, dua));
+        const df2 vv = df_add(df_mul(mlo, dvb), df_mul(mup, dva));
+        const df2 vt = df_add(df_mul(mlo, dtb), df_mul(mup, dta));
         dua = dub;
         dva = dvb;
         dta = dtb;
         const df2 zf = df_add(GD(2 * NL + k), f);
-        const df2 pgf = df_mul(df_mul(kRdD, tc), cfac[i]);
+        const df2 pgf = df_mul(df_mul(K.kRd, tc), cf);
         df2 ae = df_sub(df_sub(df_mul(zf, vc), vu), df_mul(pgf, dpx));
-        df2 an = df_sub(df_sub(df_neg(df_mul(zf, uc)), vv), df_mul(pgf, dpy));
-        const df2 ek = df_add(phi[i], df_scale(df_add(df_mul(uc, uc), df_mul(vc, vc)), 0.5f));
-        df2 dtdt = df_add(df_sub(df_neg(df_add(df_mul(uc, GD(5 * NL + k)), df_mul(vc, GD(6 * NL + k)))), vt),
-                          df_mul(df_mul(kKappaD, tc), omega));
+        df2 an = df_sub(df_neg(df_add(df_mul(zf, uc), vv)), df_mul(pgf, dpy));
+        const df2 ek = df_add(phi, df_scale(df_add(df_mul(uc, uc), df_mul(vc, vc)), 0.5f));
+        df2 dtdt = df_sub(df_mul(df_mul(K.kappa, tc), omega),
+                          df_add(df_add(df_mul(uc, GD(5 * NL + k)), df_mul(vc, GD(6 * NL + k))), vt));
         if (hs_on) {
             df2 teqn, pfk, hf, kv;
-            if (L.pure) {
-                teqn = df_sub(T0D, df_mul(GcD, Ld.lnbf));
-                pfk = df_mul(Ld.bfk, pskD);
+            if (c_lev[k].pure) {
+                teqn = df_sub(T0, df_mul(Gc, Ld.lnbf));
+                pfk = df_mul(Ld.bfk, psk);
                 hf = Ld.hf;
                 kv = Ld.kfhf;
             } else {
-                const double pf = 0.5 * (fma(L.B0, ps, L.A0) + fma(L.B1, ps, L.A1));
-                const double lnpf = log(pf / c_hs.p0);
-                teqn = d2df(tbase - Gc * lnpf);
-                pfk = d2df(exp(kKappa * lnpf));
-                const double hf8 = fmax(0.0, (pf / ps - c_hs.sigma_b) * c_hs.rsb);
-                hf = d2df(hf8);
-                kv = d2df(c_hs.k_f * hf8);
+                const df2 pf = df_scale(df_add(df_add(df_mul(Ld.B0, ps), Ld.A0), df_add(df_mul(Ld.B1, ps), Ld.A1)),
+                                        0.5f);
+                const df2 lnpf = df_log(df_mul(pf, K.rp0));
+                teqn = df_sub(tbase, df_mul(Gc, lnpf));
+                pfk = df_exp(df_mul(K.kappa, lnpf));
+                hf = df_mul(df_sub(df_mul(pf, rps), K.sigma_b), K.rsb);
+                if (hf.h < 0.0f) hf = z;
+                kv = df_mul(K.k_f, hf);
             }
-            const df2 teq = df_max(tminD, df_mul(teqn, pfk));
-            const df2 kt = df_fma(hf, K4D, kaD);
+            const df2 teq = df_max(K.t_min, df_mul(teqn, pfk));
+            const df2 kt = df_fma(hf, K4, ka);
             dtdt = df_sub(dtdt, df_mul(kt, df_sub(tc, teq)));
             ae = df_sub(ae, df_mul(kv, uc));
             an = df_sub(an, df_mul(kv, vc));
@@ -240,6 +188,4 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
 #undef GO
 #undef GD
 #undef TBD
-#undef LEVELS_UP
-#undef LEVELS_DOWN
 }

@@ -36,12 +36,12 @@ __device__ __forceinline__ df2 fast_two_sum(float a, float b) {
     const float s = __fadd_rn(a, b);
     return df2{s, __fsub_rn(b, __fsub_rn(s, a))};
 }
-// a + b with both error terms carried (the accurate double-float sum)
+// a + b: two-sum of the high parts, the low parts added to its error (the
+// "sloppy" double-float sum: error <= ~2^-47 (|a| + |b|), the FP64 error model
+// with a 48-bit significand)
 __device__ __forceinline__ df2 df_add(df2 a, df2 b) {
-    df2 s = two_sum(a.h, b.h);
-    const df2 t = two_sum(a.l, b.l);
-    s = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
-    return fast_two_sum(s.h, __fadd_rn(s.l, t.l));
+    const df2 s = two_sum(a.h, b.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
 }
 __device__ __forceinline__ df2 df_neg(df2 a) { return df2{-a.h, -a.l}; }
 __device__ __forceinline__ df2 df_sub(df2 a, df2 b) { return df_add(a, df_neg(b)); }
@@ -58,6 +58,48 @@ __device__ __forceinline__ df2 df_scale(df2 a, float s) { return df2{__fmul_rn(a
 __device__ __forceinline__ df2 df_fma(df2 a, df2 b, df2 c) { return df_add(df_mul(a, b), c); }
 __device__ __forceinline__ bool df_gt(df2 a, df2 b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
 __device__ __forceinline__ df2 df_max(df2 a, df2 b) { return df_gt(b, a) ? b : a; }
+
+// 1 / a: the float reciprocal refined by one Newton step with a double-float
+// residual (error ~2^-47).
+__device__ __forceinline__ df2 df_recip(df2 a) {
+    const float y = __frcp_rn(a.h);
+    const df2 r = df_sub(df2{1.0f, 0.0f}, df_mul(a, df2{y, 0.0f}));   // 1 - a y, |r| ~ 2^-23
+    return df_add(df2{y, 0.0f}, df_mul(df2{y, 0.0f}, r));
+}
+
+// e^x for |x| < 87: x = k ln2 + r with ln2 in three floats (k ln2_1 exact for
+// |k| < 2^11), |r| <= 0.35, e^r by its Taylor polynomial of degree 14 in
+// Horner form in double-float (truncation below 2^-60), times 2^k.
+__device__ __forceinline__ df2 df_exp(df2 x) {
+    const float k = rintf(__fmul_rn(x.h, 1.44269502f));
+    const float t = __fsub_rn(x.h, __fmul_rn(k, 0x1.62ep-1f));   // exact (Sterbenz)
+    const float p2 = __fmul_rn(k, 0x1.0bfbe8p-15f);
+    const df2 r = df_add(df_add(df2{t, 0.0f}, df2{-p2, -__fmaf_rn(k, 0x1.0bfbe8p-15f, -p2)}),
+                         df2{__fsub_rn(x.l, __fmul_rn(k, 0x1.cf79acp-40f)), 0.0f});
+    // 1/i!, i = 14 .. 3, as double-floats
+    const df2 c[12] = {{0x1.93974ap-37f, 0x1.180f94p-62f}, {0x1.612462p-33f, -0x1.8af25ep-58f},
+                       {0x1.1eed8ep-29f, 0x1.ff1b12p-54f}, {0x1.ae6456p-26f, 0x1.fd5138p-52f},
+                       {0x1.27e4fcp-22f, -0x1.10ec14p-47f}, {0x1.71de3ap-19f, 0x1.55b1ccp-45f},
+                       {0x1.a01a02p-16f, -0x1.7f97fap-42f}, {0x1.a01a02p-13f, -0x1.7f97fap-39f},
+                       {0x1.6c16c2p-10f, -0x1.27d27ep-35f}, {0x1.111112p-7f, -0x1.dddddep-32f},
+                       {0x1.555556p-5f, -0x1.555556p-30f}, {0x1.555556p-3f, -0x1.555556p-28f}};
+    df2 p = c[0];
+#pragma unroll
+    for (int i = 1; i < 12; ++i) p = df_fma(p, r, c[i]);
+    p = df_fma(p, r, df2{0.5f, 0.0f});
+    p = df_fma(p, r, df2{1.0f, 0.0f});
+    p = df_fma(p, r, df2{1.0f, 0.0f});
+    const float s = __int_as_float((int)(k + 127.0f) << 23);   // 2^k, |k| <= 126
+    return df_scale(p, s);
+}
+
+// ln a for a > 0: one Newton step on e^y = a from the float logarithm,
+// y1 = y0 + a e^-y0 - 1 (error ~2^-46).
+__device__ __forceinline__ df2 df_log(df2 a) {
+    const float y0 = logf(a.h);
+    const df2 t = df_sub(df_mul(a, df_exp(df2{-y0, 0.0f})), df2{1.0f, 0.0f});
+    return df_add(df2{y0, 0.0f}, t);
+}
 
 // FP64 -> double-float with integer operations: h = x truncated to 24
 // significant bits, l = the 29-bit remainder rounded to 24 bits (|x| error
@@ -95,6 +137,20 @@ __device__ __forceinline__ void f_split(float f, long long &m, int &E) {
     E = be - 150;
 }
 
+// z 2^E as FP64 (round to nearest, ties away; 0 below the normal range) from
+// the integer's bits; |z| < 2^63.
+__device__ __forceinline__ double i64_to_f64(long long z, int E) {
+    if (z == 0) return 0.0;
+    const unsigned long long sg = (unsigned long long)z & 0x8000000000000000ull;
+    const unsigned long long mz = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
+    const int lz = __clzll((long long)mz);
+    const unsigned long long n = mz << lz;                     // leading one at bit 63
+    const unsigned long long r = (n >> 11) + ((n >> 10) & 1);  // 53-bit mantissa, 2^53 on carry
+    const int be = 63 - lz + E + 1023;
+    if (be <= 0) return 0.0;
+    return __longlong_as_double((long long)(sg | (((unsigned long long)(be - 1) << 52) + r)));
+}
+
 // double-float -> FP64, h + l rounded to nearest (ties away) with integer
 // operations: both parts as integers on a common scale 2^(Eh - 39) (l's bits
 // below 2^-63 of h are dropped), then the FP64 bits of the sum.
@@ -115,15 +171,24 @@ __device__ __forceinline__ double df2d(df2 a) {
         if (d <= 39) z += ml * (1ll << (39 - d));
         else if (d < 63 + 39) z += ml >> (d - 39);   // arithmetic shift: floor, below double precision
     }
-    if (z == 0) return 0.0;
-    const unsigned long long sg = (unsigned long long)z & 0x8000000000000000ull;
-    const unsigned long long mz = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
-    const int lz = __clzll((long long)mz);
-    const unsigned long long n = mz << lz;                     // leading one at bit 63
-    const unsigned long long r = (n >> 11) + ((n >> 10) & 1);  // 53-bit mantissa, 2^53 on carry
-    const int be = 63 - lz + (eh - 39) + 1023;
-    if (be <= 0) return 0.0;
-    return __longlong_as_double((long long)(sg | (((unsigned long long)(be - 1) << 52) + r)));
+    return i64_to_f64(z, eh - 39);
+}
+
+// ------------------------------------------------------------ exact fixed-point dot products
+// Biased FP64 exponent field of x (0 for zero and subnormals) and the scale
+// exponent e with |x| < 2^e for a vector whose largest field is be.
+__device__ __forceinline__ int f64_bexp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
+__device__ __forceinline__ int f64_scale_exp(int be) { return be ? be - 1022 : 0; }
+
+// round(x 2^(52 - e)) for |x| < 2^e, |result| <= 2^52 (subnormals count as 0).
+__device__ __forceinline__ long long fixed53(double x, int e) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int be = (int)((bits >> 52) & 0x7FF);
+    if (be == 0) return 0;
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = e + 1023 - be;   // >= 1 because |x| < 2^e
+    const long long v = sh >= 54 ? 0 : (long long)((mant + (1ull << (sh - 1))) >> sh);
+    return (bits >> 63) ? -v : v;
 }
 #endif
 

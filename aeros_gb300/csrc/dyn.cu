@@ -50,10 +50,15 @@ struct HsConst {
 };
 // Per-handle constants in device memory (handles of different level sets or
 // forcing parameters step side by side, also concurrently inside one group graph).
+// Column constants of the double-float column kernel.
+struct ColConstDF {
+    df2 kRd, kappa, two_omega, ln2, t_eq, t_min, dtheta_z, sigma_b, rsb, rp0, lnp0, k_s, k_f;
+};
 struct DynConst {
     LevConst lev[kMaxLev];
     HsConst hs;
     double phis_mean;             // mean surface geopotential (0 without one)
+    ColConstDF cdf;
 };
 
 // ---------------------------------------------------------------- column kernel
@@ -282,6 +287,10 @@ struct SpecArgs {
     const double *GT, *TT, *WT;               // transposed [j][k] nlev x nlev
     const double *nu, *pcoef;
     const double *MinvT;                      // [l][j][k]
+    // the same matrices as 53-bit fixed-point integers split in 27 + 26-bit limbs
+    // (x = high, y = low), one scale exponent per row: the exact-product variant
+    const int2 *GTl, *TTl, *WTl, *MinvTl;
+    const int *eG, *eT, *eW, *eMinv;          // eMinv: [l][k]
     const double *dfac;                       // (T+1) diffusion factor for this h
     const int *l_of_lm;
     int nlm, NL, M, T;
@@ -422,25 +431,46 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
 // the products' NLT accumulators in registers, so 16 warps fit on an SM.  The
 // arithmetic and its order are those of k_spectral: every level product runs
 // j = 0 .. nlev-1 from zero, the nu . e sum is the warp butterfly's tree.
+//
+// EXACT (the split form): the four level products are exact fixed-point dot
+// products on the integer pipes -- each matrix row and each vector scaled by a
+// power of two to 53-bit integers, split in 27 + 26-bit limbs, the limb
+// products summed in int64 (IMAD.WIDE) and the sum rounded once to FP64 -- so
+// a product costs no FP64 instruction and is at least as accurate as the FP64
+// FMA chain (error below 2^-51 of |row| |vector| instead of ~20 2^-53).  The
+// matrices keep their FP64 values (limbs are exact); the leapfrog, semi-
+// implicit combination, diffusion and RAW filter around them stay FP64.
 template <int NLT>
 __host__ __device__ constexpr size_t spec_cols_smem(int threads) {
-    return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads);
+    return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads) + sizeof(int) * 4 * NLT;
 }
 
-template <int NLT>
+template <int NLT, bool EXACT>
 __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
     extern __shared__ double sm_cols[];
     double *sG = sm_cols, *sT = sG + NLT * NLT, *sW = sT + NLT * NLT, *sNu = sW + NLT * NLT, *sPc = sNu + NLT;
     double *v1 = sPc + NLT + threadIdx.x, *v2 = v1 + NLT * blockDim.x;   // slot k at [k * blockDim.x]
     const int nt = blockDim.x;
+    int *sE = reinterpret_cast<int *>(sPc + NLT + 2 * NLT * nt);         // row exponents of G, tau, W
     for (int i = threadIdx.x; i < NLT * NLT; i += nt) {
-        sG[i] = a.GT[i];
-        sT[i] = a.TT[i];
-        sW[i] = a.WT[i];
+        if (EXACT) {
+            reinterpret_cast<int2 *>(sG)[i] = a.GTl[i];
+            reinterpret_cast<int2 *>(sT)[i] = a.TTl[i];
+            reinterpret_cast<int2 *>(sW)[i] = a.WTl[i];
+        } else {
+            sG[i] = a.GT[i];
+            sT[i] = a.TT[i];
+            sW[i] = a.WT[i];
+        }
     }
     for (int i = threadIdx.x; i < NLT; i += nt) {
         sNu[i] = a.nu[i];
         sPc[i] = a.pcoef[i];
+        if (EXACT) {
+            sE[i] = a.eG[i];
+            sE[NLT + i] = a.eT[i];
+            sE[2 * NLT + i] = a.eW[i];
+        }
     }
     __syncthreads();
     const int warp = (blockIdx.x * nt + threadIdx.x) >> 5;
@@ -466,7 +496,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
         xw -= a.raw_beta * dx;
     };
     // acc[k] = sum_j P[k][j] v[j], j ascending; P[k][j] at P[j * NLT + k]
-    auto product = [&](const double *P, const double *v, double *acc) {
+    auto product_fp64 = [&](const double *P, const double *v, double *acc) {
 #pragma unroll
         for (int k = 0; k < NLT; ++k) acc[k] = 0.0;
 #pragma unroll
@@ -474,6 +504,45 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const double vj = v[j * nt];
 #pragma unroll
             for (int k = 0; k < NLT; ++k) acc[k] += P[j * NLT + k] * vj;
+        }
+    };
+    // the same product exactly in fixed point: P[k][j] = (x 2^26 + y) 2^(eP[k] - 52) at PL[j * NLT + k]
+    auto product_exact = [&](const int2 *PL, const int *eP, const double *v, double *acc) {
+        int be = 0;
+#pragma unroll
+        for (int j = 0; j < NLT; ++j) be = max(be, f64_bexp(v[j * nt]));
+        const int ex = f64_scale_exp(be);
+        int b1[NLT], b0[NLT];
+#pragma unroll
+        for (int j = 0; j < NLT; ++j) {
+            const long long b = fixed53(v[j * nt], ex);
+            b1[j] = (int)(b >> 26);
+            b0[j] = (int)(b & 0x3FFFFFF);
+        }
+#pragma unroll 4
+        for (int k = 0; k < NLT; ++k) {
+            long long s2 = 0, s1 = 0, s0 = 0;
+#pragma unroll
+            for (int j = 0; j < NLT; ++j) {
+                const int2 p = PL[j * NLT + k];
+                s2 += (long long)p.x * b1[j];
+                s1 += (long long)p.x * b0[j] + (long long)p.y * b1[j];
+                s0 += (long long)p.y * b0[j];
+            }
+            acc[k] = i64_to_f64(s2 + ((s1 + (s0 >> 26)) >> 26), eP[k] + ex - 52);
+        }
+    };
+    // which: 0 G, 1 tau, 2 W, 3 the inverse of degree l
+    auto product = [&](int which, const double *v, double *acc) {
+        if (EXACT) {
+            if (which == 3)
+                product_exact(a.MinvTl + (size_t)l * NLT * NLT, a.eMinv + (size_t)l * NLT, v, acc);
+            else
+                product_exact(reinterpret_cast<const int2 *>(which == 0 ? sG : which == 1 ? sT : sW),
+                              sE + which * NLT, v, acc);
+        } else {
+            product_fp64(which == 0 ? sG : which == 1 ? sT : which == 2 ? sW : a.MinvT + (size_t)l * NLT * NLT, v,
+                         acc);
         }
     };
     bool bad = false;
@@ -503,7 +572,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const size_t o = o0 + k * ls;
             v1[k * nt] = tm_o[o] - tm[o] + a.astep * tt[o];
         }
-        product(sG, v1, acc);             // G y
+        product(0, v1, acc);              // G y
 #pragma unroll
         for (int k = 0; k < NLT; ++k) v2[k * nt] = acc[k];
 #pragma unroll 4
@@ -511,14 +580,14 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const size_t o = o0 + k * ls;
             v1[k * nt] = ha * dv[o] - a.hh_old * dv_o[o];
         }
-        product(sW, v1, acc);             // W x; v2 becomes the right-hand side
+        product(2, v1, acc);              // W x; v2 becomes the right-hand side
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
             const size_t o = o0 + k * ls;
             const double pc = sPc[k];
             v2[k * nt] = dv_o[o] + h * td[o] + hl * (v2[k * nt] + pc * pz) + lam * acc[k];
         }
-        product(a.MinvT + (size_t)l * NLT * NLT, v2, acc);   // D^(n+1)
+        product(3, v2, acc);              // D^(n+1)
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {   // v1 = e = D-bar - D^n
             const size_t o = o0 + k * ls;
@@ -532,7 +601,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             dv_o[o] = dnow;
             dv[o] = dw;
         }
-        product(sT, v1, acc);             // tau e
+        product(1, v1, acc);              // tau e
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
             const size_t o = o0 + k * ls;
@@ -942,6 +1011,9 @@ struct aeros_dyn_s {
     double *G = nullptr, *GA = nullptr, *D = nullptr;          // grid fields, rhs, diagnostics
     double *GT_d = nullptr, *TT_d = nullptr, *WT_d = nullptr, *nu_d = nullptr, *pc_d = nullptr;
     double *Minv_d[2] = {nullptr, nullptr};                    // h = dt, 2 dt
+    int2 *GTl_d = nullptr, *TTl_d = nullptr, *WTl_d = nullptr;  // fixed-point limbs (exact products)
+    int2 *MinvL_d[2] = {nullptr, nullptr};
+    int *eG_d = nullptr, *eT_d = nullptr, *eW_d = nullptr, *eMinv_d[2] = {nullptr, nullptr};
     double *dfac_d[2] = {nullptr, nullptr};
     int2 *spec_wt = nullptr;                                   // column-layout spectral warps: (l, first column)
     int spec_nw = 0;
@@ -1262,6 +1334,10 @@ int upload_level_consts(Dyn &d) {
     const aeros_params &p = d.par;
     DynConst dc{};
     dc.phis_mean = d.phis_mean;
+    dc.cdf = ColConstDF{df_host(kRd), df_host(kKappa), df_host(2.0 * kOmega), df_host(0.69314718055994530942),
+                        df_host(p.hs_t_equator), df_host(p.hs_t_min), df_host(p.hs_dtheta_z), df_host(p.hs_sigma_b),
+                        df_host(1.0 / (1.0 - p.hs_sigma_b)), df_host(1.0 / p.hs_p0), df_host(std::log(p.hs_p0)),
+                        df_host(p.hs_k_s), df_host(p.hs_k_f)};
     for (int k = 0; k < n; ++k) dc.lev[k] = L[k];
     dc.hs = HsConst{p.hs_t_equator, p.hs_t_min, p.hs_dtheta_z, p.hs_sigma_b, p.hs_p0, p.hs_k_s, p.hs_k_f,
                     std::log(p.hs_p0), 1.0 / (1.0 - p.hs_sigma_b)};
@@ -1275,6 +1351,8 @@ int upload_level_consts(Dyn &d) {
         const LevConst &c = L[k];
         LevConstDF &x = ld[k];
         x.dB = df_host(c.dB);
+        x.A0 = df_host(c.A0);
+        x.A1 = df_host(c.A1);
         x.B0 = df_host(c.B0);
         x.B1 = df_host(c.B1);
         x.alpha_ref = df_host(c.alpha_ref);
@@ -1340,9 +1418,57 @@ int build_step_tables(Dyn &d) {
         for (int c = 0; c < 2 * d.M * (l + 1); c += 32) wt.push_back(make_int2(l, c));
     d.spec_nw = (int)wt.size();
     if ((rc = dput(d.spec_wt, wt))) return rc;
-    if (d.NL == 16) rc = raise_smem_limit((const void *)k_spectral_cols<16>, spec_cols_smem<16>(256));
-    if (d.NL == 20) rc = raise_smem_limit((const void *)k_spectral_cols<20>, spec_cols_smem<20>(256));
-    if (rc) return rc;
+    // fixed-point limbs of the same matrices for the exact-product variant
+    auto limbs = [&](const std::vector<double> &PT, int nmat, std::vector<int2> &L, std::vector<int> &E) {
+        L.resize((size_t)nmat * n * n);
+        E.resize((size_t)nmat * n);
+        for (int m = 0; m < nmat; ++m)
+            for (int k = 0; k < n; ++k) {
+                int ea = -100000;
+                for (int j = 0; j < n; ++j) {
+                    const double x = PT[((size_t)m * n + j) * n + k];
+                    if (x != 0.0) {
+                        int e;
+                        std::frexp(x, &e);   // |x| < 2^e
+                        ea = std::max(ea, e);
+                    }
+                }
+                if (ea == -100000) ea = 0;   // an all-zero row: any exponent works
+                E[(size_t)m * n + k] = ea;
+                for (int j = 0; j < n; ++j) {
+                    const double x = PT[((size_t)m * n + j) * n + k];
+                    const long long v = std::llround(std::ldexp(x, 52 - ea));
+                    const long long hi = v >> 26;   // floor
+                    L[((size_t)m * n + j) * n + k] = make_int2((int)hi, (int)(v - hi * (1ll << 26)));
+                }
+            }
+    };
+    {
+        std::vector<int2> L;
+        std::vector<int> E;
+        limbs(GT, 1, L, E);
+        if ((rc = dput(d.GTl_d, L)) || (rc = dput(d.eG_d, E))) return rc;
+        limbs(TT, 1, L, E);
+        if ((rc = dput(d.TTl_d, L)) || (rc = dput(d.eT_d, E))) return rc;
+        limbs(WT, 1, L, E);
+        if ((rc = dput(d.WTl_d, L)) || (rc = dput(d.eW_d, E))) return rc;
+        for (int s = 0; s < 2; ++s) {
+            std::vector<double> mi((size_t)(T + 1) * n * n);
+            AEROS_CUDA(cudaMemcpy(mi.data(), d.Minv_d[s], mi.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            limbs(mi, T + 1, L, E);
+            if ((rc = dput(d.MinvL_d[s], L)) || (rc = dput(d.eMinv_d[s], E))) return rc;
+        }
+    }
+    if (d.NL == 16) {
+        if ((rc = raise_smem_limit((const void *)k_spectral_cols<16, false>, spec_cols_smem<16>(256))) ||
+            (rc = raise_smem_limit((const void *)k_spectral_cols<16, true>, spec_cols_smem<16>(256))))
+            return rc;
+    }
+    if (d.NL == 20) {
+        if ((rc = raise_smem_limit((const void *)k_spectral_cols<20, false>, spec_cols_smem<20>(256))) ||
+            (rc = raise_smem_limit((const void *)k_spectral_cols<20, true>, spec_cols_smem<20>(256))))
+            return rc;
+    }
     return AEROS_OK;
 }
 
@@ -1414,18 +1540,14 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
                                       d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
                                       d.tmp(d.now), d.g.nlm);
     };
-    auto go_df = [&](auto kern) {
-        kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
+    auto go_df = [&](auto kern, unsigned nbd) {
+        kern<<<nbd, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
                                       d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
                                       d.ldf, d.tmp(d.now), d.g.nlm);
     };
     if (d.par.precision == AEROS_PREC_SPLIT) {
-        // split form: the column terms in double-float on the FP32/INT32 pipes
-        if (lpc == 16) go_df(k_column_df<16>);
-        else if (lpc == 8) go_df(k_column_df<8>);
-        else if (lpc == 4) go_df(k_column_df<4>);
-        else if (lpc == 2) go_df(k_column_df<2>);
-        else go_df(k_column_df<1>);
+        // split form: the column terms in double-float on the FP32/INT32 pipes, a thread per column
+        go_df(k_column_df, (unsigned)((ncol + ct - 1) / ct));
     } else if (lpc == 16) go(k_column<16>);
     else if (lpc == 8) go(k_column<8>);
     else if (lpc == 4) go(k_column<4>);
@@ -1495,12 +1617,23 @@ int enqueue_step(Dyn &d, bool startup) {
     a.raw_on = (!startup && d.par.eps_filter > 0.0) ? 1 : 0;
     a.flag = d.flag;
     const int sw = d.tune.spec_warps;
-    if (d.tune.spec_cols && spec_cols_available(d.NL)) {
+    a.GTl = d.GTl_d; a.TTl = d.TTl_d; a.WTl = d.WTl_d; a.MinvTl = d.MinvL_d[s];
+    a.eG = d.eG_d; a.eT = d.eT_d; a.eW = d.eW_d; a.eMinv = d.eMinv_d[s];
+    // the split form takes the exact-product column layout wherever it exists
+    const bool exact = d.par.precision == AEROS_PREC_SPLIT && spec_cols_available(d.NL);
+    if ((d.tune.spec_cols || exact) && spec_cols_available(d.NL)) {
         const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
-        if (d.NL == 16)
-            k_spectral_cols<16><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-        else
-            k_spectral_cols<20><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        if (d.NL == 16) {
+            if (exact)
+                k_spectral_cols<16, true><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+            else
+                k_spectral_cols<16, false><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        } else {
+            if (exact)
+                k_spectral_cols<20, true><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+            else
+                k_spectral_cols<20, false><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        }
     } else {
         long nw = (long)d.g.nlm * d.M;
         k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
@@ -1711,7 +1844,8 @@ void destroy(Dyn *d) {
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
                   d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
-                  d->dconst, d->ldf, d->spec_wt, d->agS};
+                  d->dconst, d->ldf, d->spec_wt, d->agS, d->GTl_d, d->TTl_d, d->WTl_d, d->MinvL_d[0],
+                  d->MinvL_d[1], d->eG_d, d->eT_d, d->eW_d, d->eMinv_d[0], d->eMinv_d[1]};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (d->hflag) cudaFreeHost(d->hflag);
