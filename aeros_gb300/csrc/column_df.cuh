@@ -25,9 +25,11 @@ __device__ __forceinline__ df2 df_shfl(df2 v, int src) {
 // A thread per column, two passes down the column and no per-level arrays
 // (arrays of every level would live in local memory and, for a 32-member
 // ensemble, be evicted to DRAM): pass 1 sums the mass-flux divergence SN and
-// the hydrostatic sum H = sum_k R T'_k dlnp_k over the column; pass 2 carries
-// the partial sums from the top, so the flux above a level is its running sum
-// and the geopotential below it H less the running sum.
+// the hydrostatic sum H = sum_k R T'_k dlnp_k over the column (in FP64: a few
+// operations per level on the FP64 pipe, which the double-float work leaves
+// idle); pass 2 carries the partial sums from the top, so the flux above a
+// level is its running sum and the geopotential below it H less the running
+// sum.
 __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G, double *__restrict__ GA, int NL,
                                                    int nlon, int nlat, int M, const double *__restrict__ xlat,
                                                    const double *__restrict__ phis, int hs_on,
@@ -78,10 +80,9 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
         }
     };
     // cm = dp D + dB ps g (on a pure level dB ps = dp), g = v . grad ln ps
-    auto mass = [&](int k, df2 d, df2 uc, df2 vc, df2 &g) {
+    auto mass = [&](int k, df2 d, df2 uc, df2 vc, df2 D, df2 &g) {
         g = df_add(df_mul(uc, dpx), df_mul(vc, dpy));
-        return c_lev[k].pure ? df_mul(d, df_add(GD(3 * NL + k), g))
-                             : df_add(df_mul(d, GD(3 * NL + k)), df_mul(df_mul(ldf[k].dB, ps), g));
+        return c_lev[k].pure ? df_mul(d, df_add(D, g)) : df_add(df_mul(d, D), df_mul(df_mul(ldf[k].dB, ps), g));
     };
     // R T' dlnp (+ R Tb (dlnp - dlnp_ref) where dlnp depends on ps): level k's share of the
     // hydrostatic integral of the deviation from the reference column (see k_column)
@@ -90,13 +91,27 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
         if (!c_lev[k].pure) h = df_fma(df_mul(K.kRd, TBD(k)), df_sub(dl, ldf[k].dlnp_ref), h);
         return h;
     };
-    // pass 1: column totals
-    df2 SN = z, H = z;
-    for (int k = 0; k < NL; ++k) {
-        df2 d, r, dl, al, cf, g;
-        geom(k, d, r, dl, al, cf);
-        SN = df_add(SN, mass(k, d, GD(k), GD(NL + k), g));
-        H = df_add(H, hstep(k, df_mul(K.kRd, GD(4 * NL + k)), dl));
+    // pass 1: column totals, in FP64 on the otherwise idle FP64 pipe (a few operations per level)
+    df2 SN, H;
+    {
+        const double ps8 = exp(GF(7 * NL)), dpx8 = GF(7 * NL + 1), dpy8 = GF(7 * NL + 2);
+        double sn = 0.0, h8 = 0.0;
+        for (int k = 0; k < NL; ++k) {
+            const LevConst &L = c_lev[k];
+            const double g = GF(k) * dpx8 + GF(NL + k) * dpy8;
+            const double rt = kRd * GF(4 * NL + k);
+            if (L.pure) {
+                sn = fma(L.dB * ps8, GF(3 * NL + k) + g, sn);
+                h8 = fma(rt, L.dlnp, h8);
+            } else {
+                const double ph0 = fma(L.B0, ps8, L.A0), ph1 = fma(L.B1, ps8, L.A1);
+                const double dl = ph0 <= 0.0 ? 0.0 : log(ph1 / ph0);
+                sn += (ph1 - ph0) * GF(3 * NL + k) + L.dB * ps8 * g;
+                h8 = fma(rt, dl, h8) + kRd * (tsp[(size_t)k * nlm].x * kRsqrt4Pi) * (dl - L.dlnp_ref);
+            }
+        }
+        SN = d2df(sn);
+        H = d2df(h8);
     }
     GO(4 * NL) = df2d(df_neg(df_mul(SN, rps)));
     const df2 phs = phis ? d2df(phis[c] - dc->phis_mean) : z;
@@ -114,24 +129,31 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
         psk = df_exp(df_mul(K.kappa, lnpr));   // (ps/p0)^kappa
         T0 = df_sub(tbase, df_mul(Gc, lnpr));
     }
-    // pass 2, from the top: u, v, T' of the current level and the next one carried down
+    // pass 2, from the top: u, v, T' of the current level and the next one carried down; the
+    // level's vorticity, divergence and temperature gradient loaded one level ahead
     df2 scum = z, hrun = z, dua = z, dva = z, dta = z;
     df2 un = GD(0), vn = GD(NL), tpn = GD(4 * NL), tbn = TBD(0);
+    double vo8 = GF(2 * NL), dv8 = GF(3 * NL), tx8 = GF(5 * NL), ty8 = GF(6 * NL);
     for (int k = 0; k < NL; ++k) {
         const LevConstDF &Ld = ldf[k];
         const df2 uc = un, vc = vn, tp = tpn, tc = df_add(tpn, tbn);
+        const double vo = vo8, dv = dv8, tx = tx8, ty = ty8;
         const bool below = k + 1 < NL;
         if (below) {
             un = GD(k + 1);
             vn = GD(NL + k + 1);
             tpn = GD(4 * NL + k + 1);
             tbn = TBD(k + 1);
+            vo8 = GF(2 * NL + k + 1);
+            dv8 = GF(3 * NL + k + 1);
+            tx8 = GF(5 * NL + k + 1);
+            ty8 = GF(6 * NL + k + 1);
         }
         const df2 dub = below ? df_sub(un, uc) : z, dvb = below ? df_sub(vn, vc) : z,
                   dtb = below ? df_sub(df_add(tpn, tbn), tc) : z;
         df2 d, r, dl, al, cf, g;
         geom(k, d, r, dl, al, cf);
-        const df2 cm = mass(k, d, uc, vc, g);
+        const df2 cm = mass(k, d, uc, vc, d2df(dv), g);
         // geopotential deviation: the sum below this level plus its own half layer
         const df2 rtd = df_mul(K.kRd, tp);
         hrun = df_add(hrun, hstep(k, rtd, dl));
@@ -149,13 +171,13 @@ __global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G,
         dua = dub;
         dva = dvb;
         dta = dtb;
-        const df2 zf = df_add(GD(2 * NL + k), f);
+        const df2 zf = df_add(d2df(vo), f);
         const df2 pgf = df_mul(df_mul(K.kRd, tc), cf);
         df2 ae = df_sub(df_sub(df_mul(zf, vc), vu), df_mul(pgf, dpx));
         df2 an = df_sub(df_neg(df_add(df_mul(zf, uc), vv)), df_mul(pgf, dpy));
         const df2 ek = df_add(phi, df_scale(df_add(df_mul(uc, uc), df_mul(vc, vc)), 0.5f));
         df2 dtdt = df_sub(df_mul(df_mul(K.kappa, tc), omega),
-                          df_add(df_add(df_mul(uc, GD(5 * NL + k)), df_mul(vc, GD(6 * NL + k))), vt));
+                          df_add(df_add(df_mul(uc, d2df(tx)), df_mul(vc, d2df(ty))), vt));
         if (hs_on) {
             df2 teqn, pfk, hf, kv;
             if (c_lev[k].pure) {

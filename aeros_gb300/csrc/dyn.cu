@@ -204,21 +204,23 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
         T0 = tbase - Gc * lnpr;
         K4 = (c_hs.k_s - ka) * c4;
     }
-    // x_k - x_{k-1} of u, v, T: the difference below a level is the one above the next
-    double dua = 0.0, dva = 0.0, dta = 0.0;
+    // x_k - x_{k-1} of u, v, T: the difference below a level is the one above the next;
+    // T of the next level is carried to the next iteration
+    double dua = 0.0, dva = 0.0, dta = 0.0, tn = nk > 0 ? TF(k0) : 0.0;
 #pragma unroll
     LEVELS_UP(i) {
         const int k = k0 + i;
         const LevConst &L = c_lev[k];
-        const double uc = GF(k), vc = GF(NL + k), tc = TF(k);
+        const double uc = GF(k), vc = GF(NL + k), tc = tn;
         if (i == 0 && k > 0) {
             dua = uc - GF(k - 1);
             dva = vc - GF(NL + k - 1);
             dta = tc - TF(k - 1);
         }
         const bool below = k + 1 < NL;
+        if (below) tn = TF(k + 1);
         const double dub = below ? GF(k + 1) - uc : 0.0, dvb = below ? GF(NL + k + 1) - vc : 0.0,
-                     dtb = below ? TF(k + 1) - tc : 0.0;
+                     dtb = below ? tn - tc : 0.0;
         const double r = rdp[i];
         const double omega = cfac[i] * gc[i] - (scum[i] * dlnp[i] + alpha[i] * cm[i]) * r;
         const double mup = L.B0 * SN - scum[i];        // M at half level k (above)
@@ -1516,6 +1518,18 @@ int run_physics(Dyn &d) {
     return AEROS_OK;
 }
 
+// The split form's double-float column kernel and exact-product spectral kernel
+// keep a whole column (or real spectral column) in one thread; they pay off
+// once an ensemble has enough columns to fill the GPU (measured: one T42L20
+// member is faster with the FP64 kernels, whose level lanes split a column).
+// Fixed per handle, so a handle's results never depend on launch shapes.
+bool split_column_df(const Dyn &d) {
+    return d.par.precision == AEROS_PREC_SPLIT && (long)d.M * d.g.nlon * d.g.nlat >= 65536;
+}
+bool split_spectral_exact(const Dyn &d) {
+    return d.par.precision == AEROS_PREC_SPLIT && spec_cols_available(d.NL) && 2L * d.M * d.g.nlm >= 16384;
+}
+
 int run_tendency(Dyn &d, int hs_on, bool physics) {
     Ctx c = d.ctx();
     int rc;
@@ -1545,7 +1559,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
                                       d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
                                       d.ldf, d.tmp(d.now), d.g.nlm);
     };
-    if (d.par.precision == AEROS_PREC_SPLIT) {
+    if (split_column_df(d)) {
         // split form: the column terms in double-float on the FP32/INT32 pipes, a thread per column
         go_df(k_column_df, (unsigned)((ncol + ct - 1) / ct));
     } else if (lpc == 16) go(k_column<16>);
@@ -1619,8 +1633,8 @@ int enqueue_step(Dyn &d, bool startup) {
     const int sw = d.tune.spec_warps;
     a.GTl = d.GTl_d; a.TTl = d.TTl_d; a.WTl = d.WTl_d; a.MinvTl = d.MinvL_d[s];
     a.eG = d.eG_d; a.eT = d.eT_d; a.eW = d.eW_d; a.eMinv = d.eMinv_d[s];
-    // the split form takes the exact-product column layout wherever it exists
-    const bool exact = d.par.precision == AEROS_PREC_SPLIT && spec_cols_available(d.NL);
+    // the split form of an ensemble takes the exact-product column layout
+    const bool exact = split_spectral_exact(d);
     if ((d.tune.spec_cols || exact) && spec_cols_available(d.NL)) {
         const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
         if (d.NL == 16) {

@@ -29,9 +29,15 @@ def main(argv=None):
                     help="launch shapes to set before stepping, e.g. spec_cols=1,spec_warps=2 (AerosDyn.TUNE_KEYS)")
     ap.add_argument("--sht-batch", type=int, default=0,
                     help="run `steps` scalar synthesis + analysis pairs of this many fields at --trunc instead")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="run one checkpointed forward/backward window of `steps` steps (checkpoints every "
+                         "--every) of one member instead")
+    ap.add_argument("--every", type=int, default=4)
     a = ap.parse_args(argv)
     if a.transport:
         return transport_case(a)
+    if a.adjoint:
+        return adjoint_case(a)
     if a.sht_batch > 0:
         return sht_case(a)
     from .params import held_suarez_params, PREC_FP64, PREC_SPLIT
@@ -57,6 +63,40 @@ def main(argv=None):
     for _ in range(a.steps):
         ks = dyn.profile_step()
     print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
+    return 0
+
+
+def adjoint_case(a):
+    """The differentiation form's window pair on one member: a seeded
+    red-spectrum state (vorticity 1e-5/l^2, divergence 0.2 of it, temperature
+    1 K/l about 264 K, seed 2), window_forward(steps, every), window_backward;
+    the wall times are printed."""
+    import time
+    from .params import held_suarez_params
+    from .dynamics import AerosDyn
+    from .spectral import AerosSHT
+    d = AerosDyn(held_suarez_params(trunc=a.trunc, nlev=a.nlev))
+    s = AerosSHT(a.trunc, batch_max=1)
+    rng = np.random.default_rng(2)
+    L, M = np.asarray(s.l_of_lm, float), np.asarray(s.m_of_lm)
+
+    def red(shape, slope):
+        c = (rng.standard_normal(shape + (len(L),)) + 1j * rng.standard_normal(shape + (len(L),))) * (L + 1) ** slope
+        c[..., M == 0] = c[..., M == 0].real
+        return c
+    d.set_isothermal(264.0, 1.0e5)
+    _, _, t, lnps = d.get_state()
+    vor, div = 1e-5 * red((d.nlev,), -2.0), 2e-6 * red((d.nlev,), -2.0)
+    vor[:, 0] = 0
+    div[:, 0] = 0
+    d.set_state(vor, div, t + red((d.nlev,), -1.0), lnps)
+    t0 = time.perf_counter()
+    J = d.window_forward(a.steps, a.every)
+    t1 = time.perf_counter()
+    d.window_backward()
+    t2 = time.perf_counter()
+    print(f"adjoint window: {a.steps} steps, J {float(J[0]):.6e}, forward {1e3 * (t1 - t0):.2f} ms, "
+          f"backward {1e3 * (t2 - t1):.2f} ms")
     return 0
 
 
