@@ -370,18 +370,20 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
             dtyb -= x2 * tbaseb;
         }
         lnpsb += ps * psb;
+        // Gb is grouped for batched transposes (syn_adjoint): the x components u, dT/dx, dlnps/dx
+        // (2 NL + 1 fields), the y components v, dT/dy, dlnps/dy, then the scalars vor, div, T, lnps
         for (int k = 0; k < NL; ++k) {
             GB(k) = ub[k];
-            GB(NL + k) = vb[k];
-            GB(2 * NL + k) = zb[k];
-            GB(3 * NL + k) = dvb[k];
-            GB(4 * NL + k) = tb[k];
-            GB(5 * NL + k) = txb[k];
-            GB(6 * NL + k) = tyb[k];
+            GB(NL + k) = txb[k];
+            GB(2 * NL + 1 + k) = vb[k];
+            GB(3 * NL + 1 + k) = tyb[k];
+            GB(4 * NL + 2 + k) = zb[k];
+            GB(5 * NL + 2 + k) = dvb[k];
+            GB(6 * NL + 2 + k) = tb[k];
         }
-        GB(7 * NL) = lnpsb;
-        GB(7 * NL + 1) = pxb;
-        GB(7 * NL + 2) = pyb;
+        GB(2 * NL) = pxb;
+        GB(4 * NL + 1) = pyb;
+        GB(7 * NL + 2) = lnpsb;
 #undef GF
 #undef AB
 #undef GB
@@ -624,10 +626,11 @@ int adj_ensure(Dyn &d) {
     d.adj = a;
     const size_t ng = (size_t)d.g.nlon * d.g.nlat, M = d.M, NL = d.NL, nst = d.nstate(), nlm = d.g.nlm;
     int rc;
-    if ((rc = aeros_sht_create(&a->sht, d.g.T, d.g.nlon, d.g.nlat, (int)(3 * NL)))) return rc;
+    if ((rc = aeros_sht_create(&a->sht, d.g.T, d.g.nlon, d.g.nlat, (int)(3 * NL + 1)))) return rc;
     if ((rc = aeros_sht_set_stream(a->sht, d.stream))) return rc;
     if ((rc = dalloc(a->Ob, nst)) || (rc = dalloc(a->Nb, nst)) || (rc = dalloc(a->Rb, nst)) ||
-        (rc = dalloc(a->S1, 3 * NL * nlm)) || (rc = dalloc(a->S2, 3 * NL * nlm)) || (rc = dalloc(a->post, nst)) ||
+        (rc = dalloc(a->S1, (3 * NL + 1) * nlm)) || (rc = dalloc(a->S2, (3 * NL + 1) * nlm)) ||
+        (rc = dalloc(a->post, nst)) ||
         (rc = dalloc(a->Gb, M * (7 * NL + 3) * ng)) || (rc = dalloc(a->GAb, M * (4 * NL + 1) * ng)) ||
         (rc = dalloc(a->H, M * (2 * NL + 1) * ng)) || (rc = dalloc(a->g1, M * ng)) || (rc = dalloc(a->parb, 2 * M)) ||
         (rc = dalloc(a->Mtb, M)) || (rc = dalloc(a->J, M)) || (rc = dalloc(a->E, M * nlm)))
@@ -650,54 +653,54 @@ const double *cd(const void *p) { return reinterpret_cast<const double *>(p); }
 double *dd(void *p) { return reinterpret_cast<double *>(p); }
 
 // acc += Syn^T(Gb): adjoint of the step's grid-field synthesis (Gb is scaled in place).
+// Gb per member: [u, dT/dx, dlnps/dx | v, dT/dy, dlnps/dy | vor, div, T, lnps] (k_column_ad),
+// so the transposes are one vector analysis of 2 NL + 1 (x, y) pairs and one scalar
+// analysis of 3 NL + 1 fields.
 int syn_adjoint(Dyn &d, double2 *acc) {
     AdjCtx &a = *d.adj;
-    const size_t ng = (size_t)d.g.nlon * d.g.nlat;
-    const int NL = d.NL;
+    const size_t ng = (size_t)d.g.nlon * d.g.nlat, nlm = d.g.nlm;
+    const int NL = d.NL, nx = 2 * NL + 1;
     const double a2 = kA * kA;
     int rc;
     for (int e = 0; e < d.M; ++e) {
         double *B = a.Gb + (size_t)e * (7 * NL + 3) * ng;
         grid_wscale(d, B, 7 * NL + 3, 1.0, -1);
-        // u, v  <- (vor, div)
-        if ((rc = aeros_vordiv_from_uv(a.sht, B, B + NL * ng, dd(a.S1), dd(a.S2), NL))) return rc;
+        // (u, v) <- (vor, div); T <- (dT/dx, dT/dy); lnps <- its gradient
+        if ((rc = aeros_vordiv_from_uv(a.sht, B, B + (size_t)nx * ng, dd(a.S1), dd(a.S2), nx))) return rc;
         spec_axpy(d, st_vor(d, acc, e), a.S1, NL, a2, 1, -1, 1);
         spec_axpy(d, st_div(d, acc, e), a.S2, NL, a2, 1, -1, 1);
-        // vor, div, T grid fields
-        if ((rc = aeros_sht_analysis(a.sht, B + 2 * NL * ng, dd(a.S1), 3 * NL))) return rc;
+        spec_axpy(d, st_tmp(d, acc, e), a.S2 + (size_t)NL * nlm, NL, -1.0, 1, 0, 1);
+        spec_axpy(d, st_lnp(d, acc, e), a.S2 + (size_t)2 * NL * nlm, 1, -1.0, 1, 0, 1);
+        // vor, div, T, lnps grid fields
+        if ((rc = aeros_sht_analysis(a.sht, B + (size_t)2 * nx * ng, dd(a.S1), 3 * NL + 1))) return rc;
         spec_axpy(d, st_vor(d, acc, e), a.S1, NL, 1.0, 1, 0, 1);
-        spec_axpy(d, st_div(d, acc, e), a.S1 + (size_t)NL * d.g.nlm, NL, 1.0, 1, 0, 1);
-        spec_axpy(d, st_tmp(d, acc, e), a.S1 + (size_t)2 * NL * d.g.nlm, NL, 1.0, 1, 0, 1);
-        // dT/dx, dT/dy  <- T
-        if ((rc = aeros_vordiv_from_uv(a.sht, B + 5 * NL * ng, B + 6 * NL * ng, dd(a.S1), dd(a.S2), NL))) return rc;
-        spec_axpy(d, st_tmp(d, acc, e), a.S2, NL, -1.0, 1, 0, 1);
-        // lnps and its gradient
-        if ((rc = aeros_sht_analysis(a.sht, B + 7 * NL * ng, dd(a.S1), 1))) return rc;
-        spec_axpy(d, st_lnp(d, acc, e), a.S1, 1, 1.0, 1, 0, 1);
-        if ((rc = aeros_vordiv_from_uv(a.sht, B + (7 * NL + 1) * ng, B + (7 * NL + 2) * ng, dd(a.S1), dd(a.S2), 1)))
-            return rc;
-        spec_axpy(d, st_lnp(d, acc, e), a.S2, 1, -1.0, 1, 0, 1);
+        spec_axpy(d, st_div(d, acc, e), a.S1 + (size_t)NL * nlm, NL, 1.0, 1, 0, 1);
+        spec_axpy(d, st_tmp(d, acc, e), a.S1 + (size_t)2 * NL * nlm, NL, 1.0, 1, 0, 1);
+        spec_axpy(d, st_lnp(d, acc, e), a.S1 + (size_t)3 * NL * nlm, 1, 1.0, 1, 0, 1);
     }
     return AEROS_OK;
 }
 
-// GAb = Ana^T(R): adjoint of the step's tendency analysis.
+// GAb = Ana^T(R): adjoint of the step's tendency analysis.  The scaled spectral
+// inputs sit back to back in S1 as [vor | div | temp | lnps], so the transposes
+// are one vector synthesis (ae, an) and one scalar synthesis of 2 NL + 1 fields
+// (Phi + K from the divergence part, dT/dt, dlnps/dt: contiguous in GAb).
 int ana_adjoint(Dyn &d, double2 *R) {
     AdjCtx &a = *d.adj;
-    const size_t ng = (size_t)d.g.nlon * d.g.nlat;
+    const size_t ng = (size_t)d.g.nlon * d.g.nlat, nlm = d.g.nlm;
     const int NL = d.NL;
     const double ia2 = 1.0 / (kA * kA);
     int rc;
     for (int e = 0; e < d.M; ++e) {
         double *B = a.GAb + (size_t)e * (4 * NL + 1) * ng;
-        spec_axpy(d, a.S1, st_vor(d, R, e), NL, ia2, -1, 1, 0);
-        spec_axpy(d, a.S2, st_div(d, R, e), NL, ia2, -1, 1, 0);
-        if ((rc = aeros_uv_from_vordiv(a.sht, dd(a.S1), dd(a.S2), B, B + NL * ng, NL))) return rc;
-        if ((rc = aeros_sht_synthesis(a.sht, dd(a.S2), B + 2 * NL * ng, NL))) return rc;
-        spec_axpy(d, a.S1, st_tmp(d, R, e), NL, 1.0, -1, 0, 0);
-        if ((rc = aeros_sht_synthesis(a.sht, dd(a.S1), B + 3 * NL * ng, NL))) return rc;
-        spec_axpy(d, a.S1, st_lnp(d, R, e), 1, 1.0, -1, 0, 0);
-        if ((rc = aeros_sht_synthesis(a.sht, dd(a.S1), B + 4 * NL * ng, 1))) return rc;
+        double2 *Sv = a.S1, *Sd = a.S1 + (size_t)NL * nlm, *St = a.S1 + (size_t)2 * NL * nlm,
+                *Sp = a.S1 + (size_t)3 * NL * nlm;
+        spec_axpy(d, Sv, st_vor(d, R, e), NL, ia2, -1, 1, 0);
+        spec_axpy(d, Sd, st_div(d, R, e), NL, ia2, -1, 1, 0);
+        spec_axpy(d, St, st_tmp(d, R, e), NL, 1.0, -1, 0, 0);
+        spec_axpy(d, Sp, st_lnp(d, R, e), 1, 1.0, -1, 0, 0);
+        if ((rc = aeros_uv_from_vordiv(a.sht, dd(Sv), dd(Sd), B, B + NL * ng, NL))) return rc;
+        if ((rc = aeros_sht_synthesis(a.sht, dd(Sd), B + 2 * NL * ng, 2 * NL + 1))) return rc;
         grid_wscale(d, B, 4 * NL + 1, 1.0, 1);
     }
     return AEROS_OK;
