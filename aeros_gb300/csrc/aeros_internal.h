@@ -120,6 +120,8 @@ struct Tune {
     int col_lanes = 1;              // column kernel lanes per column: 1, 2, 4, 8 or 16
     int spec_warps = 4;             // spectral kernel warps per CTA
     int spec_cols = 0;              // spectral kernel layout: 0 a warp per coefficient, 1 a thread per real column
+    int sp_cps = 8;                 // split Legendre kernels: CTAs per SM over the grid (group slots): 2, 4, 8, 16
+    int sp_dft_cps = 8;             // split DFT products: CTAs per SM over the grid: 2, 4, 8, 16
 };
 
 // Launch context for the transform kernels.

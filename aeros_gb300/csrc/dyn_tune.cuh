@@ -61,6 +61,11 @@ bool tune_load(Dyn &d) {
         if (!(in >> k >> t.fs_lpb >> t.fs_thr >> t.fa_lpb >> t.fa_thr >> t.la_ct >> t.col_thr >> t.spec_warps >>
               t.col_lanes >> t.ls_jt >> t.spec_cols))
             continue;
+        int a = 0, b = 0;
+        if (in >> a >> b) {   // the split shapes (absent in older cache lines)
+            t.sp_cps = a;
+            t.sp_dft_cps = b;
+        }
         if (k != key) continue;
         d.tune = t;
         found = true;
@@ -75,7 +80,7 @@ void tune_store(Dyn &d) {
     const Tune &t = d.tune;
     f << tune_key(d) << " " << t.fs_lpb << " " << t.fs_thr << " " << t.fa_lpb << " " << t.fa_thr << " " << t.la_ct
       << " " << t.col_thr << " " << t.spec_warps << " " << t.col_lanes << " " << t.ls_jt << " " << t.spec_cols
-      << "\n";
+      << " " << t.sp_cps << " " << t.sp_dft_cps << "\n";
 }
 
 int recapture(Dyn &d) {
@@ -149,6 +154,14 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
                     t.col_lanes = lp;
                     trial(t);
                 }
+        if (d.par.precision == AEROS_PREC_SPLIT) {
+            // split kernels: CTAs per SM over the grid (group slots of the Legendre kernels,
+            // column-tile slots of the DFT products)
+            for (int cps : {2, 4, 8, 16})
+                if (cps != d.tune.sp_cps) { Tune t = d.tune; t.sp_cps = cps; trial(t); }
+            for (int cps : {2, 4, 8, 16})
+                if (cps != d.tune.sp_dft_cps) { Tune t = d.tune; t.sp_dft_cps = cps; trial(t); }
+        }
         for (int sc : {0, 1})
             for (int sw : {1, 2, 4, 8}) {
                 if ((sc && !spec_cols_available(d.NL)) || (sc == d.tune.spec_cols && sw == d.tune.spec_warps)) continue;
@@ -176,12 +189,12 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
 }
 
 // The launch shapes in use: fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct, col_thr, spec_warps, col_lanes, ls_jt,
-// spec_cols; the first n of them (n <= 10).
+// spec_cols, sp_cps, sp_dft_cps; the first n of them (n <= 12).
 int aeros_dyn_tune_get(aeros_dyn_t h, int *shape, int n) {
-    if (!h || !shape || n < 0 || n > 10) return AEROS_ERR_ARG;
+    if (!h || !shape || n < 0 || n > 12) return AEROS_ERR_ARG;
     const Tune &t = h->tune;
-    const int v[10] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct,
-                       t.col_thr, t.spec_warps, t.col_lanes, t.ls_jt, t.spec_cols};
+    const int v[12] = {t.fs_lpb, t.fs_thr, t.fa_lpb, t.fa_thr, t.la_ct, t.col_thr,
+                       t.spec_warps, t.col_lanes, t.ls_jt, t.spec_cols, t.sp_cps, t.sp_dft_cps};
     std::memcpy(shape, v, sizeof(int) * n);
     return AEROS_OK;
 }
@@ -189,7 +202,7 @@ int aeros_dyn_tune_get(aeros_dyn_t h, int *shape, int n) {
 // Set the launch shapes explicitly (same order as aeros_dyn_tune_get, all 10);
 // each must be one the autotuner would try.  Re-captures the step graphs.
 int aeros_dyn_tune_set(aeros_dyn_t h, const int *shape, int n) {
-    if (!h || !shape || n != 10) return AEROS_ERR_ARG;
+    if (!h || !shape || (n != 10 && n != 12)) return AEROS_ERR_ARG;
     Dyn &d = *h;
     auto in = [](int v, std::initializer_list<int> ok) {
         for (int x : ok)
@@ -201,12 +214,20 @@ int aeros_dyn_tune_set(aeros_dyn_t h, const int *shape, int n) {
     Tune t;
     t.fs_lpb = shape[0]; t.fs_thr = shape[1]; t.fa_lpb = shape[2]; t.fa_thr = shape[3]; t.la_ct = shape[4];
     t.col_thr = shape[5]; t.spec_warps = shape[6]; t.col_lanes = shape[7]; t.ls_jt = shape[8]; t.spec_cols = shape[9];
+    if (n == 12) {
+        t.sp_cps = shape[10];
+        t.sp_dft_cps = shape[11];
+    } else {
+        t.sp_cps = d.tune.sp_cps;
+        t.sp_dft_cps = d.tune.sp_dft_cps;
+    }
     const bool good = (t.fs_lpb == 0 || (in(t.fs_lpb, {1, 2, 4, 8, 16}) && t.fs_lpb <= fourier_lpb_limit(fs_lat))) &&
                       (t.fa_lpb == 0 || (in(t.fa_lpb, {1, 2, 4, 8, 16}) && t.fa_lpb <= fourier_lpb_limit(fa_lat))) &&
                       in(t.fs_thr, {64, 128, 256, 512}) && in(t.fa_thr, {64, 128, 256, 512}) &&
                       in(t.la_ct, {4, 8, 16}) && in(t.col_thr, {32, 64, 128, 256}) &&
                       in(t.spec_warps, {1, 2, 4, 8}) && in(t.col_lanes, {1, 2, 4, 8, 16}) &&
-                      in(t.ls_jt, {8, 16, 32}) && (t.spec_cols == 0 || (t.spec_cols == 1 && spec_cols_available(d.NL)));
+                      in(t.ls_jt, {8, 16, 32}) && (t.spec_cols == 0 || (t.spec_cols == 1 && spec_cols_available(d.NL))) &&
+                      in(t.sp_cps, {2, 4, 8, 16}) && in(t.sp_dft_cps, {2, 4, 8, 16});
     if (!good) {
         set_error("aeros_dyn_tune_set: a launch shape outside the autotuner's candidates");
         return AEROS_ERR_ARG;

@@ -853,12 +853,14 @@ void split_destroy(SplitCtx *s) {
 // there are at least 4 slots and the slot is the fastest grid index, so the CTAs
 // sharing an (m, tile) table run together and read its chunks from L2; otherwise
 // m is the fastest index, which spreads the long and short contractions.
-static int split_slots(int ngrp, int tiles, int nsm, bool *smajor) {
+// cps: CTAs per SM over the grid (8 by default, the autotuner's sp_cps).
+static int split_slots(int ngrp, int tiles, int nsm, int cps, bool *smajor) {
     *smajor = tiles >= 2 * nsm;
-    // at most four full waves of two CTAs per SM: a grid just above a whole number
+    // at most cps / 2 full waves of two CTAs per SM: a grid just above a whole number
     // of waves would leave a last wave of a few CTAs running alone
-    return std::max(1, std::min(ngrp, std::max(*smajor ? 4 : 1, 8 * nsm / tiles)));
+    return std::max(1, std::min(ngrp, std::max(*smajor ? 4 : 1, cps * nsm / tiles)));
 }
+static int split_cps(const Ctx &c) { return c.tune && c.tune->sp_cps > 0 ? c.tune->sp_cps : 8; }
 static dim3 split_grid(int slots, int ms, int ntile, bool smajor) {
     return smajor ? dim3(slots, ms, ntile) : dim3(ms, ntile, slots);
 }
@@ -868,7 +870,7 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
     const int ngrp = (p.ncol + kNTs / 2 - 1) / (kNTs / 2);
     const int tiles = (c.T + 1) * s->ntl;
     bool smajor;
-    const int slots = split_slots(ngrp, tiles, s->nsm, &smajor);
+    const int slots = split_slots(ngrp, tiles, s->nsm, split_cps(c), &smajor);
     SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
                    nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err, smajor ? 1 : 0};
     const dim3 grid = split_grid(slots, c.T + 1, s->ntl, smajor);
@@ -902,7 +904,7 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, const int *g
     if (ngrp <= 0) return AEROS_OK;
     const int tiles = (c.T + 1) * s->ntlA;
     bool smajor;
-    const int slots = split_slots(ngrp, tiles, s->nsm, &smajor);
+    const int slots = split_slots(ngrp, tiles, s->nsm, split_cps(c), &smajor);
     AnaSplitArgs a{cols_d, gstart_d, ngrp, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F,
                    nrow, c.ms, c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err, smajor ? 1 : 0};
     const dim3 grid = split_grid(slots, c.T + 1, s->ntlA, smajor);

@@ -423,9 +423,11 @@ constexpr size_t kTwoPerSm = 110 * 1024;
 
 template <class P>
 void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, int nsm) {
-    // about 8 CTAs per SM over the grid; each loops over nct / slots column tiles
+    // about cps (8 by default, the autotuner's sp_dft_cps) CTAs per SM over the grid; each loops over
+    // nct / slots column tiles
+    const int cps = c.tune && c.tune->sp_dft_cps > 0 ? c.tune->sp_dft_cps : 8;
     const int nct = (ncol + kNT - 1) / kNT;
-    const int slots = std::max(1, std::min(nct, (8 * nsm + d.nmt - 1) / d.nmt));
+    const int slots = std::max(1, std::min(nct, (cps * nsm + d.nmt - 1) / d.nmt));
     const int Kp = (d.K + 15) & ~15;
     dim3 grid(d.nmt, slots);
     auto go = [&](auto kern, size_t smem) {

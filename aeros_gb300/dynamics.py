@@ -288,7 +288,7 @@ class AerosDyn:
 
     # ------------------------------------------------------------------ autotuner
     TUNE_KEYS = ("fs_lpb", "fs_thr", "fa_lpb", "fa_thr", "la_ct", "col_thr", "spec_warps", "col_lanes", "ls_jt",
-                 "spec_cols")
+                 "spec_cols", "sp_cps", "sp_dft_cps")
 
     def autotune(self, reps=3):
         """Choose launch shapes by timing whole steps; returns (ms before, ms after, shapes)."""
@@ -327,6 +327,17 @@ class AerosDyn:
         out = (x[:n3].reshape(s3), x[n3:2 * n3].reshape(s3), x[2 * n3:3 * n3].reshape(s3),
                x[3 * n3:].reshape(M, self.nlm))
         return self._squeeze(out)
+
+    @staticmethod
+    def host_register(arr):
+        """Page-lock a numpy array (aeros_host_register) so that aeros_dyn_step_packed
+        takes its one-graph form with it."""
+        _capi.check(_capi.lib().aeros_host_register(arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes),
+                    "aeros_host_register")
+
+    @staticmethod
+    def host_unregister(arr):
+        _capi.check(_capi.lib().aeros_host_unregister(arr.ctypes.data_as(ctypes.c_void_p)), "aeros_host_unregister")
 
     def state_size(self):
         n = ctypes.c_longlong()

@@ -33,6 +33,9 @@ def main(argv=None):
                     help="run one checkpointed forward/backward window of `steps` steps (checkpoints every "
                          "--every) of one member instead")
     ap.add_argument("--every", type=int, default=4)
+    ap.add_argument("--packed", action="store_true",
+                    help="take the steps through aeros_dyn_step_packed between page-locked host arrays "
+                         "(the end-to-end form: copy-in kernel, step, copy-out kernel in one graph)")
     a = ap.parse_args(argv)
     if a.transport:
         return transport_case(a)
@@ -60,9 +63,38 @@ def main(argv=None):
     if a.tune:
         before, after, shapes = dyn.autotune(reps=3)
         print(f"autotune: {before:.4f} -> {after:.4f} ms/step with {shapes}")
+    if a.packed:
+        return packed_case(a, dyn)
     for _ in range(a.steps):
         ks = dyn.profile_step()
     print(" ".join(f"{n}={ms:.4f}ms" for n, ms in ks))
+    return 0
+
+
+def packed_case(a, dyn):
+    """`steps` steps through aeros_dyn_step_packed with page-locked host arrays
+    (the one-graph form), after two direct steps."""
+    import ctypes
+    import time
+    dyn.step(2)
+    n = dyn.state_size()
+    arrs = []
+    for src in (dyn.pack(*dyn.get_state(squeeze=False)), dyn.pack(*dyn.get_old_state(squeeze=False)), None, None):
+        x = np.empty(n, np.complex128) if src is None else src.copy()
+        dyn.host_register(x)
+        arrs.append(x)
+    now, old, now_out, old_out = arrs
+    nstep = dyn.counters()[0]
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        dyn.step_packed(now, old, nstep, 1, now_out, old_out)
+        now, now_out = now_out, now
+        old, old_out = old_out, old
+        nstep += 1
+    t1 = time.perf_counter()
+    print(f"packed steps: {a.steps}, {1e3 * (t1 - t0) / a.steps:.4f} ms per step (host clock)")
+    for x in arrs:
+        dyn.host_unregister(x)
     return 0
 
 

@@ -420,9 +420,10 @@ int aeros_dyn_launch_count(aeros_dyn_t h, long long *count);
 /* Launch-shape autotuner (no reference counterpart): times whole steps for
  * each candidate shape of the longitude FFTs (latitudes and threads per CTA),
  * the FP64 Legendre analysis (columns per CTA) and synthesis (latitudes per
- * CTA), the column kernel (threads per CTA, lanes per column) and the
+ * CTA), the column kernel (threads per CTA, lanes per column), the
  * spectral kernel (warps per CTA; a warp per coefficient or, for 16 or 20
- * levels, a thread per real column), keeps the fastest, restores the state and
+ * levels, a thread per real column) and, in the split form, the grid sizes of
+ * the tensor-core kernels, keeps the fastest, restores the state and
  * re-captures the step graphs.  ms_before / ms_after: step time with the old and the chosen shapes.
  * With AEROS_TUNE_CACHE set to a file name, results are appended there and new
  * handles of the same GPU, grid, levels, ensemble size and precision start
@@ -430,11 +431,13 @@ int aeros_dyn_launch_count(aeros_dyn_t h, long long *count);
 int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_after);
 /* The shapes in use, in the order fs_lpb, fs_thr, fa_lpb, fa_thr, la_ct,
  * col_thr, spec_warps, col_lanes, ls_jt (0 = heuristic), spec_cols (0 a warp
- * per coefficient, 1 a thread per real column): the first n (0 <= n <= 10)
- * are written to shape. */
+ * per coefficient, 1 a thread per real column), sp_cps and sp_dft_cps (split
+ * Legendre kernels and split DFT products: CTAs per SM over the grid, 2, 4, 8
+ * or 16): the first n (0 <= n <= 12) are written to shape. */
 int aeros_dyn_tune_get(aeros_dyn_t h, int *shape, int n);
-/* Set all 10 shapes (same order; n must be 10), each one the autotuner would
- * try, and re-capture the step graphs.  AEROS_ERR_ARG for any other shape. */
+/* Set the shapes (same order; n = 12, or 10 keeping the two split shapes),
+ * each one the autotuner would try, and re-capture the step graphs.
+ * AEROS_ERR_ARG for any other shape. */
 int aeros_dyn_tune_set(aeros_dyn_t h, const int *shape, int n);
 
 /* ======================================================================== */

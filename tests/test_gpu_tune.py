@@ -79,3 +79,26 @@ def test_tune_set_rejects_shapes_outside_the_candidates(gpulib):
     assert d.tune_shapes() == before
     d.set_tune_shapes(col_thr=128, col_lanes=4)
     assert d.tune_shapes()["col_lanes"] == 4
+
+
+def test_split_grid_shapes_leave_results_unchanged(gpulib):
+    """The split form's grid sizes (CTAs per SM of the Legendre kernels and of
+    the DFT products) only decide which CTA takes which column group: the
+    steps are bitwise those of the default shapes."""
+    from aeros_gb300.params import held_suarez_params, PREC_SPLIT
+    from aeros_gb300.dynamics import AerosDyn
+    p = held_suarez_params(trunc=42, nlev=20, nmember=4, precision=PREC_SPLIT)
+    ref = AerosDyn(p)
+    st = _state(ref)
+    ref.set_state(*st)
+    ref.step(3)
+    for cps, dcps in ((2, 16), (16, 2)):
+        d = AerosDyn(p)
+        d.set_state(*st)
+        d.set_tune_shapes(sp_cps=cps, sp_dft_cps=dcps)
+        assert d.tune_shapes()["sp_cps"] == cps and d.tune_shapes()["sp_dft_cps"] == dcps
+        d.step(3)
+        for a, b in zip(ref.get_state(), d.get_state()):
+            assert np.array_equal(a, b)
+    with pytest.raises(Exception):
+        ref.set_tune_shapes(sp_cps=3)
