@@ -434,45 +434,25 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
 // arithmetic and its order are those of k_spectral: every level product runs
 // j = 0 .. nlev-1 from zero, the nu . e sum is the warp butterfly's tree.
 //
-// EXACT (the split form): the four level products are exact fixed-point dot
-// products on the integer pipes -- each matrix row and each vector scaled by a
-// power of two to 53-bit integers, split in 27 + 26-bit limbs, the limb
-// products summed in int64 (IMAD.WIDE) and the sum rounded once to FP64 -- so
-// a product costs no FP64 instruction and is at least as accurate as the FP64
-// FMA chain (error below 2^-51 of |row| |vector| instead of ~20 2^-53).  The
-// matrices keep their FP64 values (limbs are exact); the leapfrog, semi-
-// implicit combination, diffusion and RAW filter around them stay FP64.
 template <int NLT>
 __host__ __device__ constexpr size_t spec_cols_smem(int threads) {
-    return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads) + sizeof(int) * 4 * NLT;
+    return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads);
 }
 
-template <int NLT, bool EXACT>
+template <int NLT>
 __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
     extern __shared__ double sm_cols[];
     double *sG = sm_cols, *sT = sG + NLT * NLT, *sW = sT + NLT * NLT, *sNu = sW + NLT * NLT, *sPc = sNu + NLT;
     double *v1 = sPc + NLT + threadIdx.x, *v2 = v1 + NLT * blockDim.x;   // slot k at [k * blockDim.x]
     const int nt = blockDim.x;
-    int *sE = reinterpret_cast<int *>(sPc + NLT + 2 * NLT * nt);         // row exponents of G, tau, W
     for (int i = threadIdx.x; i < NLT * NLT; i += nt) {
-        if (EXACT) {
-            reinterpret_cast<int2 *>(sG)[i] = a.GTl[i];
-            reinterpret_cast<int2 *>(sT)[i] = a.TTl[i];
-            reinterpret_cast<int2 *>(sW)[i] = a.WTl[i];
-        } else {
-            sG[i] = a.GT[i];
-            sT[i] = a.TT[i];
-            sW[i] = a.WT[i];
-        }
+        sG[i] = a.GT[i];
+        sT[i] = a.TT[i];
+        sW[i] = a.WT[i];
     }
     for (int i = threadIdx.x; i < NLT; i += nt) {
         sNu[i] = a.nu[i];
         sPc[i] = a.pcoef[i];
-        if (EXACT) {
-            sE[i] = a.eG[i];
-            sE[NLT + i] = a.eT[i];
-            sE[2 * NLT + i] = a.eW[i];
-        }
     }
     __syncthreads();
     const int warp = (blockIdx.x * nt + threadIdx.x) >> 5;
@@ -498,7 +478,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
         xw -= a.raw_beta * dx;
     };
     // acc[k] = sum_j P[k][j] v[j], j ascending; P[k][j] at P[j * NLT + k]
-    auto product_fp64 = [&](const double *P, const double *v, double *acc) {
+    auto product = [&](const double *P, const double *v, double *acc) {
 #pragma unroll
         for (int k = 0; k < NLT; ++k) acc[k] = 0.0;
 #pragma unroll
@@ -506,45 +486,6 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const double vj = v[j * nt];
 #pragma unroll
             for (int k = 0; k < NLT; ++k) acc[k] += P[j * NLT + k] * vj;
-        }
-    };
-    // the same product exactly in fixed point: P[k][j] = (x 2^26 + y) 2^(eP[k] - 52) at PL[j * NLT + k]
-    auto product_exact = [&](const int2 *PL, const int *eP, const double *v, double *acc) {
-        int be = 0;
-#pragma unroll
-        for (int j = 0; j < NLT; ++j) be = max(be, f64_bexp(v[j * nt]));
-        const int ex = f64_scale_exp(be);
-        int b1[NLT], b0[NLT];
-#pragma unroll
-        for (int j = 0; j < NLT; ++j) {
-            const long long b = fixed53(v[j * nt], ex);
-            b1[j] = (int)(b >> 26);
-            b0[j] = (int)(b & 0x3FFFFFF);
-        }
-#pragma unroll 4
-        for (int k = 0; k < NLT; ++k) {
-            long long s2 = 0, s1 = 0, s0 = 0;
-#pragma unroll
-            for (int j = 0; j < NLT; ++j) {
-                const int2 p = PL[j * NLT + k];
-                s2 += (long long)p.x * b1[j];
-                s1 += (long long)p.x * b0[j] + (long long)p.y * b1[j];
-                s0 += (long long)p.y * b0[j];
-            }
-            acc[k] = i64_to_f64(s2 + ((s1 + (s0 >> 26)) >> 26), eP[k] + ex - 52);
-        }
-    };
-    // which: 0 G, 1 tau, 2 W, 3 the inverse of degree l
-    auto product = [&](int which, const double *v, double *acc) {
-        if (EXACT) {
-            if (which == 3)
-                product_exact(a.MinvTl + (size_t)l * NLT * NLT, a.eMinv + (size_t)l * NLT, v, acc);
-            else
-                product_exact(reinterpret_cast<const int2 *>(which == 0 ? sG : which == 1 ? sT : sW),
-                              sE + which * NLT, v, acc);
-        } else {
-            product_fp64(which == 0 ? sG : which == 1 ? sT : which == 2 ? sW : a.MinvT + (size_t)l * NLT * NLT, v,
-                         acc);
         }
     };
     bool bad = false;
@@ -574,7 +515,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const size_t o = o0 + k * ls;
             v1[k * nt] = tm_o[o] - tm[o] + a.astep * tt[o];
         }
-        product(0, v1, acc);              // G y
+        product(sG, v1, acc);             // G y
 #pragma unroll
         for (int k = 0; k < NLT; ++k) v2[k * nt] = acc[k];
 #pragma unroll 4
@@ -582,14 +523,14 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             const size_t o = o0 + k * ls;
             v1[k * nt] = ha * dv[o] - a.hh_old * dv_o[o];
         }
-        product(2, v1, acc);              // W x; v2 becomes the right-hand side
+        product(sW, v1, acc);             // W x; v2 becomes the right-hand side
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
             const size_t o = o0 + k * ls;
             const double pc = sPc[k];
             v2[k * nt] = dv_o[o] + h * td[o] + hl * (v2[k * nt] + pc * pz) + lam * acc[k];
         }
-        product(3, v2, acc);              // D^(n+1)
+        product(a.MinvT + (size_t)l * NLT * NLT, v2, acc);   // D^(n+1)
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {   // v1 = e = D-bar - D^n
             const size_t o = o0 + k * ls;
@@ -603,7 +544,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
             dv_o[o] = dnow;
             dv[o] = dw;
         }
-        product(1, v1, acc);              // tau e
+        product(sT, v1, acc);             // tau e
 #pragma unroll
         for (int k = 0; k < NLT; ++k) {
             const size_t o = o0 + k * ls;
@@ -653,6 +594,206 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
 
 // Level counts with a column-layout instantiation.
 constexpr int kSpecColLevels[] = {16, 20};
+// The split form's update for ensembles: the same semi-implicit step, with
+// the four level products (G y, W x, M_l^-1 rhs, tau e) as exact fixed-point
+// dot products on the integer pipes -- each matrix row and each vector scaled
+// by a power of two to 53-bit integers, split in 27 + 26-bit limbs, the limb
+// products summed in int64 (32 x 32 -> 64 multiply-adds) and the sum rounded
+// once to FP64 -- so a product costs no FP64 instruction and is at least as
+// accurate as the FP64 FMA chain (error below 2^-51 of |row| |vector|).  The
+// matrices keep their FP64 values (limbs are exact); the leapfrog, the
+// semi-implicit combination, diffusion and RAW filter stay FP64.
+// Four threads per real column: lane 4 c + q of a warp takes column c (8 per
+// warp, grouped by degree l) and the levels k = q, q + 4, ..., both for the
+// elementwise update and for the output rows of the products, whose input
+// vectors (and their limbs) sit in shared memory.  An integer sum does not
+// depend on who forms it; the nu . e sum keeps the warp butterfly's tree of
+// k_spectral (three steps within a thread, two across the four).
+constexpr int kXqCols = 8;   // real columns per warp
+template <int NLT>
+__host__ __device__ constexpr size_t spec_xq_smem(int warps) {
+    return sizeof(int2) * 3 * NLT * NLT + sizeof(int) * 3 * NLT + sizeof(double) * 2 * NLT +
+           (size_t)warps * kXqCols * NLT * (2 * sizeof(double) + sizeof(int2));
+}
+
+template <int NLT>
+__global__ void __launch_bounds__(256, 2) k_spectral_xq(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
+    static_assert(NLT % 4 == 0, "levels split four ways");
+    constexpr int NQ = NLT / 4;   // levels per thread
+    extern __shared__ double sm_xq[];
+    int2 *sG = reinterpret_cast<int2 *>(sm_xq), *sT = sG + NLT * NLT, *sW = sT + NLT * NLT;
+    int *sE = reinterpret_cast<int *>(sW + NLT * NLT);                      // row exponents of G, tau, W
+    double *sNu = reinterpret_cast<double *>(sE + 3 * NLT), *sPc = sNu + NLT;
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, cl = lane >> 2, q = lane & 3;
+    double *v1 = sPc + NLT + ((size_t)wib * kXqCols + cl) * NLT;           // [k] of this column
+    double *v2 = sPc + NLT + ((size_t)(blockDim.x >> 5) * kXqCols + wib * kXqCols + cl) * NLT;
+    int2 *vl = reinterpret_cast<int2 *>(sPc + NLT + (size_t)2 * (blockDim.x >> 5) * kXqCols * NLT) +
+               ((size_t)wib * kXqCols + cl) * NLT;                          // limbs of the vector in a product
+    for (int i = threadIdx.x; i < NLT * NLT; i += blockDim.x) {
+        sG[i] = a.GTl[i];
+        sT[i] = a.TTl[i];
+        sW[i] = a.WTl[i];
+    }
+    for (int i = threadIdx.x; i < NLT; i += blockDim.x) {
+        sNu[i] = a.nu[i];
+        sPc[i] = a.pcoef[i];
+        sE[i] = a.eG[i];
+        sE[NLT + i] = a.eT[i];
+        sE[2 * NLT + i] = a.eW[i];
+    }
+    __syncthreads();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= nwarp) return;   // whole warps leave together
+    const int2 wl = wtab[warp];
+    const int l = wl.x, idx = wl.y + cl;
+    const bool act = idx < 2 * a.M * (l + 1);
+    const int ii = act ? idx : wl.y;   // an idle column mirrors the warp's first one and writes nothing
+    const int comp = ii & 1, r = ii >> 1, e = r / (l + 1), m = r - e * (l + 1);
+    const int lm = m * (2 * a.T + 1 - m) / 2 + l;
+    const size_t ls = (size_t)2 * a.nlm;
+    const size_t o0 = ((size_t)e * NLT * a.nlm + lm) * 2 + comp;
+    const size_t op = ((size_t)e * a.nlm + lm) * 2 + comp;
+    double *vor = reinterpret_cast<double *>(a.vor), *vor_o = reinterpret_cast<double *>(a.vor_o);
+    double *dv = reinterpret_cast<double *>(a.div), *dv_o = reinterpret_cast<double *>(a.div_o);
+    double *tm = reinterpret_cast<double *>(a.tmp), *tm_o = reinterpret_cast<double *>(a.tmp_o);
+    const double *tv = reinterpret_cast<const double *>(a.tv), *td = reinterpret_cast<const double *>(a.td);
+    const double *tt = reinterpret_cast<const double *>(a.tt);
+    const double h = a.h, fd = a.dfac[l];
+    const bool raw = a.raw_on;
+    auto filt = [&](double xo, double &xn, double &xw) {
+        double dx = a.half_nu * (xo - 2.0 * xn + xw);
+        xn += a.raw_alpha * dx;
+        xw -= a.raw_beta * dx;
+    };
+    // acc[i] = row q + 4 i of P times the vector v (P[k][j] = (x 2^26 + y) 2^(eP[k] - 52) at PL[j NLT + k])
+    auto product = [&](const int2 *PL, const int *eP, const double *v, double *acc) {
+        int be = 0;
+#pragma unroll
+        for (int i = 0; i < NQ; ++i) be = max(be, f64_bexp(v[q + 4 * i]));
+        be = max(be, __shfl_xor_sync(0xffffffffu, be, 1));
+        be = max(be, __shfl_xor_sync(0xffffffffu, be, 2));
+        const int ex = f64_scale_exp(be);
+#pragma unroll
+        for (int i = 0; i < NQ; ++i) {
+            const long long b = fixed53(v[q + 4 * i], ex);
+            vl[q + 4 * i] = make_int2((int)(b >> 26), (int)(b & 0x3FFFFFF));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < NQ; ++i) {
+            const int k = q + 4 * i;
+            long long s2 = 0, s1 = 0, s0 = 0;
+#pragma unroll 4
+            for (int j = 0; j < NLT; ++j) {
+                const int2 p = PL[j * NLT + k], b = vl[j];
+                s2 += (long long)p.x * b.x;
+                s1 += (long long)p.x * b.y + (long long)p.y * b.x;
+                s0 += (long long)p.y * b.y;
+            }
+            acc[i] = i64_to_f64(s2 + ((s1 + (s0 >> 26)) >> 26), eP[k] + ex - 52);
+        }
+        __syncwarp();   // vl is rewritten by the next product
+    };
+    bool bad = false;
+    // vorticity: leapfrog, diffusion, RAW
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        const size_t o = o0 + (q + 4 * i) * ls;
+        const double vo = vor_o[o];
+        double vn = vor[o], vw = vo + h * tv[o];
+        vw = vw * fd;
+        if (raw) filt(vo, vn, vw);
+        bad |= !isfinite(vw);
+        if (act) {
+            vor_o[o] = vn;
+            vor[o] = vw;
+        }
+    }
+    const double pold = reinterpret_cast<const double *>(a.lnps_o)[op];
+    double pnow = reinterpret_cast<const double *>(a.lnps)[op];
+    const double rp = reinterpret_cast<const double *>(a.tp)[op];
+    double pnew;
+    const double lam = (double)l * (l + 1) / (kA * kA);
+    const double pz = pold - pnow + a.astep * rp;
+    const double ha = h * a.astep, hl = h * lam;
+    double acc[NQ];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {   // v1 = y
+        const size_t o = o0 + (q + 4 * i) * ls;
+        v1[q + 4 * i] = tm_o[o] - tm[o] + a.astep * tt[o];
+    }
+    __syncwarp();
+    product(sG, sE, v1, acc);   // G y
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) v2[q + 4 * i] = acc[i];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {   // v1 = x
+        const size_t o = o0 + (q + 4 * i) * ls;
+        v1[q + 4 * i] = ha * dv[o] - a.hh_old * dv_o[o];
+    }
+    __syncwarp();
+    product(sW, sE + 2 * NLT, v1, acc);   // W x; v2 becomes the right-hand side
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        const int k = q + 4 * i;
+        const size_t o = o0 + k * ls;
+        const double pc = sPc[k];
+        v2[k] = dv_o[o] + h * td[o] + hl * (v2[k] + pc * pz) + lam * acc[i];
+    }
+    __syncwarp();
+    product(a.MinvTl + (size_t)l * NLT * NLT, a.eMinv + (size_t)l * NLT, v2, acc);   // D^(n+1)
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {   // v1 = e = D-bar - D^n
+        const int k = q + 4 * i;
+        const size_t o = o0 + k * ls;
+        const double dold = dv_o[o];
+        double dnow = dv[o];
+        const double db = a.a1 * acc[i] + (1.0 - a.a1) * dold;
+        v1[k] = db - dnow;
+        double dw = acc[i] * fd;
+        if (raw) filt(dold, dnow, dw);
+        bad |= !isfinite(dw);
+        if (act) {
+            dv_o[o] = dnow;
+            dv[o] = dw;
+        }
+    }
+    __syncwarp();
+    product(sT, sE + NLT, v1, acc);   // tau e
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        const size_t o = o0 + (q + 4 * i) * ls;
+        const double told = tm_o[o];
+        double tnow = tm[o], tw = told + h * (tt[o] - acc[i]);
+        tw = tw * fd;
+        if (raw) filt(told, tnow, tw);
+        bad |= !isfinite(tw);
+        if (act) {
+            tm_o[o] = tnow;
+            tm[o] = tw;
+        }
+    }
+    // nu . e with the butterfly tree of 32 entries: positions q + 4 a, a = 0..7, within the thread
+    double sm8[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sm8[i] = q + 4 * i < NLT ? __dmul_rn(sNu[q + 4 * i], v1[q + 4 * i]) : 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) sm8[i] = sm8[i] + sm8[i + 4];   // w = 16
+#pragma unroll
+    for (int i = 0; i < 2; ++i) sm8[i] = sm8[i] + sm8[i + 2];   // w = 8
+    double t = sm8[0] + sm8[1];                                  // w = 4
+    t = t + __shfl_xor_sync(0xffffffffu, t, 2);                  // w = 2
+    t = t + __shfl_xor_sync(0xffffffffu, t, 1);                  // w = 1
+    pnew = pold + h * (rp - t);
+    if (raw) filt(pold, pnow, pnew);
+    bad |= !isfinite(pnew);
+    if (act && bad) atomicOr(a.flag, 1);
+    if (act && q == 0) {
+        reinterpret_cast<double *>(a.lnps_o)[op] = pnow;
+        reinterpret_cast<double *>(a.lnps)[op] = pnew;
+    }
+}
+
 bool spec_cols_available(int nlev) {
     for (int n : kSpecColLevels)
         if (n == nlev) return true;
@@ -1019,6 +1160,8 @@ struct aeros_dyn_s {
     double *dfac_d[2] = {nullptr, nullptr};
     int2 *spec_wt = nullptr;                                   // column-layout spectral warps: (l, first column)
     int spec_nw = 0;
+    int2 *spec_wt8 = nullptr;                                  // exact-product kernel's warps (8 columns each)
+    int spec_nw8 = 0;
     double *xlat_d = nullptr, *phis_d = nullptr;
     bool phis_set = false;
     double phis_mean = 0.0;
@@ -1461,14 +1604,20 @@ int build_step_tables(Dyn &d) {
             if ((rc = dput(d.MinvL_d[s], L)) || (rc = dput(d.eMinv_d[s], E))) return rc;
         }
     }
+    // the exact-product kernel's warps: 8 real columns of one degree each
+    std::vector<int2> wt8;
+    for (int l = 0; l <= T; ++l)
+        for (int c = 0; c < 2 * d.M * (l + 1); c += kXqCols) wt8.push_back(make_int2(l, c));
+    d.spec_nw8 = (int)wt8.size();
+    if ((rc = dput(d.spec_wt8, wt8))) return rc;
     if (d.NL == 16) {
-        if ((rc = raise_smem_limit((const void *)k_spectral_cols<16, false>, spec_cols_smem<16>(256))) ||
-            (rc = raise_smem_limit((const void *)k_spectral_cols<16, true>, spec_cols_smem<16>(256))))
+        if ((rc = raise_smem_limit((const void *)k_spectral_cols<16>, spec_cols_smem<16>(256))) ||
+            (rc = raise_smem_limit((const void *)k_spectral_xq<16>, spec_xq_smem<16>(8))))
             return rc;
     }
     if (d.NL == 20) {
-        if ((rc = raise_smem_limit((const void *)k_spectral_cols<20, false>, spec_cols_smem<20>(256))) ||
-            (rc = raise_smem_limit((const void *)k_spectral_cols<20, true>, spec_cols_smem<20>(256))))
+        if ((rc = raise_smem_limit((const void *)k_spectral_cols<20>, spec_cols_smem<20>(256))) ||
+            (rc = raise_smem_limit((const void *)k_spectral_xq<20>, spec_xq_smem<20>(8))))
             return rc;
     }
     return AEROS_OK;
@@ -1633,21 +1782,19 @@ int enqueue_step(Dyn &d, bool startup) {
     const int sw = d.tune.spec_warps;
     a.GTl = d.GTl_d; a.TTl = d.TTl_d; a.WTl = d.WTl_d; a.MinvTl = d.MinvL_d[s];
     a.eG = d.eG_d; a.eT = d.eT_d; a.eW = d.eW_d; a.eMinv = d.eMinv_d[s];
-    // the split form of an ensemble takes the exact-product column layout
-    const bool exact = split_spectral_exact(d);
-    if ((d.tune.spec_cols || exact) && spec_cols_available(d.NL)) {
+    // the split form of an ensemble takes the exact-product kernel (four threads per real column)
+    if (split_spectral_exact(d)) {
+        const unsigned nb = (unsigned)((d.spec_nw8 + sw - 1) / sw);
+        if (d.NL == 16)
+            k_spectral_xq<16><<<nb, 32 * sw, spec_xq_smem<16>(sw), d.stream>>>(a, d.spec_wt8, d.spec_nw8);
+        else
+            k_spectral_xq<20><<<nb, 32 * sw, spec_xq_smem<20>(sw), d.stream>>>(a, d.spec_wt8, d.spec_nw8);
+    } else if (d.tune.spec_cols && spec_cols_available(d.NL)) {
         const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
-        if (d.NL == 16) {
-            if (exact)
-                k_spectral_cols<16, true><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-            else
-                k_spectral_cols<16, false><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-        } else {
-            if (exact)
-                k_spectral_cols<20, true><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-            else
-                k_spectral_cols<20, false><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-        }
+        if (d.NL == 16)
+            k_spectral_cols<16><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        else
+            k_spectral_cols<20><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
     } else {
         long nw = (long)d.g.nlm * d.M;
         k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
@@ -1858,7 +2005,7 @@ void destroy(Dyn *d) {
                   d->pc_d, d->Minv_d[0], d->Minv_d[1], d->dfac_d[0], d->dfac_d[1], d->xlat_d, d->phis_d,
                   d->hs_dty_d, d->hs_ka_d, d->mass_rows, d->mass_tgt, d->lnr_last, d->lnr_cum, d->bud_rows,
                   d->bud_res, d->zm, d->flag, d->fsS, d->fsD, d->faS, d->acS, d->stage, d->mass_done,
-                  d->dconst, d->ldf, d->spec_wt, d->agS, d->GTl_d, d->TTl_d, d->WTl_d, d->MinvL_d[0],
+                  d->dconst, d->ldf, d->spec_wt, d->spec_wt8, d->agS, d->GTl_d, d->TTl_d, d->WTl_d, d->MinvL_d[0],
                   d->MinvL_d[1], d->eG_d, d->eT_d, d->eW_d, d->eMinv_d[0], d->eMinv_d[1]};
     for (void *p : ps)
         if (p) cudaFree(p);

@@ -35,32 +35,45 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
     const int tid = threadIdx.x, nthr = blockDim.x;
     const StageDiv dms(ms), dn(n), dnlon(nlon);
 
-    // X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m], m = 0..T (imag of X_0 dropped)
+    // X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m], m = 0..T (imag of X_0 dropped), with Nrm
+    // folded into the field's factors and the factors' zeros skipped (the field kind is uniform per CTA):
+    // a plain copy (a = 1, b = 0: vor, div, T, ln ps) costs two products per m
+    const double a0 = fd.a0 * kNrm, b0 = fd.b0 * kNrm, a1 = fd.a1 * kNrm, b1 = fd.b1 * kNrm;
+    const bool two = fd.src1 >= 0, pure_a = b0 == 0.0 && (!two || b1 == 0.0);
     for (int idx = tid; idx < nr * ms; idx += nthr) {
         const int r = dms.div(idx), m = idx - r * ms;
         const int j = j0 + r;
-        const double bs = m * isin[j];
         const double2 *Fr = F + (size_t)j * nrow * ms;
-        double2 x = make_double2(0.0, 0.0);
-        if (fd.src0 >= 0) {
-            const double2 f = Fr[(size_t)fd.src0 * ms + m];
-            const double bb = fd.b0 * bs;
-            x.x = fd.a0 * f.x - bb * f.y;
-            x.y = fd.a0 * f.y + bb * f.x;
-        }
-        if (fd.src1 >= 0) {
-            const double2 f = Fr[(size_t)fd.src1 * ms + m];
-            const double bb = fd.b1 * bs;
-            x.x += fd.a1 * f.x - bb * f.y;
-            x.y += fd.a1 * f.y + bb * f.x;
+        double2 x;
+        const double2 f = Fr[(size_t)fd.src0 * ms + m];
+        if (pure_a) {
+            x = make_double2(a0 * f.x, a0 * f.y);
+            if (two) {
+                const double2 g = Fr[(size_t)fd.src1 * ms + m];
+                x.x = fma(a1, g.x, x.x);
+                x.y = fma(a1, g.y, x.y);
+            }
+        } else {
+            const double bs = m * isin[j];
+            const double bb = b0 * bs;
+            x = make_double2(fma(a0, f.x, -bb * f.y), fma(a0, f.y, bb * f.x));
+            if (two) {
+                const double2 g = Fr[(size_t)fd.src1 * ms + m];
+                const double cc = b1 * bs;
+                x.x += fma(a1, g.x, -cc * g.y);
+                x.y += fma(a1, g.y, cc * g.x);
+            }
         }
         if (m == 0) x.y = 0.0;
-        X[(size_t)r * ms + m] = make_double2(x.x * kNrm, x.y * kNrm);
+        X[(size_t)r * ms + m] = x;
     }
     __syncthreads();
-    // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O
-    for (int idx = tid; idx < nr * n; idx += nthr) {
-        const int r = dn.div(idx), k = idx - r * n;
+    // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O.
+    // Z[n-k] = conj(E) + i conj(O): one pass over k = 0 .. n/2 forms both of a pair.
+    const int nhalf = n / 2 + 1;
+    const StageDiv dnh(nhalf);
+    for (int idx = tid; idx < nr * nhalf; idx += nthr) {
+        const int r = dnh.div(idx), k = idx - r * nhalf;
         const int kc = n - k;
         const double2 xk = k <= T ? X[(size_t)r * ms + k] : make_double2(0.0, 0.0);
         const double2 xc = (kc <= T && kc < n) ? X[(size_t)r * ms + kc] : make_double2(0.0, 0.0);
@@ -68,6 +81,7 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
         const double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
         const double2 O = cmulconj(D, twN[k]);
         A[(size_t)r * n + k] = make_double2(E.x - O.y, E.y + O.x);
+        if (k > 0 && k < kc) A[(size_t)r * n + kc] = make_double2(E.x + O.y, O.x - E.y);
     }
     __syncthreads();
     double2 *res = fft_rows<true>(A, B, nr, n, plan, tw, tid, nthr);

@@ -50,8 +50,17 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the T85/T170/T341 transform sweep")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner of the batched form")
+    ap.add_argument("--shapes-from-cache", action="store_true",
+                    help="take every handle's launch shapes from the AEROS_TUNE_CACHE file written by an earlier "
+                         "run (handles load them when created) instead of timing candidates; for profiling the "
+                         "same shapes under ncu")
     ap.add_argument("--no-transport", action="store_true", help="skip the tracer-transport measurement")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.shapes_from_cache:
+        if not os.environ.get("AEROS_TUNE_CACHE"):
+            ap.error("--shapes-from-cache needs AEROS_TUNE_CACHE")
+        a.no_tune = True
+    return a
 
 
 def reduce_time(local_s, world, backend="nccl"):

@@ -1,6 +1,7 @@
-"""Split precision on an ensemble large enough (T42L20 x 8 members, 65,536 grid
-columns) for its ensemble kernels: the double-float column kernel and the
-exact fixed-point level products of the semi-implicit solve.  Every member
+"""Split precision on an ensemble large enough (T42L20 x 10 members: 81,920 grid
+columns, 18,920 real spectral columns) for its ensemble kernels: the
+double-float column kernel and the exact fixed-point level products of the
+semi-implicit solve.  Every member
 against the FP64 oracle (and the divergence tendency against the long-double
 truth) at the split form's 1e-10 bar, tendencies and 5 steps, with two
 different member states interleaved so that cross-talk between members shows.
@@ -20,7 +21,7 @@ def test_split_ensemble_kernels_match_oracle(gpulib):
     from aeros_gb300.dynamics import AerosDyn
     from oracle.pyoracle import OracleDyn
     from tests.test_gpu_dyn import moving_state
-    M = 8
+    M = 10
     g = AerosDyn(held_suarez_params(trunc=42, nlev=20, nmember=M, precision=PREC_SPLIT))
     oracles, states = [], []
     for seed in (41, 42):
