@@ -118,6 +118,7 @@ _PROTOS = {
     "aeros_group_step_async": [_vp, _i],
     "aeros_group_sync": [_vp],
     "aeros_group_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "aeros_group_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "aeros_sht_synthesis_ad": [_vp, _vp, _vp, _i],
     "aeros_sht_analysis_ad": [_vp, _vp, _vp, _i],
     "aeros_sht_synthesis_vec_ad": [_vp, _vp, _vp, _vp, _vp, _i],

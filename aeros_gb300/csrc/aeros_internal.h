@@ -124,6 +124,100 @@ struct Tune {
     int sp_dft_cps = 8;             // split DFT products: CTAs per SM over the grid: 2, 4, 8, 16
 };
 
+// ---------------------------------------------------------------- ragged launches
+// The step kernels take their arguments as a RagPack: up to kRagMax argument
+// sets ("parts", one per dynamics handle), each with its own grid.  A launch
+// of one part keeps that part's grid; a fused launch runs the parts' blocks
+// back to back in one 1-D grid, and each block finds its part, block index and
+// grid from the header.  This is how an ensemble group of handles with
+// different truncations and level counts steps with one launch per kernel.
+constexpr int kRagMax = 4;
+struct RagHdr {
+    int n;                          // parts (1: the launch grid is the part's own)
+    unsigned start[kRagMax + 1];    // first linear block of each part in a fused grid
+    uint3 grid[kRagMax];            // each part's grid
+};
+template <class A>
+struct RagPack {
+    RagHdr h;
+    A a[kRagMax];
+};
+
+#ifdef __CUDACC__
+// This block's argument set, block index and grid within its part.  Every
+// step kernel is instantiated twice: RAG = false for a launch of one part
+// (the arguments are read at fixed offsets, as plain kernel parameters are)
+// and RAG = true for a fused launch.
+template <bool RAG, class A>
+__device__ __forceinline__ const A &rag_part(const RagPack<A> &p, uint3 &bid, uint3 &gdim) {
+    if (!RAG) {
+        bid = blockIdx;
+        gdim = gridDim;
+        return p.a[0];
+    }
+    const unsigned b = blockIdx.x;
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < kRagMax; ++i)
+        if (i < p.h.n && b >= p.h.start[i]) k = i;
+    const uint3 g = p.h.grid[k];
+    const unsigned li = b - p.h.start[k];
+    bid = make_uint3(li % g.x, (li / g.x) % g.y, li / (g.x * g.y));
+    gdim = g;
+    return p.a[k];
+}
+#endif
+
+// A kernel launch as recorded for fusion: the kernel (and its fused-launch
+// instantiation `rfunc`), its shape and the image of a one-part RagPack
+// (argument set at byte `aoff`, `asize` bytes).
+struct LaunchRec {
+    const void *func = nullptr, *rfunc = nullptr;
+    const void *mfunc = nullptr;   // a fused-launch kernel of the same family accepting other template variants
+
+    dim3 grid, block;
+    size_t smem = 0;
+    std::vector<unsigned char> pack;
+    size_t aoff = 0, asize = 0;
+};
+using LaunchList = std::vector<LaunchRec>;
+
+int launch_kernel(const void *func, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t st);
+
+// Launch `func` (a kernel taking RagPack<A>, RAG = false) with one part, or
+// append the launch to `rec` when recording (`rfunc`: the RAG = true
+// instantiation of the same kernel).
+template <class A>
+int emit_launch(cudaStream_t st, LaunchList *rec, const void *func, const void *rfunc, dim3 grid, dim3 block,
+                size_t smem, const A &a, const void *mfunc = nullptr) {
+    RagPack<A> p{};
+    p.h.n = 1;
+    p.h.start[1] = grid.x * grid.y * grid.z;
+    p.h.grid[0] = make_uint3(grid.x, grid.y, grid.z);
+    p.a[0] = a;
+    if (rec) {
+        LaunchRec r;
+        r.func = func;
+        r.rfunc = rfunc;
+        r.mfunc = mfunc;
+        r.grid = grid;
+        r.block = block;
+        r.smem = smem;
+        r.pack.assign(reinterpret_cast<const unsigned char *>(&p), reinterpret_cast<const unsigned char *>(&p) + sizeof p);
+        r.aoff = reinterpret_cast<const unsigned char *>(&p.a[0]) - reinterpret_cast<const unsigned char *>(&p);
+        r.asize = sizeof(A);
+        rec->push_back(std::move(r));
+        return AEROS_OK;
+    }
+    void *args[] = {&p};
+    return launch_kernel(func, grid, block, args, smem, st);
+}
+// One launch of the parts `ps` (same block shape, at most kRagMax): through the
+// fused-launch instantiation when they share the kernel, else through `mfunc`.
+LaunchRec fuse_launches(const std::vector<const LaunchRec *> &ps);
+// Launch a recorded (or fused) launch on `st`.
+int replay_launch(const LaunchRec &r, cudaStream_t st);
+
 // Launch context for the transform kernels.
 struct Ctx {
     int T, nlon, nlat, nh, nlm, ms;
@@ -131,6 +225,7 @@ struct Ctx {
     cudaStream_t stream;
     long long *launches;         // launch counter (host)
     const Tune *tune = nullptr;  // launch shapes (nullptr: defaults)
+    LaunchList *rec = nullptr;   // record the launches instead of issuing them
 };
 // Largest latitude count per Fourier CTA that fits `smem_per_lat` bytes in 200 KB.
 int fourier_lpb_limit(size_t smem_per_lat);

@@ -30,17 +30,14 @@ __device__ __forceinline__ df2 df_shfl(df2 v, int src) {
 // idle); pass 2 carries the partial sums from the top, so the flux above a
 // level is its running sum and the geopotential below it H less the running
 // sum.
-__global__ void __launch_bounds__(256) k_column_df(const double *__restrict__ G, double *__restrict__ GA, int NL,
-                                                   int nlon, int nlat, int M, const double *__restrict__ xlat,
-                                                   const double *__restrict__ phis, int hs_on,
-                                                   const double *__restrict__ hs_dty,
-                                                   const double *__restrict__ hs_ka, const DynConst *__restrict__ dc,
-                                                   const LevConstDF *__restrict__ ldf,
-                                                   const double2 *__restrict__ tspec, int nlm) {
+template <bool RAG = false>
+__global__ void __launch_bounds__(256) k_column_df(const __grid_constant__ RagPack<ColArgs> rpk) {
+    COLUMN_ARGS;
+    const LevConstDF *__restrict__ ldf = cka.ldf;
     const LevConst *c_lev = dc->lev;
     const ColConstDF &K = dc->cdf;
     const long ng = (long)nlon * nlat;
-    const long gid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long gid = bid.x * (long)blockDim.x + threadIdx.x;
     if (gid >= ng * M) return;
     const int e = (int)(gid / ng);
     const long c = gid - (long)e * ng;

@@ -13,6 +13,8 @@
 //   7-8 mass fixer: lnps synthesis + exp + quadrature, then the (0,0) fix
 // The start-up step (h = dt, old <- now, mass target capture) is its own graph.
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 #include <algorithm>
@@ -71,13 +73,37 @@ struct DynConst {
 // of levels.  The two vertical sums (mass flux from the top, geopotential from
 // the surface) are passed from lane to lane in level order, so every rounding
 // is the one-lane kernel's and the results do not depend on LPC.
-template <int LPC>
-__global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, double *__restrict__ GA, int NL,
-                                                int nlon, int nlat, int M, const double *__restrict__ xlat,
-                                                const double *__restrict__ phis, int hs_on,
-                                                const double *__restrict__ hs_dty, const double *__restrict__ hs_ka,
-                                                const DynConst *__restrict__ dc, const double2 *__restrict__ tspec,
-                                                int nlm) {
+struct LevConstDF;
+// Arguments of the column kernels (k_column, k_column_df).
+struct ColArgs {
+    const double *G;
+    double *GA;
+    int NL, nlon, nlat, M;
+    const double *xlat, *phis;
+    int hs_on;
+    const double *hs_dty, *hs_ka;
+    const DynConst *dc;
+    const LevConstDF *ldf;
+    const double2 *tspec;
+    int nlm;
+};
+#define COLUMN_ARGS                                                                      \
+    uint3 bid, gdim;                                                                     \
+    const ColArgs &cka = rag_part<RAG>(rpk, bid, gdim);                                         \
+    (void)gdim;                                                                          \
+    const double *__restrict__ G = cka.G;                                                 \
+    double *__restrict__ GA = cka.GA;                                                     \
+    const int NL = cka.NL, nlon = cka.nlon, nlat = cka.nlat, M = cka.M, hs_on = cka.hs_on;   \
+    const double *__restrict__ xlat = cka.xlat;                                           \
+    const double *__restrict__ phis = cka.phis;                                           \
+    const double *__restrict__ hs_dty = cka.hs_dty;                                       \
+    const double *__restrict__ hs_ka = cka.hs_ka;                                         \
+    const DynConst *__restrict__ dc = cka.dc;                                             \
+    const double2 *__restrict__ tspec = cka.tspec;                                        \
+    const int nlm = cka.nlm
+template <int LPC, bool RAG = false>
+__global__ void __launch_bounds__(256) k_column(const __grid_constant__ RagPack<ColArgs> rpk) {
+    COLUMN_ARGS;
     constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
     const LevConst *c_lev = dc->lev;
     const HsConst &c_hs = dc->hs;
@@ -87,7 +113,7 @@ __global__ void __launch_bounds__(256) k_column(const double *__restrict__ G, do
 #define LEVELS_UP(i) for (int i = 0; i < (kUnroll ? kChunk : nk); ++i) if (!kUnroll || i < nk)
 #define LEVELS_DOWN(i) for (int i = (kUnroll ? kChunk : nk) - 1; i >= 0; --i) if (!kUnroll || i < nk)
     const long ng = (long)nlon * nlat;
-    const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const long gt = bid.x * (long)blockDim.x + threadIdx.x;
     const long gid = gt / LPC;
     const int q = (int)(gt % LPC);
     const int base = (threadIdx.x & 31) - q;          // first lane of this column's group
@@ -313,7 +339,18 @@ __device__ __forceinline__ double2 wsum2(double2 v) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
+// Arguments of the real-column spectral kernels: the column list of each warp.
+struct SpecColArgs {
+    SpecArgs a;
+    const int2 *wtab;
+    int nwarp;
+    int exact;   // 1: exact fixed-point level products (k_spectral_xq), 0: FP64 (k_spectral_cols)
+};
+
+template <bool RAG = false>
+__global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPack<SpecArgs> rpk) {
+    uint3 bid, gdim;
+    const SpecArgs &a = rag_part<RAG>(rpk, bid, gdim);
     __shared__ double sG[kMaxLev * kMaxLev], sT[kMaxLev * kMaxLev], sW[kMaxLev * kMaxLev];
     __shared__ double sNu[kMaxLev], sPc[kMaxLev];
     const int NL = a.NL;
@@ -327,7 +364,7 @@ __global__ void __launch_bounds__(256) k_spectral(SpecArgs a) {
         sPc[i] = a.pcoef[i];
     }
     __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warp = (bid.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= a.nlm * a.M) return;
     const int e = warp / a.nlm, lm = warp - e * a.nlm;
@@ -439,8 +476,13 @@ __host__ __device__ constexpr size_t spec_cols_smem(int threads) {
     return sizeof(double) * (3 * NLT * NLT + 2 * NLT + 2 * (size_t)NLT * threads);
 }
 
-template <int NLT>
-__global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
+template <int NLT, bool RAG>
+__device__ __forceinline__ void spectral_cols_body(const RagPack<SpecColArgs> &rpk) {
+    uint3 bid, gdim;
+    const SpecColArgs &sa = rag_part<RAG>(rpk, bid, gdim);
+    const SpecArgs &a = sa.a;
+    const int2 *__restrict__ wtab = sa.wtab;
+    const int nwarp = sa.nwarp;
     extern __shared__ double sm_cols[];
     double *sG = sm_cols, *sT = sG + NLT * NLT, *sW = sT + NLT * NLT, *sNu = sW + NLT * NLT, *sPc = sNu + NLT;
     double *v1 = sPc + NLT + threadIdx.x, *v2 = v1 + NLT * blockDim.x;   // slot k at [k * blockDim.x]
@@ -455,7 +497,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
         sPc[i] = a.pcoef[i];
     }
     __syncthreads();
-    const int warp = (blockIdx.x * nt + threadIdx.x) >> 5;
+    const int warp = (bid.x * nt + threadIdx.x) >> 5;
     if (warp >= nwarp) return;
     const int2 wl = wtab[warp];
     const int l = wl.x, idx = wl.y + (threadIdx.x & 31);
@@ -592,6 +634,11 @@ __global__ void __launch_bounds__(256, 2) k_spectral_cols(SpecArgs a, const int2
     reinterpret_cast<double *>(a.lnps)[op] = pnew;
 }
 
+template <int NLT, bool RAG = false>
+__global__ void __launch_bounds__(256, 2) k_spectral_cols(const __grid_constant__ RagPack<SpecColArgs> rpk) {
+    spectral_cols_body<NLT, RAG>(rpk);
+}
+
 // Level counts with a column-layout instantiation.
 constexpr int kSpecColLevels[] = {16, 20};
 // The split form's update for ensembles: the same semi-implicit step, with
@@ -616,8 +663,13 @@ __host__ __device__ constexpr size_t spec_xq_smem(int warps) {
            (size_t)warps * kXqCols * NLT * (2 * sizeof(double) + sizeof(int2));
 }
 
-template <int NLT>
-__global__ void __launch_bounds__(256, 2) k_spectral_xq(SpecArgs a, const int2 *__restrict__ wtab, int nwarp) {
+template <int NLT, bool RAG>
+__device__ __forceinline__ void spectral_xq_body(const RagPack<SpecColArgs> &rpk) {
+    uint3 bid, gdim;
+    const SpecColArgs &sa = rag_part<RAG>(rpk, bid, gdim);
+    const SpecArgs &a = sa.a;
+    const int2 *__restrict__ wtab = sa.wtab;
+    const int nwarp = sa.nwarp;
     static_assert(NLT % 4 == 0, "levels split four ways");
     constexpr int NQ = NLT / 4;   // levels per thread
     extern __shared__ double sm_xq[];
@@ -642,7 +694,7 @@ __global__ void __launch_bounds__(256, 2) k_spectral_xq(SpecArgs a, const int2 *
         sE[2 * NLT + i] = a.eW[i];
     }
     __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warp = (bid.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= nwarp) return;   // whole warps leave together
     const int2 wl = wtab[warp];
     const int l = wl.x, idx = wl.y + cl;
@@ -794,6 +846,28 @@ __global__ void __launch_bounds__(256, 2) k_spectral_xq(SpecArgs a, const int2 *
     }
 }
 
+template <int NLT, bool RAG = false>
+__global__ void __launch_bounds__(256, 2) k_spectral_xq(const __grid_constant__ RagPack<SpecColArgs> rpk) {
+    spectral_xq_body<NLT, RAG>(rpk);
+}
+
+// A fused launch over handles whose real-column spectral kernels differ (level
+// count, exact or FP64 level products): each CTA runs its part's body.
+__global__ void __launch_bounds__(256, 2) k_spectral_mixed(const __grid_constant__ RagPack<SpecColArgs> rpk) {
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < kRagMax; ++i)
+        if (i < rpk.h.n && blockIdx.x >= rpk.h.start[i]) k = i;
+    const SpecColArgs &sa = rpk.a[k];
+    if (sa.exact) {
+        if (sa.a.NL == 16) spectral_xq_body<16, true>(rpk);
+        else spectral_xq_body<20, true>(rpk);
+    } else {
+        if (sa.a.NL == 16) spectral_cols_body<16, true>(rpk);
+        else spectral_cols_body<20, true>(rpk);
+    }
+}
+
 bool spec_cols_available(int nlev) {
     for (int n : kSpecColLevels)
         if (n == nlev) return true;
@@ -826,9 +900,17 @@ __global__ void k_relaxation(aeros_grid_view v, double k_drag, double k_temp, do
 }
 
 // Copy X^n into the old slot (start-up step, aeros_timestep.f90:825-828).
-__global__ void k_copy(double2 *dst, const double2 *src, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = src[i];
+struct CopyArgs {
+    double2 *dst;
+    const double2 *src;
+    size_t n;
+};
+template <bool RAG = false>
+__global__ void k_copy(const __grid_constant__ RagPack<CopyArgs> rpk) {
+    uint3 bid, gdim;
+    const CopyArgs &a = rag_part<RAG>(rpk, bid, gdim);
+    for (size_t i = bid.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gdim.x * blockDim.x)
+        a.dst[i] = a.src[i];
 }
 
 // The packed step's inputs: both time levels in at once (read straight from
@@ -867,15 +949,41 @@ __global__ void k_packed_out(double2 *now_dst, const double2 *__restrict__ now, 
 // captures the target (mode 0) or restores it (mode 1, aeros_timestep.f90:1225-1251);
 // it sums the rows in latitude order, so the result does not depend on which
 // block finishes last.
-__global__ void k_mass(double2 *__restrict__ lnps, int M, int T, int nlm, int nh, int nlat, int nlon,
-                       const double *__restrict__ Ps, const int *__restrict__ moff, FftPlan plan,
-                       const double2 *__restrict__ tw, const double2 *__restrict__ twN, double *__restrict__ rows,
-                       const double *__restrict__ w, double c00, double *__restrict__ target,
-                       double *__restrict__ lnr_last, double *__restrict__ lnr_cum, unsigned *__restrict__ done,
-                       int mode) {
+struct MassArgs {
+    double2 *lnps;
+    int M, T, nlm, nh, nlat, nlon;
+    const double *Ps;
+    const int *moff;
+    FftPlan plan;
+    const double2 *tw, *twN;
+    double *rows;
+    const double *w;
+    double c00;
+    double *target, *lnr_last, *lnr_cum;
+    unsigned *done;
+    int mode;
+};
+template <bool RAG = false>
+__global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
+    uint3 bid, gdim;
+    const MassArgs &mka = rag_part<RAG>(rpk, bid, gdim);
+    double2 *__restrict__ lnps = mka.lnps;
+    const int T = mka.T, nlm = mka.nlm, nh = mka.nh, nlat = mka.nlat, nlon = mka.nlon, mode = mka.mode;
+    const double *__restrict__ Ps = mka.Ps;
+    const int *__restrict__ moff = mka.moff;
+    const FftPlan &plan = mka.plan;
+    const double2 *__restrict__ tw = mka.tw;
+    const double2 *__restrict__ twN = mka.twN;
+    double *__restrict__ rows = mka.rows;
+    const double *__restrict__ w = mka.w;
+    const double c00 = mka.c00;
+    double *__restrict__ target = mka.target;
+    double *__restrict__ lnr_last = mka.lnr_last;
+    double *__restrict__ lnr_cum = mka.lnr_cum;
+    unsigned *__restrict__ done = mka.done;
     extern __shared__ double2 sm[];
     const int n = nlon / 2, ms = T + 1;
-    const int e = blockIdx.y, jn = blockIdx.x, js = nlat - 1 - jn;
+    const int e = bid.y, jn = bid.x, js = nlat - 1 - jn;
     double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * n;
     const double2 *c = lnps + (size_t)e * nlm;
     // thread per (m, parity of l - m): each sums its parity in the serial order,
@@ -1221,7 +1329,8 @@ struct aeros_dyn_s {
     double2 *div(double2 *b) const { return b + (size_t)M * ns3(); }
     double2 *tmp(double2 *b) const { return b + (size_t)2 * M * ns3(); }
     double2 *lnp(double2 *b) const { return b + (size_t)3 * M * ns3(); }
-    Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches, &tune}; }
+    LaunchList *rec = nullptr;   // record the step's launches (ensemble fusion) instead of issuing them
+    Ctx ctx() { return Ctx{g.T, g.nlon, g.nlat, g.nh, g.nlm, g.ms, &tab, stream, &launches, &tune, rec}; }
 };
 
 namespace {
@@ -1230,7 +1339,7 @@ using Dyn = aeros_dyn_s;
 
 // Record a profiling event after a launch (no-op outside aeros_dyn_profile_step).
 void mark(Dyn &d, const char *name) {
-    if (!d.prof) return;
+    if (!d.prof || d.rec) return;
     cudaEvent_t e;
     cudaEventCreate(&e);
     cudaEventRecord(e, d.stream);
@@ -1698,24 +1807,20 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
     const int ct = d.tune.col_thr, lpc = d.tune.col_lanes;
     const unsigned nb = (unsigned)((ncol * lpc + ct - 1) / ct);
-    auto go = [&](auto kern) {
-        kern<<<nb, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
-                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
-                                      d.tmp(d.now), d.g.nlm);
-    };
-    auto go_df = [&](auto kern, unsigned nbd) {
-        kern<<<nbd, ct, 0, d.stream>>>(d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d,
-                                      d.phis_set ? d.phis_d : nullptr, hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst,
-                                      d.ldf, d.tmp(d.now), d.g.nlm);
+    const ColArgs ca{d.G, d.GA, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d, d.phis_set ? d.phis_d : nullptr,
+                     hs_on, d.hs_dty_d, d.hs_ka_d, d.dconst, d.ldf, d.tmp(d.now), d.g.nlm};
+    auto go = [&](const void *kern, const void *rkern, unsigned nbk) {
+        return emit_launch(d.stream, d.rec, kern, rkern, dim3(nbk), dim3(ct), 0, ca);
     };
     if (split_column_df(d)) {
         // split form: the column terms in double-float on the FP32/INT32 pipes, a thread per column
-        go_df(k_column_df, (unsigned)((ncol + ct - 1) / ct));
-    } else if (lpc == 16) go(k_column<16>);
-    else if (lpc == 8) go(k_column<8>);
-    else if (lpc == 4) go(k_column<4>);
-    else if (lpc == 2) go(k_column<2>);
-    else go(k_column<1>);
+        rc = go((const void *)k_column_df<>, (const void *)k_column_df<true>, (unsigned)((ncol + ct - 1) / ct));
+    } else if (lpc == 16) rc = go((const void *)k_column<16>, (const void *)k_column<16, true>, nb);
+    else if (lpc == 8) rc = go((const void *)k_column<8>, (const void *)k_column<8, true>, nb);
+    else if (lpc == 4) rc = go((const void *)k_column<4>, (const void *)k_column<4, true>, nb);
+    else if (lpc == 2) rc = go((const void *)k_column<2>, (const void *)k_column<2, true>, nb);
+    else rc = go((const void *)k_column<1>, (const void *)k_column<1, true>, nb);
+    if (rc) return rc;
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "column");
@@ -1737,11 +1842,11 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
 int run_mass(Dyn &d, int mode) {
     const int n = d.g.nlon / 2;
     size_t smem = (size_t)(2 * d.g.ms + 4 * n) * sizeof(double2);
-    if (int rc = raise_smem_limit((const void *)k_mass, smem)) return rc;
-    k_mass<<<dim3(d.g.nh, d.M), 128, smem, d.stream>>>(d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat,
-                                                       d.g.nlon, d.tab.Ps, d.tab.moff, d.tab.plan, d.tab.tw,
-                                                       d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt,
-                                                       d.lnr_last, d.lnr_cum, d.mass_done, mode);
+    if (int rc = raise_smem_limit((const void *)k_mass<>, smem)) return rc;
+    const MassArgs ma{d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat, d.g.nlon, d.tab.Ps, d.tab.moff,
+                      d.tab.plan, d.tab.tw, d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt, d.lnr_last,
+                      d.lnr_cum, d.mass_done, mode};
+    if (int rc = emit_launch(d.stream, d.rec, (const void *)k_mass<>, (const void *)k_mass<true>, dim3(d.g.nh, d.M), dim3(128), smem, ma)) return rc;
     mark(d, "mass");
     d.launches += 1;
     AEROS_CUDA(cudaGetLastError());
@@ -1753,7 +1858,9 @@ int enqueue_step(Dyn &d, bool startup) {
     int rc;
     const size_t nst = d.nstate();
     if (startup) {
-        k_copy<<<256, 256, 0, d.stream>>>(d.old, d.now, nst);
+        if ((rc = emit_launch(d.stream, d.rec, (const void *)k_copy<>, (const void *)k_copy<true>, dim3(256), dim3(256), 0,
+                              CopyArgs{d.old, d.now, nst})))
+            return rc;
         ++d.launches;
         mark(d, "copy");
         if (d.par.mass_fixer && (rc = run_mass(d, 0))) return rc;
@@ -1785,20 +1892,28 @@ int enqueue_step(Dyn &d, bool startup) {
     // the split form of an ensemble takes the exact-product kernel (four threads per real column)
     if (split_spectral_exact(d)) {
         const unsigned nb = (unsigned)((d.spec_nw8 + sw - 1) / sw);
-        if (d.NL == 16)
-            k_spectral_xq<16><<<nb, 32 * sw, spec_xq_smem<16>(sw), d.stream>>>(a, d.spec_wt8, d.spec_nw8);
-        else
-            k_spectral_xq<20><<<nb, 32 * sw, spec_xq_smem<20>(sw), d.stream>>>(a, d.spec_wt8, d.spec_nw8);
+        const SpecColArgs sa{a, d.spec_wt8, d.spec_nw8, 1};
+        rc = d.NL == 16 ? emit_launch(d.stream, d.rec, (const void *)k_spectral_xq<16>,
+                                      (const void *)k_spectral_xq<16, true>, dim3(nb), dim3(32 * sw),
+                                      spec_xq_smem<16>(sw), sa, (const void *)k_spectral_mixed)
+                        : emit_launch(d.stream, d.rec, (const void *)k_spectral_xq<20>,
+                                      (const void *)k_spectral_xq<20, true>, dim3(nb), dim3(32 * sw),
+                                      spec_xq_smem<20>(sw), sa, (const void *)k_spectral_mixed);
     } else if (d.tune.spec_cols && spec_cols_available(d.NL)) {
         const unsigned nb = (unsigned)((d.spec_nw + sw - 1) / sw);
-        if (d.NL == 16)
-            k_spectral_cols<16><<<nb, 32 * sw, spec_cols_smem<16>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
-        else
-            k_spectral_cols<20><<<nb, 32 * sw, spec_cols_smem<20>(32 * sw), d.stream>>>(a, d.spec_wt, d.spec_nw);
+        const SpecColArgs sa{a, d.spec_wt, d.spec_nw, 0};
+        rc = d.NL == 16 ? emit_launch(d.stream, d.rec, (const void *)k_spectral_cols<16>,
+                                      (const void *)k_spectral_cols<16, true>, dim3(nb), dim3(32 * sw),
+                                      spec_cols_smem<16>(32 * sw), sa, (const void *)k_spectral_mixed)
+                        : emit_launch(d.stream, d.rec, (const void *)k_spectral_cols<20>,
+                                      (const void *)k_spectral_cols<20, true>, dim3(nb), dim3(32 * sw),
+                                      spec_cols_smem<20>(32 * sw), sa, (const void *)k_spectral_mixed);
     } else {
         long nw = (long)d.g.nlm * d.M;
-        k_spectral<<<(unsigned)((nw + sw - 1) / sw), 32 * sw, 0, d.stream>>>(a);
+        rc = emit_launch(d.stream, d.rec, (const void *)k_spectral<>, (const void *)k_spectral<true>, dim3((unsigned)((nw + sw - 1) / sw)),
+                         dim3(32 * sw), 0, a);
     }
+    if (rc) return rc;
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
     mark(d, "spectral");
@@ -2547,10 +2662,131 @@ struct aeros_group_s {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    bool fused = false;   // one launch per kernel over the members' handles (else one child graph per handle)
     long long kernels[2] = {0, 0};
     long long launches = 0;
     int nstep = 0;
 };
+
+namespace {
+
+// The step's launches of every handle, recorded and fused position by position:
+// at each position of the (equally long) launch sequences, the handles that use
+// the same kernel with the same block shape share one ragged launch (at most
+// kRagMax per launch), the heaviest truncation first so that the lighter blocks
+// fill the tail.  Returns AEROS_ERR_UNSUPPORTED when the sequences differ.
+int fused_step_launches(aeros_group_s *g, bool startup, std::vector<LaunchRec> &out) {
+    const int n = (int)g->dyn.size();
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return g->dyn[a]->g.T * g->dyn[a]->M > g->dyn[b]->g.T * g->dyn[b]->M; });
+    std::vector<LaunchList> L(n);
+    for (int i = 0; i < n; ++i) {
+        Dyn &d = *g->dyn[order[i]];
+        if (d.phys_fn) return AEROS_ERR_UNSUPPORTED;   // a hook may launch anything
+        const long long before = d.launches;
+        d.rec = &L[i];
+        const int rc = enqueue_step(d, startup);
+        d.rec = nullptr;
+        d.launches = before;
+        if (rc) return rc;
+        if (L[i].size() != L[0].size()) return AEROS_ERR_UNSUPPORTED;
+    }
+    out.clear();
+    for (size_t pos = 0; pos < L[0].size(); ++pos) {
+        std::vector<bool> used(n, false);
+        for (int i = 0; i < n; ++i) {
+            if (used[i]) continue;
+            const LaunchRec &r = L[i][pos];
+            std::vector<const LaunchRec *> parts;
+            // the same kernel, or kernels of one family with a mixed fused form
+            auto same = [&](const LaunchRec &q) {
+                return q.func == r.func || (q.mfunc && q.mfunc == r.mfunc);
+            };
+            for (int j = i; j < n; ++j) {
+                const LaunchRec &q = L[j][pos];
+                if (used[j] || !same(q) || q.block.x != r.block.x || q.block.y != r.block.y ||
+                    q.block.z != r.block.z)
+                    continue;
+                used[j] = true;
+                parts.push_back(&q);
+                if ((int)parts.size() == kRagMax) {
+                    out.push_back(fuse_launches(parts));
+                    parts.clear();
+                }
+            }
+            if (parts.size() == 1) out.push_back(*parts[0]);
+            else if (!parts.empty()) out.push_back(fuse_launches(parts));
+        }
+    }
+    return AEROS_OK;
+}
+
+// The block shapes of the kernels the handles share (Fourier and Legendre
+// block sizes, column and spectral block sizes and layouts) taken from the
+// heaviest handle, so that their launches fuse; grid-only shapes stay per
+// handle.  Each changed handle re-captures its own step graphs.
+int unify_shapes(aeros_group_s *g) {
+    Dyn *top = g->dyn[0];
+    for (Dyn *d : g->dyn)
+        if (d->g.T * d->M > top->g.T * top->M) top = d;
+    for (Dyn *d : g->dyn) {
+        Tune &t = d->tune;
+        const Tune &u = top->tune;
+        if (t.fs_thr == u.fs_thr && t.fa_thr == u.fa_thr && t.la_ct == u.la_ct && t.ls_jt == u.ls_jt &&
+            t.col_thr == u.col_thr && t.col_lanes == u.col_lanes && t.spec_warps == u.spec_warps &&
+            t.spec_cols == u.spec_cols)
+            continue;
+        t.fs_thr = u.fs_thr;
+        t.fa_thr = u.fa_thr;
+        t.la_ct = u.la_ct;
+        t.ls_jt = u.ls_jt;
+        t.col_thr = u.col_thr;
+        t.col_lanes = u.col_lanes;
+        t.spec_warps = u.spec_warps;
+        t.spec_cols = u.spec_cols;
+        if (int rc = capture_graphs(*d)) return rc;
+    }
+    return AEROS_OK;
+}
+
+int capture_fused(aeros_group_s *g, bool startup, cudaGraphExec_t *exec, long long *kernels) {
+    std::vector<LaunchRec> seq;
+    if (int rc = fused_step_launches(g, startup, seq)) return rc;
+    for (const LaunchRec &r : seq)
+        if (int rc = raise_smem_limit(r.func, r.smem)) return rc;
+    const char *tr = std::getenv("AEROS_GROUP_TRACE");
+    if (tr && tr[0] == '1')
+        for (const LaunchRec &r : seq) {
+            const char *name = nullptr;
+            if (cudaFuncGetName(&name, r.func) != cudaSuccess) name = "?";
+            std::fprintf(stderr, "group %s launch: %s parts %d grid %u block %u smem %zu\n",
+                         startup ? "start-up" : "step", name, reinterpret_cast<const RagHdr *>(r.pack.data())->n,
+                         r.grid.x * r.grid.y * r.grid.z, r.block.x, r.smem);
+        }
+    cudaGraph_t graph;
+    AEROS_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = AEROS_OK;
+    for (const LaunchRec &r : seq)
+        if ((rc = replay_launch(r, g->stream))) break;
+    cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) {
+        set_error(std::string("group capture: ") + cudaGetErrorString(e));
+        return AEROS_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error(std::string("group graph: ") + cudaGetErrorString(e));
+        return AEROS_ERR_CUDA;
+    }
+    *kernels = (long long)seq.size();
+    return AEROS_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -2565,6 +2801,28 @@ int aeros_group_create(aeros_group_t *out, aeros_dyn_t *handles, int n) {
         g->dyn.push_back(handles[i]);
     }
     g->nstep = handles[0]->nstep;
+    AEROS_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    g->own_stream = true;
+    const char *fz = std::getenv("AEROS_GROUP_FUSE");
+    if (!(fz && fz[0] == '0')) {
+        g->fused = true;
+        for (auto *h : g->dyn)
+            if (h->phys_fn) g->fused = false;
+        if (g->fused)
+            if (int rc = unify_shapes(g)) { aeros_group_destroy(g); return rc; }
+        for (int s = 0; s < 2 && g->fused; ++s) {
+            const int rc = capture_fused(g, s == 0, &g->exec[s], &g->kernels[s]);
+            if (rc == AEROS_ERR_UNSUPPORTED) g->fused = false;
+            else if (rc) { aeros_group_destroy(g); return rc; }
+        }
+        if (g->fused) {
+            *out = g;
+            return AEROS_OK;
+        }
+        for (auto &e : g->exec)
+            if (e) { cudaGraphExecDestroy(e); e = nullptr; }
+        g->kernels[0] = g->kernels[1] = 0;
+    }
     for (int s = 0; s < 2; ++s) {
         cudaGraph_t root;
         AEROS_CUDA(cudaGraphCreate(&root, 0));
@@ -2577,12 +2835,10 @@ int aeros_group_create(aeros_group_t *out, aeros_dyn_t *handles, int n) {
         cudaGraphDestroy(root);
         if (e != cudaSuccess) {
             set_error(std::string("group graph: ") + cudaGetErrorString(e));
-            delete g;
+            aeros_group_destroy(g);
             return AEROS_ERR_CUDA;
         }
     }
-    AEROS_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
-    g->own_stream = true;
     *out = g;
     return AEROS_OK;
 }
@@ -2642,6 +2898,14 @@ int aeros_group_step(aeros_group_t g, int nsteps) {
 int aeros_group_launch_count(aeros_group_t g, long long *count) {
     if (!g || !count) return AEROS_ERR_ARG;
     *count = g->launches;
+    return AEROS_OK;
+}
+
+int aeros_group_info(aeros_group_t g, int *fused, long long *kernels_startup, long long *kernels_step) {
+    if (!g) return AEROS_ERR_ARG;
+    if (fused) *fused = g->fused ? 1 : 0;
+    if (kernels_startup) *kernels_startup = g->kernels[0];
+    if (kernels_step) *kernels_step = g->kernels[1];
     return AEROS_OK;
 }
 

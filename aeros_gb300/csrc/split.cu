@@ -147,8 +147,10 @@ static_assert((size_t)7 * kNTa * kKC * 2 + kNTa * kSt * 8 >= 128 * kSdStride * 8
 // (for a one-chunk contraction) the table tile kept.  Software pipeline: the
 // next group's coefficients are gathered (and its column scales formed) into
 // the second stage buffer while the tensor core works on the current group.
-template <int S, int B>
-__global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
+template <int S, int B, bool RAG = false>
+__global__ void __launch_bounds__(kThreads, 2) k_split_synth(const __grid_constant__ RagPack<SynSplitArgs> rp) {
+    uint3 bid, gdim;
+    const SynSplitArgs &a = rag_part<RAG>(rp, bid, gdim);
     // shared memory: sA | stage 1 | sB | stage 0, so that sB with the stage
     // buffer of the current group is one contiguous block for the epilogue
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -168,14 +170,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(SynSplitArgs a) {
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int slot = a.smajor ? blockIdx.x : blockIdx.z, m = a.smajor ? blockIdx.y : blockIdx.x,
-              t = a.smajor ? blockIdx.z : blockIdx.y;
+    const int slot = a.smajor ? bid.x : bid.z, m = a.smajor ? bid.y : bid.x, t = a.smajor ? bid.z : bid.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = a.T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
     const int mo = a.moff[m];
     const int ngrp = (a.ncol + kNTs / 2 - 1) / (kNTs / 2);
     if (slot >= ngrp) return;
-    const int gstep = a.smajor ? gridDim.x : gridDim.z;
+    const int gstep = a.smajor ? gdim.x : gdim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -455,8 +456,10 @@ struct AnaMeta {
 // contraction) the table tile kept.  Software pipeline: the next group's grid
 // values are gathered (and its column scales formed) into the second stage
 // buffer while the tensor core works on the current group.
-template <int S, int B>
-__global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
+template <int S, int B, bool RAG = false>
+__global__ void __launch_bounds__(kThreads, 2) k_split_anal(const __grid_constant__ RagPack<AnaSplitArgs> rp) {
+    uint3 bid, gdim;
+    const AnaSplitArgs &a = rag_part<RAG>(rp, bid, gdim);
     // shared memory: sA | stage 1 | sB | stage 0; the epilogue's row table
     // takes sB with the current group's stage buffer (contiguous either way)
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -475,14 +478,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(AnaSplitArgs a) {
         if (threadIdx.x == 0) atomicOr(a.err, 2);
         return;
     }
-    const int slot = a.smajor ? blockIdx.x : blockIdx.z, m = a.smajor ? blockIdx.y : blockIdx.x,
-              t = a.smajor ? blockIdx.z : blockIdx.y;
+    const int slot = a.smajor ? bid.x : bid.z, m = a.smajor ? bid.y : bid.x, t = a.smajor ? bid.z : bid.y;
     const int K = a.T - m + 1;
     const int ngrp = a.ngrp;
     if (64 * t >= K || slot >= ngrp) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
-    const int gstep = a.smajor ? gridDim.x : gridDim.z;
+    const int gstep = a.smajor ? gdim.x : gdim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -874,8 +876,11 @@ int split_leg_synth(SplitCtx *s, const Ctx &c, const SynPlan &p, double2 *F, int
     SynSplitArgs a{p.cols_d, p.ncol, c.tab->lfac, c.tab->moff, s->sbase, s->digS, s->rexpS, F,
                    nrow, c.ms, c.T, c.nh, c.nlat, s->ntl, s->err, smajor ? 1 : 0};
     const dim3 grid = split_grid(slots, c.T + 1, s->ntl, smajor);
-    if (s->S == 7) k_split_synth<7, 8><<<grid, kThreads, synth_smem<7>(), c.stream>>>(a);
-    else k_split_synth<8, 7><<<grid, kThreads, synth_smem<8>(), c.stream>>>(a);
+    int rc = s->S == 7 ? emit_launch(c.stream, c.rec, (const void *)k_split_synth<7, 8>, (const void *)k_split_synth<7, 8, true>, grid, dim3(kThreads),
+                                     synth_smem<7>(), a)
+                       : emit_launch(c.stream, c.rec, (const void *)k_split_synth<8, 7>, (const void *)k_split_synth<8, 7, true>, grid, dim3(kThreads),
+                                     synth_smem<8>(), a);
+    if (rc) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -908,8 +913,11 @@ int split_leg_anal(SplitCtx *s, const Ctx &c, const AnaCol *cols_d, const int *g
     AnaSplitArgs a{cols_d, gstart_d, ngrp, c.tab->lfac, c.tab->sint, c.tab->moff, s->abase, s->digA, s->rexpA, F,
                    nrow, c.ms, c.T, c.nh, c.nlat, s->ntlA, s->KpA, s->err, smajor ? 1 : 0};
     const dim3 grid = split_grid(slots, c.T + 1, s->ntlA, smajor);
-    if (s->S == 7) k_split_anal<7, 8><<<grid, kThreads, anal_smem<7>(), c.stream>>>(a);
-    else k_split_anal<8, 7><<<grid, kThreads, anal_smem<8>(), c.stream>>>(a);
+    int rc = s->S == 7 ? emit_launch(c.stream, c.rec, (const void *)k_split_anal<7, 8>, (const void *)k_split_anal<7, 8, true>, grid, dim3(kThreads),
+                                     anal_smem<7>(), a)
+                       : emit_launch(c.stream, c.rec, (const void *)k_split_anal<8, 7>, (const void *)k_split_anal<8, 7, true>, grid, dim3(kThreads),
+                                     anal_smem<8>(), a);
+    if (rc) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;

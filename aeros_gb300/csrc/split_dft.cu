@@ -150,16 +150,31 @@ struct DftAnalP {
 
 // ---------------------------------------------------------------- the product
 // CTA (M tile mt, group slot): rows mt*128.. of the table times column tiles
-// ct = slot, slot + gridDim.y, ... (32 data columns each), over the whole
+// ct = slot, slot + (number of slots), ... (32 data columns each), over the whole
 // contraction in 32-wide chunks.  TMEM and the barriers are set up once per CTA;
 // the first table chunk of the next tile is fetched during the epilogue.
 // FULL: the gather of a tile stages every contraction entry (each data value is
 // formed once; the synthesis columns' wind combinations cost FP64), otherwise
 // chunk 0 is staged and later chunks are formed again while the previous
 // chunk's MMA runs.
-template <int S, int B, class P, bool FULL>
-__global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch, const __nv_bfloat16 *dig,
-                                                            const int *rexp, int *err) {
+template <class P>
+struct GemmArgs {
+    P p;
+    int S;   // digits (7 or 8)
+    int K, nch;
+    const __nv_bfloat16 *dig;
+    const int *rexp;
+    int *err;
+};
+template <int S, int B, class P, bool FULL, bool RAG>
+__device__ __forceinline__ void split_gemm_body(const RagPack<GemmArgs<P>> &rp) {
+    uint3 bid, gdim;
+    const GemmArgs<P> &ga = rag_part<RAG>(rp, bid, gdim);
+    const P &p = ga.p;
+    const int K = ga.K, nch = ga.nch;
+    const __nv_bfloat16 *dig = ga.dig;
+    const int *rexp = ga.rexp;
+    int *err = ga.err;
     extern __shared__ __align__(1024) unsigned char smraw[];
     if (smem_u32(smraw) & 1023u) {
         if (threadIdx.x == 0) atomicOr(err, 2);
@@ -174,11 +189,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     __shared__ double *cbase[2][kNT];   // output column bases of the tile
     __shared__ int fail;
 
-    const int mt = blockIdx.x;
+    const int mt = bid.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Kp = (K + 15) & ~15;
     const int nct = (p.ncol() + kNT - 1) / kNT;
-    if ((int)blockIdx.y >= nct) return;
+    if ((int)bid.y >= nct) return;
     if (tid == 0) fail = 0;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -194,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     const __nv_bfloat16 *gA = dig + (size_t)mt * nch * S * kTM * kSlice;
     const int nk8 = Kp / 8, kc0 = min(kKC, Kp);
     const int Kst = FULL ? Kp + 1 : kSt;   // stage row stride (odd: conflict-free)
-    const int gstep = gridDim.y;
+    const int gstep = gdim.y;
     // phase 1 of column tile ct into buffer b: column scales over the whole contraction, chunk 0 staged
     const FastDiv dk8(nk8);
     auto gather = [&](int ct, int b) {
@@ -225,7 +240,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     if (tid < kNT) cexp[0][tid] = 0;
     __syncthreads();
     if (tid == 0) bulk_load(sA, gA, (uint32_t)(S * kTM * kSlice * 2), &mbarA);
-    gather(blockIdx.y, 0);
+    gather(bid.y, 0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -238,7 +253,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     bool ok = true;
 
     int cb = 0;   // buffer of the current tile
-    for (int ct = blockIdx.y; ct < nct && ok; ct += gstep, cb ^= 1) {
+    for (int ct = bid.y; ct < nct && ok; ct += gstep, cb ^= 1) {
         const int c0 = ct * kNT, ncl = min(kNT, p.ncol() - c0);
         const bool more = ct + gstep < nct;
         double *stage = FULL ? stage0 : stage0 + (size_t)cb * kNT * kSt;
@@ -334,6 +349,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_gemm(P p, int K, int nch,
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
+template <int S, int B, class P, bool FULL, bool RAG = false>
+__global__ void __launch_bounds__(kThreads, 2) k_split_gemm(const __grid_constant__ RagPack<GemmArgs<P>> rp) {
+    split_gemm_body<S, B, P, FULL, RAG>(rp);
+}
+
+// A fused launch over handles whose contraction lengths take different digit
+// counts ((7, 8) up to 126, (8, 7) beyond): each CTA runs the body of its part's.
+template <class P, bool FULL>
+__global__ void __launch_bounds__(kThreads, 2) k_split_gemm_mixed(const __grid_constant__ RagPack<GemmArgs<P>> rp) {
+    int k = 0;
+#pragma unroll
+    for (int i = 1; i < kRagMax; ++i)
+        if (i < rp.h.n && blockIdx.x >= rp.h.start[i]) k = i;
+    if (rp.a[k].S == 7) split_gemm_body<7, 8, P, FULL, true>(rp);
+    else split_gemm_body<8, 7, P, FULL, true>(rp);
+}
+
 }  // namespace
 
 // One direction's table: Mpad x K FP64 values cut into (M tile, K chunk) images.
@@ -422,7 +454,7 @@ template <> constexpr bool kWantFull<DftSynthP> = true;
 constexpr size_t kTwoPerSm = 110 * 1024;
 
 template <class P>
-void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, int nsm) {
+int launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, int nsm) {
     // about cps (8 by default, the autotuner's sp_dft_cps) CTAs per SM over the grid; each loops over
     // nct / slots column tiles
     const int cps = c.tune && c.tune->sp_dft_cps > 0 ? c.tune->sp_dft_cps : 8;
@@ -430,17 +462,30 @@ void launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err,
     const int slots = std::max(1, std::min(nct, (cps * nsm + d.nmt - 1) / d.nmt));
     const int Kp = (d.K + 15) & ~15;
     dim3 grid(d.nmt, slots);
-    auto go = [&](auto kern, size_t smem) {
-        kern<<<grid, kThreads, smem, c.stream>>>(p, d.K, d.nch, d.dig, d.rexp, err);
+    const GemmArgs<P> ga{p, d.S, d.K, d.nch, d.dig, d.rexp, err};
+    // kern: one part; rkern: a fused launch; mkern: a fused launch over parts of both digit counts
+    auto go = [&](const void *kern, const void *rkern, const void *mkern, size_t smem) {
+        return emit_launch(c.stream, c.rec, kern, rkern, grid, dim3(kThreads), smem, ga, mkern);
     };
-    if (d.S == 7) {
-        if (kWantFull<P> && gemm_smem<7, true>(Kp) <= kTwoPerSm) go(k_split_gemm<7, 8, P, kWantFull<P>>, gemm_smem<7, true>(Kp));
-        else go(k_split_gemm<7, 8, P, false>, gemm_smem<7, false>(Kp));
+    constexpr bool F = kWantFull<P>;
+    const bool full = F && (d.S == 7 ? gemm_smem<7, true>(Kp) : gemm_smem<8, true>(Kp)) <= kTwoPerSm;
+    int rc;
+    if (full) {
+        const void *mk = (const void *)k_split_gemm_mixed<P, F>;
+        rc = d.S == 7 ? go((const void *)k_split_gemm<7, 8, P, F>, (const void *)k_split_gemm<7, 8, P, F, true>, mk,
+                           gemm_smem<7, true>(Kp))
+                      : go((const void *)k_split_gemm<8, 7, P, F>, (const void *)k_split_gemm<8, 7, P, F, true>, mk,
+                           gemm_smem<8, true>(Kp));
     } else {
-        if (kWantFull<P> && gemm_smem<8, true>(Kp) <= kTwoPerSm) go(k_split_gemm<8, 7, P, kWantFull<P>>, gemm_smem<8, true>(Kp));
-        else go(k_split_gemm<8, 7, P, false>, gemm_smem<8, false>(Kp));
+        const void *mk = (const void *)k_split_gemm_mixed<P, false>;
+        rc = d.S == 7 ? go((const void *)k_split_gemm<7, 8, P, false>, (const void *)k_split_gemm<7, 8, P, false, true>,
+                           mk, gemm_smem<7, false>(Kp))
+                      : go((const void *)k_split_gemm<8, 7, P, false>, (const void *)k_split_gemm<8, 7, P, false, true>,
+                           mk, gemm_smem<8, false>(Kp));
     }
+    if (rc) return rc;
     if (c.launches) ++*c.launches;
+    return AEROS_OK;
 }
 
 }  // namespace
@@ -505,7 +550,7 @@ bool split_dft_has_anal(const SplitDft *s) { return s && s->ana.S > 0; }
 int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     DftSynthP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, s->msin, FastDiv(c.nlat)};
-    launch_gemm(s->syn, c, p, nf * c.nlat, s->err, s->nsm);
+    if (int rc = launch_gemm(s->syn, c, p, nf * c.nlat, s->err, s->nsm)) return rc;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
 }
@@ -513,7 +558,7 @@ int split_fourier_synth(SplitDft *s, const Ctx &c, const FsynField *fields_d, in
 int split_fourier_anal(SplitDft *s, const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
     DftAnalP p{fields_d, nf, nrow, c.ms, c.nlat, c.nlon, F, FastDiv(c.nlat)};
-    launch_gemm(s->ana, c, p, nf * c.nlat, s->err, s->nsm);
+    if (int rc = launch_gemm(s->ana, c, p, nf * c.nlat, s->err, s->nsm)) return rc;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
 }

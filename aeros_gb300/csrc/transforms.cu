@@ -1,4 +1,6 @@
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 // transforms.cu -- FP64 spherical-harmonic transform kernels for sm_103a.
@@ -22,14 +24,29 @@ constexpr double kSq2Pi = 2.50662827463100050242;    // sqrt(2 pi)
 // ============================================================ Fourier synthesis
 // grid[j][i] = FFT^-1[ X ],  X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m].
 // CTA = (field, group of LPB latitudes); each row uses 2 n complex of smem.
-__global__ void k_fourier_synth(const FsynField *__restrict__ fields, const double2 *__restrict__ F, int nrow,
-                                int ms, int T, int nlat, int nlon, int lpb, FftPlan plan,
-                                const double2 *__restrict__ tw, const double2 *__restrict__ twN,
-                                const double *__restrict__ isin) {
+struct FsynArgs {
+    const FsynField *fields;
+    const double2 *F;
+    int nrow, ms, T, nlat, nlon, lpb;
+    FftPlan plan;
+    const double2 *tw, *twN;
+    const double *isin;
+};
+template <bool RAG = false>
+__global__ void k_fourier_synth(const __grid_constant__ RagPack<FsynArgs> rp) {
+    uint3 bid, gdim;
+    const FsynArgs &ka = rag_part<RAG>(rp, bid, gdim);
+    const FsynField *__restrict__ fields = ka.fields;
+    const double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, T = ka.T, nlat = ka.nlat, nlon = ka.nlon, lpb = ka.lpb;
+    const FftPlan &plan = ka.plan;
+    const double2 *__restrict__ tw = ka.tw;
+    const double2 *__restrict__ twN = ka.twN;
+    const double *__restrict__ isin = ka.isin;
     extern __shared__ double2 sm[];
-    const FsynField fd = fields[blockIdx.x];
+    const FsynField fd = fields[bid.x];
     const int n = nlon / 2;
-    const int j0 = blockIdx.y * lpb;
+    const int j0 = bid.y * lpb;
     const int nr = min(lpb, nlat - j0);
     double2 *A = sm, *B = sm + (size_t)lpb * n, *X = sm + (size_t)2 * lpb * n;
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -94,13 +111,27 @@ __global__ void k_fourier_synth(const FsynField *__restrict__ fields, const doub
 
 // ============================================================ Fourier analysis
 // F[j][row][m] = sqrt(2pi)/nlon * sum_i grid[j][i] e^{-i m lambda_i},  m = 0..T.
-__global__ void k_fourier_anal(const FanaField *__restrict__ fields, double2 *__restrict__ F, int nrow, int ms,
-                               int T, int nlat, int nlon, int lpb, FftPlan plan, const double2 *__restrict__ tw,
-                               const double2 *__restrict__ twN) {
+struct FanaArgs {
+    const FanaField *fields;
+    double2 *F;
+    int nrow, ms, T, nlat, nlon, lpb;
+    FftPlan plan;
+    const double2 *tw, *twN;
+};
+template <bool RAG = false>
+__global__ void k_fourier_anal(const __grid_constant__ RagPack<FanaArgs> rp) {
+    uint3 bid, gdim;
+    const FanaArgs &ka = rag_part<RAG>(rp, bid, gdim);
+    const FanaField *__restrict__ fields = ka.fields;
+    double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, nlat = ka.nlat, nlon = ka.nlon, lpb = ka.lpb;
+    const FftPlan &plan = ka.plan;
+    const double2 *__restrict__ tw = ka.tw;
+    const double2 *__restrict__ twN = ka.twN;
     extern __shared__ double2 sm[];
-    const FanaField fd = fields[blockIdx.x];
+    const FanaField fd = fields[bid.x];
     const int n = nlon / 2;
-    const int j0 = blockIdx.y * lpb;
+    const int j0 = bid.y * lpb;
     const int nr = min(lpb, nlat - j0);
     double2 *A = sm, *B = sm + (size_t)lpb * n;
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -138,6 +169,37 @@ static int fourier_lpb(int nlon) {
 
 int fourier_lpb_limit(size_t smem_per_lat) { return (int)std::max<size_t>(1, (200 * 1024) / smem_per_lat); }
 
+LaunchRec fuse_launches(const std::vector<const LaunchRec *> &ps) {
+    LaunchRec f = *ps[0];
+    RagHdr *h = reinterpret_cast<RagHdr *>(f.pack.data());
+    h->n = (int)ps.size();
+    unsigned acc = 0;
+    for (size_t i = 0; i < ps.size(); ++i) {
+        const LaunchRec &p = *ps[i];
+        h->start[i] = acc;
+        h->grid[i] = make_uint3(p.grid.x, p.grid.y, p.grid.z);
+        acc += p.grid.x * p.grid.y * p.grid.z;
+        std::memcpy(f.pack.data() + f.aoff + i * f.asize, p.pack.data() + p.aoff, f.asize);
+        f.smem = std::max(f.smem, p.smem);
+    }
+    h->start[ps.size()] = acc;
+    f.grid = dim3(acc);
+    f.func = f.rfunc;
+    for (const LaunchRec *p : ps)
+        if (p->func != ps[0]->func) f.func = f.mfunc;
+    return f;
+}
+
+int replay_launch(const LaunchRec &r, cudaStream_t st) {
+    void *args[] = {const_cast<unsigned char *>(r.pack.data())};
+    return launch_kernel(r.func, r.grid, r.block, args, r.smem, st);
+}
+
+int launch_kernel(const void *func, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t st) {
+    AEROS_CUDA(cudaLaunchKernel(func, grid, block, args, smem, st));
+    return AEROS_OK;
+}
+
 int raise_smem_limit(const void *func, size_t bytes) {
     static std::mutex mu;
     static std::map<const void *, size_t> cur;
@@ -156,9 +218,9 @@ int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const 
     const int thr = c.tune ? c.tune->fs_thr : 256;
     size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
-    if (int rc = raise_smem_limit((const void *)k_fourier_synth, smem)) return rc;
-    k_fourier_synth<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
-                                                   c.tab->tw, c.tab->twN, c.tab->sint);
+    if (int rc = raise_smem_limit((const void *)k_fourier_synth<>, smem)) return rc;
+    const FsynArgs ka{fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan, c.tab->tw, c.tab->twN, c.tab->sint};
+    if (int rc = emit_launch(c.stream, c.rec, (const void *)k_fourier_synth<>, (const void *)k_fourier_synth<true>, grid, dim3(thr), smem, ka)) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -171,9 +233,9 @@ int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2
     const int thr = c.tune ? c.tune->fa_thr : 256;
     size_t smem = per_lat * lpb;
     dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
-    if (int rc = raise_smem_limit((const void *)k_fourier_anal, smem)) return rc;
-    k_fourier_anal<<<grid, thr, smem, c.stream>>>(fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
-                                                  c.tab->tw, c.tab->twN);
+    if (int rc = raise_smem_limit((const void *)k_fourier_anal<>, smem)) return rc;
+    const FanaArgs ka{fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan, c.tab->tw, c.tab->twN};
+    if (int rc = emit_launch(c.stream, c.rec, (const void *)k_fourier_anal<>, (const void *)k_fourier_anal<true>, grid, dim3(thr), smem, ka)) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -190,23 +252,40 @@ constexpr int kSynCT = 16;   // columns per tile
 constexpr int kSynKC = 16;   // degrees per smem chunk (even)
 constexpr int kSynThreads = 128;
 
-template <int kSynJT>
-__global__ void __launch_bounds__(kSynThreads) k_leg_synth_fp64(
-    const SynCol *__restrict__ cols, int ncol, int ncolD_first, const int *__restrict__ tile_first,
-    const double *__restrict__ Ps, const double *__restrict__ dPs, const double *__restrict__ lfac,
-    const int *__restrict__ moff, double2 *__restrict__ F, int nrow, int ms, int T, int nh, int nlat) {
+struct LsynArgs {
+    const SynCol *cols;
+    int ncol, ncolD_first;
+    const int *tile_first;
+    const double *Ps, *dPs, *lfac;
+    const int *moff;
+    double2 *F;
+    int nrow, ms, T, nh, nlat;
+};
+template <int kSynJT, bool RAG = false>
+__global__ void __launch_bounds__(kSynThreads) k_leg_synth_fp64(const __grid_constant__ RagPack<LsynArgs> rp) {
+    uint3 bid, gdim;
+    const LsynArgs &ka = rag_part<RAG>(rp, bid, gdim);
+    const SynCol *__restrict__ cols = ka.cols;
+    const int ncolD_first = ka.ncolD_first;
+    const int *__restrict__ tile_first = ka.tile_first;
+    const double *__restrict__ Ps = ka.Ps;
+    const double *__restrict__ dPs = ka.dPs;
+    const double *__restrict__ lfac = ka.lfac;
+    const int *__restrict__ moff = ka.moff;
+    double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, T = ka.T, nh = ka.nh, nlat = ka.nlat;
     constexpr int kSynQ = kSynJT * kSynCT / kSynThreads;
     __shared__ double sP[kSynKC][kSynJT];
     __shared__ double sD[kSynKC][kSynJT];
     __shared__ double2 sC[kSynKC][kSynCT];
     __shared__ SynCol sCol[kSynCT];
 
-    const int m = blockIdx.x;
-    const int c0 = tile_first[blockIdx.y];
-    const int c1 = tile_first[blockIdx.y + 1];
+    const int m = bid.x;
+    const int c0 = tile_first[bid.y];
+    const int c1 = tile_first[bid.y + 1];
     const int nct = c1 - c0;
     const bool hasD = c0 >= ncolD_first;
-    const int j0 = blockIdx.z * kSynJT;
+    const int j0 = bid.z * kSynJT;
     const int jt = min(kSynJT, nh - j0);
     const int K = T - m + 1;
     const int mo = moff[m];
@@ -320,14 +399,17 @@ void free_syn_plan(SynPlan &p) {
 int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) {
     if (p.ncol <= 0) return AEROS_OK;
     const int jt = c.tune ? c.tune->ls_jt : 32;
-    auto go = [&](auto kern, int JT) {
+    auto go = [&](const void *kern, const void *rkern, int JT) {
         dim3 grid(c.T + 1, p.ntile, (c.nh + JT - 1) / JT);
-        kern<<<grid, kSynThreads, 0, c.stream>>>(p.cols_d, p.ncol, p.ncolD_first, p.tiles_d, c.tab->Ps, c.tab->dPs,
-                                                 c.tab->lfac, c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+        const LsynArgs ka{p.cols_d, p.ncol, p.ncolD_first, p.tiles_d, c.tab->Ps, c.tab->dPs, c.tab->lfac,
+                          c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat};
+        return emit_launch(c.stream, c.rec, kern, rkern, grid, dim3(kSynThreads), 0, ka);
     };
-    if (jt == 8) go(k_leg_synth_fp64<8>, 8);
-    else if (jt == 16) go(k_leg_synth_fp64<16>, 16);
-    else go(k_leg_synth_fp64<32>, 32);
+    int rc;
+    if (jt == 8) rc = go((const void *)k_leg_synth_fp64<8>, (const void *)k_leg_synth_fp64<8, true>, 8);
+    else if (jt == 16) rc = go((const void *)k_leg_synth_fp64<16>, (const void *)k_leg_synth_fp64<16, true>, 16);
+    else rc = go((const void *)k_leg_synth_fp64<32>, (const void *)k_leg_synth_fp64<32, true>, 32);
+    if (rc) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;
@@ -340,22 +422,38 @@ int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) 
 constexpr int kAnaJC = 16;      // latitudes per smem chunk
 constexpr int kAnaLT = 32;
 
-template <int kAnaCT>   // output columns (warps) per CTA
-__global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(
-    const AnaCol *__restrict__ cols, int ncol, const double *__restrict__ PaT, const double *__restrict__ dPaT,
-    const double *__restrict__ lfac, const double *__restrict__ isin, const int *__restrict__ moff,
-    const double2 *__restrict__ F, int nrow, int ms, int T, int nh, int nlat) {
+struct LanaArgs {
+    const AnaCol *cols;
+    int ncol;
+    const double *PaT, *dPaT, *lfac, *isin;
+    const int *moff;
+    const double2 *F;
+    int nrow, ms, T, nh, nlat;
+};
+template <int kAnaCT, bool RAG = false>   // output columns (warps) per CTA
+__global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_constant__ RagPack<LanaArgs> rp) {
+    uint3 bid, gdim;
+    const LanaArgs &ka = rag_part<RAG>(rp, bid, gdim);
+    const AnaCol *__restrict__ cols = ka.cols;
+    const int ncol = ka.ncol;
+    const double *__restrict__ PaT = ka.PaT;
+    const double *__restrict__ dPaT = ka.dPaT;
+    const double *__restrict__ lfac = ka.lfac;
+    const double *__restrict__ isin = ka.isin;
+    const int *__restrict__ moff = ka.moff;
+    const double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, T = ka.T, nh = ka.nh, nlat = ka.nlat;
     __shared__ double sP[kAnaJC][kAnaLT];
     __shared__ double sD[kAnaJC][kAnaLT];
     __shared__ double2 sX[kAnaCT][3][2][kAnaJC];   // [col][slot][even/odd][j]
     __shared__ AnaCol sCol[kAnaCT];
 
-    const int m = blockIdx.x;
+    const int m = bid.x;
     const int K = T - m + 1;
-    const int l0 = blockIdx.z * kAnaLT;            // offset (l - m) of this tile
+    const int l0 = bid.z * kAnaLT;                 // offset (l - m) of this tile
     if (l0 >= K) return;
     const int lt = min(kAnaLT, K - l0);
-    const int c0 = blockIdx.y * kAnaCT;
+    const int c0 = bid.y * kAnaCT;
     const int nct = min(kAnaCT, ncol - c0);
     const int mo = moff[m];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -461,14 +559,17 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(
 int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow) {
     if (ncol <= 0) return AEROS_OK;
     const int ct = c.tune ? c.tune->la_ct : 8;
-    auto go = [&](auto kern, int CT) {
+    auto go = [&](const void *kern, const void *rkern, int CT) {
         dim3 grid(c.T + 1, (ncol + CT - 1) / CT, (c.T + 1 + kAnaLT - 1) / kAnaLT);
-        kern<<<grid, CT * 32, 0, c.stream>>>(cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac, c.tab->sint,
-                                             c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat);
+        const LanaArgs ka{cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac, c.tab->sint,
+                          c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat};
+        return emit_launch(c.stream, c.rec, kern, rkern, grid, dim3(CT * 32), 0, ka);
     };
-    if (ct == 4) go(k_leg_anal_fp64<4>, 4);
-    else if (ct == 16) go(k_leg_anal_fp64<16>, 16);
-    else go(k_leg_anal_fp64<8>, 8);
+    int rc;
+    if (ct == 4) rc = go((const void *)k_leg_anal_fp64<4>, (const void *)k_leg_anal_fp64<4, true>, 4);
+    else if (ct == 16) rc = go((const void *)k_leg_anal_fp64<16>, (const void *)k_leg_anal_fp64<16, true>, 16);
+    else rc = go((const void *)k_leg_anal_fp64<8>, (const void *)k_leg_anal_fp64<8, true>, 8);
+    if (rc) return rc;
     if (c.launches) ++*c.launches;
     AEROS_CUDA(cudaGetLastError());
     return AEROS_OK;

@@ -380,9 +380,13 @@ class AerosGroup:
     """Several AerosDyn handles stepped by one CUDA graph launch per step.
 
     Members may differ in truncation and level count (e.g. 32 x T21L16,
-    32 x T31L20 and 32 x T42L20); each handle's step graph is an independent
-    branch of the group's graph.  Configure the handles (state, forcing) before
-    grouping and step them only through the group afterwards.
+    32 x T31L20 and 32 x T42L20).  The group fuses the handles' launches: each
+    kernel of the step runs once over every handle that uses it (a ragged
+    launch whose CTAs look up their handle), so the step is about one launch
+    per kernel type.  With a physics hook installed (or AEROS_GROUP_FUSE=0)
+    each handle's own step graph is a branch of the group's graph instead.
+    Configure the handles (state, forcing) before grouping and step them only
+    through the group afterwards.
     """
 
     def __init__(self, handles):
@@ -415,6 +419,13 @@ class AerosGroup:
         c = ctypes.c_longlong()
         _capi.lib().aeros_group_launch_count(self._g, ctypes.byref(c))
         return c.value
+
+    def info(self):
+        """{'fused': bool, 'kernels_startup': n, 'kernels_step': n} (launches per step)."""
+        f, k0, k1 = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+        _capi.check(_capi.lib().aeros_group_info(self._g, ctypes.byref(f), ctypes.byref(k0), ctypes.byref(k1)),
+                    "aeros_group_info")
+        return {"fused": bool(f.value), "kernels_startup": k0.value, "kernels_step": k1.value}
 
     @property
     def nmember(self):

@@ -153,9 +153,17 @@ def fp64_peak_tflops(torch):
 
 
 # ---------------------------------------------------------------- work model
+# FP64 flops of the column terms and Held-Suarez forcing per grid point and
+# level: ncu's count for the one-lane column kernel at T42L20 x 16 members
+# (dadd + dmul + 2 dfma thread instructions, 260.4 M per launch), divided by
+# the points and levels.  It includes the operations of the exp and log calls.
+COLUMN_FP64_FLOPS_PER_POINT_LEVEL = 99.35
+
+
 def kernel_work(T, nlat, nlon, nlm, nlev):
     """Algorithmic work per launch of each step kernel at one member:
-    flops for the contractions and FFTs (FP64), bytes for the memory-bound ones.
+    flops for the contractions, FFTs and column terms (FP64, the pipe that
+    bounds them on GB300), bytes for the memory-bound ones.
     F_leg = 2 nlat nlm flops per scalar Legendre sum (hemisphere-folded);
     FFT = 2.5 nlon log2(nlon) flops per real row."""
     import math
@@ -166,7 +174,7 @@ def kernel_work(T, nlat, nlon, nlm, nlev):
     return {
         "legendre_synth": ("flops", F_leg * (8 * nlev + 2)),
         "fourier_synth": ("flops", fft * nlat * (7 * nlev + 3)),
-        "column": ("bytes", 8.0 * ng * ((7 * nlev + 3) + (4 * nlev + 1))),
+        "column": ("flops", COLUMN_FP64_FLOPS_PER_POINT_LEVEL * ng * nlev),
         "fourier_anal": ("flops", fft * nlat * (4 * nlev + 1)),
         "legendre_anal": ("flops", F_leg * (6 * nlev + 1)),
         "spectral": ("bytes", 5.0 * st_bytes),
@@ -445,6 +453,7 @@ def time_group(hs, steps, torch):
     n0 = g.launch_count()
     t = time_steps(g, s, steps, torch)
     launches = (g.launch_count() - n0) / steps
+    time_group.last_info = g.info()
     del g
     return t, launches
 
@@ -452,9 +461,10 @@ def time_group(hs, steps, torch):
 def batched_form(args, torch, t_single):
     """The batching form.  (1) T42L20 ensembles: 96 members of the headline
     configuration (each its own seed and dT_y), one CUDA graph launch per step,
-    FP64 and split precision, as 3 handles of 32 (three graph branches) and
-    the split members also as one handle of 96 (one launch per kernel type
-    and step); the better split aggregate SYPD over the single-member FP64
+    FP64 and split precision, as 3 handles of 32 (the group fuses their
+    launches: one ragged launch per kernel over the handles) and the split
+    members also as one handle of 96 (one launch per kernel type and step);
+    the better split aggregate SYPD over the single-member FP64
     path's is the ratio the >= 20x target is stated for.  (2) The mixed
     configuration of 96 uneven members, 32 x T21L16 + 32 x T31L20 + 32 x
     T42L20, FP64 and split, beside the same members stepped one by one through
@@ -473,7 +483,8 @@ def batched_form(args, torch, t_single):
         t, nl = time_group(hs, args.batched_steps, torch)
         del hs
         t42[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "us_per_member_step": t * 1e6 / 96,
-                     "gpu_launches_per_step": nl, "vs_fp64_single": 96 * sypd(t) / sypd(t_single)}
+                     "gpu_launches_per_step": nl, "fused_launches": time_group.last_info["fused"],
+                     "vs_fp64_single": 96 * sypd(t) / sypd(t_single)}
     # the same 96 split members as one handle: one launch per kernel type and step
     if nh != 1:
         hs = build_members([(42, 20, 96)], PREC_SPLIT, 5000, not args.no_tune, tunelog.setdefault("t42_split_1x96", {}))
@@ -491,6 +502,7 @@ def batched_form(args, torch, t_single):
         t, nl = time_group(hs, args.batched_steps, torch)
         del hs
         mixed[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "gpu_launches_per_step": nl,
+                       "fused_launches": time_group.last_info["fused"],
                        "vs_fp64_single_mixed": 96 * sypd(t) / sypd(t_single)}
     seq = 0.0
     perm = {}
@@ -701,6 +713,11 @@ def run_gpu(args, rank, world, local):
                 "frac": achieved / fp64_tf, "traffic": traffic, "kernel": dom,
                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)",
                 "work_per_launch": amount}
+        if dom == "column":
+            # the grid bytes the column kernel must move, against the HBM peak (not what bounds it)
+            gb = 8.0 * dyn.nlon * dyn.nlat * ((7 * args.nlev + 3) + (4 * args.nlev + 1))
+            roof["hbm"] = {"bytes_per_launch": gb, "achieved_GBs": gb / (prof[dom] / 1e3) / 1e9,
+                           "frac": gb / (prof[dom] / 1e3) / 1e9 / hbm_gbs}
     else:
         achieved = amount / (prof[dom] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",

@@ -442,8 +442,16 @@ int aeros_dyn_tune_set(aeros_dyn_t h, const int *shape, int n);
 
 /* ======================================================================== */
 /* Ensemble groups: several dyn handles (e.g. members of different          */
-/* truncations) stepped by ONE CUDA graph launch per time step; each        */
-/* handle's step graph is an independent branch.  Handles must be fully      */
+/* truncations and level counts) stepped by ONE CUDA graph launch per time  */
+/* step.  The group records every handle's step launches and fuses them:   */
+/* at each kernel of the step, the handles that run the same kernel share   */
+/* one ragged launch (up to 4 handles per launch; each CTA finds its        */
+/* handle, block index and grid in a descriptor table), so a step of 96     */
+/* members in three truncations is about one launch per kernel type.  The   */
+/* kernels the handles share get the launch shapes of the heaviest handle   */
+/* (results do not depend on launch shapes).  A group with a physics hook,  */
+/* or with AEROS_GROUP_FUSE=0 in the environment, makes each handle's own   */
+/* step graph a branch of the group's graph instead.  Handles must be fully */
 /* configured (state, forcing, phis) and at the same step count; while in a */
 /* group, step them only through the group.  No reference counterpart: the */
 /* reference steps one configuration per process.                          */
@@ -455,6 +463,10 @@ int aeros_group_step(aeros_group_t g, int nsteps);
 int aeros_group_step_async(aeros_group_t g, int nsteps);
 int aeros_group_sync(aeros_group_t g);
 int aeros_group_launch_count(aeros_group_t g, long long *count);
+/* fused: 1 when the launches are fused, 0 for one branch per handle;
+ * kernels_startup / kernels_step: kernel launches of the start-up and of a
+ * regular step (any pointer may be NULL). */
+int aeros_group_info(aeros_group_t g, int *fused, long long *kernels_startup, long long *kernels_step);
 
 /* ======================================================================== */
 /* Differentiation: adjoints of the transforms and of the step              */
