@@ -984,7 +984,8 @@ __global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
     extern __shared__ double2 sm[];
     const int n = nlon / 2, ms = T + 1;
     const int e = bid.y, jn = bid.x, js = nlat - 1 - jn;
-    double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * n;
+    const int rsz = frow(n);   // padded FFT row stride (fft.cuh)
+    double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * rsz;
     const double2 *c = lnps + (size_t)e * nlm;
     // thread per (m, parity of l - m): each sums its parity in the serial order,
     // in batches of 16 degrees whose loads are all issued before the sums
@@ -1029,15 +1030,15 @@ __global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
         double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
         double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
         double2 O = cmulconj(D, twN[k]);
-        A[idx] = make_double2((E.x - O.y) * kNrmD, (E.y + O.x) * kNrmD);
+        A[(size_t)r * rsz + fpad(k)] = make_double2((E.x - O.y) * kNrmD, (E.y + O.x) * kNrmD);
     }
     __syncthreads();
-    double2 *res = fft_rows<true>(A, B, 2, n, plan, tw, threadIdx.x, blockDim.x);
+    double2 *res = fft_rows<true>(A, B, 2, rsz, plan, tw, threadIdx.x, blockDim.x);
     const double *rr = reinterpret_cast<const double *>(res);
     __shared__ double red[2][128];
     for (int r = 0; r < 2; ++r) {
         double s = 0.0;
-        for (int i = threadIdx.x; i < nlon; i += blockDim.x) s += exp(rr[(size_t)r * nlon + i]);
+        for (int i = threadIdx.x; i < nlon; i += blockDim.x) s += exp(rr[2 * ((size_t)r * rsz + fpad(i >> 1)) + (i & 1)]);
         red[r][threadIdx.x] = s;
     }
     __syncthreads();
@@ -1841,7 +1842,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
 
 int run_mass(Dyn &d, int mode) {
     const int n = d.g.nlon / 2;
-    size_t smem = (size_t)(2 * d.g.ms + 4 * n) * sizeof(double2);
+    size_t smem = (size_t)(2 * d.g.ms + 4 * frow(n)) * sizeof(double2);
     if (int rc = raise_smem_limit((const void *)k_mass<>, smem)) return rc;
     const MassArgs ma{d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat, d.g.nlon, d.tab.Ps, d.tab.moff,
                       d.tab.plan, d.tab.tw, d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt, d.lnr_last,

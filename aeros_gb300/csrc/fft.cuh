@@ -66,6 +66,14 @@ __device__ __forceinline__ void dft_small(double2 *v) {
     }
 }
 
+// Row layout in shared memory: complex element i of a row sits at fpad(i) =
+// i + i/8, one spare slot after every 8 values, so that the strided writes of
+// a stage (stride R at Ns = 1, R^2 at Ns = R) spread over all 32 banks instead
+// of two or four; a row of n values takes frow(n) = n + n/8 slots (n is a
+// multiple of 8 for every grid here).
+__host__ __device__ constexpr int frow(int n) { return n + n / 8; }
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
+
 // n / d for a divisor fixed per stage: multiply-high by m = ceil(2^32 / d), exact
 // for n < 2^32 / d (every index here is far below that)
 struct StageDiv {
@@ -89,7 +97,7 @@ __device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int 
         int k = j - dns.div(j) * Ns;
         double2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = x[j + r * nb];
+        for (int r = 0; r < R; ++r) v[r] = x[fpad(j + r * nb)];
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
@@ -100,12 +108,13 @@ __device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int 
         dft_small<R, INV>(v);
         int base = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) y[base + r * Ns] = v[r];
+        for (int r = 0; r < R; ++r) y[fpad(base + r * Ns)] = v[r];
     }
 }
 
-// Transform nrows rows of n complex points held in `a` (row stride `stride`),
-// using `b` as the ping-pong buffer.  Returns the buffer holding the result.
+// Transform nrows rows of n complex points held in `a` (row stride `stride`,
+// at least frow(n); element i of a row at fpad(i)), using `b` as the
+// ping-pong buffer.  Returns the buffer holding the result (same layout).
 // All threads of the block must call it; ends with __syncthreads().
 template <bool INV>
 __device__ double2 *fft_rows(double2 *a, double2 *b, int nrows, int stride, const FftPlan &P,

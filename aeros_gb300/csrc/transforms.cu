@@ -23,7 +23,7 @@ constexpr double kSq2Pi = 2.50662827463100050242;    // sqrt(2 pi)
 
 // ============================================================ Fourier synthesis
 // grid[j][i] = FFT^-1[ X ],  X_m = Nrm sum_t (a_t + i b_t m / sin_j) F[j][src_t][m].
-// CTA = (field, group of LPB latitudes); each row uses 2 n complex of smem.
+// CTA = (field, group of LPB latitudes); each row uses 2 frow(n) + T + 1 complex of smem.
 struct FsynArgs {
     const FsynField *fields;
     const double2 *F;
@@ -48,7 +48,8 @@ __global__ void k_fourier_synth(const __grid_constant__ RagPack<FsynArgs> rp) {
     const int n = nlon / 2;
     const int j0 = bid.y * lpb;
     const int nr = min(lpb, nlat - j0);
-    double2 *A = sm, *B = sm + (size_t)lpb * n, *X = sm + (size_t)2 * lpb * n;
+    const int rs = frow(n);   // padded row stride (fft.cuh)
+    double2 *A = sm, *B = sm + (size_t)lpb * rs, *X = sm + (size_t)2 * lpb * rs;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const StageDiv dms(ms), dn(n), dnlon(nlon);
 
@@ -97,15 +98,15 @@ __global__ void k_fourier_synth(const __grid_constant__ RagPack<FsynArgs> rp) {
         const double2 E = make_double2(xk.x + xc.x, xk.y - xc.y);
         const double2 D = make_double2(xk.x - xc.x, xk.y + xc.y);
         const double2 O = cmulconj(D, twN[k]);
-        A[(size_t)r * n + k] = make_double2(E.x - O.y, E.y + O.x);
-        if (k > 0 && k < kc) A[(size_t)r * n + kc] = make_double2(E.x + O.y, O.x - E.y);
+        A[(size_t)r * rs + fpad(k)] = make_double2(E.x - O.y, E.y + O.x);
+        if (k > 0 && k < kc) A[(size_t)r * rs + fpad(kc)] = make_double2(E.x + O.y, O.x - E.y);
     }
     __syncthreads();
-    double2 *res = fft_rows<true>(A, B, nr, n, plan, tw, tid, nthr);
+    double2 *res = fft_rows<true>(A, B, nr, rs, plan, tw, tid, nthr);
     const double *rr = reinterpret_cast<const double *>(res);
     for (int idx = tid; idx < nr * nlon; idx += nthr) {
         int r = dnlon.div(idx), i = idx - r * nlon;
-        fd.dst[(size_t)(j0 + r) * nlon + i] = rr[(size_t)r * 2 * n + i];
+        fd.dst[(size_t)(j0 + r) * nlon + i] = rr[2 * ((size_t)r * rs + fpad(i >> 1)) + (i & 1)];
     }
 }
 
@@ -133,22 +134,23 @@ __global__ void k_fourier_anal(const __grid_constant__ RagPack<FanaArgs> rp) {
     const int n = nlon / 2;
     const int j0 = bid.y * lpb;
     const int nr = min(lpb, nlat - j0);
-    double2 *A = sm, *B = sm + (size_t)lpb * n;
+    const int rs = frow(n);   // padded row stride (fft.cuh)
+    double2 *A = sm, *B = sm + (size_t)lpb * rs;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const StageDiv dms(ms), dnlon(nlon);
     double *Ar = reinterpret_cast<double *>(A);
     for (int idx = tid; idx < nr * nlon; idx += nthr) {
         int r = dnlon.div(idx), i = idx - r * nlon;
-        Ar[(size_t)r * 2 * n + i] = fd.src[(size_t)(j0 + r) * nlon + i];
+        Ar[2 * ((size_t)r * rs + fpad(i >> 1)) + (i & 1)] = fd.src[(size_t)(j0 + r) * nlon + i];
     }
     __syncthreads();
-    double2 *Z = fft_rows<false>(A, B, nr, n, plan, tw, tid, nthr);
+    double2 *Z = fft_rows<false>(A, B, nr, rs, plan, tw, tid, nthr);
     const double sc = kSq2Pi / nlon;
     for (int idx = tid; idx < nr * ms; idx += nthr) {
         int r = dms.div(idx), m = idx - r * ms;
         // m <= T < n, so m % n = m and (n - m) % n = (m == 0 ? 0 : n - m)
-        double2 a = Z[(size_t)r * n + m];
-        double2 b = Z[(size_t)r * n + (m == 0 ? 0 : n - m)];
+        double2 a = Z[(size_t)r * rs + fpad(m)];
+        double2 b = Z[(size_t)r * rs + fpad(m == 0 ? 0 : n - m)];
         // E = (a + conj b)/2, O = -i/2 (a - conj b),  X = E + e^{-2 pi i m/N} O
         double2 E = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
         double2 O = make_double2(0.5 * (a.y + b.y), -0.5 * (a.x - b.x));
@@ -161,7 +163,7 @@ __global__ void k_fourier_anal(const __grid_constant__ RagPack<FanaArgs> rp) {
 static int fourier_lpb(int nlon) {
     // two rows of n complex per latitude; keep <= 64 KB of shared memory
     int n = nlon / 2;
-    int lpb = (64 * 1024) / (2 * n * (int)sizeof(double2));
+    int lpb = (64 * 1024) / (2 * frow(n) * (int)sizeof(double2));
     if (lpb > 8) lpb = 8;
     if (lpb < 1) lpb = 1;
     return lpb;
@@ -213,7 +215,7 @@ int raise_smem_limit(const void *func, size_t bytes) {
 
 int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    const size_t per_lat = (size_t)(2 * (c.nlon / 2) + c.ms) * sizeof(double2);
+    const size_t per_lat = (size_t)(2 * frow(c.nlon / 2) + c.ms) * sizeof(double2);
     int lpb = c.tune && c.tune->fs_lpb > 0 ? std::min(c.tune->fs_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
     const int thr = c.tune ? c.tune->fs_thr : 256;
     size_t smem = per_lat * lpb;
@@ -228,7 +230,7 @@ int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const 
 
 int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
     if (nf <= 0) return AEROS_OK;
-    const size_t per_lat = (size_t)2 * (c.nlon / 2) * sizeof(double2);
+    const size_t per_lat = (size_t)2 * frow(c.nlon / 2) * sizeof(double2);
     int lpb = c.tune && c.tune->fa_lpb > 0 ? std::min(c.tune->fa_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
     const int thr = c.tune ? c.tune->fa_thr : 256;
     size_t smem = per_lat * lpb;
