@@ -63,3 +63,7 @@ def test_bad_arguments_return_codes(lib):
         assert lib.aeros_dyn_create(ctypes.byref(h), ctypes.byref(p), None, None) == -1, bad
     p = held_suarez_params(trunc=21, nlev=40)
     assert lib.aeros_dyn_create(ctypes.byref(h), ctypes.byref(p), None, None) == -7
+    # groups: no handles, or a null group
+    g = ctypes.c_void_p()
+    assert lib.aeros_group_create(ctypes.byref(g), None, 0) == -1
+    assert lib.aeros_group_info(None, None, None, None) == -1
