@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(const __grid_consta
     const int slot = a.smajor ? bid.x : bid.z, m = a.smajor ? bid.y : bid.x, t = a.smajor ? bid.z : bid.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int K = a.T - m + 1, Kp = (K + 15) & ~15, nch = (Kp + kKC - 1) / kKC;
+    const int zmode = zmode_for<S>(Kp);
     const int mo = a.moff[m];
     const int ngrp = (a.ncol + kNTs / 2 - 1) / (kNTs / 2);
     if (slot >= ngrp) return;
@@ -371,12 +372,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_synth(const __grid_consta
                     tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNTs + c16 + h), r[q]);
                 tmem_wait_ld();
                 long long z[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) z[i] = 0;
-#pragma unroll
-                for (int q = 0; q < S; ++q)
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+                if (zmode == 2) zsum<S, B, 2>(r, z);
+                else if (zmode == 1) zsum<S, B, 1>(r, z);
+                else zsum<S, B, 0>(r, z);
 #pragma unroll
                 for (int i = 0; i < 8; ++i) zst[(size_t)(quarter * 32 + lane) * 17 + (c16 >> 1) + i] = z[i];
             }
@@ -484,6 +482,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(const __grid_constan
     if (64 * t >= K || slot >= ngrp) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int KpA = a.KpA, nch = (KpA + kKC - 1) / kKC;
+    const int zmode = zmode_for<S>(KpA);
     const int gstep = a.smajor ? gdim.x : gdim.z;
     if (tid == 0) fail = 0;
     if (warp == 0) {
@@ -707,15 +706,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_split_anal(const __grid_constan
         const int half = ((nv / 2 + 1) / 2) * 2;                                // warp 0's share (even)
         const int v0 = gw == 0 ? 0 : half, v1 = gw == 0 ? half : nv;
         for (int c = v0; c < v1; c += 2) {   // warp-uniform bounds
-            long long z[2] = {0, 0};
+            long long z[2];
             uint32_t r[S][2];
 #pragma unroll
             for (int q = 0; q < S; ++q) tmem_ld<2>(tl + (uint32_t)(q * kNTa + cbase + c), r[q]);
             tmem_wait_ld();
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-#pragma unroll
-                for (int i = 0; i < 2; ++i) z[i] += zterm<B>(r[q][i], q);
+            if (zmode == 2) zsum<S, B, 2>(r, z);
+            else if (zmode == 1) zsum<S, B, 1>(r, z);
+            else zsum<S, B, 0>(r, z);
 #pragma unroll
             for (int i = 0; i < 2; ++i)
                 sd[(size_t)row * kSdStride + c + i] = z_to_f64(z[i], zexp<B>(er, scale_exp(cexp[cb][cbase + c + i])));

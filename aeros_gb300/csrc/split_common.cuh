@@ -227,6 +227,44 @@ __device__ __forceinline__ long long zterm(uint32_t y, int q) {
     return sh >= 0 ? ((long long)v << sh) : (long long)(v >> (-sh));
 }
 
+// Z = sum_q Y_q 2^(40 - q B) for the W accumulator columns r[q][0 .. W), exactly.
+// With (S, B) = (7, 8) every digit is at most 128 in magnitude, so
+// |Y_q| <= (q + 1) Kc 2^14 for a contraction of Kc terms, and the sum can skip
+// most of the int64 work: pairs of shifts 8 apart combine in int32 first,
+//   hi = Y0 2^8 + Y1,  mid = Y2 2^8 + Y3,  lo = Y4 2^8 + Y5 + (Y6 >> 8),
+//   Z = hi 2^32 + mid 2^16 + lo,
+// exact while |lo| < 2^31, i.e. Kc <= 101 (ZMODE 1), the same integer as the
+// term-by-term sum.  For Kc <= 36 every |Y_q| <= 2^22 (ZMODE 2), and the fp32
+// value converts to its integer on the full-rate pipes: the bits of
+// Y + 1.5 2^23 are 0x4B400000 + Y.  ZMODE 0: the term-by-term int64 sum.
+template <int B>
+__device__ __forceinline__ long long zterm(uint32_t y, int q);
+template <int S, int B, int ZMODE, int W>
+__device__ __forceinline__ void zsum(const uint32_t (&r)[S][W], long long (&z)[W]) {
+    if constexpr (S == 7 && B == 8 && ZMODE > 0) {
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            int v[7];
+#pragma unroll
+            for (int q = 0; q < 7; ++q)
+                v[q] = ZMODE == 2 ? __float_as_int(__uint_as_float(r[q][i]) + 12582912.0f) - 0x4B400000
+                                  : __float2int_rn(__uint_as_float(r[q][i]));
+            const int hi = v[0] * 256 + v[1], mid = v[2] * 256 + v[3], lo = v[4] * 256 + v[5] + (v[6] >> 8);
+            z[i] = ((long long)hi << 32) + ((long long)mid << 16) + (long long)lo;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < W; ++i) z[i] = 0;
+#pragma unroll
+        for (int q = 0; q < S; ++q)
+#pragma unroll
+            for (int i = 0; i < W; ++i) z[i] += zterm<B>(r[q][i], q);
+    }
+}
+// The fastest exact form of zsum for a contraction padded to Kp terms.
+template <int S>
+__host__ __device__ __forceinline__ int zmode_for(int Kp) { return S == 7 ? (Kp <= 32 ? 2 : (Kp <= 96 ? 1 : 0)) : 0; }
+
 // z 2^E as a double (round to nearest, ties away); 0 below the normal range
 // (|z| < 2^63, so no overflow is possible for the exponents used here).
 __device__ __forceinline__ double z_to_f64(long long z, int E) {

@@ -192,6 +192,7 @@ __device__ __forceinline__ void split_gemm_body(const RagPack<GemmArgs<P>> &rp) 
     const int mt = bid.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Kp = (K + 15) & ~15;
+    const int zmode = zmode_for<S>(Kp);
     const int nct = (p.ncol() + kNT - 1) / kNT;
     if ((int)bid.y >= nct) return;
     if (tid == 0) fail = 0;
@@ -325,12 +326,9 @@ __device__ __forceinline__ void split_gemm_body(const RagPack<GemmArgs<P>> &rp) 
                 tmem_ld<8>(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(q * kNT + c16 + h), r[q]);
             tmem_wait_ld();
             long long z[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) z[i] = 0;
-#pragma unroll
-            for (int q = 0; q < S; ++q)
-#pragma unroll
-                for (int i = 0; i < 8; ++i) z[i] += zterm<B>(r[q][i], q);
+            if (zmode == 2) zsum<S, B, 2>(r, z);
+            else if (zmode == 1) zsum<S, B, 1>(r, z);
+            else zsum<S, B, 0>(r, z);
             if (grow < p.nrows())
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
