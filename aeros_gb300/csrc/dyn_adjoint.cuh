@@ -110,7 +110,7 @@ __global__ void k_mass_target_ad(double2 *__restrict__ pb, const double2 *__rest
 // Given the forward grid fields G and the adjoints GAb of the column outputs,
 // write the adjoints Gb of the column inputs (same layouts as k_column) and add
 // d/dk_a, d/ddT_y to parb[2 e], parb[2 e + 1].
-__global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, const double *__restrict__ GAb,
+__global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, const double *__restrict__ GAb,
                                                   double *__restrict__ Gb, int NL, int nlon, int nlat, int M,
                                                   const double *__restrict__ xlat, const double *__restrict__ phis,
                                                   int hs_on, const double *__restrict__ hs_dty,
@@ -389,8 +389,8 @@ __global__ void __launch_bounds__(64) k_column_ad(const double *__restrict__ G, 
 #undef GB
 #undef TF
     }
-    // parameter adjoints: a 64-column block spans at most two members when the
-    // grid has >= 64 points; reduce in shared memory, then one atomic each
+    // parameter adjoints: a 32-column block spans at most two members when the
+    // grid has >= 32 points; reduce in shared memory, then one atomic each
     __shared__ double sacc[4];
     if (threadIdx.x < 4) sacc[threadIdx.x] = 0.0;
     __syncthreads();
@@ -598,6 +598,10 @@ struct AdjCtx {
     std::vector<int> ckpt_nstep;
     double2 *seg = nullptr, *fin = nullptr;
     int seg_cap = 0;
+    // the grid fields G of every step of a segment, kept from its recomputation so the
+    // backward steps need not synthesise them again (nullptr: synthesise)
+    double *segG = nullptr;
+    int segG_cap = 0;
     int win_nsteps = 0, win_every = 0, win_n0 = 0, win_nend = 0;
     bool win_capture = false, win_ready = false;
 };
@@ -608,7 +612,7 @@ void adj_free(AdjCtx *a) {
     if (!a) return;
     if (a->sht) aeros_sht_destroy(a->sht);
     void *ps[] = {a->Ob, a->Nb, a->Rb, a->S1, a->S2, a->post, a->Gb, a->GAb, a->H, a->g1, a->E,
-                  a->parb, a->Mtb, a->J, a->seg, a->fin};
+                  a->parb, a->Mtb, a->J, a->seg, a->fin, a->segG};
     for (void *p : ps)
         if (p) cudaFree(p);
     for (double2 *p : a->ckpt)
@@ -747,7 +751,9 @@ int ke_accumulate(Dyn &d, double wgt, bool seed) {
 // after it (now slot).  On entry a.Ob / a.Nb are the adjoints of the post-step
 // old / now slots, on exit those of the pre-step slots.  `capture`: the mass
 // target was captured by this step.
-int step_adjoint(Dyn &d, double2 *post, bool capture) {
+// Gs: the step's forward grid fields kept from the segment's recomputation, or nullptr
+// to synthesise them from the pre-step state.
+int step_adjoint(Dyn &d, double2 *post, bool capture, const double *Gs) {
     AdjCtx &a = *d.adj;
     const bool startup = d.nstep == 0;
     int rc;
@@ -778,14 +784,24 @@ int step_adjoint(Dyn &d, double2 *post, bool capture) {
     ++d.launches;
     // tendencies -> column outputs -> column inputs -> state
     if ((rc = ana_adjoint(d, a.Rb))) return rc;
-    Ctx c = d.ctx();
-    const int rowsS = d.M * d.nrowS;
-    if (d.par.precision == AEROS_PREC_SPLIT && d.split) rc = split_leg_synth(d.split, c, d.synS, d.FS, rowsS);
-    else rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
-    if (rc) return rc;
-    if ((rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS))) return rc;
     const long ncol = (long)d.g.nlon * d.g.nlat * d.M;
-    k_column_ad<<<(unsigned)((ncol + 63) / 64), 64, 0, d.stream>>>(
+    if (Gs) {
+        AEROS_CUDA(cudaMemcpyAsync(d.G, Gs, sizeof(double) * ncol * (7 * d.NL + 3), cudaMemcpyDeviceToDevice,
+                                   d.stream));
+    } else {
+        Ctx c = d.ctx();
+        const int rowsS = d.M * d.nrowS;
+        if (d.par.precision == AEROS_PREC_SPLIT && d.split) rc = split_leg_synth(d.split, c, d.synS, d.FS, rowsS);
+        else rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
+        if (rc) return rc;
+        if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_synth(d.dft))
+            rc = split_fourier_synth(d.dft, c, d.fsS, d.nfsS, d.FS, rowsS);
+        else
+            rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS);
+        if (rc) return rc;
+    }
+    // a warp per CTA: one member's 8,192 columns then reach all SMs (the kernel is latency-bound there)
+    k_column_ad<<<(unsigned)((ncol + 31) / 32), 32, 0, d.stream>>>(
         d.G, a.GAb, a.Gb, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d, d.phis_set ? d.phis_d : nullptr,
         d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb, d.dconst, d.tmp(d.now), d.g.nlm);
     ++d.launches;
@@ -877,7 +893,7 @@ int aeros_dyn_step_ad(aeros_dyn_t h, const double *old_ad_in, const double *now_
     if ((rc = put_packed(d, a.Ob, old_ad_in)) || (rc = put_packed(d, a.Nb, now_ad_in))) return rc;
     AEROS_CUDA(cudaMemsetAsync(a.parb, 0, 2 * d.M * sizeof(double), d.stream));
     AEROS_CUDA(cudaMemsetAsync(a.Mtb, 0, d.M * sizeof(double), d.stream));
-    if ((rc = step_adjoint(d, a.post, capture))) return rc;
+    if ((rc = step_adjoint(d, a.post, capture, nullptr))) return rc;
     if ((rc = get_packed(d, old_ad_out, a.Ob)) || (rc = get_packed(d, now_ad_out, a.Nb))) return rc;
     std::vector<double> pb(2 * d.M);
     AEROS_CUDA(cudaMemcpyAsync(pb.data(), a.parb, 2 * d.M * sizeof(double), cudaMemcpyDeviceToHost, d.stream));
@@ -962,15 +978,31 @@ int aeros_dyn_window_backward(aeros_dyn_t h, double *now_ad, double *old_ad, dou
     AEROS_CUDA(cudaMemsetAsync(a.parb, 0, 2 * d.M * sizeof(double), d.stream));
     AEROS_CUDA(cudaMemsetAsync(a.Mtb, 0, d.M * sizeof(double), d.stream));
     AEROS_CUDA(cudaMemsetAsync(a.J, 0, d.M * sizeof(double), d.stream));
+    // keep each recomputed step's grid fields when they fit (at most 4 GiB for a segment)
+    const size_t gsz = (size_t)d.M * (7 * d.NL + 3) * d.g.nlon * d.g.nlat;
+    if (a.segG_cap < every && (size_t)every * gsz * sizeof(double) <= (4ull << 30)) {
+        if (a.segG) cudaFree(a.segG);
+        a.segG = nullptr;
+        a.segG_cap = 0;
+        if (cudaMalloc(&a.segG, (size_t)every * gsz * sizeof(double)) == cudaSuccess) a.segG_cap = every;
+        else {
+            a.segG = nullptr;
+            cudaGetLastError();   // fall back to synthesising the fields in each backward step
+        }
+    }
+    const bool keepG = a.segG && a.segG_cap >= every;
     for (int sg = ncp - 1; sg >= 0; --sg) {
         const int s0 = sg * every, s1 = std::min(N, s0 + every);
-        // recompute the segment, keeping every pre-step state
+        // recompute the segment, keeping every pre-step state (and its grid fields)
         if ((rc = copy_state(d, d.old, a.ckpt[sg])) || (rc = copy_state(d, d.now, a.ckpt[sg] + nst))) return rc;
         d.nstep = a.ckpt_nstep[sg];
         for (int s = s0; s < s1; ++s) {
             double2 *sv = a.seg + (size_t)2 * nst * (s - s0);
             if ((rc = copy_state(d, sv, d.old)) || (rc = copy_state(d, sv + nst, d.now))) return rc;
             if ((rc = graph_step(d))) return rc;
+            if (keepG)
+                AEROS_CUDA(cudaMemcpyAsync(a.segG + (size_t)(s - s0) * gsz, d.G, gsz * sizeof(double),
+                                           cudaMemcpyDeviceToDevice, d.stream));
         }
         if ((rc = copy_state(d, a.post, d.now))) return rc;   // state after step s1 - 1
         for (int s = s1 - 1; s >= s0; --s) {
@@ -981,7 +1013,9 @@ int aeros_dyn_window_backward(aeros_dyn_t h, double *now_ad, double *old_ad, dou
             if ((rc = ke_accumulate(d, 1.0 / N, true))) return rc;
             if ((rc = copy_state(d, d.old, sv)) || (rc = copy_state(d, d.now, sv + nst))) return rc;
             d.nstep = a.win_n0 + s;
-            if ((rc = step_adjoint(d, a.post, a.win_capture && s == 0))) return rc;
+            if ((rc = step_adjoint(d, a.post, a.win_capture && s == 0,
+                                   keepG ? a.segG + (size_t)(s - s0) * gsz : nullptr)))
+                return rc;
         }
     }
     if ((rc = get_packed(d, now_ad, a.Nb)) || (rc = get_packed(d, old_ad, a.Ob))) return rc;
