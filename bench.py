@@ -723,6 +723,17 @@ def run_gpu(args, rank, world, local):
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
                 "frac": achieved / hbm_gbs, "traffic": traffic, "kernel": dom,
                 "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_src})", "work_per_launch": amount}
+    # the same fraction for every kernel of the step (the dominant one changes with small timing shifts)
+    per_kernel = {}
+    for name, ms in prof.items():
+        k_kind, k_amount = work.get(name, ("flops", 0.0))
+        if k_kind == "flops":
+            a = k_amount / (ms / 1e3) / 1e12
+            per_kernel[name] = {"ms": ms, "achieved": a, "unit": "TFLOP/s", "frac": a / fp64_tf}
+        else:
+            a = k_amount / (ms / 1e3) / 1e9
+            per_kernel[name] = {"ms": ms, "achieved": a, "unit": "GB/s", "frac": a / hbm_gbs}
+    roof["per_kernel"] = per_kernel
 
     # e2e through the C-ABI with pinned host buffers
     e2e = None

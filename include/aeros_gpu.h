@@ -147,8 +147,8 @@ int aeros_sht_launch_count(aeros_sht_t h, long long *count);
  * device arrays that every GPU loading the library holds until exit:
  * nbatch <= 256 and nlat * nbatch * (T+1) <= 2^19, else AEROS_ERR_ARG.  All
  * calls share those arrays, so calls that overlap on the GPU race.  The first
- * call on a device resolves the arrays' addresses; make it before any stream
- * capture.  Synchronous. */
+ * call on a device resolves the arrays' addresses.  Synchronous (it waits for
+ * its stream), so it cannot be called inside a stream capture. */
 int aeros_sht_synthesis_noalloc(aeros_sht_t h, const double *coeffs, double *field, int nbatch);
 
 /* ======================================================================== */
