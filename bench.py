@@ -301,9 +301,33 @@ def transform_sweep(args, torch):
         res["split_round_trip"] = rel(cb[1], cd)
         res["fp64_round_trip"] = rel(cb[0], cd)
         res["grid"] = f"{h0.nlon}x{h0.nlat}"
+        # the CPU oracle's timing build on the host cores, 16 of the 240 fields (one per thread), scaled to 240
+        res["cpu_oracle"] = oracle_sweep_time(T, c[:16], B)
         out[f"T{T}"] = res
         del hs, g, cb, cd
     return out
+
+
+def oracle_sweep_time(T, c16, B):
+    """Synthesis and analysis time of the CPU oracle's timing build (OpenMP over
+    fields, all host cores) for a sample of fields, scaled to a batch of B."""
+    import numpy as np
+    import oracle.pyoracle as po
+    cores, _ = host_cpu()
+    po.use_variant("fast")
+    po.set_threads(cores)
+    s = po.OracleSHT(T)
+    n = len(c16)
+    f = s.synthesis(c16)
+    s.analysis(f)
+    t0 = time.perf_counter()
+    f = s.synthesis(c16)
+    ts = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s.analysis(f)
+    ta = time.perf_counter() - t0
+    return {"synthesis_ms": ts * 1e3 * B / n, "analysis_ms": ta * 1e3 * B / n, "cores": cores, "kind": "port",
+            "sample": f"{n} fields on {cores} threads (one field per thread), scaled to {B}"}
 
 
 def ctypes_void(p):
@@ -356,7 +380,9 @@ def adjoint_form(args):
     return {"workload": f"T{args.trunc}L{args.nlev} window of {nst} steps, checkpoints every {every}",
             "J": j0, "forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
             "backward_over_forward": (t2 - t1) / (t1 - t0), "dJ_dka": float(ka_b[0]), "dJ_ddTy": float(dty_b[0]),
-            "fd_rel_err_ka": abs(fd - ka_b[0]) / abs(ka_b[0])}
+            "fd_rel_err_ka": abs(fd - ka_b[0]) / abs(ka_b[0]),
+            # the oracle has no adjoint: the CPU reference point is the forward window's steps on all host cores
+            "cpu_oracle_forward_ms": oracle_step_time(args, host_cpu()[0], nst) * nst * 1e3}
 
 
 def transport_form(args, torch):
@@ -521,6 +547,17 @@ def batched_form(args, torch, t_single):
         seq += n * t1
         del d
     mixed["one_by_one_fp64"] = {"sypd": 96 * sypd(seq), "ms_per_step": seq * 1e3, "ms_per_member_step": perm}
+    # the same 96 members on the host cores: the CPU oracle's timing build, every member stepped with all
+    # threads (one member of each configuration timed, 3 steps after 3 warm-up, times 32)
+    cores, _ = host_cpu()
+    cpu_seq, cpu_perm = 0.0, {}
+    for T, L, n in cfg:
+        t1 = oracle_step_time(args, cores, 3, trunc=T, nlev=L)
+        cpu_perm[f"T{T}L{L}"] = t1 * 1e3
+        cpu_seq += n * t1
+    mixed["cpu_oracle"] = {"sypd": 96 * sypd(cpu_seq), "ms_per_step": cpu_seq * 1e3, "ms_per_member_step": cpu_perm,
+                           "cores": cores, "kind": "port",
+                           "sample": "3 steps of one member per configuration on all cores, times 32 members"}
     for name in ("fp64", "split"):
         mixed[name]["vs_one_by_one_fp64"] = mixed[name]["sypd"] / mixed["one_by_one_fp64"]["sypd"]
     out["mixed"] = mixed
@@ -586,17 +623,19 @@ def host_cpu():
     return os.cpu_count() or 1, model
 
 
-def oracle_step_time(args, threads, nsteps):
+def oracle_step_time(args, threads, nsteps, trunc=None, nlev=None):
     """Seconds per Held-Suarez step of the CPU oracle's timing build on `threads`
     OpenMP threads, from the config's initial state after 3 warm-up steps."""
     import numpy as np
     import oracle.pyoracle as po
     from aeros_gb300.params import held_suarez_params
+    trunc = trunc or args.trunc
+    nlev = nlev or args.nlev
     po.use_variant("fast")
     po.set_threads(threads)
-    p = held_suarez_params(trunc=args.trunc, nlev=args.nlev)
+    p = held_suarez_params(trunc=trunc, nlev=nlev)
     o = po.OracleDyn(p, nthreads=threads)
-    s = po.OracleSHT(args.trunc)
+    s = po.OracleSHT(trunc)
     o.set_isothermal(264.0, 1.0e5)
     vor, div, t, lnps = o.get_state()
     rng = np.random.default_rng(0)
