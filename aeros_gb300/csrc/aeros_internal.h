@@ -103,6 +103,8 @@ struct DevTables {
     double *lfac = nullptr;      // LF_COUNT * (T+1)
     double2 *tw = nullptr;       // n entries exp(-2 pi i t/n), n = nlon/2
     double2 *twN = nullptr;      // nlon/2+1 entries exp(-2 pi i k/nlon)
+    float4 *twD = nullptr;       // tw and twN as complex double-floats (re hi, re lo, im hi, im lo)
+    float4 *twND = nullptr;
     int *moff = nullptr;         // (T+1)
     int *l_of_lm = nullptr, *m_of_lm = nullptr;
     FftPlan plan{};
@@ -252,6 +254,9 @@ int launch_fourier_synth(const Ctx &c, const FsynField *fields_d, int nf, const 
 int launch_fourier_anal(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow);
 // Legendre analysis (FP64).
 int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const double2 *F, int nrow);
+// Fourier synthesis and analysis in double-float arithmetic (the split form).
+int launch_fourier_synth_df(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow);
+int launch_fourier_anal_df(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow);
 
 // Elementwise helpers.
 // Diagonal operators used by the adjoints (transforms.cu):

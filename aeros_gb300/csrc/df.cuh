@@ -59,6 +59,22 @@ __device__ __forceinline__ df2 df_fma(df2 a, df2 b, df2 c) { return df_add(df_mu
 __device__ __forceinline__ bool df_gt(df2 a, df2 b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
 __device__ __forceinline__ df2 df_max(df2 a, df2 b) { return df_gt(b, a) ? b : a; }
 
+// a b - c d and a b + c d in one pass: the two products' rounding errors
+// (fused multiply-adds) and cross terms gathered into the low part of one
+// two-sum (error ~2^-47 (|a b| + |c d|)).
+__device__ __forceinline__ df2 df_dot2(df2 a, df2 b, df2 c, df2 d, bool minus) {
+    const float cq = minus ? -c.h : c.h, cl = minus ? -c.l : c.l;
+    const float p = __fmul_rn(a.h, b.h), q = __fmul_rn(cq, d.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fadd_rn(e, __fmaf_rn(cq, d.h, -q));
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    e = __fmaf_rn(cq, d.l, e);
+    e = __fmaf_rn(cl, d.h, e);
+    const df2 s = two_sum(p, q);
+    return fast_two_sum(s.h, __fadd_rn(s.l, e));
+}
+
 // 1 / a: the float reciprocal refined by one Newton step with a double-float
 // residual (error ~2^-47).
 __device__ __forceinline__ df2 df_recip(df2 a) {
@@ -190,6 +206,28 @@ __device__ __forceinline__ long long fixed53(double x, int e) {
     const long long v = sh >= 54 ? 0 : (long long)((mant + (1ull << (sh - 1))) >> sh);
     return (bits >> 63) ? -v : v;
 }
+// ------------------------------------------------------------ complex double-float
+// A complex value as two double-floats (16 bytes, the size of a double2), for
+// the split form's longitude transforms on the FP32 pipes.
+struct __align__(16) dfc {
+    df2 r, i;
+};
+__device__ __forceinline__ dfc cadd(dfc a, dfc b) { return dfc{df_add(a.r, b.r), df_add(a.i, b.i)}; }
+__device__ __forceinline__ dfc csub(dfc a, dfc b) { return dfc{df_sub(a.r, b.r), df_sub(a.i, b.i)}; }
+__device__ __forceinline__ dfc cmul(dfc a, dfc w) {
+    return dfc{df_dot2(a.r, w.r, a.i, w.i, true), df_dot2(a.r, w.i, a.i, w.r, false)};
+}
+__device__ __forceinline__ dfc cmulconj(dfc a, dfc w) {   // a * conj(w)
+    return dfc{df_dot2(a.r, w.r, a.i, w.i, false), df_dot2(a.i, w.r, a.r, w.i, true)};
+}
+__device__ __forceinline__ dfc cscale(dfc a, df2 s) { return dfc{df_mul(a.r, s), df_mul(a.i, s)}; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ dfc rot90(dfc a) {
+    return INV ? dfc{df_neg(a.i), a.r} : dfc{a.i, df_neg(a.r)};
+}
+__device__ __forceinline__ dfc d2dfc(double2 x) { return dfc{d2df(x.x), d2df(x.y)}; }
+__device__ __forceinline__ double2 dfc2d(dfc a) { return make_double2(df2d(a.r), df2d(a.i)); }
 #endif
 
 // Host: nearest double-float of an FP64 constant.

@@ -1789,6 +1789,20 @@ bool split_spectral_exact(const Dyn &d) {
     return d.par.precision == AEROS_PREC_SPLIT && spec_cols_available(d.NL) && 2L * d.M * d.g.nlm >= 16384;
 }
 
+// The step's longitude transforms: FP64 FFTs, or in the split form double-float
+// FFTs on the FP32 pipes (the exact-digit DFT products on the tensor cores with
+// AEROS_SPLIT_DFT=1, for rows of at most 128).
+int fourier_synth_step(Dyn &d, const Ctx &c, int rows) {
+    if (d.par.precision != AEROS_PREC_SPLIT) return launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rows);
+    if (split_dft_has_synth(d.dft)) return split_fourier_synth(d.dft, c, d.fsS, d.nfsS, d.FS, rows);
+    return launch_fourier_synth_df(c, d.fsS, d.nfsS, d.FS, rows);
+}
+int fourier_anal_step(Dyn &d, const Ctx &c, int rows) {
+    if (d.par.precision != AEROS_PREC_SPLIT) return launch_fourier_anal(c, d.faS, d.nfaS, d.FA, rows);
+    if (split_dft_has_anal(d.dft)) return split_fourier_anal(d.dft, c, d.faS, d.nfaS, d.FA, rows);
+    return launch_fourier_anal_df(c, d.faS, d.nfaS, d.FA, rows);
+}
+
 int run_tendency(Dyn &d, int hs_on, bool physics) {
     Ctx c = d.ctx();
     int rc;
@@ -1799,10 +1813,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
         rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
     if (rc) return rc;
     mark(d, "legendre_synth");
-    if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_synth(d.dft))
-        rc = split_fourier_synth(d.dft, c, d.fsS, d.nfsS, d.FS, rowsS);
-    else
-        rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS);
+    rc = fourier_synth_step(d, c, rowsS);
     if (rc) return rc;
     mark(d, "fourier_synth");
     long ncol = (long)d.g.nlon * d.g.nlat * d.M;
@@ -1826,10 +1837,7 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     AEROS_CUDA(cudaGetLastError());
     mark(d, "column");
     if (physics && (rc = run_physics(d))) return rc;
-    if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_anal(d.dft))
-        rc = split_fourier_anal(d.dft, c, d.faS, d.nfaS, d.FA, rowsA);
-    else
-        rc = launch_fourier_anal(c, d.faS, d.nfaS, d.FA, rowsA);
+    rc = fourier_anal_step(d, c, rowsA);
     if (rc) return rc;
     mark(d, "fourier_anal");
     if (d.par.precision == AEROS_PREC_SPLIT && d.split)

@@ -794,10 +794,7 @@ int step_adjoint(Dyn &d, double2 *post, bool capture, const double *Gs) {
         if (d.par.precision == AEROS_PREC_SPLIT && d.split) rc = split_leg_synth(d.split, c, d.synS, d.FS, rowsS);
         else rc = launch_leg_synth_fp64(c, d.synS, d.FS, rowsS);
         if (rc) return rc;
-        if (d.par.precision == AEROS_PREC_SPLIT && split_dft_has_synth(d.dft))
-            rc = split_fourier_synth(d.dft, c, d.fsS, d.nfsS, d.FS, rowsS);
-        else
-            rc = launch_fourier_synth(c, d.fsS, d.nfsS, d.FS, rowsS);
+        rc = fourier_synth_step(d, c, rowsS);
         if (rc) return rc;
     }
     // a warp per CTA: one member's 8,192 columns then reach all SMs (the kernel is latency-bound there)

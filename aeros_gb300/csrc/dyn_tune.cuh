@@ -159,8 +159,9 @@ int aeros_dyn_autotune(aeros_dyn_t h, int reps, double *ms_before, double *ms_af
             // column-tile slots of the DFT products)
             for (int cps : {2, 4, 8, 16})
                 if (cps != d.tune.sp_cps) { Tune t = d.tune; t.sp_cps = cps; trial(t); }
-            for (int cps : {2, 4, 8, 16})
-                if (cps != d.tune.sp_dft_cps) { Tune t = d.tune; t.sp_dft_cps = cps; trial(t); }
+            if (d.dft)   // only the DFT products use it
+                for (int cps : {2, 4, 8, 16})
+                    if (cps != d.tune.sp_dft_cps) { Tune t = d.tune; t.sp_dft_cps = cps; trial(t); }
         }
         for (int sc : {0, 1})
             for (int sw : {1, 2, 4, 8}) {

@@ -8,7 +8,9 @@
 //   v_r = x[j + r n/R] * w^{(j mod Ns) r n/(Ns R)},  v <- DFT_R(v),
 //   y[(j - j mod Ns) R + j mod Ns + r Ns] = v_r.
 #pragma once
+#include <type_traits>
 #include "aeros_internal.h"
+#include "df.cuh"
 
 namespace aeros {
 
@@ -74,6 +76,46 @@ __device__ __forceinline__ void dft_small(double2 *v) {
 __host__ __device__ constexpr int frow(int n) { return n + n / 8; }
 __device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
 
+// The same small DFTs in double-float (the split form's transforms on the FP32
+// pipes); the constants are the nearest double-floats of cos and sin of 2 pi k/R.
+template <int R, bool INV>
+__device__ __forceinline__ void dft_small(dfc *v) {
+    if constexpr (R == 2) {
+        dfc a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+        dfc a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+        dfc a2 = cadd(v[1], v[3]), a3 = rot90<INV>(csub(v[1], v[3]));
+        v[0] = cadd(a0, a2);
+        v[2] = csub(a0, a2);
+        v[1] = cadd(a1, a3);
+        v[3] = csub(a1, a3);
+    } else if constexpr (R == 3) {
+        const df2 s1{0x1.bb67aep-1f, 0x1.0b0996p-26f};   // sin(2 pi / 3)
+        dfc t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+        dfc b = csub(v[0], dfc{df_scale(t1.r, 0.5f), df_scale(t1.i, 0.5f)});   // v0 + cos(2 pi/3) t1
+        dfc r = rot90<INV>(cscale(t2, s1));
+        v[0] = cadd(v[0], t1);
+        v[1] = cadd(b, r);
+        v[2] = csub(b, r);
+    } else if constexpr (R == 5) {
+        const df2 c1{0x1.3c6ef4p-2f, -0x1.1a02d6p-27f}, c2{-0x1.9e377ap-1f, 0x1.1a02d6p-27f};
+        const df2 s1{0x1.e6f0e2p-1f, -0x1.97756p-26f}, s2{0x1.2cf23p-1f, 0x1.1d5698p-27f};
+        dfc t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+        dfc t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+        dfc b1 = cadd(v[0], cadd(cscale(t1, c1), cscale(t2, c2)));
+        dfc b2 = cadd(v[0], cadd(cscale(t1, c2), cscale(t2, c1)));
+        dfc r1 = rot90<INV>(cadd(cscale(t3, s1), cscale(t4, s2)));
+        dfc r2 = rot90<INV>(csub(cscale(t3, s2), cscale(t4, s1)));
+        v[0] = cadd(v[0], cadd(t1, t2));
+        v[1] = cadd(b1, r1);
+        v[4] = csub(b1, r1);
+        v[2] = cadd(b2, r2);
+        v[3] = csub(b2, r2);
+    }
+}
+
 // n / d for a divisor fixed per stage: multiply-high by m = ceil(2^32 / d), exact
 // for n < 2^32 / d (every index here is far below that)
 struct StageDiv {
@@ -82,9 +124,9 @@ struct StageDiv {
     __device__ __forceinline__ int div(int n) const { return d == 1 ? n : (int)__umulhi((unsigned)n, m); }
 };
 
-template <int R, bool INV>
-__device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int nrows, int stride, int n, int Ns,
-                                          const double2 *__restrict__ tw, int tid, int nthr) {
+template <int R, bool INV, class V>
+__device__ __forceinline__ void fft_stage(const V *src, V *dst, int nrows, int stride, int n, int Ns,
+                                          const V *__restrict__ tw, int tid, int nthr) {
     const int nb = n / R;
     const int tstep = n / (Ns * R);
     const int total = nrows * nb;
@@ -92,16 +134,18 @@ __device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int 
     for (int idx = tid; idx < total; idx += nthr) {
         int row = dnb.div(idx);
         int j = idx - row * nb;
-        const double2 *x = src + row * stride;
-        double2 *y = dst + row * stride;
+        const V *x = src + row * stride;
+        V *y = dst + row * stride;
         int k = j - dns.div(j) * Ns;
-        double2 v[R];
+        V v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = x[fpad(j + r * nb)];
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
-                double2 w = __ldg(&tw[k * r * tstep]);
+                V w;
+                if constexpr (std::is_same<V, double2>::value) w = __ldg(&tw[k * r * tstep]);
+                else w = tw[k * r * tstep];
                 v[r] = INV ? cmulconj(v[r], w) : cmul(v[r], w);
             }
         }
@@ -116,10 +160,10 @@ __device__ __forceinline__ void fft_stage(const double2 *src, double2 *dst, int 
 // at least frow(n); element i of a row at fpad(i)), using `b` as the
 // ping-pong buffer.  Returns the buffer holding the result (same layout).
 // All threads of the block must call it; ends with __syncthreads().
-template <bool INV>
-__device__ double2 *fft_rows(double2 *a, double2 *b, int nrows, int stride, const FftPlan &P,
-                             const double2 *__restrict__ tw, int tid, int nthr) {
-    double2 *src = a, *dst = b;
+template <bool INV, class V>
+__device__ V *fft_rows(V *a, V *b, int nrows, int stride, const FftPlan &P, const V *__restrict__ tw, int tid,
+                       int nthr) {
+    V *src = a, *dst = b;
     int Ns = 1;
     for (int s = 0; s < P.nstage; ++s) {
         int R = P.rad[s];
@@ -130,7 +174,7 @@ __device__ double2 *fft_rows(double2 *a, double2 *b, int nrows, int stride, cons
             default: fft_stage<5, INV>(src, dst, nrows, stride, P.n, Ns, tw, tid, nthr); break;
         }
         __syncthreads();
-        double2 *t = src;
+        V *t = src;
         src = dst;
         dst = t;
         Ns *= R;

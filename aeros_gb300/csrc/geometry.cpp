@@ -207,6 +207,18 @@ int upload_tables(const Geometry &g, DevTables &t) {
     }
     if ((rc = upload(t.tw, tw.data(), n))) return rc;
     if ((rc = upload(t.twN, twN.data(), n + 1))) return rc;
+    // the same twiddles as double-floats, from extended-precision cos and sin
+    auto dfc_of = [](long double a) {
+        const long double c = std::cos(a), s = std::sin(a);
+        const float ch = (float)c, sh = (float)s;
+        return make_float4(ch, (float)(c - (long double)ch), sh, (float)(s - (long double)sh));
+    };
+    const long double pi_l = 3.141592653589793238462643383279502884L;
+    std::vector<float4> twD(n), twND(n + 1);
+    for (int k = 0; k < n; ++k) twD[k] = dfc_of(-2.0L * pi_l * k / n);
+    for (int k = 0; k <= n; ++k) twND[k] = dfc_of(-2.0L * pi_l * k / g.nlon);
+    if ((rc = upload(t.twD, twD.data(), n))) return rc;
+    if ((rc = upload(t.twND, twND.data(), n + 1))) return rc;
     if ((rc = upload(t.moff, g.moff.data(), g.moff.size()))) return rc;
     if ((rc = upload(t.l_of_lm, g.l_of_lm.data(), g.l_of_lm.size()))) return rc;
     if ((rc = upload(t.m_of_lm, g.m_of_lm.data(), g.m_of_lm.size()))) return rc;
@@ -215,7 +227,8 @@ int upload_tables(const Geometry &g, DevTables &t) {
 }
 
 void free_tables(DevTables &t) {
-    void *ps[] = {t.Ps, t.dPs, t.PaT, t.dPaT, t.sint, t.x, t.w, t.lfac, t.tw, t.twN, t.moff, t.l_of_lm, t.m_of_lm};
+    void *ps[] = {t.Ps, t.dPs, t.PaT, t.dPaT, t.sint, t.x, t.w, t.lfac, t.tw, t.twN, t.twD, t.twND, t.moff,
+                  t.l_of_lm, t.m_of_lm};
     for (void *p : ps)
         if (p) cudaFree(p);
     t = DevTables{};

@@ -213,8 +213,10 @@ int run_synth(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, v
     } else {
         if ((rc = launch_leg_synth_fp64(c, d->syn, h->F, d->nrow))) return rc;
     }
-    if (h->precision == AEROS_PREC_SPLIT && split_dft_has_synth(h->dft))
-        return split_fourier_synth(h->dft, c, d->fsyn, d->nfsyn, h->F, d->nrow);
+    if (h->precision == AEROS_PREC_SPLIT) {
+        if (split_dft_has_synth(h->dft)) return split_fourier_synth(h->dft, c, d->fsyn, d->nfsyn, h->F, d->nrow);
+        return launch_fourier_synth_df(c, d->fsyn, d->nfsyn, h->F, d->nrow);
+    }
     return launch_fourier_synth(c, d->fsyn, d->nfsyn, h->F, d->nrow);
 }
 
@@ -225,6 +227,8 @@ int run_anal(aeros_sht_t h, int op, const void *i0, const void *i1, void *o0, vo
     Ctx c = h->ctx();
     if (h->precision == AEROS_PREC_SPLIT && split_dft_has_anal(h->dft))
         rc = split_fourier_anal(h->dft, c, d->fana, d->nfana, h->F, d->nrow);
+    else if (h->precision == AEROS_PREC_SPLIT)
+        rc = launch_fourier_anal_df(c, d->fana, d->nfana, h->F, d->nrow);
     else
         rc = launch_fourier_anal(c, d->fana, d->nfana, h->F, d->nrow);
     if (rc) return rc;

@@ -31,8 +31,9 @@ int split_flag_status(int flag);
 // Longitude transforms of the split form as exact-digit DFT products on the
 // tensor cores (split_dft.cu).  Same contracts as launch_fourier_synth /
 // launch_fourier_anal; a direction whose contraction exceeds 441 is not built
-// (has_* false) and keeps the FFT.  Creation returns a null context when the
-// environment sets AEROS_SPLIT_FFT=1 (the FFT is kept in both directions).
+// (has_* false) and keeps the FFT.  Creation returns a null context unless the
+// environment sets AEROS_SPLIT_DFT=1: by default the split form's longitude
+// transforms are the double-float FFTs (launch_fourier_*_df).
 struct SplitDft;
 int split_dft_create(const Geometry &g, SplitDft **out);
 void split_dft_destroy(SplitDft *s);

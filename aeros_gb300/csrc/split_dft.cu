@@ -490,8 +490,10 @@ int launch_gemm(const DftPart &d, const Ctx &c, const P &p, int ncol, int *err, 
 
 int split_dft_create(const Geometry &g, SplitDft **out) {
     *out = nullptr;
-    const char *keep_fft = std::getenv("AEROS_SPLIT_FFT");
-    if (keep_fft && keep_fft[0] == '1') return AEROS_OK;
+    // the split form's longitude transforms are double-float FFTs unless AEROS_SPLIT_DFT=1
+    // asks for these exact-digit DFT products
+    const char *want = std::getenv("AEROS_SPLIT_DFT");
+    if (!(want && want[0] == '1')) return AEROS_OK;
     SplitDft *s = new SplitDft;
     {
         int dev = 0;

@@ -171,6 +171,180 @@ static int fourier_lpb(int nlon) {
 
 int fourier_lpb_limit(size_t smem_per_lat) { return (int)std::max<size_t>(1, (200 * 1024) / smem_per_lat); }
 
+// ============================================================ double-float Fourier transforms
+// The split form's longitude transforms: the same algorithm as k_fourier_synth /
+// k_fourier_anal (combination, half-length complex FFT, untangling) in
+// double-float arithmetic on the FP32 pipes (df.cuh; ~48-bit significands,
+// relative error ~1e-14 per output) instead of on GB300's narrow FP64 pipe.
+// Inputs and outputs stay FP64, converted with integer operations.
+struct FsynArgsDF {
+    const FsynField *fields;
+    const double2 *F;
+    int nrow, ms, T, nlat, nlon, lpb;
+    FftPlan plan;
+    const dfc *tw, *twN;
+    const double *isin;
+};
+template <bool RAG = false>
+__global__ void k_fourier_synth_df(const __grid_constant__ RagPack<FsynArgsDF> rp) {
+    uint3 bid, gdim;
+    const FsynArgsDF &ka = rag_part<RAG>(rp, bid, gdim);
+    const FsynField *__restrict__ fields = ka.fields;
+    const double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, T = ka.T, nlat = ka.nlat, nlon = ka.nlon, lpb = ka.lpb;
+    const FftPlan &plan = ka.plan;
+    const dfc *__restrict__ tw = ka.tw;
+    const dfc *__restrict__ twN = ka.twN;
+    const double *__restrict__ isin = ka.isin;
+    extern __shared__ dfc smd[];
+    const FsynField fd = fields[bid.x];
+    const int n = nlon / 2;
+    const int j0 = bid.y * lpb;
+    const int nr = min(lpb, nlat - j0);
+    const int rs = frow(n);
+    dfc *A = smd, *B = smd + (size_t)lpb * rs, *X = smd + (size_t)2 * lpb * rs;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const StageDiv dms(ms), dnlon(nlon);
+    // the field's factors with 1/sqrt(2 pi) folded in, as double-floats (a few FP64 products per CTA)
+    const df2 a0 = d2df(fd.a0 * kNrm), b0 = d2df(fd.b0 * kNrm), a1 = d2df(fd.a1 * kNrm), b1 = d2df(fd.b1 * kNrm);
+    const bool two = fd.src1 >= 0, pure_a = fd.b0 == 0.0 && (!two || fd.b1 == 0.0);
+    for (int idx = tid; idx < nr * ms; idx += nthr) {
+        const int r = dms.div(idx), m = idx - r * ms;
+        const int j = j0 + r;
+        const double2 *Fr = F + (size_t)j * nrow * ms;
+        const dfc f = d2dfc(Fr[(size_t)fd.src0 * ms + m]);
+        dfc x;
+        if (pure_a) {
+            x = cscale(f, a0);
+            if (two) x = cadd(x, cscale(d2dfc(Fr[(size_t)fd.src1 * ms + m]), a1));
+        } else {
+            const df2 bs = df_mul(d2df(isin[j]), df2{(float)m, 0.0f});   // m / sin(theta_j)
+            const df2 bb = df_mul(b0, bs);
+            // (a0 + i bb) f
+            x = dfc{df_dot2(a0, f.r, bb, f.i, true), df_dot2(a0, f.i, bb, f.r, false)};
+            if (two) {
+                const dfc g = d2dfc(Fr[(size_t)fd.src1 * ms + m]);
+                const df2 cc = df_mul(b1, bs);
+                x = cadd(x, dfc{df_dot2(a1, g.r, cc, g.i, true), df_dot2(a1, g.i, cc, g.r, false)});
+            }
+        }
+        if (m == 0) x.i = df2{0.0f, 0.0f};
+        X[(size_t)r * ms + m] = x;
+    }
+    __syncthreads();
+    // E = X[k] + conj(X[n-k]),  O = (X[k] - conj(X[n-k])) e^{+2 pi i k/N},  Z = E + i O,
+    // Z[n-k] = conj(E) + i conj(O): one pass over k = 0 .. n/2 forms both of a pair
+    const int nhalf = n / 2 + 1;
+    const StageDiv dnh(nhalf);
+    const dfc zero{df2{0.0f, 0.0f}, df2{0.0f, 0.0f}};
+    for (int idx = tid; idx < nr * nhalf; idx += nthr) {
+        const int r = dnh.div(idx), k = idx - r * nhalf;
+        const int kc = n - k;
+        const dfc xk = k <= T ? X[(size_t)r * ms + k] : zero;
+        const dfc xc = (kc <= T && kc < n) ? X[(size_t)r * ms + kc] : zero;
+        const dfc E{df_add(xk.r, xc.r), df_sub(xk.i, xc.i)};
+        const dfc D{df_sub(xk.r, xc.r), df_add(xk.i, xc.i)};
+        const dfc O = cmulconj(D, twN[k]);
+        A[(size_t)r * rs + fpad(k)] = dfc{df_sub(E.r, O.i), df_add(E.i, O.r)};
+        if (k > 0 && k < kc) A[(size_t)r * rs + fpad(kc)] = dfc{df_add(E.r, O.i), df_sub(O.r, E.i)};
+    }
+    __syncthreads();
+    dfc *res = fft_rows<true>(A, B, nr, rs, plan, tw, tid, nthr);
+    for (int idx = tid; idx < nr * nlon; idx += nthr) {
+        const int r = dnlon.div(idx), i = idx - r * nlon;
+        const dfc z = res[(size_t)r * rs + fpad(i >> 1)];
+        fd.dst[(size_t)(j0 + r) * nlon + i] = df2d((i & 1) ? z.i : z.r);
+    }
+}
+
+struct FanaArgsDF {
+    const FanaField *fields;
+    double2 *F;
+    int nrow, ms, T, nlat, nlon, lpb;
+    FftPlan plan;
+    const dfc *tw, *twN;
+};
+template <bool RAG = false>
+__global__ void k_fourier_anal_df(const __grid_constant__ RagPack<FanaArgsDF> rp) {
+    uint3 bid, gdim;
+    const FanaArgsDF &ka = rag_part<RAG>(rp, bid, gdim);
+    const FanaField *__restrict__ fields = ka.fields;
+    double2 *__restrict__ F = ka.F;
+    const int nrow = ka.nrow, ms = ka.ms, nlat = ka.nlat, nlon = ka.nlon, lpb = ka.lpb;
+    const FftPlan &plan = ka.plan;
+    const dfc *__restrict__ tw = ka.tw;
+    const dfc *__restrict__ twN = ka.twN;
+    extern __shared__ dfc smd[];
+    const FanaField fd = fields[bid.x];
+    const int n = nlon / 2;
+    const int j0 = bid.y * lpb;
+    const int nr = min(lpb, nlat - j0);
+    const int rs = frow(n);
+    dfc *A = smd, *B = smd + (size_t)lpb * rs;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const StageDiv dms(ms), dn(n);
+    // grid values in pairs (even, odd longitude) as one complex value
+    for (int idx = tid; idx < nr * n; idx += nthr) {
+        const int r = dn.div(idx), k = idx - r * n;
+        const double2 g = *reinterpret_cast<const double2 *>(fd.src + (size_t)(j0 + r) * nlon + 2 * k);
+        A[(size_t)r * rs + fpad(k)] = d2dfc(g);
+    }
+    __syncthreads();
+    dfc *Z = fft_rows<false>(A, B, nr, rs, plan, tw, tid, nthr);
+    const df2 sc = d2df(kSq2Pi / nlon), half{0.5f, 0.0f};
+    for (int idx = tid; idx < nr * ms; idx += nthr) {
+        const int r = dms.div(idx), m = idx - r * ms;
+        // m <= T < n, so m % n = m and (n - m) % n = (m == 0 ? 0 : n - m)
+        const dfc a = Z[(size_t)r * rs + fpad(m)];
+        const dfc b = Z[(size_t)r * rs + fpad(m == 0 ? 0 : n - m)];
+        // E = (a + conj b)/2, O = -i/2 (a - conj b),  X = E + e^{-2 pi i m/N} O
+        const dfc E{df_scale(df_add(a.r, b.r), 0.5f), df_scale(df_sub(a.i, b.i), 0.5f)};
+        const dfc O{df_scale(df_add(a.i, b.i), 0.5f), df_scale(df_sub(b.r, a.r), 0.5f)};
+        dfc X = cadd(E, cmul(O, twN[m]));
+        X = cscale(X, sc);
+        if (m == 0) X.i = df2{0.0f, 0.0f};
+        F[((size_t)(j0 + r) * nrow + fd.row) * ms + m] = dfc2d(X);
+    }
+    (void)half;
+}
+
+int launch_fourier_synth_df(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    const size_t per_lat = (size_t)(2 * frow(c.nlon / 2) + c.ms) * sizeof(dfc);
+    int lpb = c.tune && c.tune->fs_lpb > 0 ? std::min(c.tune->fs_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
+    const int thr = c.tune ? c.tune->fs_thr : 256;
+    const size_t smem = per_lat * lpb;
+    const dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
+    if (int rc = raise_smem_limit((const void *)k_fourier_synth_df<>, smem)) return rc;
+    const FsynArgsDF ka{fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+                        reinterpret_cast<const dfc *>(c.tab->twD), reinterpret_cast<const dfc *>(c.tab->twND),
+                        c.tab->sint};
+    if (int rc = emit_launch(c.stream, c.rec, (const void *)k_fourier_synth_df<>, (const void *)k_fourier_synth_df<true>,
+                             grid, dim3(thr), smem, ka))
+        return rc;
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
+int launch_fourier_anal_df(const Ctx &c, const FanaField *fields_d, int nf, double2 *F, int nrow) {
+    if (nf <= 0) return AEROS_OK;
+    const size_t per_lat = (size_t)2 * frow(c.nlon / 2) * sizeof(dfc);
+    int lpb = c.tune && c.tune->fa_lpb > 0 ? std::min(c.tune->fa_lpb, fourier_lpb_limit(per_lat)) : fourier_lpb(c.nlon);
+    const int thr = c.tune ? c.tune->fa_thr : 256;
+    const size_t smem = per_lat * lpb;
+    const dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
+    if (int rc = raise_smem_limit((const void *)k_fourier_anal_df<>, smem)) return rc;
+    const FanaArgsDF ka{fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
+                        reinterpret_cast<const dfc *>(c.tab->twD), reinterpret_cast<const dfc *>(c.tab->twND)};
+    if (int rc = emit_launch(c.stream, c.rec, (const void *)k_fourier_anal_df<>, (const void *)k_fourier_anal_df<true>,
+                             grid, dim3(thr), smem, ka))
+        return rc;
+    if (c.launches) ++*c.launches;
+    AEROS_CUDA(cudaGetLastError());
+    return AEROS_OK;
+}
+
 LaunchRec fuse_launches(const std::vector<const LaunchRec *> &ps) {
     LaunchRec f = *ps[0];
     RagHdr *h = reinterpret_cast<RagHdr *>(f.pack.data());

@@ -146,3 +146,40 @@ def test_split_analysis_groups_are_per_column(gpulib, T):
         assert np.array_equal(S[i], S1[0]) and np.array_equal(Tt[i], T1[0])
     so, to = o.analysis_vec(vth, vph)
     assert relerr(S, so) < TOL and relerr(Tt, to) < TOL
+
+
+@pytest.mark.parametrize("T", [21, 42])
+def test_split_fourier_paths_agree(gpulib, T, monkeypatch):
+    """The split form's two longitude-transform paths: double-float FFTs (the
+    default) and exact-digit DFT products on the tensor cores (AEROS_SPLIT_DFT=1),
+    each against the oracle, and the step tendencies of both at T42L20."""
+    from aeros_gb300.spectral import AerosSHT
+    from aeros_gb300.params import PREC_SPLIT, held_suarez_params
+    from aeros_gb300.dynamics import AerosDyn
+    from oracle.pyoracle import OracleSHT, OracleDyn
+    from tests.test_gpu_dyn import moving_state
+    o = OracleSHT(T)
+    rng = np.random.default_rng(34)
+    c = red_spectrum(rng, o.l_of_lm, o.m_of_lm, (3,))
+    f = o.synthesis(c)
+    res = {}
+    for path in ("0", "1"):
+        monkeypatch.setenv("AEROS_SPLIT_DFT", path)
+        g = AerosSHT(T, batch_max=3, precision=PREC_SPLIT)
+        res[path] = (g.synthesis(c), g.analysis(f))
+        e1, e2 = relerr(res[path][0], f), relerr(res[path][1], o.analysis(f))
+        print(f"T{T} split Fourier path AEROS_SPLIT_DFT={path}: synthesis {e1:.2e} analysis {e2:.2e}")
+        assert e1 < TOL and e2 < TOL
+    assert relerr(res["0"][0], res["1"][0]) < 1e-12 and relerr(res["0"][1], res["1"][1]) < 1e-12
+    if T == 42:
+        od = OracleDyn(held_suarez_params(trunc=42, nlev=20))
+        st = moving_state(od, seed=43)
+        od.set_state(*st)
+        ref = od.tendency()
+        for path in ("0", "1"):
+            monkeypatch.setenv("AEROS_SPLIT_DFT", path)
+            d = AerosDyn(held_suarez_params(trunc=42, nlev=20, precision=PREC_SPLIT))
+            d.set_state(*st)
+            et = [relerr(a, b) for a, b in zip(d.tendency(), ref)]
+            print(f"T42L20 split tendencies, AEROS_SPLIT_DFT={path}:", ["%.1e" % x for x in et])
+            assert max(et) < TOL
