@@ -205,9 +205,20 @@ __global__ void k_fourier_synth_df(const __grid_constant__ RagPack<FsynArgsDF> r
     dfc *A = smd, *B = smd + (size_t)lpb * rs, *X = smd + (size_t)2 * lpb * rs;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const StageDiv dms(ms), dnlon(nlon);
-    // the field's factors with 1/sqrt(2 pi) folded in, as double-floats (a few FP64 products per CTA)
-    const df2 a0 = d2df(fd.a0 * kNrm), b0 = d2df(fd.b0 * kNrm), a1 = d2df(fd.a1 * kNrm), b1 = d2df(fd.b1 * kNrm);
-    const bool two = fd.src1 >= 0, pure_a = fd.b0 == 0.0 && (!two || fd.b1 == 0.0);
+    // the field's factors with 1/sqrt(2 pi) folded in, as double-floats: formed once per CTA
+    // (four FP64 products) and shared
+    __shared__ df2 fac[4];
+    if (tid == 0) {
+        fac[0] = d2df(fd.a0 * kNrm);
+        fac[1] = d2df(fd.b0 * kNrm);
+        fac[2] = d2df(fd.a1 * kNrm);
+        fac[3] = d2df(fd.b1 * kNrm);
+    }
+    __syncthreads();
+    const df2 a0 = fac[0], b0 = fac[1], a1 = fac[2], b1 = fac[3];
+    // zero tests on the bits (no FP64 comparison)
+    const bool b0z = (__double_as_longlong(fd.b0) << 1) == 0, b1z = (__double_as_longlong(fd.b1) << 1) == 0;
+    const bool two = fd.src1 >= 0, pure_a = b0z && (!two || b1z);
     for (int idx = tid; idx < nr * ms; idx += nthr) {
         const int r = dms.div(idx), m = idx - r * ms;
         const int j = j0 + r;
@@ -263,6 +274,7 @@ struct FanaArgsDF {
     int nrow, ms, T, nlat, nlon, lpb;
     FftPlan plan;
     const dfc *tw, *twN;
+    df2 sc;   // sqrt(2 pi) / nlon
 };
 template <bool RAG = false>
 __global__ void k_fourier_anal_df(const __grid_constant__ RagPack<FanaArgsDF> rp) {
@@ -291,7 +303,7 @@ __global__ void k_fourier_anal_df(const __grid_constant__ RagPack<FanaArgsDF> rp
     }
     __syncthreads();
     dfc *Z = fft_rows<false>(A, B, nr, rs, plan, tw, tid, nthr);
-    const df2 sc = d2df(kSq2Pi / nlon), half{0.5f, 0.0f};
+    const df2 sc = ka.sc;
     for (int idx = tid; idx < nr * ms; idx += nthr) {
         const int r = dms.div(idx), m = idx - r * ms;
         // m <= T < n, so m % n = m and (n - m) % n = (m == 0 ? 0 : n - m)
@@ -305,7 +317,6 @@ __global__ void k_fourier_anal_df(const __grid_constant__ RagPack<FanaArgsDF> rp
         if (m == 0) X.i = df2{0.0f, 0.0f};
         F[((size_t)(j0 + r) * nrow + fd.row) * ms + m] = dfc2d(X);
     }
-    (void)half;
 }
 
 int launch_fourier_synth_df(const Ctx &c, const FsynField *fields_d, int nf, const double2 *F, int nrow) {
@@ -336,7 +347,8 @@ int launch_fourier_anal_df(const Ctx &c, const FanaField *fields_d, int nf, doub
     const dim3 grid(nf, (c.nlat + lpb - 1) / lpb);
     if (int rc = raise_smem_limit((const void *)k_fourier_anal_df<>, smem)) return rc;
     const FanaArgsDF ka{fields_d, F, nrow, c.ms, c.T, c.nlat, c.nlon, lpb, c.tab->plan,
-                        reinterpret_cast<const dfc *>(c.tab->twD), reinterpret_cast<const dfc *>(c.tab->twND)};
+                        reinterpret_cast<const dfc *>(c.tab->twD), reinterpret_cast<const dfc *>(c.tab->twND),
+                        df_host(kSq2Pi / c.nlon)};
     if (int rc = emit_launch(c.stream, c.rec, (const void *)k_fourier_anal_df<>, (const void *)k_fourier_anal_df<true>,
                              grid, dim3(thr), smem, ka))
         return rc;
