@@ -469,9 +469,19 @@ def build_members(cfg, prec, seed_base, tune, autotune_log):
     return hs
 
 
-def time_group(hs, steps, torch):
+def time_group(hs, steps, torch, fuse=True):
+    """Device time per step of a group of handles: fused launches (one per kernel
+    over the handles) or, with fuse=False, one graph branch per handle."""
     from aeros_gb300.dynamics import AerosGroup
-    g = AerosGroup(hs)
+    prev = os.environ.get("AEROS_GROUP_FUSE")
+    os.environ["AEROS_GROUP_FUSE"] = "1" if fuse else "0"
+    try:
+        g = AerosGroup(hs)
+    finally:
+        if prev is None:
+            del os.environ["AEROS_GROUP_FUSE"]
+        else:
+            os.environ["AEROS_GROUP_FUSE"] = prev
     s = torch.cuda.Stream()
     g.set_stream(s.cuda_stream)
     g.step_async(3)
@@ -488,12 +498,14 @@ def batched_form(args, torch, t_single):
     """The batching form.  (1) T42L20 ensembles: 96 members of the headline
     configuration (each its own seed and dT_y), one CUDA graph launch per step,
     FP64 and split precision, as 3 handles of 32 (the group fuses their
-    launches: one ragged launch per kernel over the handles) and the split
-    members also as one handle of 96 (one launch per kernel type and step);
-    the better split aggregate SYPD over the single-member FP64
+    launches: one ragged launch per kernel over the handles; the split ones
+    also as one graph branch per handle) and the split members also as one
+    handle of 96 (one launch per kernel type and step); the best split
+    aggregate SYPD over the single-member FP64
     path's is the ratio the >= 20x target is stated for.  (2) The mixed
     configuration of 96 uneven members, 32 x T21L16 + 32 x T31L20 + 32 x
-    T42L20, FP64 and split, beside the same members stepped one by one through
+    T42L20, FP64 and split, each with fused launches and as one graph branch
+    per handle, beside the same members stepped one by one through
     the single-member FP64 path (32 x the step time of one member of each
     configuration).  Working sets > L2, so no flush is needed."""
     from aeros_gb300.params import held_suarez_params, PREC_FP64, PREC_SPLIT
@@ -506,6 +518,12 @@ def batched_form(args, torch, t_single):
     t42 = {"members": f"96 x T42L20 ({nh} handles of {per})"}
     for name, prec in (("fp64", PREC_FP64), ("split", PREC_SPLIT)):
         hs = build_members([(42, 20, per)] * nh, prec, 5000, not args.no_tune, tunelog.setdefault("t42_" + name, {}))
+        if prec == PREC_SPLIT and nh > 1:
+            # the same handles as one graph branch each (before fusion unifies their launch shapes)
+            tb, nlb = time_group(hs, args.batched_steps, torch, fuse=False)
+            t42["split_branches"] = {"sypd": 96 * sypd(tb), "ms_per_step": tb * 1e3, "us_per_member_step": tb * 1e6 / 96,
+                                     "gpu_launches_per_step": nlb, "fused_launches": False,
+                                     "vs_fp64_single": 96 * sypd(tb) / sypd(t_single)}
         t, nl = time_group(hs, args.batched_steps, torch)
         del hs
         t42[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "us_per_member_step": t * 1e6 / 96,
@@ -525,6 +543,9 @@ def batched_form(args, torch, t_single):
     mixed = {"members": "32 x T21L16 + 32 x T31L20 + 32 x T42L20"}
     for name, prec in (("fp64", PREC_FP64), ("split", PREC_SPLIT)):
         hs = build_members(cfg, prec, 1000, not args.no_tune, tunelog.setdefault("mixed_" + name, {}))
+        tb, nlb = time_group(hs, args.batched_steps, torch, fuse=False)
+        mixed[name + "_branches"] = {"sypd": 96 * sypd(tb), "ms_per_step": tb * 1e3, "gpu_launches_per_step": nlb,
+                                     "fused_launches": False, "vs_fp64_single_mixed": 96 * sypd(tb) / sypd(t_single)}
         t, nl = time_group(hs, args.batched_steps, torch)
         del hs
         mixed[name] = {"sypd": 96 * sypd(t), "ms_per_step": t * 1e3, "gpu_launches_per_step": nl,
@@ -558,7 +579,7 @@ def batched_form(args, torch, t_single):
     mixed["cpu_oracle"] = {"sypd": 96 * sypd(cpu_seq), "ms_per_step": cpu_seq * 1e3, "ms_per_member_step": cpu_perm,
                            "cores": cores, "kind": "port",
                            "sample": "3 steps of one member per configuration on all cores, times 32 members"}
-    for name in ("fp64", "split"):
+    for name in ("fp64", "split", "fp64_branches", "split_branches"):
         mixed[name]["vs_one_by_one_fp64"] = mixed[name]["sypd"] / mixed["one_by_one_fp64"]["sypd"]
     out["mixed"] = mixed
     out["autotune"] = tunelog
