@@ -637,6 +637,7 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
     __shared__ AnaCol sCol[kAnaCT];
 
     const int m = bid.x;
+    const double md = m;
     const int K = T - m + 1;
     const int l0 = bid.z * kAnaLT;                 // offset (l - m) of this tile
     if (l0 >= K) return;
@@ -686,14 +687,26 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
                     int jn = j0 + jj, js = nlat - 1 - jn;
                     double2 fn = F[((size_t)jn * nrow + row) * ms + m];
                     double2 fs = F[((size_t)js * nrow + row) * ms + m];
-                    if (s < 2) {
-                        double a = s == 0 ? q.a1 : q.a2, b = s == 0 ? q.b1 : q.b2;
-                        double bb = b * m * isin[jn];
-                        fn = make_double2(a * fn.x - bb * fn.y, a * fn.y + bb * fn.x);
-                        fs = make_double2(a * fs.x - bb * fs.y, a * fs.y + bb * fs.x);
-                    }
+                    // fold first (the scaling is linear and the same at j and its mirror, whose
+                    // sin theta is equal), then scale by (a + i b m / sin): skipped for a = 1, b = 0
                     e = cadd(fn, fs);
                     o = csub(fn, fs);
+                    if (s < 2) {
+                        const double a = s == 0 ? q.a1 : q.a2, b = s == 0 ? q.b1 : q.b2;
+                        if (b != 0.0) {
+                            const double bb = b * md * isin[jn];
+                            if (a != 0.0) {
+                                e = make_double2(a * e.x - bb * e.y, a * e.y + bb * e.x);
+                                o = make_double2(a * o.x - bb * o.y, a * o.y + bb * o.x);
+                            } else {
+                                e = make_double2(-bb * e.y, bb * e.x);
+                                o = make_double2(-bb * o.y, bb * o.x);
+                            }
+                        } else if (a != 1.0) {
+                            e = make_double2(a * e.x, a * e.y);
+                            o = make_double2(a * o.x, a * o.y);
+                        }
+                    }
                 }
             }
             sX[cc][s][0][jj] = e;
