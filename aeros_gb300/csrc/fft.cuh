@@ -8,7 +8,6 @@
 //   v_r = x[j + r n/R] * w^{(j mod Ns) r n/(Ns R)},  v <- DFT_R(v),
 //   y[(j - j mod Ns) R + j mod Ns + r Ns] = v_r.
 #pragma once
-#include <type_traits>
 #include "aeros_internal.h"
 #include "df.cuh"
 
@@ -143,9 +142,7 @@ __device__ __forceinline__ void fft_stage(const V *src, V *dst, int nrows, int s
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
-                V w;
-                if constexpr (std::is_same<V, double2>::value) w = __ldg(&tw[k * r * tstep]);
-                else w = tw[k * r * tstep];
+                const V w = tw[k * r * tstep];   // global or shared memory
                 v[r] = INV ? cmulconj(v[r], w) : cmul(v[r], w);
             }
         }
