@@ -85,3 +85,21 @@ def test_smaller_handle_created_later_keeps_larger_launches(gpulib):
     big.step(2)
     for x, y in zip(big.get_state(), ref.get_state()):
         assert np.array_equal(x, y)
+
+
+def test_fused_group_of_more_handles_than_one_launch_takes(gpulib):
+    """Six handles (one launch fuses at most four): the launches split into
+    parts of four and two, and the states stay bit-identical."""
+    from aeros_gb300.dynamics import AerosGroup
+    cfg = [(21, 16, 1, 1000 + i) for i in range(4)] + [(31, 20, 1, 1100), (42, 20, 1, 1200)]
+    grouped = [_make(*c)[0] for c in cfg]
+    single = [_make(*c)[0] for c in cfg]
+    g = AerosGroup(grouped)
+    info = g.info()
+    assert info["fused"] and 7 < info["kernels_step"] <= 21, info
+    g.step(3)
+    for d in single:
+        d.step(3)
+    for a, b in zip(grouped, single):
+        for x, y in zip(a.get_state(squeeze=False), b.get_state(squeeze=False)):
+            assert np.array_equal(x, y)
