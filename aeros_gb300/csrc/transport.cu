@@ -8,12 +8,14 @@
 //   k_tr_zonal   block per (level, latitude) row, threads over longitude:
 //                periodic van Leer face values, fluxes staged in shared memory
 //   k_tr_mfaces  thread per (level, face, longitude): meridional face fluxes
-//   k_tr_mupdate thread per cell: the meridional update from its two faces
-//   k_tr_vert    thread per grid column, streamed down the column: vertical mass
-//                flux from the layer-mass change of the two sweeps, levels updated
-//                top down
+//   k_tr_vert    block of grid columns: the meridional update from each column's
+//                two faces at every level, then the vertical mass flux from the
+//                layer-mass change of the two sweeps, levels updated top down
 //                (a level's upper-face flux sees the level above already updated,
 //                as the reference's loop does)
+// Each kernel hands the next the ratios q = qm / dp it has formed (qr after the
+// vertical update, qz after the zonal sweep), so no ratio is divided twice, and
+// the grid spacings enter as per-row reciprocals fixed at create.
 // Grids are (nlev, nlat, nlon) in C order, latitude north to south: the
 // Fortran (nlon, nlat, nlev) arrays unchanged.
 #include <algorithm>
@@ -27,19 +29,20 @@ using namespace aeros;
 
 namespace {
 
-constexpr double kCflMax = 0.9;      // CFL_MAX of src/dynamics/aeros_transport.f90
+constexpr double kCflMax = 0.9;      // CFL_MAX, src/dynamics/aeros_transport.f90:144
 constexpr int kTrMaxLev = 64;
 
 __device__ __forceinline__ double vanleer(double a, double b) {
-    // harmonic-mean slope, zero at an extremum (vanleer, :442-452)
+    // harmonic-mean slope, zero at an extremum (vanleer, :575-594)
     return a * b > 0.0 ? 2.0 * a * b / (a + b) : 0.0;
 }
 
 // Layer air mass from the surface pressure (aeros_vgrid_pressure,
-// src/dynamics/aeros_vertical.f90:344-380) and qm = q dp.
+// src/dynamics/aeros_vertical.f90:344-380), qm = q dp and the ratio qm / dp that
+// the first zonal sweep starts from.
 __global__ void k_tr_begin(const double *__restrict__ lnps, const double *__restrict__ q,
                            const double *__restrict__ A, const double *__restrict__ B, int nlev, long ng,
-                           double *__restrict__ dp, double *__restrict__ qm) {
+                           double *__restrict__ dp, double *__restrict__ qm, double *__restrict__ qr) {
     const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (c >= ng) return;
     const double ps = exp(lnps[c]);
@@ -47,71 +50,83 @@ __global__ void k_tr_begin(const double *__restrict__ lnps, const double *__rest
     for (int k = 0; k < nlev; ++k) {
         const double ph1 = A[k + 1] + B[k + 1] * ps;
         const double d = ph1 - ph0;
+        const double m = q[k * ng + c] * d;
         dp[k * ng + c] = d;
-        qm[k * ng + c] = q[k * ng + c] * d;
+        qm[k * ng + c] = m;
+        qr[k * ng + c] = m / d;
         ph0 = ph1;
     }
 }
 
-// Largest total Courant number (max_courant, :555-586); non-negative doubles
-// order like their bit patterns, so the maximum is an integer atomicMax.
+// Largest total Courant number (max_courant, :690-741); non-negative doubles
+// order like their bit patterns, so the maximum is an integer atomicMax.  The
+// column sum of the zonal mass flux is formed first, then the running sum is
+// rebuilt from the same terms in the same order, so it ends on the same value.
 __global__ void k_tr_courant(const double *__restrict__ u, const double *__restrict__ v,
                              const double *__restrict__ lnps, const double *__restrict__ A,
-                             const double *__restrict__ B, const double *__restrict__ coslat,
-                             const double *__restrict__ dmu, int nlev, int nlon, long ng, double dlam, double dt,
+                             const double *__restrict__ B, const double *__restrict__ rdx,
+                             const double *__restrict__ rdyc, int nlev, int nlon, long ng, double dt,
                              unsigned long long *__restrict__ cmax) {
     const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double best = 0.0;
     if (c < ng) {
         const int j = (int)(c / nlon);
         const double ps = exp(lnps[c]);
-        const double dx = kA * coslat[j] * dlam;
-        double dpc[kTrMaxLev], scum[kTrMaxLev + 1];
-        double ph0 = A[0] + B[0] * ps;
-        scum[0] = 0.0;
+        const double rx = rdx[j], ry = rdyc[j];
+        double SN = 0.0, ph0 = A[0] + B[0] * ps;
+#pragma unroll 4
         for (int k = 0; k < nlev; ++k) {
             const double ph1 = A[k + 1] + B[k + 1] * ps;
-            dpc[k] = ph1 - ph0;
+            SN = SN + (ph1 - ph0) * fabs(u[k * ng + c]) * rx;
             ph0 = ph1;
-            scum[k + 1] = scum[k] + dpc[k] * fabs(u[k * ng + c]) / dx;
         }
-        const double dy = kA * dmu[j] / fmax(coslat[j], 1.0e-6);
-        const double SN = scum[nlev];
+        double scum0 = 0.0;
+        ph0 = A[0] + B[0] * ps;
+#pragma unroll 4
         for (int k = 0; k < nlev; ++k) {
-            const double cx = fabs(u[k * ng + c]) * dt / dx;
-            const double cy = fabs(v[k * ng + c]) * dt / dy;
-            const double cz = (fabs(B[k + 1] * SN - scum[k + 1]) + fabs(B[k] * SN - scum[k])) * dt / dpc[k];
+            const double ph1 = A[k + 1] + B[k + 1] * ps;
+            const double d = ph1 - ph0, au = fabs(u[k * ng + c]);
+            const double scum1 = scum0 + d * au * rx;
+            const double cx = au * dt * rx;
+            const double cy = fabs(v[k * ng + c]) * dt * ry;
+            const double cz = (fabs(B[k + 1] * SN - scum1) + fabs(B[k] * SN - scum0)) * dt / d;
             best = fmax(best, cx + cy + cz);
+            scum0 = scum1;
+            ph0 = ph1;
         }
     }
     for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
     if ((threadIdx.x & 31) == 0) atomicMax(cmax, (unsigned long long)__double_as_longlong(best));
 }
 
-// Zonal sweep (sweep_zonal, :299-340); also keeps dp at the start of the
-// sub-step for the vertical mass flux.
+// Zonal sweep (sweep_zonal, :374-437).  Starts from the ratios qr = qm / dp that
+// the previous vertical update (or k_tr_begin) left, keeps dp at the start of the
+// sub-step for the vertical mass flux and leaves the ratios after the sweep in
+// qz for the meridional faces.
 __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp, double *__restrict__ qm,
-                           double *__restrict__ dp0, const double *__restrict__ coslat, int nlon, int nlat, long ng,
-                           double dlam, double dt) {
+                           const double *__restrict__ qr, double *__restrict__ qz, double *__restrict__ dp0,
+                           const double *__restrict__ rdx, int nlon, long ng, double dt) {
     extern __shared__ double zs[];
     double *qc = zs, *dc = zs + nlon, *fa = zs + 2 * nlon, *fq = zs + 3 * nlon;
     const int j = blockIdx.x, k = blockIdx.y, i = threadIdx.x;
     const long row = k * ng + (long)j * nlon;
+    const double cx = dt * rdx[j];   // dt / dx of this row
+    double m = 0.0;
     if (i < nlon) {
         const double d = dp[row + i];
+        m = qm[row + i];
         dc[i] = d;
-        qc[i] = qm[row + i] / d;
+        qc[i] = qr[row + i];
         dp0[row + i] = d;
     }
     __syncthreads();
-    const double dx = kA * coslat[j] * dlam;
     if (i < nlon) {
         // face i + 1/2
         const int ip = i + 1 == nlon ? 0 : i + 1;
         const int im = i == 0 ? nlon - 1 : i - 1;
         const int ip2 = ip + 1 == nlon ? 0 : ip + 1;
         const double uf = 0.5 * (u[row + i] + u[row + ip]);
-        const double cour = fabs(uf) * dt / dx;
+        const double cour = fabs(uf) * cx;
         double qf, f;
         if (uf >= 0.0) {
             qf = qc[i] + 0.5 * (1.0 - cour) * vanleer(qc[i] - qc[im], qc[ip] - qc[i]);
@@ -126,18 +141,21 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
     __syncthreads();
     if (i < nlon) {
         const int im = i == 0 ? nlon - 1 : i - 1;
-        dp[row + i] = dc[i] - dt * (fa[i] - fa[im]) / dx;
-        qm[row + i] = qm[row + i] - dt * (fq[i] - fq[im]) / dx;
+        const double dn = dc[i] - cx * (fa[i] - fa[im]);
+        const double mn = m - cx * (fq[i] - fq[im]);
+        dp[row + i] = dn;
+        qm[row + i] = mn;
+        qz[row + i] = mn / dn;
     }
 }
 
-// Meridional sweep (sweep_merid, :342-386) with the bounded van Leer face
-// value (vl_face_bounded, :413-440), as two fully parallel passes over the
-// start-of-sweep state: face fluxes (face f between rows f and f + 1, stored at
-// [k][f][i]; the pole faces 0 and nlat stay zero), then the row updates.
+// Meridional face fluxes (sweep_merid, :439-503) with the bounded van Leer face
+// value (vl_face_bounded, :542-573), fully parallel over the start-of-sweep
+// state: face f between rows f and f + 1, stored at [k][f][i]; the pole faces 0
+// and nlat stay zero.  The row updates from these faces run in k_tr_vert.
 __global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restrict__ dp,
-                            const double *__restrict__ qm, const double *__restrict__ cosface,
-                            const double *__restrict__ dmu, int nlon, int nlat, int nlev, long ng, double dt,
+                            const double *__restrict__ qz, const double *__restrict__ cosface,
+                            const double *__restrict__ rdyf, int nlon, int nlat, int nlev, long ng, double dt,
                             double *__restrict__ fa, double *__restrict__ fq) {
     const long nf = (long)(nlat - 1) * nlon;
     const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -147,18 +165,17 @@ __global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restri
     const int f = 1 + (int)(rem / nlon), i = (int)(rem - (long)(f - 1) * nlon);
     const long base = k * ng + i;
     auto at = [&](int r) { return base + (long)(r - 1) * nlon; };   // Fortran row r = 1..nlat
-    auto qa = [&](int r) { return qm[at(r)] / dp[at(r)]; };
     const double vf = 0.5 * (v[at(f)] + v[at(f + 1)]);
-    const double dy = kA * dmu[f - 1] / fmax(cosface[f], 1.0e-6);
-    const double cour = fabs(vf) * dt / dy;
+    const double cour = fabs(vf) * dt * rdyf[f];
     double qf, a;
     if (vf >= 0.0) {
-        const double q0 = qa(f);
-        qf = (f <= 1 || f >= nlat) ? q0 : q0 + 0.5 * (1.0 - cour) * vanleer(q0 - qa(f - 1), qa(f + 1) - q0);
+        const double q0 = qz[at(f)];
+        qf = (f <= 1 || f >= nlat) ? q0 : q0 + 0.5 * (1.0 - cour) * vanleer(q0 - qz[at(f - 1)], qz[at(f + 1)] - q0);
         a = dp[at(f)] * vf * cosface[f];
     } else {
-        const double q1 = qa(f + 1);
-        qf = (f + 1 <= 1 || f + 1 >= nlat) ? q1 : q1 + 0.5 * (1.0 - cour) * vanleer(q1 - qa(f + 2), qa(f) - q1);
+        const double q1 = qz[at(f + 1)];
+        qf = (f + 1 <= 1 || f + 1 >= nlat) ? q1
+                                            : q1 + 0.5 * (1.0 - cour) * vanleer(q1 - qz[at(f + 2)], qz[at(f)] - q1);
         a = dp[at(f + 1)] * vf * cosface[f];
     }
     const long o = (long)k * (nlat + 1) * nlon + (long)f * nlon + i;
@@ -166,32 +183,75 @@ __global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restri
     fq[o] = qf * a;
 }
 
-__global__ void k_tr_mupdate(double *__restrict__ dp, double *__restrict__ qm, const double *__restrict__ fa,
-                             const double *__restrict__ fq, const double *__restrict__ dmu, int nlon, int nlat,
-                             int nlev, long ng, double dt) {
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)nlev * ng) return;
-    const int k = (int)(t / ng);
-    const long c = t - (long)k * ng;
-    const int j = (int)(c / nlon), i = (int)(c - (long)j * nlon);   // Fortran row j + 1: faces j + 1 and j
-    const long fo = (long)k * (nlat + 1) * nlon + (long)j * nlon + i;
-    const double den = kA * dmu[j];
-    dp[t] = dp[t] - dt * (fa[fo + nlon] - fa[fo]) / den;
-    qm[t] = qm[t] - dt * (fq[fo + nlon] - fq[fo]) / den;
-}
+constexpr int kVertCols = 16;   // grid columns per k_tr_vert block
+constexpr int kVertLanes = 8;   // threads per column in its level-parallel phases
 
-// Vertical mass flux and the top-down update (transport_substep, :238-297;
-// vflux_q :491-513, vflux_q_vl :515-553), streamed over the column: a first
-// pass forms the column sum of the layer-mass change, a second recomputes the
-// running sums in the same order while it walks down, holding only the levels
-// around the one being updated (two above, updated; two below, not yet).
-__global__ void k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
-                          const double *__restrict__ B, int nlev, long ng, double dt, int vl) {
-    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (c >= ng) return;
-    auto at = [&](int kk) { return (long)(kk - 1) * ng + c; };   // Fortran level kk
-    double SN = 0.0;                                             // scum(nlev)
-    for (int kk = 1; kk <= nlev; ++kk) SN = SN + (dp0[at(kk)] - dp[at(kk)]) / dt;
+// Shared memory of one k_tr_vert block: four [nlev][kVertCols] arrays and the
+// [nlev + 1][kVertCols] mass fluxes.
+inline size_t tr_vert_smem(int nlev) { return ((size_t)5 * nlev + 1) * kVertCols * sizeof(double); }
+
+// The meridional row update, the vertical mass flux and the top-down vertical
+// update of a grid column (transport_substep, :289-372; sweep_merid's update,
+// :491-496; vflux_q :596-630, vflux_q_vl :632-688), in four phases over a block of
+// kVertCols columns x kVertLanes threads, the column staged in shared memory:
+//   1. all threads, levels strided: the meridional update of dp and qm from the
+//      column's two faces, the layer-mass change over dt and the ratio qm / dp;
+//   2. one thread per column: the column sum of the mass change and the running
+//      sums in level order, giving the vertical mass flux at every face;
+//   3. all threads: the new layer thicknesses (they depend on the fluxes only);
+//   4. one thread per column, top down: the tracer update, whose upper-face flux
+//      sees the level above already updated (the only serial dependence).
+// The updated ratios go to qr for the next sub-step's zonal sweep.
+__global__ void __launch_bounds__(kVertCols *kVertLanes)
+    k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
+              double *__restrict__ qr, const double *__restrict__ fa, const double *__restrict__ fq,
+              const double *__restrict__ rden, const double *__restrict__ B, int nlon, int nlat, int nlev, long ng,
+              double dt, double rdt, int vl) {
+    extern __shared__ double vs[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long c = blockIdx.x * (long)kVertCols + tx;
+    const bool live = c < ng;
+    const long lv = (long)nlev * kVertCols;
+    // not yet updated dp, qm and ratio; mass change over dt, then the new dp; mass flux at faces 0..nlev
+    double *sd = vs, *sm = vs + lv, *sq = vs + 2 * lv, *sx = vs + 3 * lv, *sf = vs + 4 * lv;
+    auto sl = [&](int kk) { return (kk - 1) * kVertCols + tx; };   // Fortran level kk
+    auto sfl = [&](int kf) { return kf * kVertCols + tx; };        // face kf below level kf
+    const int j = live ? (int)(c / nlon) : 0, i = live ? (int)(c - (long)j * nlon) : 0;
+    const long fstride = (long)(nlat + 1) * nlon;
+    if (live) {
+        const double cm = dt * rden[j];
+        for (int kk = 1 + ty; kk <= nlev; kk += kVertLanes) {
+            const long t = (long)(kk - 1) * ng + c;
+            const long fo = (long)(kk - 1) * fstride + (long)j * nlon + i;
+            const double d = dp[t] - cm * (fa[fo + nlon] - fa[fo]);
+            const double m = qm[t] - cm * (fq[fo + nlon] - fq[fo]);
+            sd[sl(kk)] = d;
+            sm[sl(kk)] = m;
+            sq[sl(kk)] = m / d;
+            sx[sl(kk)] = (dp0[t] - d) * rdt;
+        }
+    }
+    __syncthreads();
+    if (live && ty == 0) {
+        double SN = 0.0;   // scum(nlev)
+        for (int kk = 1; kk <= nlev; ++kk) SN = SN + sx[sl(kk)];
+        double scum = 0.0;
+        sf[sfl(0)] = B[0] * SN;
+        for (int kk = 1; kk <= nlev; ++kk) {
+            scum = scum + sx[sl(kk)];
+            sf[sfl(kk)] = B[kk] * SN - scum;
+        }
+    }
+    __syncthreads();
+    if (live) {
+        for (int kk = 1 + ty; kk <= nlev; kk += kVertLanes) {
+            const double dn = sd[sl(kk)] - dt * (sf[sfl(kk)] - sf[sfl(kk - 1)]);
+            dp[(long)(kk - 1) * ng + c] = dn;
+            sx[sl(kk)] = dn;
+        }
+    }
+    __syncthreads();
+    if (!live || ty != 0) return;
     // flux through face kf (between levels kf and kf + 1) with mass flux mm, from the ratios of
     // levels kf - 1 .. kf + 2 and the thicknesses of levels kf, kf + 1 as the loop sees them
     auto flux = [&](int kf, double mm, double qa_m1, double qa_0, double qa_p1, double qa_p2, double d0,
@@ -203,44 +263,27 @@ __global__ void k_tr_vert(const double *__restrict__ dp0, double *__restrict__ d
         const double qd = down ? qa_0 : qa_p1;
         const double cour = fabs(mm) * dt / (down ? d0 : d1);
         if (kd - 1 < 1 || kd + 1 > nlev) return qd * mm;
-        const double sm = down ? qd - qa_m1 : qd - qa_p2;
-        const double sp = down ? qa_p1 - qd : qa_0 - qd;
-        return (qd + 0.5 * (1.0 - cour) * vanleer(sm, sp)) * mm;
+        const double sm_ = down ? qd - qa_m1 : qd - qa_p2;
+        const double sp_ = down ? qa_p1 - qd : qa_0 - qd;
+        return (qd + 0.5 * (1.0 - cour) * vanleer(sm_, sp_)) * mm;
     };
-    double m0 = qm[at(1)], d0 = dp[at(1)];                                      // level k, not yet updated
-    double m1 = nlev > 1 ? qm[at(2)] : 0.0, d1 = nlev > 1 ? dp[at(2)] : 1.0;    // level k + 1
-    double q2 = nlev > 2 ? qm[at(3)] / dp[at(3)] : 0.0;                         // ratio of level k + 2
     double qu1 = 0.0, qu2 = 0.0, du1 = 1.0;   // updated ratios of levels k - 1, k - 2; thickness of k - 1
-    double scum_prev = 0.0, mfl_prev = B[0] * SN;   // scum(0) = 0, mfl(0)
     for (int k = 1; k <= nlev; ++k) {
-        const double scum = scum_prev + (dp0[at(k)] - d0) / dt;
-        const double mfl = B[k] * SN - scum;
-        const double q0 = m0 / d0, q1 = m1 / d1;
-        const double da = mfl - mfl_prev;
+        // level k and the two below it, not yet updated (past the bottom: unused fillers)
+        const double d0 = sd[sl(k)], m0 = sm[sl(k)], q0 = sq[sl(k)], dn = sx[sl(k)];
+        const double d1 = k + 1 <= nlev ? sd[sl(k + 1)] : 1.0;
+        const double q1 = k + 1 <= nlev ? sq[sl(k + 1)] : 0.0;
+        const double q2 = k + 2 <= nlev ? sq[sl(k + 2)] : 0.0;
+        const double mfl = sf[sfl(k)], mfl_prev = sf[sfl(k - 1)];
         const double dq = flux(k, mfl, qu1, q0, q1, q2, d0, d1) - flux(k - 1, mfl_prev, qu2, qu1, q0, q1, du1, d0);
-        const double dn = d0 - dt * da, mn = m0 - dt * dq;
-        dp[at(k)] = dn;
-        qm[at(k)] = mn;
-        // slide one level down
+        const double mn = m0 - dt * dq;
+        const long t = (long)(k - 1) * ng + c;
+        qm[t] = mn;
         qu2 = qu1;
         qu1 = mn / dn;
+        qr[t] = qu1;
         du1 = dn;
-        m0 = m1;
-        d0 = d1;
-        if (k + 2 <= nlev) {
-            m1 = qm[at(k + 2)];
-            d1 = dp[at(k + 2)];
-        }
-        q2 = k + 3 <= nlev ? qm[at(k + 3)] / dp[at(k + 3)] : 0.0;
-        scum_prev = scum;
-        mfl_prev = mfl;
     }
-}
-
-__global__ void k_tr_end(const double *__restrict__ qm, const double *__restrict__ dp, double *__restrict__ q,
-                         long n) {
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
-        q[t] = qm[t] / dp[t];
 }
 
 // Column water sums of one latitude row, summed over longitude in a fixed tree.
@@ -287,8 +330,11 @@ struct aeros_transport_s {
     long ng = 0;
     double dlam = 0.0;
     std::vector<double> w;                                       // Gauss weights (host)
-    double *A = nullptr, *B = nullptr, *dmu = nullptr, *coslat = nullptr, *cosface = nullptr;
+    double *A = nullptr, *B = nullptr, *cosface = nullptr;
+    // per-row reciprocals: 1/dx of a row, 1/dy of a row (Courant number) and of a face, 1/(a dmu) of a row
+    double *rdx = nullptr, *rdyc = nullptr, *rdyf = nullptr, *rden = nullptr;
     double *dp = nullptr, *qm = nullptr, *dp0 = nullptr;         // (nlev, nlat, nlon)
+    double *qr = nullptr, *qz = nullptr;                         // qm / dp after the vertical / zonal update
     double *mfa = nullptr, *mfq = nullptr;                       // meridional face fluxes (nlev, nlat + 1, nlon)
     double *su = nullptr, *sv = nullptr, *sq = nullptr, *sl = nullptr, *rows = nullptr;   // staging
     unsigned long long *cmax = nullptr;
@@ -302,8 +348,8 @@ struct aeros_transport_s {
 namespace {
 
 void tr_free(aeros_transport_s *h) {
-    double *ps[] = {h->A, h->B, h->dmu, h->coslat, h->cosface, h->dp, h->qm, h->dp0, h->su, h->sv, h->sq, h->sl,
-                    h->rows, h->mfa, h->mfq};
+    double *ps[] = {h->A,  h->B,  h->cosface, h->rdx, h->rdyc, h->rdyf, h->rden, h->dp, h->qm, h->dp0,
+                    h->qr, h->qz, h->su,      h->sv,  h->sq,   h->sl,   h->rows, h->mfa, h->mfq};
     for (double *p : ps)
         if (p) cudaFree(p);
     if (h->cmax) cudaFree(h->cmax);
@@ -348,7 +394,7 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
     h->ng = (long)g.nlon * g.nlat;
     h->dlam = 2.0 * kPi / g.nlon;
     h->w = g.w;
-    // transport geometry (aeros_transport_init, src/dynamics/aeros_transport.f90:153-186):
+    // transport geometry (aeros_transport_init, src/dynamics/aeros_transport.f90:155-203):
     // cells tile mu = sin(lat) in [-1, 1] with widths equal to the Gauss weights
     std::vector<double> cl(g.nlat), cf(g.nlat + 1, 0.0);
     double muh = 1.0;
@@ -359,10 +405,20 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
     }
     cf[0] = 0.0;
     cf[g.nlat] = 0.0;
+    // the spacings of sweep_zonal (:374-437), sweep_merid (:439-503) and max_courant (:690-741), inverted once
+    std::vector<double> rdx(g.nlat), rdyc(g.nlat), rdyf(g.nlat + 1, 0.0), rden(g.nlat);
+    for (int j = 0; j < g.nlat; ++j) {
+        rdx[j] = 1.0 / (kA * cl[j] * h->dlam);
+        rdyc[j] = 1.0 / (kA * g.w[j] / std::max(cl[j], 1.0e-6));
+        rden[j] = 1.0 / (kA * g.w[j]);
+    }
+    for (int f = 1; f < g.nlat; ++f) rdyf[f] = 1.0 / (kA * g.w[f - 1] / std::max(cf[f], 1.0e-6));
     const size_t n3 = (size_t)nlev * h->ng;
-    if ((rc = tr_alloc(h->A, nlev + 1)) || (rc = tr_alloc(h->B, nlev + 1)) || (rc = tr_alloc(h->dmu, g.nlat)) ||
-        (rc = tr_alloc(h->coslat, g.nlat)) || (rc = tr_alloc(h->cosface, g.nlat + 1)) || (rc = tr_alloc(h->dp, n3)) ||
-        (rc = tr_alloc(h->qm, n3)) || (rc = tr_alloc(h->dp0, n3)) || (rc = tr_alloc(h->su, n3)) ||
+    if ((rc = tr_alloc(h->A, nlev + 1)) || (rc = tr_alloc(h->B, nlev + 1)) || (rc = tr_alloc(h->rdx, g.nlat)) ||
+        (rc = tr_alloc(h->rdyc, g.nlat)) || (rc = tr_alloc(h->rdyf, g.nlat + 1)) || (rc = tr_alloc(h->rden, g.nlat)) ||
+        (rc = tr_alloc(h->cosface, g.nlat + 1)) || (rc = tr_alloc(h->dp, n3)) || (rc = tr_alloc(h->qr, n3)) ||
+        (rc = tr_alloc(h->qz, n3)) || (rc = tr_alloc(h->qm, n3)) || (rc = tr_alloc(h->dp0, n3)) ||
+        (rc = tr_alloc(h->su, n3)) ||
         (rc = tr_alloc(h->sv, n3)) || (rc = tr_alloc(h->sq, n3)) || (rc = tr_alloc(h->sl, (size_t)h->ng)) ||
         (rc = tr_alloc(h->rows, g.nlat)) || (rc = tr_alloc(h->cmax, 1)) ||
         (rc = tr_alloc(h->mfa, (size_t)nlev * (g.nlat + 1) * g.nlon)) ||
@@ -372,11 +428,15 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
     }
     bool ok = cudaMemcpy(h->A, a_half, 8 * (nlev + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemcpy(h->B, b_half, 8 * (nlev + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMemcpy(h->dmu, g.w.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
-              cudaMemcpy(h->coslat, cl.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(h->rdx, rdx.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(h->rdyc, rdyc.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(h->rdyf, rdyf.data(), 8 * (g.nlat + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(h->rden, rden.data(), 8 * g.nlat, cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemcpy(h->cosface, cf.data(), 8 * (g.nlat + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
               cudaMemset(h->mfa, 0, 8 * (size_t)nlev * (g.nlat + 1) * g.nlon) == cudaSuccess &&   // pole faces stay 0
               cudaMemset(h->mfq, 0, 8 * (size_t)nlev * (g.nlat + 1) * g.nlon) == cudaSuccess &&
+              cudaFuncSetAttribute(k_tr_vert, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tr_vert_smem(kTrMaxLev)) == cudaSuccess &&
               cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -432,9 +492,9 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
         return rc;
     const unsigned nbc = (unsigned)((ng + 127) / 128);
     AEROS_CUDA(cudaMemsetAsync(h->cmax, 0, sizeof(unsigned long long), h->stream));
-    k_tr_begin<<<nbc, 128, 0, h->stream>>>(ld, qd, h->A, h->B, h->nlev, ng, h->dp, h->qm);
-    k_tr_courant<<<nbc, 128, 0, h->stream>>>(ud, vd, ld, h->A, h->B, h->coslat, h->dmu, h->nlev, h->nlon, ng, h->dlam,
-                                             dt, h->cmax);
+    k_tr_begin<<<nbc, 128, 0, h->stream>>>(ld, qd, h->A, h->B, h->nlev, ng, h->dp, h->qm, h->qr);
+    k_tr_courant<<<nbc, 128, 0, h->stream>>>(ud, vd, ld, h->A, h->B, h->rdx, h->rdyc, h->nlev, h->nlon, ng, dt,
+                                             h->cmax);
     AEROS_CUDA(cudaGetLastError());
     unsigned long long bits = 0;
     AEROS_CUDA(cudaMemcpyAsync(&bits, h->cmax, 8, cudaMemcpyDeviceToHost, h->stream));
@@ -453,28 +513,22 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
     if (zthr > 1024) { set_error("transport: nlon above 1024"); return AEROS_ERR_UNSUPPORTED; }
     const size_t zsm = (size_t)4 * h->nlon * sizeof(double);
     const unsigned nbf = (unsigned)(((long)h->nlev * (h->nlat - 1) * h->nlon + 255) / 256);
-    const unsigned nbu = (unsigned)(((long)h->nlev * ng + 255) / 256);
+    const unsigned nbv = (unsigned)((ng + kVertCols - 1) / kVertCols);
+    const size_t vsm = tr_vert_smem(h->nlev);
     for (int s = 0; s < nsub; ++s) {
-        k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(ud, h->dp, h->qm, h->dp0, h->coslat, h->nlon,
-                                                                     h->nlat, ng, h->dlam, dts);
+        k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(ud, h->dp, h->qm, h->qr, h->qz, h->dp0, h->rdx,
+                                                                     h->nlon, ng, dts);
         if (h->nlat > 1)
-            k_tr_mfaces<<<nbf, 256, 0, h->stream>>>(vd, h->dp, h->qm, h->cosface, h->dmu, h->nlon, h->nlat, h->nlev,
+            k_tr_mfaces<<<nbf, 256, 0, h->stream>>>(vd, h->dp, h->qz, h->cosface, h->rdyf, h->nlon, h->nlat, h->nlev,
                                                     ng, dts, h->mfa, h->mfq);
-        k_tr_mupdate<<<nbu, 256, 0, h->stream>>>(h->dp, h->qm, h->mfa, h->mfq, h->dmu, h->nlon, h->nlat, h->nlev,
-                                                 ng, dts);
-        k_tr_vert<<<nbc, 128, 0, h->stream>>>(h->dp0, h->dp, h->qm, h->B, h->nlev, ng, dts, h->vert_vanleer);
+        k_tr_vert<<<nbv, dim3(kVertCols, kVertLanes), vsm, h->stream>>>(h->dp0, h->dp, h->qm, h->qr, h->mfa, h->mfq, h->rden, h->B,
+                                                      h->nlon, h->nlat, h->nlev, ng, dts, 1.0 / dts, h->vert_vanleer);
     }
     AEROS_CUDA(cudaGetLastError());
-    if (tr_is_device(q)) {
-        k_tr_end<<<(unsigned)std::min<size_t>((n3 + 255) / 256, 4096), 256, 0, h->stream>>>(h->qm, h->dp, q, (long)n3);
-        AEROS_CUDA(cudaGetLastError());
-    } else {
-        k_tr_end<<<(unsigned)std::min<size_t>((n3 + 255) / 256, 4096), 256, 0, h->stream>>>(h->qm, h->dp, h->sq,
-                                                                                            (long)n3);
-        AEROS_CUDA(cudaGetLastError());
-        AEROS_CUDA(cudaMemcpyAsync(q, h->sq, n3 * 8, cudaMemcpyDeviceToHost, h->stream));
-        AEROS_CUDA(cudaStreamSynchronize(h->stream));
-    }
+    // the last vertical update left q = qm / dp in qr
+    AEROS_CUDA(cudaMemcpyAsync(q, h->qr, n3 * 8, tr_is_device(q) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               h->stream));
+    if (!tr_is_device(q)) AEROS_CUDA(cudaStreamSynchronize(h->stream));
     return AEROS_OK;
 }
 
@@ -497,7 +551,7 @@ int aeros_transport_water(aeros_transport_t h, const double *ps, const double *q
     std::vector<double> rows(h->nlat);
     AEROS_CUDA(cudaMemcpyAsync(rows.data(), h->rows, 8 * h->nlat, cudaMemcpyDeviceToHost, h->stream));
     AEROS_CUDA(cudaStreamSynchronize(h->stream));
-    // aeros_transport_water (:588-612): sum col * area / g, area = w_j dlambda a^2 (src/aeros_grid.f90:71-77)
+    // aeros_transport_water (:743-779): sum col * area / g, area = w_j dlambda a^2 (src/aeros_grid.f90:71-77)
     double tot = 0.0;
     for (int j = 0; j < h->nlat; ++j) tot += rows[j] * (h->w[j] * h->dlam * kA * kA) / kGrav;
     *water = tot;

@@ -304,7 +304,7 @@ int aeros_dyn_tendency_forced(aeros_dyn_t h, double *dvor, double *ddiv, double 
  * south; pointers host or device. */
 typedef struct aeros_transport_s *aeros_transport_t;
 
-/* aeros_transport_init (:153-186): Gaussian grid of truncation trunc, nlev
+/* aeros_transport_init (:155-203): Gaussian grid of truncation trunc, nlev
  * layers with half-level coefficients p_half = a_half + b_half ps (nlev + 1,
  * top to bottom, host memory; nlev <= 64). */
 int aeros_transport_create(aeros_transport_t *h, int trunc, int nlev, const double *a_half,
@@ -314,13 +314,13 @@ int aeros_transport_set_stream(aeros_transport_t h, void *stream);   /* NULL: th
 int aeros_transport_grid(aeros_transport_t h, int *nlon, int *nlat, int *nlev);
 /* The vert_vanleer switch of aeros_transport_class (default off: donor cell). */
 int aeros_transport_set_vert_vanleer(aeros_transport_t h, int on);
-/* aeros_transport_transport (:188-236): advance q in place over dt [s] with the
+/* aeros_transport_transport (:225-287): advance q in place over dt [s] with the
  * winds u, v [m/s] and ln ps [ln Pa] (nlon, nlat). */
 int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, const double *lnps,
                          double *q, double dt);
 /* last_cfl and last_nsub of the previous call. */
 int aeros_transport_last(aeros_transport_t h, double *cfl, int *nsub);
-/* aeros_transport_water (:588-612): total tracer mass [kg] of q with surface
+/* aeros_transport_water (:743-779): total tracer mass [kg] of q with surface
  * pressure ps [Pa] (nlon, nlat). */
 int aeros_transport_water(aeros_transport_t h, const double *ps, const double *q, double *water);
 

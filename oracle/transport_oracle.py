@@ -19,11 +19,11 @@ import numpy as np
 
 R_EARTH = 6.371e6   # src/aeros_defs.f90:84
 GRAV = 9.80665      # src/aeros_defs.f90:85
-CFL_MAX = 0.9       # src/dynamics/aeros_transport.f90 (module parameter)
+CFL_MAX = 0.9       # src/dynamics/aeros_transport.f90:144
 
 
 class OracleTransport:
-    """aeros_transport_class with its init (src/dynamics/aeros_transport.f90:153-186)."""
+    """aeros_transport_class with its init (src/dynamics/aeros_transport.f90:155-203)."""
 
     def __init__(self, sinlat, gauss_w, nlon, a_half, b_half, vert_vanleer=False):
         self.nlat = len(sinlat)
@@ -52,7 +52,7 @@ class OracleTransport:
         return ph[1:] - ph[:-1]
 
     def transport(self, u, v, lnps, q, dt):
-        """aeros_transport_transport (:188-236); returns the new q."""
+        """aeros_transport_transport (:225-287); returns the new q."""
         ps = np.exp(lnps)
         self.dp_lev = self._dp(ps)
         self.qm = q * self.dp_lev
@@ -65,7 +65,7 @@ class OracleTransport:
         return self.qm / self.dp_lev
 
     def _substep(self, u, v, dt):
-        """transport_substep (:238-297): zonal and meridional sweeps, then the
+        """transport_substep (:289-372): zonal and meridional sweeps, then the
         vertical mass flux from the layer-mass change, updated top down in place."""
         dp0 = self.dp_lev.copy()
         self._sweep_zonal(u, dt)
@@ -83,7 +83,7 @@ class OracleTransport:
             dpl[k - 1] = dpl[k - 1] - dt * da
             qm[k - 1] = qm[k - 1] - dt * dq
 
-    # vflux_q (:491-513): donor cell through face k (between levels k and k + 1)
+    # vflux_q (:596-630): donor cell through face k (between levels k and k + 1)
     def _vflux(self, k, mfl, dt):
         nlev = self.nlev
         if k <= 0 or k >= nlev:
@@ -92,7 +92,7 @@ class OracleTransport:
         q_up = np.where(mfl >= 0.0, qm[k - 1] / dpl[k - 1], qm[k] / dpl[k])
         return q_up * mfl
 
-    # vflux_q_vl (:515-553): van Leer through face k
+    # vflux_q_vl (:632-688): van Leer through face k
     def _vflux_vl(self, k, mfl, dt):
         nlev = self.nlev
         if k <= 0 or k >= nlev:
@@ -122,7 +122,7 @@ class OracleTransport:
         return res
 
     def _sweep_zonal(self, u, dt):
-        """sweep_zonal (:299-340): periodic van Leer fluxes at faces i + 1/2."""
+        """sweep_zonal (:374-437): periodic van Leer fluxes at faces i + 1/2."""
         dc = self.dp_lev
         qc = self.qm / dc
         dx = (R_EARTH * self.coslat * self.dlam)[None, :, None]
@@ -142,7 +142,7 @@ class OracleTransport:
         self.qm = self.qm - dt * (fq - fq_m) / dx
 
     def _sweep_merid(self, v, dt):
-        """sweep_merid (:342-386): van Leer fluxes at faces j + 1/2, zero at the poles."""
+        """sweep_merid (:439-503): van Leer fluxes at faces j + 1/2, zero at the poles."""
         nlat = self.nlat
         dc = self.dp_lev
         qc = self.qm / dc
@@ -164,7 +164,7 @@ class OracleTransport:
         self.qm = self.qm - dt * (fq[:, 1:] - fq[:, :-1]) / den
 
     def _vl_bounded(self, qc, jup, d, cour):
-        """vl_face_bounded (:413-440), Fortran row jup."""
+        """vl_face_bounded (:542-573), Fortran row jup."""
         n = self.nlat
         q = lambda jf: qc[:, jf - 1]
         if jup <= 1 or jup >= n:
@@ -176,7 +176,7 @@ class OracleTransport:
         return q(jup) + 0.5 * (1.0 - cour) * _vanleer(sm, sp)
 
     def max_courant(self, u, v, lnps, dt):
-        """max_courant (:555-586)."""
+        """max_courant (:690-741)."""
         dpc = self._dp(np.exp(lnps))
         dxc = (R_EARTH * self.coslat * self.dlam)[None, :, None]
         cmass = dpc * np.abs(u) / dxc
@@ -191,7 +191,7 @@ class OracleTransport:
         return float(np.max(cx + cy + cz))
 
     def water(self, ps, q):
-        """aeros_transport_water (:588-612): total tracer mass [kg]."""
+        """aeros_transport_water (:743-779): total tracer mass [kg]."""
         dpc = self._dp(ps)
         col = np.zeros(ps.shape)
         for k in range(self.nlev):
@@ -205,7 +205,7 @@ class OracleTransport:
 
 
 def _vanleer(a, b):
-    """vanleer (:442-452): harmonic-mean slope, 0 at an extremum."""
+    """vanleer (:575-594): harmonic-mean slope, 0 at an extremum."""
     ab = a * b
     with np.errstate(divide="ignore", invalid="ignore"):
         s = 2.0 * a * b / (a + b)
