@@ -32,71 +32,117 @@ namespace {
 constexpr double kCflMax = 0.9;      // CFL_MAX, src/dynamics/aeros_transport.f90:144
 constexpr int kTrMaxLev = 64;
 
-__device__ __forceinline__ double vanleer(double a, double b) {
-    // harmonic-mean slope, zero at an extremum (vanleer, :575-594)
-    return a * b > 0.0 ? 2.0 * a * b / (a + b) : 0.0;
+// Reciprocal of y by Newton-Raphson on f(r) = 1/r - y: from the approximate
+// reciprocal of rcp.approx.ftz.f64 (relative error near 2^-23), each step
+// e = 1 - y r, r <- r + r e squares the relative error, so two steps leave only
+// the rounding of the last fused multiply-add (within an ulp of 1/y).  For y
+// whose magnitude and reciprocal are both normal doubles; the ratios qm / dp
+// and the van Leer slope sums are (a sum a + b with a b > 0 is at least the
+// larger of |a|, |b|, and a b > 0 rules out two subnormal terms).  Four FP64
+// fused multiply-adds against about twice that for an IEEE division, on a GPU
+// whose FP64 pipe bounds these kernels.
+__device__ __forceinline__ double recip_nr(double y) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(y));
+    double e = fma(-y, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-y, r, 1.0);
+    return fma(r, e, r);
 }
+
+// Half the van Leer slope (vanleer, :575-594): the harmonic mean a b / (a + b)
+// of two one-sided slopes, zero at an extremum.  The face value
+// q + 0.5 (1 - cour) vanleer(a, b) is q + (1 - cour) vl_half(a, b).
+__device__ __forceinline__ double vl_half(double a, double b) {
+    const double p = a * b;
+    return p > 0.0 ? p * recip_nr(a + b) : 0.0;
+}
+
+constexpr int kVertCols = 16;   // grid columns per block of the column kernels
+constexpr int kVertLanes = 8;   // threads per column in their level-parallel phases
 
 // Layer air mass from the surface pressure (aeros_vgrid_pressure,
 // src/dynamics/aeros_vertical.f90:344-380), qm = q dp and the ratio qm / dp that
-// the first zonal sweep starts from.
-__global__ void k_tr_begin(const double *__restrict__ lnps, const double *__restrict__ q,
-                           const double *__restrict__ A, const double *__restrict__ B, int nlev, long ng,
-                           double *__restrict__ dp, double *__restrict__ qm, double *__restrict__ qr) {
-    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+// the first zonal sweep starts from; a block of kVertCols columns x kVertLanes
+// threads, levels strided over the lanes.
+__global__ void __launch_bounds__(kVertCols *kVertLanes)
+    k_tr_begin(const double *__restrict__ lnps, const double *__restrict__ q, const double *__restrict__ A,
+               const double *__restrict__ B, int nlev, long ng, double *__restrict__ dp, double *__restrict__ qm,
+               double *__restrict__ qr) {
+    __shared__ double sps[kVertCols];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long c = blockIdx.x * (long)kVertCols + tx;
+    if (c < ng && ty == 0) sps[tx] = exp(lnps[c]);
+    __syncthreads();
     if (c >= ng) return;
-    const double ps = exp(lnps[c]);
-    double ph0 = A[0] + B[0] * ps;
-    for (int k = 0; k < nlev; ++k) {
-        const double ph1 = A[k + 1] + B[k + 1] * ps;
+    const double ps = sps[tx];
+    for (int k = ty; k < nlev; k += kVertLanes) {
+        const double ph0 = A[k] + B[k] * ps, ph1 = A[k + 1] + B[k + 1] * ps;
         const double d = ph1 - ph0;
         const double m = q[k * ng + c] * d;
         dp[k * ng + c] = d;
         qm[k * ng + c] = m;
         qr[k * ng + c] = m / d;
-        ph0 = ph1;
     }
 }
 
+// Shared memory of one k_tr_courant block: the column mass-flux terms
+// [nlev][kVertCols], their running sums [nlev + 1][kVertCols] and the surface
+// pressure.
+inline size_t tr_courant_smem(int nlev) { return ((size_t)2 * nlev + 2) * kVertCols * sizeof(double); }
+
 // Largest total Courant number (max_courant, :690-741); non-negative doubles
-// order like their bit patterns, so the maximum is an integer atomicMax.  The
-// column sum of the zonal mass flux is formed first, then the running sum is
-// rebuilt from the same terms in the same order, so it ends on the same value.
-__global__ void k_tr_courant(const double *__restrict__ u, const double *__restrict__ v,
-                             const double *__restrict__ lnps, const double *__restrict__ A,
-                             const double *__restrict__ B, const double *__restrict__ rdx,
-                             const double *__restrict__ rdyc, int nlev, int nlon, long ng, double dt,
-                             unsigned long long *__restrict__ cmax) {
-    const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    double best = 0.0;
-    if (c < ng) {
-        const int j = (int)(c / nlon);
-        const double ps = exp(lnps[c]);
-        const double rx = rdx[j], ry = rdyc[j];
-        double SN = 0.0, ph0 = A[0] + B[0] * ps;
-#pragma unroll 4
-        for (int k = 0; k < nlev; ++k) {
-            const double ph1 = A[k + 1] + B[k + 1] * ps;
-            SN = SN + (ph1 - ph0) * fabs(u[k * ng + c]) * rx;
-            ph0 = ph1;
+// order like their bit patterns, so the maximum is an integer atomicMax.  Per
+// block of kVertCols columns: the zonal mass-flux terms of every level (lanes
+// over levels), their column sum and running sums in level order (one thread
+// per column), then every level's Courant number (lanes over levels).
+__global__ void __launch_bounds__(kVertCols *kVertLanes)
+    k_tr_courant(const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ lnps,
+                 const double *__restrict__ A, const double *__restrict__ B, const double *__restrict__ rdx,
+                 const double *__restrict__ rdyc, int nlev, int nlon, long ng, double dt,
+                 unsigned long long *__restrict__ cmax) {
+    extern __shared__ double cs[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const long c = blockIdx.x * (long)kVertCols + tx;
+    const bool live = c < ng;
+    double *sc = cs, *su = cs + (long)nlev * kVertCols, *sps = su + (long)(nlev + 1) * kVertCols;
+    if (live && ty == 0) sps[tx] = exp(lnps[c]);
+    __syncthreads();
+    const int j = live ? (int)(c / nlon) : 0;
+    const double rx = live ? rdx[j] : 0.0;
+    if (live) {
+        const double ps = sps[tx];
+        for (int k = ty; k < nlev; k += kVertLanes) {
+            const double d = (A[k + 1] + B[k + 1] * ps) - (A[k] + B[k] * ps);
+            sc[k * kVertCols + tx] = d * fabs(u[k * ng + c]) * rx;
         }
-        double scum0 = 0.0;
-        ph0 = A[0] + B[0] * ps;
-#pragma unroll 4
+    }
+    __syncthreads();
+    if (live && ty == 0) {
+        double scum = 0.0;
+        su[tx] = 0.0;
         for (int k = 0; k < nlev; ++k) {
-            const double ph1 = A[k + 1] + B[k + 1] * ps;
-            const double d = ph1 - ph0, au = fabs(u[k * ng + c]);
-            const double scum1 = scum0 + d * au * rx;
-            const double cx = au * dt * rx;
+            scum = scum + sc[k * kVertCols + tx];
+            su[(k + 1) * kVertCols + tx] = scum;
+        }
+    }
+    __syncthreads();
+    double best = 0.0;
+    if (live) {
+        const double ps = sps[tx], ry = rdyc[j];
+        const double SN = su[nlev * kVertCols + tx];
+        for (int k = ty; k < nlev; k += kVertLanes) {
+            const double d = (A[k + 1] + B[k + 1] * ps) - (A[k] + B[k] * ps);
+            const double cx = fabs(u[k * ng + c]) * dt * rx;
             const double cy = fabs(v[k * ng + c]) * dt * ry;
-            const double cz = (fabs(B[k + 1] * SN - scum1) + fabs(B[k] * SN - scum0)) * dt / d;
+            const double cz =
+                (fabs(B[k + 1] * SN - su[(k + 1) * kVertCols + tx]) + fabs(B[k] * SN - su[k * kVertCols + tx])) * dt /
+                d;
             best = fmax(best, cx + cy + cz);
-            scum0 = scum1;
-            ph0 = ph1;
         }
     }
     for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(cmax, (unsigned long long)__double_as_longlong(best));
+    if (((ty * kVertCols + tx) & 31) == 0) atomicMax(cmax, (unsigned long long)__double_as_longlong(best));
 }
 
 // Zonal sweep (sweep_zonal, :374-437).  Starts from the ratios qr = qm / dp that
@@ -129,10 +175,10 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
         const double cour = fabs(uf) * cx;
         double qf, f;
         if (uf >= 0.0) {
-            qf = qc[i] + 0.5 * (1.0 - cour) * vanleer(qc[i] - qc[im], qc[ip] - qc[i]);
+            qf = qc[i] + (1.0 - cour) * vl_half(qc[i] - qc[im], qc[ip] - qc[i]);
             f = dc[i] * uf;
         } else {
-            qf = qc[ip] + 0.5 * (1.0 - cour) * vanleer(qc[ip] - qc[ip2], qc[i] - qc[ip]);
+            qf = qc[ip] + (1.0 - cour) * vl_half(qc[ip] - qc[ip2], qc[i] - qc[ip]);
             f = dc[ip] * uf;
         }
         fa[i] = f;
@@ -145,7 +191,7 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
         const double mn = m - cx * (fq[i] - fq[im]);
         dp[row + i] = dn;
         qm[row + i] = mn;
-        qz[row + i] = mn / dn;
+        qz[row + i] = mn * recip_nr(dn);
     }
 }
 
@@ -170,12 +216,12 @@ __global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restri
     double qf, a;
     if (vf >= 0.0) {
         const double q0 = qz[at(f)];
-        qf = (f <= 1 || f >= nlat) ? q0 : q0 + 0.5 * (1.0 - cour) * vanleer(q0 - qz[at(f - 1)], qz[at(f + 1)] - q0);
+        qf = (f <= 1 || f >= nlat) ? q0 : q0 + (1.0 - cour) * vl_half(q0 - qz[at(f - 1)], qz[at(f + 1)] - q0);
         a = dp[at(f)] * vf * cosface[f];
     } else {
         const double q1 = qz[at(f + 1)];
         qf = (f + 1 <= 1 || f + 1 >= nlat) ? q1
-                                            : q1 + 0.5 * (1.0 - cour) * vanleer(q1 - qz[at(f + 2)], qz[at(f)] - q1);
+                                            : q1 + (1.0 - cour) * vl_half(q1 - qz[at(f + 2)], qz[at(f)] - q1);
         a = dp[at(f + 1)] * vf * cosface[f];
     }
     const long o = (long)k * (nlat + 1) * nlon + (long)f * nlon + i;
@@ -183,12 +229,9 @@ __global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restri
     fq[o] = qf * a;
 }
 
-constexpr int kVertCols = 16;   // grid columns per k_tr_vert block
-constexpr int kVertLanes = 8;   // threads per column in its level-parallel phases
-
-// Shared memory of one k_tr_vert block: four [nlev][kVertCols] arrays and the
+// Shared memory of one k_tr_vert block: five [nlev][kVertCols] arrays and the
 // [nlev + 1][kVertCols] mass fluxes.
-inline size_t tr_vert_smem(int nlev) { return ((size_t)5 * nlev + 1) * kVertCols * sizeof(double); }
+inline size_t tr_vert_smem(int nlev) { return ((size_t)6 * nlev + 1) * kVertCols * sizeof(double); }
 
 // The meridional row update, the vertical mass flux and the top-down vertical
 // update of a grid column (transport_substep, :289-372; sweep_merid's update,
@@ -198,9 +241,12 @@ inline size_t tr_vert_smem(int nlev) { return ((size_t)5 * nlev + 1) * kVertCols
 //      column's two faces, the layer-mass change over dt and the ratio qm / dp;
 //   2. one thread per column: the column sum of the mass change and the running
 //      sums in level order, giving the vertical mass flux at every face;
-//   3. all threads: the new layer thicknesses (they depend on the fluxes only);
+//   3. all threads: the new layer thicknesses (they depend on the fluxes only)
+//      and their reciprocals;
 //   4. one thread per column, top down: the tracer update, whose upper-face flux
-//      sees the level above already updated (the only serial dependence).
+//      sees the level above already updated (the only serial dependence); the
+//      updated ratio is the new qm times the reciprocal of the new dp, so no
+//      division sits on that chain (within an ulp of the quotient).
 // The updated ratios go to qr for the next sub-step's zonal sweep.
 __global__ void __launch_bounds__(kVertCols *kVertLanes)
     k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
@@ -212,8 +258,9 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
     const long c = blockIdx.x * (long)kVertCols + tx;
     const bool live = c < ng;
     const long lv = (long)nlev * kVertCols;
-    // not yet updated dp, qm and ratio; mass change over dt, then the new dp; mass flux at faces 0..nlev
-    double *sd = vs, *sm = vs + lv, *sq = vs + 2 * lv, *sx = vs + 3 * lv, *sf = vs + 4 * lv;
+    // not yet updated dp, qm and ratio; mass change over dt, then the new dp; 1 / new dp;
+    // mass flux at faces 0..nlev
+    double *sd = vs, *sm = vs + lv, *sq = vs + 2 * lv, *sx = vs + 3 * lv, *sr = vs + 4 * lv, *sf = vs + 5 * lv;
     auto sl = [&](int kk) { return (kk - 1) * kVertCols + tx; };   // Fortran level kk
     auto sfl = [&](int kf) { return kf * kVertCols + tx; };        // face kf below level kf
     const int j = live ? (int)(c / nlon) : 0, i = live ? (int)(c - (long)j * nlon) : 0;
@@ -227,7 +274,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
             const double m = qm[t] - cm * (fq[fo + nlon] - fq[fo]);
             sd[sl(kk)] = d;
             sm[sl(kk)] = m;
-            sq[sl(kk)] = m / d;
+            sq[sl(kk)] = m * recip_nr(d);
             sx[sl(kk)] = (dp0[t] - d) * rdt;
         }
     }
@@ -248,6 +295,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
             const double dn = sd[sl(kk)] - dt * (sf[sfl(kk)] - sf[sfl(kk - 1)]);
             dp[(long)(kk - 1) * ng + c] = dn;
             sx[sl(kk)] = dn;
+            sr[sl(kk)] = recip_nr(dn);
         }
     }
     __syncthreads();
@@ -265,7 +313,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
         if (kd - 1 < 1 || kd + 1 > nlev) return qd * mm;
         const double sm_ = down ? qd - qa_m1 : qd - qa_p2;
         const double sp_ = down ? qa_p1 - qd : qa_0 - qd;
-        return (qd + 0.5 * (1.0 - cour) * vanleer(sm_, sp_)) * mm;
+        return (qd + (1.0 - cour) * vl_half(sm_, sp_)) * mm;
     };
     double qu1 = 0.0, qu2 = 0.0, du1 = 1.0;   // updated ratios of levels k - 1, k - 2; thickness of k - 1
     for (int k = 1; k <= nlev; ++k) {
@@ -280,7 +328,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
         const long t = (long)(k - 1) * ng + c;
         qm[t] = mn;
         qu2 = qu1;
-        qu1 = mn / dn;
+        qu1 = mn * sr[sl(k)];
         qr[t] = qu1;
         du1 = dn;
     }
@@ -490,11 +538,12 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
     if ((rc = tr_in(h, u, h->su, n3, &ud)) || (rc = tr_in(h, v, h->sv, n3, &vd)) ||
         (rc = tr_in(h, lnps, h->sl, (size_t)ng, &ld)) || (rc = tr_in(h, q, h->sq, n3, &qd)))
         return rc;
-    const unsigned nbc = (unsigned)((ng + 127) / 128);
+    const unsigned nbv = (unsigned)((ng + kVertCols - 1) / kVertCols);
+    const dim3 cblk(kVertCols, kVertLanes);
     AEROS_CUDA(cudaMemsetAsync(h->cmax, 0, sizeof(unsigned long long), h->stream));
-    k_tr_begin<<<nbc, 128, 0, h->stream>>>(ld, qd, h->A, h->B, h->nlev, ng, h->dp, h->qm, h->qr);
-    k_tr_courant<<<nbc, 128, 0, h->stream>>>(ud, vd, ld, h->A, h->B, h->rdx, h->rdyc, h->nlev, h->nlon, ng, dt,
-                                             h->cmax);
+    k_tr_begin<<<nbv, cblk, 0, h->stream>>>(ld, qd, h->A, h->B, h->nlev, ng, h->dp, h->qm, h->qr);
+    k_tr_courant<<<nbv, cblk, tr_courant_smem(h->nlev), h->stream>>>(ud, vd, ld, h->A, h->B, h->rdx, h->rdyc,
+                                                                      h->nlev, h->nlon, ng, dt, h->cmax);
     AEROS_CUDA(cudaGetLastError());
     unsigned long long bits = 0;
     AEROS_CUDA(cudaMemcpyAsync(&bits, h->cmax, 8, cudaMemcpyDeviceToHost, h->stream));
@@ -513,7 +562,6 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
     if (zthr > 1024) { set_error("transport: nlon above 1024"); return AEROS_ERR_UNSUPPORTED; }
     const size_t zsm = (size_t)4 * h->nlon * sizeof(double);
     const unsigned nbf = (unsigned)(((long)h->nlev * (h->nlat - 1) * h->nlon + 255) / 256);
-    const unsigned nbv = (unsigned)((ng + kVertCols - 1) / kVertCols);
     const size_t vsm = tr_vert_smem(h->nlev);
     for (int s = 0; s < nsub; ++s) {
         k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(ud, h->dp, h->qm, h->qr, h->qz, h->dp0, h->rdx,
@@ -521,7 +569,7 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
         if (h->nlat > 1)
             k_tr_mfaces<<<nbf, 256, 0, h->stream>>>(vd, h->dp, h->qz, h->cosface, h->rdyf, h->nlon, h->nlat, h->nlev,
                                                     ng, dts, h->mfa, h->mfq);
-        k_tr_vert<<<nbv, dim3(kVertCols, kVertLanes), vsm, h->stream>>>(h->dp0, h->dp, h->qm, h->qr, h->mfa, h->mfq, h->rden, h->B,
+        k_tr_vert<<<nbv, cblk, vsm, h->stream>>>(h->dp0, h->dp, h->qm, h->qr, h->mfa, h->mfq, h->rden, h->B,
                                                       h->nlon, h->nlat, h->nlev, ng, dts, 1.0 / dts, h->vert_vanleer);
     }
     AEROS_CUDA(cudaGetLastError());
