@@ -4,7 +4,9 @@
 // The tracer mass qm = q dp and the layer air mass dp are advanced by the same
 // face fluxes, so a uniform q stays uniform, tracer mass is conserved and q
 // stays non-negative under the Courant limit, which sub-stepping enforces
-// (nsub from the largest total Courant number of the call).  One sub-step:
+// (nsub from the largest total Courant number of the call).  Once per call,
+// k_tr_winds forms the face winds and van Leer weights of every sub-step.  One
+// sub-step:
 //   k_tr_zonal   block per (level, latitude) row, threads over longitude:
 //                periodic van Leer face values, fluxes staged in shared memory
 //   k_tr_mfaces  thread per (level, face, longitude): meridional face fluxes
@@ -58,7 +60,7 @@ __device__ __forceinline__ double vl_half(double a, double b) {
     return p > 0.0 ? p * recip_nr(a + b) : 0.0;
 }
 
-constexpr int kVertCols = 16;   // grid columns per block of the column kernels
+constexpr int kVertCols = 32;   // grid columns per block of the column kernels (a full warp)
 constexpr int kVertLanes = 8;   // threads per column in their level-parallel phases
 
 // Layer air mass from the surface pressure (aeros_vgrid_pressure,
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
         const double m = q[k * ng + c] * d;
         dp[k * ng + c] = d;
         qm[k * ng + c] = m;
-        qr[k * ng + c] = m / d;
+        qr[k * ng + c] = m * recip_nr(d);
     }
 }
 
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
     double *sc = cs, *su = cs + (long)nlev * kVertCols, *sps = su + (long)(nlev + 1) * kVertCols;
     if (live && ty == 0) sps[tx] = exp(lnps[c]);
     __syncthreads();
-    const int j = live ? (int)(c / nlon) : 0;
+    const int j = live ? (int)((unsigned)c / (unsigned)nlon) : 0;   // ng < 2^31
     const double rx = live ? rdx[j] : 0.0;
     if (live) {
         const double ps = sps[tx];
@@ -135,9 +137,9 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
             const double d = (A[k + 1] + B[k + 1] * ps) - (A[k] + B[k] * ps);
             const double cx = fabs(u[k * ng + c]) * dt * rx;
             const double cy = fabs(v[k * ng + c]) * dt * ry;
-            const double cz =
-                (fabs(B[k + 1] * SN - su[(k + 1) * kVertCols + tx]) + fabs(B[k] * SN - su[k * kVertCols + tx])) * dt /
-                d;
+            const double cz = (fabs(B[k + 1] * SN - su[(k + 1) * kVertCols + tx]) +
+                               fabs(B[k] * SN - su[k * kVertCols + tx])) *
+                              dt * recip_nr(d);
             best = fmax(best, cx + cy + cz);
         }
     }
@@ -145,13 +147,40 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
     if (((ty * kVertCols + tx) & 31) == 0) atomicMax(cmax, (unsigned long long)__double_as_longlong(best));
 }
 
+// Face winds and van Leer weights of a call: the winds do not change over its
+// sub-steps, so the zonal face wind uf = (u_i + u_i+1) / 2 with 1 - |uf| dt / dx,
+// and the meridional face wind vf = (v_f + v_f+1) / 2 with 1 - |vf| dt / dy and
+// vf cos(face) (sweep_zonal :374-437, sweep_merid :439-503), are formed once
+// per call.  Layout [5][nlev][nlat][nlon]: uf, its weight, then vf, its weight
+// and vf cos for face f (between rows f and f + 1, f = 1..nlat - 1) at row f - 1.
+__global__ void k_tr_winds(const double *__restrict__ u, const double *__restrict__ v,
+                           const double *__restrict__ rdx, const double *__restrict__ rdyf,
+                           const double *__restrict__ cosface, int nlon, int nlat, long ng, long n3, double dt,
+                           double *__restrict__ w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nlon) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long at = k * ng + (long)j * nlon + i;
+    const int ip = i + 1 == nlon ? 0 : i + 1;
+    const double uf = 0.5 * (u[at] + u[at - i + ip]);
+    w[at] = uf;
+    w[n3 + at] = 1.0 - fabs(uf) * (dt * rdx[j]);
+    if (j + 1 < nlat) {
+        const int f = j + 1;
+        const double vf = 0.5 * (v[at] + v[at + nlon]);
+        w[2 * n3 + at] = vf;
+        w[3 * n3 + at] = 1.0 - fabs(vf) * dt * rdyf[f];
+        w[4 * n3 + at] = vf * cosface[f];
+    }
+}
+
 // Zonal sweep (sweep_zonal, :374-437).  Starts from the ratios qr = qm / dp that
 // the previous vertical update (or k_tr_begin) left, keeps dp at the start of the
 // sub-step for the vertical mass flux and leaves the ratios after the sweep in
 // qz for the meridional faces.
-__global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp, double *__restrict__ qm,
+__global__ void k_tr_zonal(const double *__restrict__ w, double *__restrict__ dp, double *__restrict__ qm,
                            const double *__restrict__ qr, double *__restrict__ qz, double *__restrict__ dp0,
-                           const double *__restrict__ rdx, int nlon, long ng, double dt) {
+                           const double *__restrict__ rdx, int nlon, long ng, long n3, double dt) {
     extern __shared__ double zs[];
     double *qc = zs, *dc = zs + nlon, *fa = zs + 2 * nlon, *fq = zs + 3 * nlon;
     const int j = blockIdx.x, k = blockIdx.y, i = threadIdx.x;
@@ -171,16 +200,13 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
         const int ip = i + 1 == nlon ? 0 : i + 1;
         const int im = i == 0 ? nlon - 1 : i - 1;
         const int ip2 = ip + 1 == nlon ? 0 : ip + 1;
-        const double uf = 0.5 * (u[row + i] + u[row + ip]);
-        const double cour = fabs(uf) * cx;
-        double qf, f;
-        if (uf >= 0.0) {
-            qf = qc[i] + (1.0 - cour) * vl_half(qc[i] - qc[im], qc[ip] - qc[i]);
-            f = dc[i] * uf;
-        } else {
-            qf = qc[ip] + (1.0 - cour) * vl_half(qc[ip] - qc[ip2], qc[i] - qc[ip]);
-            f = dc[ip] * uf;
-        }
+        const double uf = w[row + i], wt = w[n3 + row + i];   // face wind, 1 - Courant number
+        // upwind cell, the cell beyond it and the downwind cell, chosen by select rather than
+        // by branch: a warp whose faces blow both ways would otherwise issue both paths' FP64 work
+        const bool up = uf >= 0.0;
+        const int iu = up ? i : ip, ib = up ? im : ip2, id = up ? ip : i;
+        const double qf = qc[iu] + wt * vl_half(qc[iu] - qc[ib], qc[id] - qc[iu]);
+        const double f = dc[iu] * uf;
         fa[i] = f;
         fq[i] = qf * f;
     }
@@ -198,40 +224,35 @@ __global__ void k_tr_zonal(const double *__restrict__ u, double *__restrict__ dp
 // Meridional face fluxes (sweep_merid, :439-503) with the bounded van Leer face
 // value (vl_face_bounded, :542-573), fully parallel over the start-of-sweep
 // state: face f between rows f and f + 1, stored at [k][f][i]; the pole faces 0
-// and nlat stay zero.  The row updates from these faces run in k_tr_vert.
-__global__ void k_tr_mfaces(const double *__restrict__ v, const double *__restrict__ dp,
-                            const double *__restrict__ qz, const double *__restrict__ cosface,
-                            const double *__restrict__ rdyf, int nlon, int nlat, int nlev, long ng, double dt,
+// and nlat stay zero.  Grid (longitude blocks, interior faces, levels), so the
+// indices need no integer division (a 64-bit one costs FP64 and XU work on a GPU
+// whose FP64 pipe bounds this kernel).  The row updates from these faces run in
+// k_tr_vert.
+__global__ void k_tr_mfaces(const double *__restrict__ w, const double *__restrict__ dp,
+                            const double *__restrict__ qz, int nlon, int nlat, long ng, long n3,
                             double *__restrict__ fa, double *__restrict__ fq) {
-    const long nf = (long)(nlat - 1) * nlon;
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)nlev * nf) return;
-    const int k = (int)(t / nf);
-    const long rem = t - (long)k * nf;
-    const int f = 1 + (int)(rem / nlon), i = (int)(rem - (long)(f - 1) * nlon);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nlon) return;
+    const int f = blockIdx.y + 1, k = blockIdx.z;
     const long base = k * ng + i;
     auto at = [&](int r) { return base + (long)(r - 1) * nlon; };   // Fortran row r = 1..nlat
-    const double vf = 0.5 * (v[at(f)] + v[at(f + 1)]);
-    const double cour = fabs(vf) * dt * rdyf[f];
-    double qf, a;
-    if (vf >= 0.0) {
-        const double q0 = qz[at(f)];
-        qf = (f <= 1 || f >= nlat) ? q0 : q0 + (1.0 - cour) * vl_half(q0 - qz[at(f - 1)], qz[at(f + 1)] - q0);
-        a = dp[at(f)] * vf * cosface[f];
-    } else {
-        const double q1 = qz[at(f + 1)];
-        qf = (f + 1 <= 1 || f + 1 >= nlat) ? q1
-                                            : q1 + (1.0 - cour) * vl_half(q1 - qz[at(f + 2)], qz[at(f)] - q1);
-        a = dp[at(f + 1)] * vf * cosface[f];
-    }
+    // face wind, 1 - Courant number, face wind x cos(face)
+    const double vf = w[2 * n3 + at(f)], wt = w[3 * n3 + at(f)], vfc = w[4 * n3 + at(f)];
+    // upwind row, the row beyond it and the downwind row, chosen by select (see k_tr_zonal); a
+    // pole-adjacent upwind row keeps its own value (the rows beyond do not exist)
+    const bool up = vf >= 0.0;
+    const int ru = up ? f : f + 1, rb = up ? f - 1 : f + 2, rd = up ? f + 1 : f;
+    double qf = qz[at(ru)];
+    if (ru > 1 && ru < nlat) qf = qf + wt * vl_half(qf - qz[at(rb)], qz[at(rd)] - qf);
+    const double a = dp[at(ru)] * vfc;
     const long o = (long)k * (nlat + 1) * nlon + (long)f * nlon + i;
     fa[o] = a;
     fq[o] = qf * a;
 }
 
-// Shared memory of one k_tr_vert block: five [nlev][kVertCols] arrays and the
-// [nlev + 1][kVertCols] mass fluxes.
-inline size_t tr_vert_smem(int nlev) { return ((size_t)6 * nlev + 1) * kVertCols * sizeof(double); }
+// Shared memory of one k_tr_vert block: six [nlev][kVertCols] arrays and the
+// [nlev + 1][kVertCols] running sums of the mass change.
+inline size_t tr_vert_smem(int nlev) { return ((size_t)7 * nlev + 1) * kVertCols * sizeof(double); }
 
 // The meridional row update, the vertical mass flux and the top-down vertical
 // update of a grid column (transport_substep, :289-372; sweep_merid's update,
@@ -239,14 +260,18 @@ inline size_t tr_vert_smem(int nlev) { return ((size_t)6 * nlev + 1) * kVertCols
 // kVertCols columns x kVertLanes threads, the column staged in shared memory:
 //   1. all threads, levels strided: the meridional update of dp and qm from the
 //      column's two faces, the layer-mass change over dt and the ratio qm / dp;
-//   2. one thread per column: the column sum of the mass change and the running
-//      sums in level order, giving the vertical mass flux at every face;
+//   2. one thread per column: the running sums of the mass change in level
+//      order; the last is the column sum, and with it they give the vertical
+//      mass flux at every face;
 //   3. all threads: the new layer thicknesses (they depend on the fluxes only)
-//      and their reciprocals;
-//   4. one thread per column, top down: the tracer update, whose upper-face flux
-//      sees the level above already updated (the only serial dependence); the
-//      updated ratio is the new qm times the reciprocal of the new dp, so no
-//      division sits on that chain (within an ulp of the quotient).
+//      and their reciprocals; for donor-cell fluxes also every part of the
+//      tracer fluxes that does not wait on an updated level: the lower face's
+//      flux, and the upper face's as weight x updated ratio + rest;
+//   4. one thread per column (a warp per block), top down: the tracer update,
+//      whose upper-face flux sees the level above already updated (the only
+//      serial dependence); the updated ratio is the new qm times the reciprocal
+//      of the new dp, so no division sits on that chain (within an ulp of the
+//      quotient), and a donor-cell level costs it four FP64 operations.
 // The updated ratios go to qr for the next sub-step's zonal sweep.
 __global__ void __launch_bounds__(kVertCols *kVertLanes)
     k_tr_vert(const double *__restrict__ dp0, double *__restrict__ dp, double *__restrict__ qm,
@@ -258,12 +283,16 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
     const long c = blockIdx.x * (long)kVertCols + tx;
     const bool live = c < ng;
     const long lv = (long)nlev * kVertCols;
-    // not yet updated dp, qm and ratio; mass change over dt, then the new dp; 1 / new dp;
-    // mass flux at faces 0..nlev
-    double *sd = vs, *sm = vs + lv, *sq = vs + 2 * lv, *sx = vs + 3 * lv, *sr = vs + 4 * lv, *sf = vs + 5 * lv;
+    // sd: not yet updated dp (donor cell: then the upper face's weight); sm, sq: not yet updated qm
+    // and ratio; sx: mass change over dt, then the new dp (donor cell: the lower face's flux);
+    // sr: 1 / new dp; sg: the rest of the upper face's donor-cell flux; sf: running sums of the
+    // mass change at faces 0..nlev
+    double *sd = vs, *sm = vs + lv, *sq = vs + 2 * lv, *sx = vs + 3 * lv, *sr = vs + 4 * lv, *sg = vs + 5 * lv,
+           *sf = vs + 6 * lv;
     auto sl = [&](int kk) { return (kk - 1) * kVertCols + tx; };   // Fortran level kk
     auto sfl = [&](int kf) { return kf * kVertCols + tx; };        // face kf below level kf
-    const int j = live ? (int)(c / nlon) : 0, i = live ? (int)(c - (long)j * nlon) : 0;
+    const unsigned cu = live ? (unsigned)c : 0u;   // ng < 2^31
+    const int j = (int)(cu / (unsigned)nlon), i = (int)(cu - (unsigned)j * nlon);
     const long fstride = (long)(nlat + 1) * nlon;
     if (live) {
         const double cm = dt * rden[j];
@@ -280,32 +309,57 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
     }
     __syncthreads();
     if (live && ty == 0) {
-        double SN = 0.0;   // scum(nlev)
-        for (int kk = 1; kk <= nlev; ++kk) SN = SN + sx[sl(kk)];
         double scum = 0.0;
-        sf[sfl(0)] = B[0] * SN;
+        sf[sfl(0)] = 0.0;
         for (int kk = 1; kk <= nlev; ++kk) {
             scum = scum + sx[sl(kk)];
-            sf[sfl(kk)] = B[kk] * SN - scum;
+            sf[sfl(kk)] = scum;
         }
     }
     __syncthreads();
+    const double SN = live ? sf[sfl(nlev)] : 0.0;   // scum(nlev)
+    // vertical mass flux through face kf: mfl(kf) = B(kf) SN - scum(kf)
+    auto mflux = [&](int kf) { return B[kf] * SN - sf[sfl(kf)]; };
     if (live) {
         for (int kk = 1 + ty; kk <= nlev; kk += kVertLanes) {
-            const double dn = sd[sl(kk)] - dt * (sf[sfl(kk)] - sf[sfl(kk - 1)]);
+            const double mk = mflux(kk), mkm = mflux(kk - 1);
+            const double dn = sd[sl(kk)] - dt * (mk - mkm);
             dp[(long)(kk - 1) * ng + c] = dn;
-            sx[sl(kk)] = dn;
             sr[sl(kk)] = recip_nr(dn);
+            if (vl) {
+                sx[sl(kk)] = dn;
+            } else {
+                // vflux_q: the lower face's flux needs only not yet updated ratios; the upper
+                // face's is qu(k - 1) mfl(k - 1) when mfl(k - 1) >= 0, else q(k) mfl(k - 1), and
+                // zero at the top (these slots are read only by this thread in this phase)
+                const double q0 = sq[sl(kk)];
+                sx[sl(kk)] = kk < nlev ? (mk >= 0.0 ? q0 : sq[sl(kk + 1)]) * mk : 0.0;
+                sd[sl(kk)] = kk >= 2 && mkm >= 0.0 ? mkm : 0.0;
+                sg[sl(kk)] = kk >= 2 && mkm < 0.0 ? q0 * mkm : 0.0;
+            }
         }
     }
     __syncthreads();
     if (!live || ty != 0) return;
-    // flux through face kf (between levels kf and kf + 1) with mass flux mm, from the ratios of
-    // levels kf - 1 .. kf + 2 and the thicknesses of levels kf, kf + 1 as the loop sees them
+    if (!vl) {
+        // fma(qu, w, rest) is qu mfl(k - 1) or q(k) mfl(k - 1) exactly, as the select would give
+        double qu = 0.0;
+        for (int k = 1; k <= nlev; ++k) {
+            const double fup = fma(qu, sd[sl(k)], sg[sl(k)]);
+            const double mn = sm[sl(k)] - dt * (sx[sl(k)] - fup);
+            const long t = (long)(k - 1) * ng + c;
+            qm[t] = mn;
+            qu = mn * sr[sl(k)];
+            qr[t] = qu;
+        }
+        return;
+    }
+    // van Leer flux (vflux_q_vl) through face kf (between levels kf and kf + 1) with mass flux mm,
+    // from the ratios of levels kf - 1 .. kf + 2 and the thicknesses of levels kf, kf + 1 as the
+    // loop sees them
     auto flux = [&](int kf, double mm, double qa_m1, double qa_0, double qa_p1, double qa_p2, double d0,
                     double d1) -> double {
         if (kf <= 0 || kf >= nlev) return 0.0;
-        if (!vl) return (mm >= 0.0 ? qa_0 : qa_p1) * mm;
         const bool down = mm >= 0.0;
         const int kd = down ? kf : kf + 1;
         const double qd = down ? qa_0 : qa_p1;
@@ -316,13 +370,14 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
         return (qd + (1.0 - cour) * vl_half(sm_, sp_)) * mm;
     };
     double qu1 = 0.0, qu2 = 0.0, du1 = 1.0;   // updated ratios of levels k - 1, k - 2; thickness of k - 1
+    double mfl_prev = mflux(0);
     for (int k = 1; k <= nlev; ++k) {
         // level k and the two below it, not yet updated (past the bottom: unused fillers)
         const double d0 = sd[sl(k)], m0 = sm[sl(k)], q0 = sq[sl(k)], dn = sx[sl(k)];
         const double d1 = k + 1 <= nlev ? sd[sl(k + 1)] : 1.0;
         const double q1 = k + 1 <= nlev ? sq[sl(k + 1)] : 0.0;
         const double q2 = k + 2 <= nlev ? sq[sl(k + 2)] : 0.0;
-        const double mfl = sf[sfl(k)], mfl_prev = sf[sfl(k - 1)];
+        const double mfl = mflux(k);
         const double dq = flux(k, mfl, qu1, q0, q1, q2, d0, d1) - flux(k - 1, mfl_prev, qu2, qu1, q0, q1, du1, d0);
         const double mn = m0 - dt * dq;
         const long t = (long)(k - 1) * ng + c;
@@ -331,6 +386,7 @@ __global__ void __launch_bounds__(kVertCols *kVertLanes)
         qu1 = mn * sr[sl(k)];
         qr[t] = qu1;
         du1 = dn;
+        mfl_prev = mfl;
     }
 }
 
@@ -383,6 +439,7 @@ struct aeros_transport_s {
     double *rdx = nullptr, *rdyc = nullptr, *rdyf = nullptr, *rden = nullptr;
     double *dp = nullptr, *qm = nullptr, *dp0 = nullptr;         // (nlev, nlat, nlon)
     double *qr = nullptr, *qz = nullptr;                         // qm / dp after the vertical / zonal update
+    double *wind = nullptr;                                      // face winds and weights of a call (5 x nlev grid)
     double *mfa = nullptr, *mfq = nullptr;                       // meridional face fluxes (nlev, nlat + 1, nlon)
     double *su = nullptr, *sv = nullptr, *sq = nullptr, *sl = nullptr, *rows = nullptr;   // staging
     unsigned long long *cmax = nullptr;
@@ -397,7 +454,7 @@ namespace {
 
 void tr_free(aeros_transport_s *h) {
     double *ps[] = {h->A,  h->B,  h->cosface, h->rdx, h->rdyc, h->rdyf, h->rden, h->dp, h->qm, h->dp0,
-                    h->qr, h->qz, h->su,      h->sv,  h->sq,   h->sl,   h->rows, h->mfa, h->mfq};
+                    h->qr, h->qz, h->su,      h->sv,  h->sq,   h->sl,   h->rows, h->mfa, h->mfq, h->wind};
     for (double *p : ps)
         if (p) cudaFree(p);
     if (h->cmax) cudaFree(h->cmax);
@@ -434,6 +491,10 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
     Geometry g;
     int rc = build_geometry(g, trunc, -1, -1);
     if (rc) return rc;
+    if ((long)g.nlon * g.nlat >= (1L << 31)) {   // the column kernels index a level in 32 bits
+        set_error("transport: grid above 2^31 columns");
+        return AEROS_ERR_UNSUPPORTED;
+    }
     aeros_transport_s *h = new aeros_transport_s;
     h->T = trunc;
     h->nlon = g.nlon;
@@ -466,6 +527,7 @@ int aeros_transport_create(aeros_transport_t *out, int trunc, int nlev, const do
         (rc = tr_alloc(h->rdyc, g.nlat)) || (rc = tr_alloc(h->rdyf, g.nlat + 1)) || (rc = tr_alloc(h->rden, g.nlat)) ||
         (rc = tr_alloc(h->cosface, g.nlat + 1)) || (rc = tr_alloc(h->dp, n3)) || (rc = tr_alloc(h->qr, n3)) ||
         (rc = tr_alloc(h->qz, n3)) || (rc = tr_alloc(h->qm, n3)) || (rc = tr_alloc(h->dp0, n3)) ||
+        (rc = tr_alloc(h->wind, 5 * n3)) ||
         (rc = tr_alloc(h->su, n3)) ||
         (rc = tr_alloc(h->sv, n3)) || (rc = tr_alloc(h->sq, n3)) || (rc = tr_alloc(h->sl, (size_t)h->ng)) ||
         (rc = tr_alloc(h->rows, g.nlat)) || (rc = tr_alloc(h->cmax, 1)) ||
@@ -561,14 +623,15 @@ int aeros_transport_step(aeros_transport_t h, const double *u, const double *v, 
     const int zthr = (h->nlon + 31) / 32 * 32;
     if (zthr > 1024) { set_error("transport: nlon above 1024"); return AEROS_ERR_UNSUPPORTED; }
     const size_t zsm = (size_t)4 * h->nlon * sizeof(double);
-    const unsigned nbf = (unsigned)(((long)h->nlev * (h->nlat - 1) * h->nlon + 255) / 256);
     const size_t vsm = tr_vert_smem(h->nlev);
+    k_tr_winds<<<dim3((h->nlon + 127) / 128, h->nlat, h->nlev), 128, 0, h->stream>>>(
+        ud, vd, h->rdx, h->rdyf, h->cosface, h->nlon, h->nlat, ng, (long)n3, dts, h->wind);
     for (int s = 0; s < nsub; ++s) {
-        k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(ud, h->dp, h->qm, h->qr, h->qz, h->dp0, h->rdx,
-                                                                     h->nlon, ng, dts);
+        k_tr_zonal<<<dim3(h->nlat, h->nlev), zthr, zsm, h->stream>>>(h->wind, h->dp, h->qm, h->qr, h->qz, h->dp0,
+                                                                     h->rdx, h->nlon, ng, (long)n3, dts);
         if (h->nlat > 1)
-            k_tr_mfaces<<<nbf, 256, 0, h->stream>>>(vd, h->dp, h->qz, h->cosface, h->rdyf, h->nlon, h->nlat, h->nlev,
-                                                    ng, dts, h->mfa, h->mfq);
+            k_tr_mfaces<<<dim3((h->nlon + 127) / 128, h->nlat - 1, h->nlev), 128, 0, h->stream>>>(
+                h->wind, h->dp, h->qz, h->nlon, h->nlat, ng, (long)n3, h->mfa, h->mfq);
         k_tr_vert<<<nbv, cblk, vsm, h->stream>>>(h->dp0, h->dp, h->qm, h->qr, h->mfa, h->mfq, h->rden, h->B,
                                                       h->nlon, h->nlat, h->nlev, ng, dts, 1.0 / dts, h->vert_vanleer);
     }

@@ -157,8 +157,9 @@ def sht_case(a):
 def transport_case(a):
     """The bench's transport workload: winds of a 35 m/s solid-body rotation
     plus a divergent part and 2 m/s seeded noise, the wavenumber-1 surface
-    pressure of the reference's transport test, q = 0.01, dt = 1800 s, device
-    arrays; `steps` calls of AerosTransport.step."""
+    pressure of the reference's transport test, the blob tracer of the bench
+    (0.002 + 0.015 exp(-6 r^2)), dt = 1800 s, device arrays; `steps` calls of
+    AerosTransport.step."""
     import torch
     from .params import held_suarez_params
     from .dynamics import AerosDyn
@@ -173,7 +174,8 @@ def transport_case(a):
          + rng.normal(0.0, 2.0, (nlev, nlat, nlon)))
     v = 17.5 * np.cos(lon)[None, None, :] + rng.normal(0.0, 2.0, (nlev, nlat, nlon))
     lnps = np.log(1.0e5 * (1.0 + 0.05 * np.sin(lon)[None, :] * np.cos(lat)[:, None]))
-    q = np.full((nlev, nlat, nlon), 0.01)
+    r2 = (lon[None, :] - np.pi) ** 2 + 4.0 * lat[:, None] ** 2
+    q = np.broadcast_to(0.002 + 0.015 * np.exp(-6.0 * r2), (nlev, nlat, nlon)).copy()
     g = AerosTransport(a.trunc, d.A, d.B)
     dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (u, v, lnps, q)]
     for _ in range(a.steps):
