@@ -604,11 +604,25 @@ int launch_leg_synth_fp64(const Ctx &c, const SynPlan &p, double2 *F, int nrow) 
 }
 
 // ============================================================ Legendre analysis (FP64)
-// CTA = (m, column tile, l tile).  Warp = one output column, lanes = degrees
-// (split into j partitions when the tile is narrower than 32).  Inputs are
-// folded to even/odd latitude sums in shared memory.
-constexpr int kAnaJC = 16;      // latitudes per smem chunk
+// CTA = (m, column tile, l tile of 32).  Warp = one output column, lanes =
+// degrees, the tile's degrees split into at most two pieces, the highest power
+// of two in lt and the rest padded to a power of two (lt = 32, or e.g. 20 =
+// 16 + 4, 27 = 16 + 11 -> 16): a piece of width LW runs 32 / LW latitude
+// partitions, summed by a shuffle tree at the end, so more lanes of each FP64
+// warp instruction do work than with one piece rounded up to a power of two
+// (on GB300 an FP64 warp instruction costs the same 16 pipe cycles however many
+// lanes it uses; a third piece cost more in its shuffle-tree adds than it
+// saved).  The pieces share the CTA's
+// staging of each latitude chunk: the Fourier rows folded to even/odd sums and
+// scaled by (a + i b m / sin), one (column, slot) row per warp with lanes over
+// latitude, so the scaling branches are uniform across a warp.
 constexpr int kAnaLT = 32;
+constexpr int kAnaPieces = 2;
+// latitudes per shared-memory chunk, the same for every CTA width: a lane's partial sums then
+// run over the same latitudes in the same order whatever launch shape the tuner picks
+constexpr int kAnaJC = 32;
+// dynamic shared memory of one CTA: the staged rows [col][slot][even/odd][j]
+inline size_t ana_smem(int ct) { return (size_t)ct * 3 * 2 * kAnaJC * sizeof(double2); }
 
 struct LanaArgs {
     const AnaCol *cols;
@@ -620,6 +634,7 @@ struct LanaArgs {
 };
 template <int kAnaCT, bool RAG = false>   // output columns (warps) per CTA
 __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_constant__ RagPack<LanaArgs> rp) {
+    constexpr int JC = kAnaJC;
     uint3 bid, gdim;
     const LanaArgs &ka = rag_part<RAG>(rp, bid, gdim);
     const AnaCol *__restrict__ cols = ka.cols;
@@ -631,9 +646,10 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
     const int *__restrict__ moff = ka.moff;
     const double2 *__restrict__ F = ka.F;
     const int nrow = ka.nrow, ms = ka.ms, T = ka.T, nh = ka.nh, nlat = ka.nlat;
-    __shared__ double sP[kAnaJC][kAnaLT];
-    __shared__ double sD[kAnaJC][kAnaLT];
-    __shared__ double2 sX[kAnaCT][3][2][kAnaJC];   // [col][slot][even/odd][j]
+    __shared__ double sP[JC][kAnaLT];
+    __shared__ double sD[JC][kAnaLT];
+    extern __shared__ double2 sXd[];   // [col][slot][even/odd][j], ana_smem(kAnaCT) bytes
+    auto sX = [&](int cc, int s, int par) { return sXd + ((cc * 3 + s) * 2 + par) * JC; };
     __shared__ AnaCol sCol[kAnaCT];
 
     const int m = bid.x;
@@ -649,22 +665,28 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
     if (tid < nct) sCol[tid] = cols[c0 + tid];
     __syncthreads();
 
-    // lane mapping: width LW (power of two >= lt), JP = 32/LW latitude partitions
-    int LW = 32;
-    while (LW / 2 >= lt && LW > 1) LW /= 2;
-    const int JP = 32 / LW;
-    const int lk = lane % LW, jp = lane / LW;
-    const bool lvalid = lk < lt;
-    const int par = (l0 + lk) & 1;                 // parity of l - m
+    // the tile's pieces: the highest power of two in lt, then the rest padded to a power of two
+    // (lane width pw, degrees pn, offset po in the tile); scalars, so that the unrolled piece
+    // loops below index registers
+    const int b0 = 1 << (31 - __clz(lt)), r1 = lt - b0;
+    const int w1 = r1 > 1 ? 1 << (32 - __clz(r1 - 1)) : r1;
+    const int np = 1 + (r1 > 0);
+    auto pw = [&](int p) { return p == 0 ? b0 : w1; };
+    auto pn = [&](int p) { return p == 0 ? b0 : r1; };
+    auto po = [&](int p) { return p == 0 ? 0 : b0; };
     const bool wvalid = warp < nct;
     AnaCol cd;
     if (wvalid) cd = sCol[warp];
-    double2 a1 = make_double2(0, 0), a2 = make_double2(0, 0), a3 = make_double2(0, 0);
+    double2 acc[kAnaPieces][3];
+#pragma unroll
+    for (int p = 0; p < kAnaPieces; ++p)
+#pragma unroll
+        for (int s = 0; s < 3; ++s) acc[p][s] = make_double2(0, 0);
 
-    for (int j0 = 0; j0 < nh; j0 += kAnaJC) {
-        const int jc = min(kAnaJC, nh - j0);
+    for (int j0 = 0; j0 < nh; j0 += JC) {
+        const int jc = min(JC, nh - j0);
         __syncthreads();
-        for (int idx = tid; idx < kAnaJC * kAnaLT; idx += blockDim.x) {
+        for (int idx = tid; idx < JC * kAnaLT; idx += blockDim.x) {
             int jj = idx / kAnaLT, kk = idx - jj * kAnaLT;
             double p = 0.0, d = 0.0;
             if (jj < jc && kk < lt) {
@@ -675,10 +697,10 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
             sP[jj][kk] = p;
             sD[jj][kk] = d;
         }
-        for (int idx = tid; idx < kAnaCT * 3 * kAnaJC; idx += blockDim.x) {
-            int cc = idx / (3 * kAnaJC);
-            int rem = idx - cc * 3 * kAnaJC;
-            int s = rem / kAnaJC, jj = rem - s * kAnaJC;
+        // one (column, slot) row of JC latitudes per JC threads
+        for (int idx = tid; idx < kAnaCT * 3 * JC; idx += blockDim.x) {
+            const int rr = idx / JC, jj = idx - rr * JC;
+            const int cc = rr / 3, s = rr - cc * 3;
             double2 e = make_double2(0, 0), o = make_double2(0, 0);
             if (cc < nct && jj < jc) {
                 const AnaCol &q = sCol[cc];
@@ -709,51 +731,68 @@ __global__ void __launch_bounds__(kAnaCT * 32) k_leg_anal_fp64(const __grid_cons
                     }
                 }
             }
-            sX[cc][s][0][jj] = e;
-            sX[cc][s][1][jj] = o;
+            sX(cc, s, 0)[jj] = e;
+            sX(cc, s, 1)[jj] = o;
         }
         __syncthreads();
-        if (wvalid && lvalid) {
-            for (int jj = jp; jj < jc; jj += JP) {
-                double p = sP[jj][lk], d = sD[jj][lk];
-                if (cd.row1 >= 0) {
-                    double2 x = sX[warp][0][par][jj];
-                    a1.x = fma(p, x.x, a1.x);
-                    a1.y = fma(p, x.y, a1.y);
-                }
-                if (cd.row2 >= 0) {
-                    double2 x = sX[warp][1][par ^ 1][jj];
-                    a2.x = fma(d, x.x, a2.x);
-                    a2.y = fma(d, x.y, a2.y);
-                }
-                if (cd.row3 >= 0) {
-                    double2 x = sX[warp][2][par][jj];
-                    a3.x = fma(p, x.x, a3.x);
-                    a3.y = fma(p, x.y, a3.y);
+        if (wvalid) {
+#pragma unroll
+            for (int p = 0; p < kAnaPieces; ++p) {
+                if (p >= np) break;
+                const int LW = pw(p), JP = 32 / LW;
+                const int lk = lane & (LW - 1), jp = lane / LW;
+                if (lk >= pn(p)) continue;
+                const int kk = po(p) + lk;
+                const int par = (l0 + kk) & 1;   // parity of l - m
+                for (int jj = jp; jj < jc; jj += JP) {
+                    const double pv = sP[jj][kk], dv = sD[jj][kk];
+                    if (cd.row1 >= 0) {
+                        const double2 x = sX(warp, 0, par)[jj];
+                        acc[p][0].x = fma(pv, x.x, acc[p][0].x);
+                        acc[p][0].y = fma(pv, x.y, acc[p][0].y);
+                    }
+                    if (cd.row2 >= 0) {
+                        const double2 x = sX(warp, 1, par ^ 1)[jj];
+                        acc[p][1].x = fma(dv, x.x, acc[p][1].x);
+                        acc[p][1].y = fma(dv, x.y, acc[p][1].y);
+                    }
+                    if (cd.row3 >= 0) {
+                        const double2 x = sX(warp, 2, par)[jj];
+                        acc[p][2].x = fma(pv, x.x, acc[p][2].x);
+                        acc[p][2].y = fma(pv, x.y, acc[p][2].y);
+                    }
                 }
             }
         }
     }
-    // reduce the latitude partitions
-    for (int off = LW; off < 32; off <<= 1) {
-        a1.x += __shfl_xor_sync(0xffffffffu, a1.x, off);
-        a1.y += __shfl_xor_sync(0xffffffffu, a1.y, off);
-        a2.x += __shfl_xor_sync(0xffffffffu, a2.x, off);
-        a2.y += __shfl_xor_sync(0xffffffffu, a2.y, off);
-        a3.x += __shfl_xor_sync(0xffffffffu, a3.x, off);
-        a3.y += __shfl_xor_sync(0xffffffffu, a3.y, off);
-    }
-    if (wvalid && lvalid && jp == 0) {
-        int l = m + l0 + lk;
-        double post = lfac[cd.post * ms + l];
-        double2 r = make_double2(post * (a1.x + a2.x), post * (a1.y + a2.y));
-        if (cd.row3 >= 0) {
-            double f3 = lfac[cd.lf3 * ms + l];
-            r.x += f3 * a3.x;
-            r.y += f3 * a3.y;
+    if (!wvalid) return;   // whole warps only: the shuffles below need every lane of a valid warp
+#pragma unroll
+    for (int p = 0; p < kAnaPieces; ++p) {
+        if (p >= np) break;
+        const int LW = pw(p);
+        // reduce the latitude partitions of this piece, for the slots the column uses (uniform
+        // across the warp)
+        for (int off = LW; off < 32; off <<= 1) {
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                if ((s == 1 && cd.row2 < 0) || (s == 2 && cd.row3 < 0)) continue;
+                acc[p][s].x += __shfl_xor_sync(0xffffffffu, acc[p][s].x, off);
+                acc[p][s].y += __shfl_xor_sync(0xffffffffu, acc[p][s].y, off);
+            }
         }
-        if (m == 0) r.y = 0.0;
-        cd.dst[mo + l0 + lk] = r;
+        const int lk = lane & (LW - 1);
+        if (lane < LW && lk < pn(p)) {
+            const int kk = po(p) + lk, l = m + l0 + kk;
+            const double post = lfac[cd.post * ms + l];
+            double2 r = make_double2(post * (acc[p][0].x + acc[p][1].x), post * (acc[p][0].y + acc[p][1].y));
+            if (cd.row3 >= 0) {
+                const double f3 = lfac[cd.lf3 * ms + l];
+                r.x += f3 * acc[p][2].x;
+                r.y += f3 * acc[p][2].y;
+            }
+            if (m == 0) r.y = 0.0;
+            cd.dst[mo + l0 + kk] = r;
+        }
     }
 }
 
@@ -764,7 +803,11 @@ int launch_leg_anal_fp64(const Ctx &c, const AnaCol *cols_d, int ncol, const dou
         dim3 grid(c.T + 1, (ncol + CT - 1) / CT, (c.T + 1 + kAnaLT - 1) / kAnaLT);
         const LanaArgs ka{cols_d, ncol, c.tab->PaT, c.tab->dPaT, c.tab->lfac, c.tab->sint,
                           c.tab->moff, F, nrow, c.ms, c.T, c.nh, c.nlat};
-        return emit_launch(c.stream, c.rec, kern, rkern, grid, dim3(CT * 32), 0, ka);
+        // static: the P and dP chunks and the column records
+        const size_t dyn = ana_smem(CT), stat = 2 * kAnaJC * kAnaLT * sizeof(double) + CT * sizeof(AnaCol);
+        if (int rc = raise_smem_limit(kern, dyn + stat)) return rc;
+        if (int rc = raise_smem_limit(rkern, dyn + stat)) return rc;
+        return emit_launch(c.stream, c.rec, kern, rkern, grid, dim3(CT * 32), dyn, ka);
     };
     int rc;
     if (ct == 4) rc = go((const void *)k_leg_anal_fp64<4>, (const void *)k_leg_anal_fp64<4, true>, 4);

@@ -159,6 +159,15 @@ def fp64_peak_tflops(torch):
 # the points and levels.  It includes the operations of the exp and log calls.
 COLUMN_FP64_FLOPS_PER_POINT_LEVEL = 99.35
 
+# FP64-pipe issue slots (warp instructions on the FP64 pipe x 32) per grid cell
+# of the tracer transport at T42L20 on the bench's workload, from ncu's
+# sm__inst_executed_pipe_fp64 count: per call (k_tr_begin 9.8, k_tr_courant
+# 25.8, k_tr_winds 8.9) and per sub-step (k_tr_zonal 25.0, k_tr_mfaces 13.7,
+# k_tr_vert 29.3).  Every FP64 warp instruction holds the pipe for 16 cycles (2
+# lanes per clock per SM), whether it is an add, a multiply, an FMA or a compare.
+TRANSPORT_FP64_SLOTS_PER_CELL = {"call": 44.5, "substep": 68.0}
+FP64_LANES_PER_CLOCK_PER_SM = 2
+
 
 def kernel_work(T, nlat, nlon, nlm, nlev):
     """Algorithmic work per launch of each step kernel at one member:
@@ -433,9 +442,18 @@ def transport_form(args, torch):
     cells = nlev * nlat * nlon
     # algorithmic bytes of one sub-step: zonal 6, meridional 5, vertical 6 doubles per cell
     sub_bytes = 17 * 8 * cells
+    # the bound: FP64-pipe issue slots (ncu's count per cell) at 2 lanes per clock per SM
+    props = torch.cuda.get_device_properties(0)
+    sm_hz = getattr(props, "clock_rate", 0) * 1e3 or 2.07e9
+    slots = cells * (TRANSPORT_FP64_SLOTS_PER_CELL["call"] + TRANSPORT_FP64_SLOTS_PER_CELL["substep"] * nsub)
+    pipe_s = slots / (FP64_LANES_PER_CLOCK_PER_SM * props.multi_processor_count * sm_hz)
     return {"workload": f"T{args.trunc}L{nlev} grid {nlon}x{nlat}, dt 1800 s, device arrays", "ms_per_call": t_gpu * 1e3,
             "max_courant": cfl, "substeps": nsub, "cell_substeps_per_s": cells * nsub / t_gpu,
             "achieved_GBs": sub_bytes * nsub / t_gpu / 1e9, "bytes_per_substep": sub_bytes,
+            "roofline": {"bound": "fp64 pipe issue", "fp64_pipe_ms": pipe_s * 1e3, "frac": pipe_s / t_gpu,
+                         "sm_clock_ghz": sm_hz / 1e9,
+                         "note": "FP64-pipe slots per cell from ncu; the call also holds one host read of the "
+                                 "Courant number"},
             "cpu_oracle_ms_per_call": t_cpu * 1e3, "cpu_oracle": "numpy restatement, 1 core"}
 
 
