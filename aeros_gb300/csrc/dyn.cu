@@ -963,8 +963,9 @@ struct MassArgs {
     unsigned *done;
     int mode;
 };
+constexpr int kMassThreads = 256;   // threads of a k_mass block (a power of two: the row-sum tree)
 template <bool RAG = false>
-__global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
+__global__ void __launch_bounds__(kMassThreads) k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
     uint3 bid, gdim;
     const MassArgs &mka = rag_part<RAG>(rpk, bid, gdim);
     double2 *__restrict__ lnps = mka.lnps;
@@ -987,35 +988,36 @@ __global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
     const int rsz = frow(n);   // padded FFT row stride (fft.cuh)
     double2 *Fn = sm, *Fs = sm + ms, *A = sm + 2 * ms, *B = A + 2 * rsz;
     const double2 *c = lnps + (size_t)e * nlm;
-    // thread per (m, parity of l - m): each sums its parity in the serial order,
-    // in batches of 16 degrees whose loads are all issued before the sums
-    double2 *Eo = A;   // even / odd parts [2][ms], combined below (A is free until the FFT prep)
-    for (int t = threadIdx.x; t < 2 * ms; t += blockDim.x) {
-        const int m = t >> 1, par = t & 1;
+    // thread per (m, parity of l - m, half): each sums every fourth degree (k = par + 2 h, + 4, ...)
+    // in the serial order, in batches of 16 degrees whose loads are all issued before the sums;
+    // two halves per parity halve the dependent chains of a block that is alone on its SM
+    double2 *Eo = A;   // [half][parity][ms], combined below (A and B are free until the FFT prep)
+    for (int t = threadIdx.x; t < 4 * ms; t += blockDim.x) {
+        const int m = t >> 2, h = (t >> 1) & 1, par = t & 1;
         double2 acc = make_double2(0, 0);
         const int mo = moff[m], K = T - m + 1;
-        for (int k0 = par; k0 < K; k0 += 32) {
+        for (int k0 = par + 2 * h; k0 < K; k0 += 64) {
             double p[16];
             double2 v[16];
 #pragma unroll
             for (int u = 0; u < 16; ++u) {
-                const int k = k0 + 2 * u;
+                const int k = k0 + 4 * u;
                 const bool in = k < K;
                 p[u] = in ? Ps[(size_t)(mo + k) * nh + jn] : 0.0;
                 v[u] = in ? c[mo + k] : make_double2(0.0, 0.0);
             }
 #pragma unroll
             for (int u = 0; u < 16; ++u) {
-                if (k0 + 2 * u >= K) break;
+                if (k0 + 4 * u >= K) break;
                 acc.x += p[u] * v[u].x;
                 acc.y += p[u] * v[u].y;
             }
         }
-        Eo[par * ms + m] = acc;
+        Eo[(h * 2 + par) * ms + m] = acc;
     }
     __syncthreads();
     for (int m = threadIdx.x; m <= T; m += blockDim.x) {
-        const double2 ev = Eo[m], od = Eo[ms + m];
+        const double2 ev = cadd(Eo[m], Eo[2 * ms + m]), od = cadd(Eo[ms + m], Eo[3 * ms + m]);
         Fn[m] = cadd(ev, od);
         Fs[m] = csub(ev, od);
     }
@@ -1035,12 +1037,17 @@ __global__ void k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
     __syncthreads();
     double2 *res = fft_rows<true>(A, B, 2, rsz, plan, tw, threadIdx.x, blockDim.x);
     const double *rr = reinterpret_cast<const double *>(res);
-    __shared__ double red[2][128];
-    for (int r = 0; r < 2; ++r) {
-        double s = 0.0;
-        for (int i = threadIdx.x; i < nlon; i += blockDim.x) s += exp(rr[2 * ((size_t)r * rsz + fpad(i >> 1)) + (i & 1)]);
-        red[r][threadIdx.x] = s;
+    __shared__ double red[2][kMassThreads];
+    // the two rows' points spread over all threads
+    double s0 = 0.0, s1 = 0.0;
+    for (int idx = threadIdx.x; idx < 2 * nlon; idx += blockDim.x) {
+        const int r = idx >= nlon, i = idx - r * nlon;
+        const double x = exp(rr[2 * ((size_t)r * rsz + fpad(i >> 1)) + (i & 1)]);
+        if (r) s1 += x;
+        else s0 += x;
     }
+    red[0][threadIdx.x] = s0;
+    red[1][threadIdx.x] = s1;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) {
@@ -1855,7 +1862,9 @@ int run_mass(Dyn &d, int mode) {
     const MassArgs ma{d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat, d.g.nlon, d.tab.Ps, d.tab.moff,
                       d.tab.plan, d.tab.tw, d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt, d.lnr_last,
                       d.lnr_cum, d.mass_done, mode};
-    if (int rc = emit_launch(d.stream, d.rec, (const void *)k_mass<>, (const void *)k_mass<true>, dim3(d.g.nh, d.M), dim3(128), smem, ma)) return rc;
+    if (int rc = emit_launch(d.stream, d.rec, (const void *)k_mass<>, (const void *)k_mass<true>, dim3(d.g.nh, d.M),
+                             dim3(kMassThreads), smem, ma))
+        return rc;
     mark(d, "mass");
     d.launches += 1;
     AEROS_CUDA(cudaGetLastError());
