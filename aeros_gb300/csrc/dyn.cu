@@ -28,7 +28,8 @@ using namespace aeros;
 
 namespace {
 
-constexpr int kMaxLev = 32;   // warp-per-coefficient solve: one lane per level
+constexpr int kMaxLev = 64;    // levels of a handle
+constexpr int kLaneLev = 32;   // levels of the lane-per-level kernels (k_spectral, the adjoint's kernels)
 constexpr double kNrmD = 0.39894228040143267794;   // 1/sqrt(2 pi)
 constexpr double kRsqrt4Pi = 0.28209479177387814347;   // 1/sqrt(4 pi): field mean per (0,0) coefficient
 
@@ -101,10 +102,12 @@ struct ColArgs {
     const DynConst *__restrict__ dc = cka.dc;                                             \
     const double2 *__restrict__ tspec = cka.tspec;                                        \
     const int nlm = cka.nlm
-template <int LPC, bool RAG = false>
+// MAXL: the most levels a launch holds (32, or 64 for handles of more than 32 levels, so that
+// the register-resident chunks of the <= 32-level instantiations stay as they are).
+template <int LPC, bool RAG = false, int MAXL = kLaneLev>
 __global__ void __launch_bounds__(256) k_column(const __grid_constant__ RagPack<ColArgs> rpk) {
     COLUMN_ARGS;
-    constexpr int kChunk = (kMaxLev + LPC - 1) / LPC;
+    constexpr int kChunk = (MAXL + LPC - 1) / LPC;
     const LevConst *c_lev = dc->lev;
     const HsConst &c_hs = dc->hs;
     // with up to 8 levels per lane every level loop is unrolled over kChunk with a
@@ -351,8 +354,8 @@ template <bool RAG = false>
 __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPack<SpecArgs> rpk) {
     uint3 bid, gdim;
     const SpecArgs &a = rag_part<RAG>(rpk, bid, gdim);
-    __shared__ double sG[kMaxLev * kMaxLev], sT[kMaxLev * kMaxLev], sW[kMaxLev * kMaxLev];
-    __shared__ double sNu[kMaxLev], sPc[kMaxLev];
+    __shared__ double sG[kLaneLev * kLaneLev], sT[kLaneLev * kLaneLev], sW[kLaneLev * kLaneLev];
+    __shared__ double sNu[kLaneLev], sPc[kLaneLev];
     const int NL = a.NL;
     for (int i = threadIdx.x; i < NL * NL; i += blockDim.x) {
         sG[i] = a.GT[i];
@@ -405,12 +408,12 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPac
                                    dold.y + h * rd.y + hl * (gy.y + pc * pz.y) + lam * wx.y);
         if (!act) rhs = z;
         const double *Mi = a.MinvT + (size_t)l * NL * NL;
-        double mrow[kMaxLev];   // this lane's row of the inverse, loaded before the solve
+        double mrow[kLaneLev];   // this lane's row of the inverse, loaded before the solve
 #pragma unroll
-        for (int j = 0; j < kMaxLev; ++j) mrow[j] = (act && j < NL) ? Mi[j * NL + k] : 0.0;
+        for (int j = 0; j < kLaneLev; ++j) mrow[j] = (act && j < NL) ? Mi[j * NL + k] : 0.0;
         dnew = z;
 #pragma unroll
-        for (int j = 0; j < kMaxLev; ++j) {
+        for (int j = 0; j < kLaneLev; ++j) {
             if (j >= NL) break;
             double2 rj = shfl2(rhs, j);
             dnew.x += mrow[j] * rj.x; dnew.y += mrow[j] * rj.y;
@@ -452,6 +455,180 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPac
         if (bad) atomicOr(a.flag, 1);
         a.vor_o[o] = vn; a.div_o[o] = dnow; a.tmp_o[o] = tnow;
         a.vor[o] = vnew; a.div[o] = dnew; a.tmp[o] = tnew;
+    }
+    if (lane == 0) {
+        a.lnps_o[op] = pnow;
+        a.lnps[op] = pnew;
+    }
+}
+
+// k_spectral for 33 to 64 levels: a warp per (member, lm), lane k holding levels
+// k and k + 32 (kWideLev per lane), the level matrices in dynamic shared memory
+// (spec_wide_smem) and the rows of M^-1 read from L2 inside the solve.  Per
+// level the arithmetic is k_spectral's, in the same order; only the nu . ed
+// sum adds a lane's two levels before the warp sum.
+constexpr int kWideLev = 2;
+inline size_t spec_wide_smem(int NL) { return ((size_t)3 * NL * NL + 2 * NL) * sizeof(double); }
+template <bool RAG = false>
+__global__ void __launch_bounds__(256) k_spectral_wide(const __grid_constant__ RagPack<SpecArgs> rpk) {
+    uint3 bid, gdim;
+    const SpecArgs &a = rag_part<RAG>(rpk, bid, gdim);
+    extern __shared__ double swd[];
+    const int NL = a.NL;
+    double *sG = swd, *sT = swd + NL * NL, *sW = swd + 2 * NL * NL, *sNu = swd + 3 * NL * NL, *sPc = sNu + NL;
+    for (int i = threadIdx.x; i < NL * NL; i += blockDim.x) {
+        sG[i] = a.GT[i];
+        sT[i] = a.TT[i];
+        sW[i] = a.WT[i];
+    }
+    for (int i = threadIdx.x; i < NL; i += blockDim.x) {
+        sNu[i] = a.nu[i];
+        sPc[i] = a.pcoef[i];
+    }
+    __syncthreads();
+    const int warp = (bid.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= a.nlm * a.M) return;
+    const int e = warp / a.nlm, lm = warp - e * a.nlm;
+    const int l = a.l_of_lm[lm];
+    const double lam = (double)l * (l + 1) / (kA * kA);
+    const double2 z = make_double2(0.0, 0.0);
+    bool act[kWideLev];
+    int k[kWideLev];
+    size_t o[kWideLev];
+    double2 vo[kWideLev], vn[kWideLev], tv[kWideLev], dold[kWideLev], dnow[kWideLev], rd[kWideLev],
+        told[kWideLev], tnow[kWideLev], rt[kWideLev];
+#pragma unroll
+    for (int r = 0; r < kWideLev; ++r) {
+        act[r] = lane + 32 * r < NL;
+        k[r] = act[r] ? lane + 32 * r : 0;
+        o[r] = ((size_t)e * NL + k[r]) * a.nlm + lm;
+        vo[r] = act[r] ? a.vor_o[o[r]] : z;
+        vn[r] = act[r] ? a.vor[o[r]] : z;
+        tv[r] = act[r] ? a.tv[o[r]] : z;
+        dold[r] = act[r] ? a.div_o[o[r]] : z;
+        dnow[r] = act[r] ? a.div[o[r]] : z;
+        rd[r] = act[r] ? a.td[o[r]] : z;
+        told[r] = act[r] ? a.tmp_o[o[r]] : z;
+        tnow[r] = act[r] ? a.tmp[o[r]] : z;
+        rt[r] = act[r] ? a.tt[o[r]] : z;
+    }
+    const size_t op = (size_t)e * a.nlm + lm;
+    double2 pold = a.lnps_o[op], pnow = a.lnps[op], rp = a.tp[op];
+    const double h = a.h;
+    double2 vnew[kWideLev], dnew[kWideLev], tnew[kWideLev], pnew;
+#pragma unroll
+    for (int r = 0; r < kWideLev; ++r) vnew[r] = make_double2(vo[r].x + h * tv[r].x, vo[r].y + h * tv[r].y);
+    // level j of a warp-wide vector v[kWideLev]: slot j / 32 of lane j % 32
+#define WIDE_LEVELS(j, s, jj)                                   \
+    _Pragma("unroll") for (int s = 0; s < kWideLev; ++s)        \
+        for (int jj = 0, j = 32 * s; jj < 32 && j < NL; ++jj, ++j)
+    if (a.semi_implicit) {
+        // the correction form of k_spectral
+        const double2 pz = make_double2(pold.x - pnow.x + a.astep * rp.x, pold.y - pnow.y + a.astep * rp.y);
+        const double ha = h * a.astep;
+        double2 y[kWideLev], x[kWideLev], gy[kWideLev], wx[kWideLev];
+#pragma unroll
+        for (int r = 0; r < kWideLev; ++r) {
+            y[r] = act[r] ? make_double2(told[r].x - tnow[r].x + a.astep * rt[r].x,
+                                         told[r].y - tnow[r].y + a.astep * rt[r].y)
+                          : z;
+            x[r] = act[r] ? make_double2(ha * dnow[r].x - a.hh_old * dold[r].x, ha * dnow[r].y - a.hh_old * dold[r].y)
+                          : z;
+            gy[r] = wx[r] = z;
+        }
+        WIDE_LEVELS(j, s, jj) {
+            const double2 yj = shfl2(y[s], jj), xj = shfl2(x[s], jj);
+#pragma unroll
+            for (int r = 0; r < kWideLev; ++r) {
+                const double gk = sG[j * NL + k[r]], wk = sW[j * NL + k[r]];   // G[k][j], W[k][j]
+                gy[r].x += gk * yj.x; gy[r].y += gk * yj.y;
+                wx[r].x += wk * xj.x; wx[r].y += wk * xj.y;
+            }
+        }
+        const double hl = h * lam;
+        double2 rhs[kWideLev];
+#pragma unroll
+        for (int r = 0; r < kWideLev; ++r) {
+            const double pc = sPc[k[r]];
+            rhs[r] = act[r] ? make_double2(dold[r].x + h * rd[r].x + hl * (gy[r].x + pc * pz.x) + lam * wx[r].x,
+                                           dold[r].y + h * rd[r].y + hl * (gy[r].y + pc * pz.y) + lam * wx[r].y)
+                            : z;
+            dnew[r] = z;
+        }
+        const double *Mi = a.MinvT + (size_t)l * NL * NL;
+        WIDE_LEVELS(j, s, jj) {
+            const double2 rj = shfl2(rhs[s], jj);
+#pragma unroll
+            for (int r = 0; r < kWideLev; ++r) {
+                const double mk = act[r] ? Mi[j * NL + k[r]] : 0.0;
+                dnew[r].x += mk * rj.x; dnew[r].y += mk * rj.y;
+            }
+        }
+        double2 ed[kWideLev], te[kWideLev];
+#pragma unroll
+        for (int r = 0; r < kWideLev; ++r) {
+            const double2 db = make_double2(a.a1 * dnew[r].x + (1.0 - a.a1) * dold[r].x,
+                                            a.a1 * dnew[r].y + (1.0 - a.a1) * dold[r].y);
+            ed[r] = act[r] ? make_double2(db.x - dnow[r].x, db.y - dnow[r].y) : z;
+            te[r] = z;
+        }
+        WIDE_LEVELS(j, s, jj) {
+            const double2 ej = shfl2(ed[s], jj);
+#pragma unroll
+            for (int r = 0; r < kWideLev; ++r) {
+                const double tk = sT[j * NL + k[r]];   // tau[k][j]
+                te[r].x += tk * ej.x; te[r].y += tk * ej.y;
+            }
+        }
+        double2 nl = z;
+#pragma unroll
+        for (int r = 0; r < kWideLev; ++r) {
+            tnew[r] = make_double2(told[r].x + h * (rt[r].x - te[r].x), told[r].y + h * (rt[r].y - te[r].y));
+            if (act[r]) {
+                nl.x += sNu[k[r]] * ed[r].x;
+                nl.y += sNu[k[r]] * ed[r].y;
+            }
+        }
+        const double2 ne = wsum2(nl);
+        pnew = make_double2(pold.x + h * (rp.x - ne.x), pold.y + h * (rp.y - ne.y));
+    } else {
+#pragma unroll
+        for (int r = 0; r < kWideLev; ++r) {
+            dnew[r] = make_double2(dold[r].x + h * rd[r].x, dold[r].y + h * rd[r].y);
+            tnew[r] = make_double2(told[r].x + h * rt[r].x, told[r].y + h * rt[r].y);
+        }
+        pnew = make_double2(pold.x + h * rp.x, pold.y + h * rp.y);
+    }
+#undef WIDE_LEVELS
+    const double fd = a.dfac[l];
+    auto filt = [&](double2 xo, double2 &xn, double2 &xw) {
+        double dx = a.half_nu * (xo.x - 2.0 * xn.x + xw.x), dy = a.half_nu * (xo.y - 2.0 * xn.y + xw.y);
+        xn.x += a.raw_alpha * dx; xn.y += a.raw_alpha * dy;
+        xw.x -= a.raw_beta * dx; xw.y -= a.raw_beta * dy;
+    };
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r < kWideLev; ++r) {
+        vnew[r] = make_double2(vnew[r].x * fd, vnew[r].y * fd);
+        dnew[r] = make_double2(dnew[r].x * fd, dnew[r].y * fd);
+        tnew[r] = make_double2(tnew[r].x * fd, tnew[r].y * fd);
+        if (a.raw_on) {
+            filt(vo[r], vn[r], vnew[r]);
+            filt(dold[r], dnow[r], dnew[r]);
+            filt(told[r], tnow[r], tnew[r]);
+        }
+        bad = bad || (act[r] && !(isfinite(vnew[r].x) && isfinite(vnew[r].y) && isfinite(dnew[r].x) &&
+                                  isfinite(dnew[r].y) && isfinite(tnew[r].x) && isfinite(tnew[r].y)));
+    }
+    if (a.raw_on) filt(pold, pnow, pnew);
+    bad = bad || !(isfinite(pnew.x) && isfinite(pnew.y));
+    if (bad) atomicOr(a.flag, 1);
+#pragma unroll
+    for (int r = 0; r < kWideLev; ++r) {
+        if (!act[r]) continue;
+        a.vor_o[o[r]] = vn[r]; a.div_o[o[r]] = dnow[r]; a.tmp_o[o[r]] = tnow[r];
+        a.vor[o[r]] = vnew[r]; a.div[o[r]] = dnew[r]; a.tmp[o[r]] = tnew[r];
     }
     if (lane == 0) {
         a.lnps_o[op] = pnow;
@@ -1834,6 +2011,13 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     if (split_column_df(d)) {
         // split form: the column terms in double-float on the FP32/INT32 pipes, a thread per column
         rc = go((const void *)k_column_df<>, (const void *)k_column_df<true>, (unsigned)((ncol + ct - 1) / ct));
+    } else if (d.NL > kLaneLev) {
+        // more than 32 levels: the instantiations whose per-lane chunks hold 64 levels
+        if (lpc == 16) rc = go((const void *)k_column<16, false, kMaxLev>, (const void *)k_column<16, true, kMaxLev>, nb);
+        else if (lpc == 8) rc = go((const void *)k_column<8, false, kMaxLev>, (const void *)k_column<8, true, kMaxLev>, nb);
+        else if (lpc == 4) rc = go((const void *)k_column<4, false, kMaxLev>, (const void *)k_column<4, true, kMaxLev>, nb);
+        else if (lpc == 2) rc = go((const void *)k_column<2, false, kMaxLev>, (const void *)k_column<2, true, kMaxLev>, nb);
+        else rc = go((const void *)k_column<1, false, kMaxLev>, (const void *)k_column<1, true, kMaxLev>, nb);
     } else if (lpc == 16) rc = go((const void *)k_column<16>, (const void *)k_column<16, true>, nb);
     else if (lpc == 8) rc = go((const void *)k_column<8>, (const void *)k_column<8, true>, nb);
     else if (lpc == 4) rc = go((const void *)k_column<4>, (const void *)k_column<4, true>, nb);
@@ -1926,6 +2110,14 @@ int enqueue_step(Dyn &d, bool startup) {
                         : emit_launch(d.stream, d.rec, (const void *)k_spectral_cols<20>,
                                       (const void *)k_spectral_cols<20, true>, dim3(nb), dim3(32 * sw),
                                       spec_cols_smem<20>(32 * sw), sa, (const void *)k_spectral_mixed);
+    } else if (d.NL > kLaneLev) {
+        const long nw = (long)d.g.nlm * d.M;
+        const size_t smem = spec_wide_smem(d.NL);
+        if ((rc = raise_smem_limit((const void *)k_spectral_wide<>, smem)) ||
+            (rc = raise_smem_limit((const void *)k_spectral_wide<true>, smem)))
+            return rc;
+        rc = emit_launch(d.stream, d.rec, (const void *)k_spectral_wide<>, (const void *)k_spectral_wide<true>,
+                         dim3((unsigned)((nw + sw - 1) / sw)), dim3(32 * sw), smem, a);
     } else {
         long nw = (long)d.g.nlm * d.M;
         rc = emit_launch(d.stream, d.rec, (const void *)k_spectral<>, (const void *)k_spectral<true>, dim3((unsigned)((nw + sw - 1) / sw)),

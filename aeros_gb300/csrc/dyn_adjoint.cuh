@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, 
         const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
         const double ps = exp(lnps), rps = 1.0 / ps;
         // ---- forward recomputation (k_column)
-        double ph0[kMaxLev], ph1[kMaxLev], dp[kMaxLev], rdp[kMaxLev], dlnp[kMaxLev], alpha[kMaxLev], cfac[kMaxLev],
-            gc[kMaxLev], cm[kMaxLev], scum[kMaxLev + 1];
+        double ph0[kLaneLev], ph1[kLaneLev], dp[kLaneLev], rdp[kLaneLev], dlnp[kLaneLev], alpha[kLaneLev], cfac[kLaneLev],
+            gc[kLaneLev], cm[kLaneLev], scum[kLaneLev + 1];
         scum[0] = 0.0;
         for (int k = 0; k < NL; ++k) {
             const LevConst &L = c_lev[k];
@@ -182,9 +182,9 @@ __global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, 
             tbase = c_hs.t_eq - dty * x2;
         }
         // ---- adjoint accumulators
-        double ub[kMaxLev], vb[kMaxLev], zb[kMaxLev], dvb[kMaxLev], tb[kMaxLev], txb[kMaxLev], tyb[kMaxLev];
-        double gcb[kMaxLev], cmb[kMaxLev], scumb[kMaxLev + 1], rb[kMaxLev], dlnpb[kMaxLev], alphab[kMaxLev],
-            cfacb[kMaxLev], phib[kMaxLev];
+        double ub[kLaneLev], vb[kLaneLev], zb[kLaneLev], dvb[kLaneLev], tb[kLaneLev], txb[kLaneLev], tyb[kLaneLev];
+        double gcb[kLaneLev], cmb[kLaneLev], scumb[kLaneLev + 1], rb[kLaneLev], dlnpb[kLaneLev], alphab[kLaneLev],
+            cfacb[kLaneLev], phib[kLaneLev];
         for (int k = 0; k < NL; ++k) {
             ub[k] = vb[k] = zb[k] = dvb[k] = tb[k] = txb[k] = tyb[k] = 0.0;
             gcb[k] = cmb[k] = rb[k] = dlnpb[k] = alphab[k] = cfacb[k] = phib[k] = 0.0;
@@ -423,8 +423,8 @@ struct SpecAdArgs {
 };
 
 __global__ void __launch_bounds__(128) k_spectral_ad(SpecAdArgs a) {
-    __shared__ double sG[kMaxLev * kMaxLev], sT[kMaxLev * kMaxLev], sW[kMaxLev * kMaxLev];
-    __shared__ double sNu[kMaxLev], sPc[kMaxLev];
+    __shared__ double sG[kLaneLev * kLaneLev], sT[kLaneLev * kLaneLev], sW[kLaneLev * kLaneLev];
+    __shared__ double sNu[kLaneLev], sPc[kLaneLev];
     const int NL = a.NL;
     for (int i = threadIdx.x; i < NL * NL; i += blockDim.x) {
         sG[i] = a.GT[i];
@@ -626,6 +626,10 @@ int adj_ensure(Dyn &d) {
         return AEROS_ERR_UNSUPPORTED;
     }
     if (d.adj) return aeros_sht_set_stream(d.adj->sht, d.stream);   // follow aeros_dyn_set_stream
+    if (d.NL > kLaneLev) {   // its column and spectral kernels hold one level per lane or register slot
+        set_error("adjoint: more than 32 levels");
+        return AEROS_ERR_UNSUPPORTED;
+    }
     AdjCtx *a = new AdjCtx;
     d.adj = a;
     const size_t ng = (size_t)d.g.nlon * d.g.nlat, M = d.M, NL = d.NL, nst = d.nstate(), nlm = d.g.nlm;

@@ -190,7 +190,8 @@ int aeros_params_default(aeros_params *p);
 /* Build the integrator: vertical grid, semi-implicit operators, diffusion
  * ratios, Held-Suarez factors, device state for p->nmember members.
  * a_half/b_half (nlev+1) may be NULL (generated from the stretching
- * parameters) or an explicit hybrid table.  Replaces aeros_timestep_init
+ * parameters) or an explicit hybrid table; 2 to 64 levels (AEROS_ERR_UNSUPPORTED
+ * above).  Replaces aeros_timestep_init
  * (src/dynamics/aeros_timestep.f90:452-598), aeros_vgrid_init
  * (src/dynamics/aeros_vertical.f90:126-298) and aeros_semiimp_init
  * (src/dynamics/aeros_semiimp.f90:171-276). */
@@ -496,7 +497,8 @@ int aeros_dyn_state_size(aeros_dyn_t h, long long *n);
  * current state; the state is left unchanged).  In: adjoints of the post-step
  * old slot (the RAW-filtered X^n) and now slot (X^(n+1)), packed.  Out:
  * adjoints of the pre-step old (X^(n-1)) and now (X^n) slots, packed, and per
- * member d/dk_a, d/ddT_y (any output may be NULL). */
+ * member d/dk_a, d/ddT_y (any output may be NULL).  Handles of more than 32
+ * levels: AEROS_ERR_UNSUPPORTED (so for every adjoint entry point). */
 int aeros_dyn_step_ad(aeros_dyn_t h, const double *old_ad_in, const double *now_ad_in, double *old_ad_out,
                       double *now_ad_out, double *ka_ad, double *dty_ad);
 

@@ -61,7 +61,7 @@ def test_bad_arguments_return_codes(lib):
                 dict(si_alpha=0.4), dict(nmember=0)):
         p = held_suarez_params(trunc=21, nlev=12, **bad)
         assert lib.aeros_dyn_create(ctypes.byref(h), ctypes.byref(p), None, None) == -1, bad
-    p = held_suarez_params(trunc=21, nlev=40)
+    p = held_suarez_params(trunc=21, nlev=65)   # 2 to 64 levels
     assert lib.aeros_dyn_create(ctypes.byref(h), ctypes.byref(p), None, None) == -7
     # groups: no handles, or a null group
     g = ctypes.c_void_p()

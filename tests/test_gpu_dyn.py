@@ -71,7 +71,7 @@ def check_against_truth(tg, to, tt, label):
         assert relerr(tg[i], to[i]) < 1e-12
 
 
-@pytest.mark.parametrize("trunc,nlev", [(21, 12), (31, 20), (42, 20)])
+@pytest.mark.parametrize("trunc,nlev", [(21, 12), (31, 20), (42, 20), (21, 40), (21, 64)])
 def test_adiabatic_tendency(gpulib, trunc, nlev):
     g, o, s = make_pair(trunc, nlev)
     st = moving_state(o)
@@ -115,6 +115,41 @@ def test_hs_steps_match_oracle(gpulib, trunc):
     assert ng == no == 10
     assert abs(mg - mo) / mo < 1e-13
     assert abs(lg - lo) < 1e-14 and abs(cg - co) < 1e-13
+
+
+@pytest.mark.parametrize("nlev", [33, 40, 64])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_many_levels_steps_match_oracle(gpulib, nlev, precision):
+    """More than 32 levels (the 64-level column kernels and the two-levels-per-lane
+    spectral solve): forced steps from a moving state against the oracle, with the
+    bars of the 20-level case; the split form within its own 1e-10 bar."""
+    g, o, s = make_pair(21, nlev, precision=precision)
+    st = moving_state(o, seed=23)
+    o.set_state(*st)
+    g.set_state(*st)
+    o.step(4)
+    g.step(4)
+    for a, b in zip(g.get_state(), o.get_state()):
+        assert relerr(a, b) < 1e-10, nlev
+    for a, b in zip(g.get_old_state(), o.get_old_state()):
+        assert relerr(a, b) < 1e-10, nlev
+    ng, mg, _, _ = g.counters()
+    no, mo, _, _ = o.counters()
+    assert ng == no == 4
+    assert abs(mg - mo) / mo < 1e-13
+
+
+def test_many_levels_adjoint_refused(gpulib):
+    """The adjoint holds one level per lane: above 32 levels it returns
+    AEROS_ERR_UNSUPPORTED instead of running."""
+    from aeros_gb300 import _capi
+    g, o, s = make_pair(21, 40)
+    st = moving_state(o, seed=5)
+    g.set_state(*st)
+    n = g.state_size()
+    with pytest.raises(_capi.AerosError) as ei:
+        g.step_ad(np.zeros(n, np.complex128), np.zeros(n, np.complex128))
+    assert ei.value.code == -7
 
 
 def test_hs_rest_noise_start(gpulib):

@@ -103,3 +103,20 @@ def test_fused_group_of_more_handles_than_one_launch_takes(gpulib):
     for a, b in zip(grouped, single):
         for x, y in zip(a.get_state(squeeze=False), b.get_state(squeeze=False)):
             assert np.array_equal(x, y)
+
+
+def test_group_with_a_many_level_handle(gpulib):
+    """A handle of 40 levels beside one of 16 in a fused group: its column and
+    spectral kernels differ from the others', so they launch apart, and every
+    state equals stepping the handles on their own."""
+    from aeros_gb300.dynamics import AerosGroup
+    cfg = [(21, 16, 2, 400), (21, 40, 2, 500)]
+    grouped = [_make(*c)[0] for c in cfg]
+    single = [_make(*c)[0] for c in cfg]
+    g = AerosGroup(grouped)
+    g.step(3)
+    for d in single:
+        d.step(3)
+    for a, b in zip(grouped, single):
+        for x, y in zip(a.get_state(squeeze=False), b.get_state(squeeze=False)):
+            assert np.array_equal(x, y)
