@@ -1140,7 +1140,10 @@ struct MassArgs {
     unsigned *done;
     int mode;
 };
-constexpr int kMassThreads = 256;   // threads of a k_mass block (a power of two: the row-sum tree)
+// threads of a k_mass block: kMassThreads when its grid leaves most SMs idle (one handle of few
+// members), half that when the grid fills the GPU or the launch joins a group's fused launch (one
+// block shape for all its handles); the results do not depend on the choice
+constexpr int kMassThreads = 256;
 template <bool RAG = false>
 __global__ void __launch_bounds__(kMassThreads) k_mass(const __grid_constant__ RagPack<MassArgs> rpk) {
     uint3 bid, gdim;
@@ -1214,22 +1217,26 @@ __global__ void __launch_bounds__(kMassThreads) k_mass(const __grid_constant__ R
     __syncthreads();
     double2 *res = fft_rows<true>(A, B, 2, rsz, plan, tw, threadIdx.x, blockDim.x);
     const double *rr = reinterpret_cast<const double *>(res);
+    // row sums over kMassThreads fixed slots (slot t: the points idx = t, t + kMassThreads, ... of
+    // the two rows' 2 nlon points, in order, each added to its row's sum) and a fixed tree over the
+    // slots, whatever the block size, so the sums' rounding does not depend on the launch shape
     __shared__ double red[2][kMassThreads];
-    // the two rows' points spread over all threads
-    double s0 = 0.0, s1 = 0.0;
-    for (int idx = threadIdx.x; idx < 2 * nlon; idx += blockDim.x) {
-        const int r = idx >= nlon, i = idx - r * nlon;
-        const double x = exp(rr[2 * ((size_t)r * rsz + fpad(i >> 1)) + (i & 1)]);
-        if (r) s1 += x;
-        else s0 += x;
+    for (int t = threadIdx.x; t < kMassThreads; t += blockDim.x) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int idx = t; idx < 2 * nlon; idx += kMassThreads) {
+            const int r = idx >= nlon, i = idx - r * nlon;
+            const double x = exp(rr[2 * ((size_t)r * rsz + fpad(i >> 1)) + (i & 1)]);
+            if (r) s1 += x;
+            else s0 += x;
+        }
+        red[0][t] = s0;
+        red[1][t] = s1;
     }
-    red[0][threadIdx.x] = s0;
-    red[1][threadIdx.x] = s1;
     __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            red[0][threadIdx.x] += red[0][threadIdx.x + o];
-            red[1][threadIdx.x] += red[1][threadIdx.x + o];
+    for (int o = kMassThreads / 2; o > 0; o >>= 1) {
+        for (int t = threadIdx.x; t < o; t += blockDim.x) {
+            red[0][t] += red[0][t + o];
+            red[1][t] += red[1][t + o];
         }
         __syncthreads();
     }
@@ -2046,8 +2053,9 @@ int run_mass(Dyn &d, int mode) {
     const MassArgs ma{d.lnp(d.now), d.M, d.g.T, d.g.nlm, d.g.nh, d.g.nlat, d.g.nlon, d.tab.Ps, d.tab.moff,
                       d.tab.plan, d.tab.tw, d.tab.twN, d.mass_rows, d.tab.w, d.c00, d.mass_tgt, d.lnr_last,
                       d.lnr_cum, d.mass_done, mode};
+    const int thr = (d.rec || (long)d.g.nh * d.M >= 256) ? kMassThreads / 2 : kMassThreads;
     if (int rc = emit_launch(d.stream, d.rec, (const void *)k_mass<>, (const void *)k_mass<true>, dim3(d.g.nh, d.M),
-                             dim3(kMassThreads), smem, ma))
+                             dim3(thr), smem, ma))
         return rc;
     mark(d, "mass");
     d.launches += 1;

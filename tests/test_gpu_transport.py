@@ -30,7 +30,10 @@ def _mixed_case(lon, lat, nlev, seed):
     return u, v, set_lnps(lon, lat), q
 
 
-@pytest.mark.parametrize("trunc,nlev,vl", [(21, 8, False), (42, 20, False), (21, 8, True)])
+# 64 levels: the vertical kernel's largest shared-memory stage; T31: 96 longitudes, a partial
+# thread block in every longitude row; 33 levels: a level count that no lane stride divides
+@pytest.mark.parametrize("trunc,nlev,vl", [(21, 8, False), (42, 20, False), (21, 8, True), (21, 64, False),
+                                          (21, 64, True), (31, 20, True), (21, 33, False)])
 def test_matches_oracle(gpulib, trunc, nlev, vl):
     g, o, lon, lat = _pair(trunc, nlev, vl)
     u, v, lnps, q = _mixed_case(lon, lat, nlev, seed=trunc + nlev)
