@@ -109,7 +109,9 @@ __global__ void k_mass_target_ad(double2 *__restrict__ pb, const double2 *__rest
 // ---------------------------------------------------------------- column adjoint
 // Given the forward grid fields G and the adjoints GAb of the column outputs,
 // write the adjoints Gb of the column inputs (same layouts as k_column) and add
-// d/dk_a, d/ddT_y to parb[2 e], parb[2 e + 1].
+// d/dk_a, d/ddT_y to parb[2 e], parb[2 e + 1].  MAXL: the most levels of the
+// per-column arrays (32, or 64 for handles of more than 32 levels).
+template <int MAXL = kLaneLev>
 __global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, const double *__restrict__ GAb,
                                                   double *__restrict__ Gb, int NL, int nlon, int nlat, int M,
                                                   const double *__restrict__ xlat, const double *__restrict__ phis,
@@ -138,8 +140,8 @@ __global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, 
         const double lnps = GF(7 * NL), dpx = GF(7 * NL + 1), dpy = GF(7 * NL + 2);
         const double ps = exp(lnps), rps = 1.0 / ps;
         // ---- forward recomputation (k_column)
-        double ph0[kLaneLev], ph1[kLaneLev], dp[kLaneLev], rdp[kLaneLev], dlnp[kLaneLev], alpha[kLaneLev], cfac[kLaneLev],
-            gc[kLaneLev], cm[kLaneLev], scum[kLaneLev + 1];
+        double ph0[MAXL], ph1[MAXL], dp[MAXL], rdp[MAXL], dlnp[MAXL], alpha[MAXL], cfac[MAXL],
+            gc[MAXL], cm[MAXL], scum[MAXL + 1];
         scum[0] = 0.0;
         for (int k = 0; k < NL; ++k) {
             const LevConst &L = c_lev[k];
@@ -182,9 +184,9 @@ __global__ void __launch_bounds__(32) k_column_ad(const double *__restrict__ G, 
             tbase = c_hs.t_eq - dty * x2;
         }
         // ---- adjoint accumulators
-        double ub[kLaneLev], vb[kLaneLev], zb[kLaneLev], dvb[kLaneLev], tb[kLaneLev], txb[kLaneLev], tyb[kLaneLev];
-        double gcb[kLaneLev], cmb[kLaneLev], scumb[kLaneLev + 1], rb[kLaneLev], dlnpb[kLaneLev], alphab[kLaneLev],
-            cfacb[kLaneLev], phib[kLaneLev];
+        double ub[MAXL], vb[MAXL], zb[MAXL], dvb[MAXL], tb[MAXL], txb[MAXL], tyb[MAXL];
+        double gcb[MAXL], cmb[MAXL], scumb[MAXL + 1], rb[MAXL], dlnpb[MAXL], alphab[MAXL],
+            cfacb[MAXL], phib[MAXL];
         for (int k = 0; k < NL; ++k) {
             ub[k] = vb[k] = zb[k] = dvb[k] = tb[k] = txb[k] = tyb[k] = 0.0;
             gcb[k] = cmb[k] = rb[k] = dlnpb[k] = alphab[k] = cfacb[k] = phib[k] = 0.0;
@@ -584,6 +586,237 @@ __global__ void __launch_bounds__(128) k_spectral_ad(SpecAdArgs a) {
     }
 }
 
+// k_spectral_ad for 33 to 64 levels: lane k holds levels k and k + 32 (the
+// layout of k_spectral_wide), the level matrices in dynamic shared memory
+// (spec_wide_smem), the rows of M^-1 read from L2.  Per level the arithmetic of
+// k_spectral_ad in the same order; the two level sums over nu and pcoef add a
+// lane's two levels before the warp sum.
+__global__ void __launch_bounds__(128) k_spectral_ad_wide(SpecAdArgs a) {
+    extern __shared__ double swa[];
+    const int NL = a.NL;
+    double *sG = swa, *sT = swa + NL * NL, *sW = swa + 2 * NL * NL, *sNu = swa + 3 * NL * NL, *sPc = sNu + NL;
+    for (int i = threadIdx.x; i < NL * NL; i += blockDim.x) {
+        sG[i] = a.GT[i];
+        sT[i] = a.TT[i];
+        sW[i] = a.WT[i];
+    }
+    for (int i = threadIdx.x; i < NL; i += blockDim.x) {
+        sNu[i] = a.nu[i];
+        sPc[i] = a.pcoef[i];
+    }
+    __syncthreads();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= a.nlm * a.M) return;
+    constexpr int R = kWideLev;
+    const int e = warp / a.nlm, lm = warp - e * a.nlm;
+    const int l = a.l_of_lm[lm];
+    const double lam = (double)l * (l + 1) / (kA * kA);
+    const size_t nsl = (size_t)a.M * NL * a.nlm;   // one 3-D field block of the state
+    const size_t op = 3 * nsl + (size_t)e * a.nlm + lm;
+    const double2 z = make_double2(0.0, 0.0);
+    bool act[R];
+    int k[R];
+    size_t o[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        act[r] = lane + 32 * r < NL;
+        k[r] = act[r] ? lane + 32 * r : 0;
+        o[r] = ((size_t)e * NL + k[r]) * a.nlm + lm;
+    }
+    auto ld = [&](const double2 *p, size_t i, int r) { return act[r] ? p[i] : z; };
+    const double h = a.h, hn = a.half_nu;
+    // RAW filter: Xn' = Xn + alpha dx, Xw' = Xw - beta dx, dx = hn (Xo - 2 Xn + Xw)
+    auto raw = [&](double2 O, double2 N, double2 &xn, double2 &xo, double2 &xw) {
+        if (a.raw_on) {
+            const double2 dxb = make_double2(a.raw_alpha * O.x - a.raw_beta * N.x, a.raw_alpha * O.y - a.raw_beta * N.y);
+            xn = make_double2(O.x - 2.0 * hn * dxb.x, O.y - 2.0 * hn * dxb.y);
+            xo = make_double2(hn * dxb.x, hn * dxb.y);
+            xw = make_double2(N.x + hn * dxb.x, N.y + hn * dxb.y);
+        } else {
+            xn = O;
+            xo = z;
+            xw = N;
+        }
+    };
+    double2 vnb[R], vob[R], vwb[R], dnb[R], dob[R], dwb[R], tnb[R], tob[R], twb[R], tvb[R], rdb[R], rtb[R];
+    const double fd = a.dfac[l];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        raw(ld(a.ob, o[r], r), ld(a.nb, o[r], r), vnb[r], vob[r], vwb[r]);
+        raw(ld(a.ob, nsl + o[r], r), ld(a.nb, nsl + o[r], r), dnb[r], dob[r], dwb[r]);
+        raw(ld(a.ob, 2 * nsl + o[r], r), ld(a.nb, 2 * nsl + o[r], r), tnb[r], tob[r], twb[r]);
+        // diffusion (not on lnps), vorticity leapfrog
+        vwb[r] = make_double2(fd * vwb[r].x, fd * vwb[r].y);
+        dwb[r] = make_double2(fd * dwb[r].x, fd * dwb[r].y);
+        twb[r] = make_double2(fd * twb[r].x, fd * twb[r].y);
+        vob[r] = make_double2(vob[r].x + vwb[r].x, vob[r].y + vwb[r].y);
+        tvb[r] = make_double2(h * vwb[r].x, h * vwb[r].y);
+    }
+    double2 pnb, pob, pwb;
+    raw(a.ob[op], a.nb[op], pnb, pob, pwb);
+    double2 rpb;
+    // level j of a warp-wide vector v[R]: slot j / 32 of lane j % 32
+#define WIDE_LEVELS(j, s, jj)                                   \
+    _Pragma("unroll") for (int s = 0; s < R; ++s)               \
+        for (int jj = 0, j = 32 * s; jj < 32 && j < NL; ++jj, ++j)
+    if (a.semi_implicit) {
+        // pnew = pold + h (rp - nb - lpn)
+        pob = make_double2(pob.x + pwb.x, pob.y + pwb.y);
+        rpb = make_double2(h * pwb.x, h * pwb.y);
+        const double2 nbb = make_double2(-h * pwb.x, -h * pwb.y);
+        double2 lpnb = nbb;
+        double2 dbb[R], tdb[R], ltnb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            // nb = sum nu_j db_j
+            dbb[r] = act[r] ? make_double2(sNu[k[r]] * nbb.x, sNu[k[r]] * nbb.y) : z;
+            // tnew = told + h (rt - td - ltn)
+            tob[r] = make_double2(tob[r].x + twb[r].x, tob[r].y + twb[r].y);
+            rtb[r] = make_double2(h * twb[r].x, h * twb[r].y);
+            tdb[r] = make_double2(-h * twb[r].x, -h * twb[r].y);
+            ltnb[r] = tdb[r];
+        }
+        // td = tau db  ->  db_b += tau^T td_b
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(tdb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double tk = act[r] ? sT[k[r] * NL + j] : 0.0;   // tau[j][k]
+                dbb[r].x += tk * xj.x;
+                dbb[r].y += tk * xj.y;
+            }
+        }
+        // db = a1 dnew + (1 - a1) dold ; dnew (before diffusion) also feeds the output
+        double2 dnewb[R], rhsb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            dnewb[r] = make_double2(dwb[r].x + a.a1 * dbb[r].x, dwb[r].y + a.a1 * dbb[r].y);
+            dob[r] = make_double2(dob[r].x + (1.0 - a.a1) * dbb[r].x, dob[r].y + (1.0 - a.a1) * dbb[r].y);
+            rhsb[r] = z;
+        }
+        // dnew = Minv rhs -> rhs_b = Minv^T dnew_b
+        const double *Mi = a.MinvT + (size_t)l * NL * NL;
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(dnewb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double mk = act[r] ? Mi[k[r] * NL + j] : 0.0;   // Minv[j][k]
+                rhsb[r].x += mk * xj.x;
+                rhsb[r].y += mk * xj.y;
+            }
+        }
+        double2 wdb[R], ldsb[R], ldnb[R], tstb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (!act[r]) rhsb[r] = z;
+            // rhs = dold - hh lam W dold + h (rd + lds - ldn)
+            dob[r] = make_double2(dob[r].x + rhsb[r].x, dob[r].y + rhsb[r].y);
+            wdb[r] = make_double2(-a.hh_old * lam * rhsb[r].x, -a.hh_old * lam * rhsb[r].y);
+            rdb[r] = make_double2(h * rhsb[r].x, h * rhsb[r].y);
+            ldsb[r] = make_double2(h * rhsb[r].x, h * rhsb[r].y);
+            ldnb[r] = make_double2(-h * rhsb[r].x, -h * rhsb[r].y);
+            tstb[r] = z;
+        }
+        // lds = lam (G tst + pc pst)
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(ldsb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double gk = act[r] ? sG[k[r] * NL + j] : 0.0;   // G[j][k]
+                tstb[r].x += lam * gk * xj.x;
+                tstb[r].y += lam * gk * xj.y;
+            }
+        }
+        double2 ps = z;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (act[r]) {
+                ps.x += lam * sPc[k[r]] * ldsb[r].x;
+                ps.y += lam * sPc[k[r]] * ldsb[r].y;
+            }
+        const double2 pstb = wsum2(ps);
+        // pst = pold + a (rp - lpn)
+        pob = make_double2(pob.x + pstb.x, pob.y + pstb.y);
+        rpb = make_double2(rpb.x + a.astep * pstb.x, rpb.y + a.astep * pstb.y);
+        lpnb = make_double2(lpnb.x - a.astep * pstb.x, lpnb.y - a.astep * pstb.y);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            // tst = told + a (rt - ltn)
+            tob[r] = make_double2(tob[r].x + tstb[r].x, tob[r].y + tstb[r].y);
+            rtb[r] = make_double2(rtb[r].x + a.astep * tstb[r].x, rtb[r].y + a.astep * tstb[r].y);
+            ltnb[r] = make_double2(ltnb[r].x - a.astep * tstb[r].x, ltnb[r].y - a.astep * tstb[r].y);
+            // lpn = -sum nu_j dnow_j
+            if (act[r]) {
+                dnb[r].x -= sNu[k[r]] * lpnb.x;
+                dnb[r].y -= sNu[k[r]] * lpnb.y;
+            }
+        }
+        // wd = W dold -> dold_b += W^T wd_b
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(wdb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double wk = act[r] ? sW[k[r] * NL + j] : 0.0;   // W[j][k]
+                dob[r].x += wk * xj.x;
+                dob[r].y += wk * xj.y;
+            }
+        }
+        // ldn = lam (G tnow + pc pnow)
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(ldnb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double gk = act[r] ? sG[k[r] * NL + j] : 0.0;
+                tnb[r].x += lam * gk * xj.x;
+                tnb[r].y += lam * gk * xj.y;
+            }
+        }
+        double2 pn = z;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (act[r]) {
+                pn.x += lam * sPc[k[r]] * ldnb[r].x;
+                pn.y += lam * sPc[k[r]] * ldnb[r].y;
+            }
+        const double2 pnowb = wsum2(pn);
+        pnb = make_double2(pnb.x + pnowb.x, pnb.y + pnowb.y);
+        // ltn = -tau dnow -> dnow_b -= tau^T ltn_b
+        WIDE_LEVELS(j, s, jj) {
+            const double2 xj = shfl2(ltnb[s], jj);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const double tk = act[r] ? sT[k[r] * NL + j] : 0.0;
+                dnb[r].x -= tk * xj.x;
+                dnb[r].y -= tk * xj.y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            dob[r] = make_double2(dob[r].x + dwb[r].x, dob[r].y + dwb[r].y);
+            rdb[r] = make_double2(h * dwb[r].x, h * dwb[r].y);
+            tob[r] = make_double2(tob[r].x + twb[r].x, tob[r].y + twb[r].y);
+            rtb[r] = make_double2(h * twb[r].x, h * twb[r].y);
+        }
+        pob = make_double2(pob.x + pwb.x, pob.y + pwb.y);
+        rpb = make_double2(h * pwb.x, h * pwb.y);
+    }
+#undef WIDE_LEVELS
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (!act[r]) continue;
+        a.ob[o[r]] = vob[r]; a.ob[nsl + o[r]] = dob[r]; a.ob[2 * nsl + o[r]] = tob[r];
+        a.nb[o[r]] = vnb[r]; a.nb[nsl + o[r]] = dnb[r]; a.nb[2 * nsl + o[r]] = tnb[r];
+        a.rb[o[r]] = tvb[r]; a.rb[nsl + o[r]] = rdb[r]; a.rb[2 * nsl + o[r]] = rtb[r];
+    }
+    if (lane == 0) {
+        a.ob[op] = pob;
+        a.nb[op] = pnb;
+        a.rb[op] = rpb;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host side
@@ -626,10 +859,6 @@ int adj_ensure(Dyn &d) {
         return AEROS_ERR_UNSUPPORTED;
     }
     if (d.adj) return aeros_sht_set_stream(d.adj->sht, d.stream);   // follow aeros_dyn_set_stream
-    if (d.NL > kLaneLev) {   // its column and spectral kernels hold one level per lane or register slot
-        set_error("adjoint: more than 32 levels");
-        return AEROS_ERR_UNSUPPORTED;
-    }
     AdjCtx *a = new AdjCtx;
     d.adj = a;
     const size_t ng = (size_t)d.g.nlon * d.g.nlat, M = d.M, NL = d.NL, nst = d.nstate(), nlm = d.g.nlm;
@@ -784,7 +1013,13 @@ int step_adjoint(Dyn &d, double2 *post, bool capture, const double *Gs) {
     s.semi_implicit = d.par.semi_implicit;
     s.raw_on = (!startup && d.par.eps_filter > 0.0) ? 1 : 0;
     const long nw = (long)d.g.nlm * d.M;
-    k_spectral_ad<<<(unsigned)((nw + 3) / 4), 128, 0, d.stream>>>(s);
+    if (d.NL > kLaneLev) {
+        const size_t smem = spec_wide_smem(d.NL);
+        if ((rc = raise_smem_limit((const void *)k_spectral_ad_wide, smem))) return rc;
+        k_spectral_ad_wide<<<(unsigned)((nw + 3) / 4), 128, smem, d.stream>>>(s);
+    } else {
+        k_spectral_ad<<<(unsigned)((nw + 3) / 4), 128, 0, d.stream>>>(s);
+    }
     ++d.launches;
     // tendencies -> column outputs -> column inputs -> state
     if ((rc = ana_adjoint(d, a.Rb))) return rc;
@@ -802,7 +1037,8 @@ int step_adjoint(Dyn &d, double2 *post, bool capture, const double *Gs) {
         if (rc) return rc;
     }
     // a warp per CTA: one member's 8,192 columns then reach all SMs (the kernel is latency-bound there)
-    k_column_ad<<<(unsigned)((ncol + 31) / 32), 32, 0, d.stream>>>(
+    auto col_ad = d.NL > kLaneLev ? k_column_ad<kMaxLev> : k_column_ad<kLaneLev>;
+    col_ad<<<(unsigned)((ncol + 31) / 32), 32, 0, d.stream>>>(
         d.G, a.GAb, a.Gb, d.NL, d.g.nlon, d.g.nlat, d.M, d.xlat_d, d.phis_set ? d.phis_d : nullptr,
         d.par.held_suarez, d.hs_dty_d, d.hs_ka_d, a.parb, d.dconst, d.tmp(d.now), d.g.nlm);
     ++d.launches;

@@ -497,8 +497,7 @@ int aeros_dyn_state_size(aeros_dyn_t h, long long *n);
  * current state; the state is left unchanged).  In: adjoints of the post-step
  * old slot (the RAW-filtered X^n) and now slot (X^(n+1)), packed.  Out:
  * adjoints of the pre-step old (X^(n-1)) and now (X^n) slots, packed, and per
- * member d/dk_a, d/ddT_y (any output may be NULL).  Handles of more than 32
- * levels: AEROS_ERR_UNSUPPORTED (so for every adjoint entry point). */
+ * member d/dk_a, d/ddT_y (any output may be NULL). */
 int aeros_dyn_step_ad(aeros_dyn_t h, const double *old_ad_in, const double *now_ad_in, double *old_ad_out,
                       double *now_ad_out, double *ka_ad, double *dty_ad);
 

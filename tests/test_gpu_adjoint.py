@@ -82,16 +82,17 @@ def _weights(dyn, rng):
     return f, (dyn.nlev,)
 
 
-def _step_pair(nstep):
+def _step_pair(nstep, nlev=8):
     from aeros_gb300.params import held_suarez_params
     from aeros_gb300.dynamics import AerosDyn
-    p = held_suarez_params(trunc=21, nlev=8)
+    p = held_suarez_params(trunc=21, nlev=nlev)
     return AerosDyn(p)
 
 
-@pytest.mark.parametrize("nstep", [0, 5])
-def test_step_adjoint_fd(gpulib, nstep):
-    dyn = _step_pair(nstep)
+# 40 levels: the 64-level column adjoint and the two-levels-per-lane spectral adjoint
+@pytest.mark.parametrize("nstep,nlev", [(0, 8), (5, 8), (5, 40)])
+def test_step_adjoint_fd(gpulib, nstep, nlev):
+    dyn = _step_pair(nstep, nlev)
     rng = np.random.default_rng(11 + nstep)
     x_now = adjoint_initial_state(dyn, seed=3)
     f, sh = _weights(dyn, rng)
@@ -183,6 +184,10 @@ def _check_window(trunc, nlev, nsteps, every):
 
 def test_window_gradient_small(gpulib):
     _check_window(21, 8, 24, 6)
+
+
+def test_window_gradient_many_levels(gpulib):
+    _check_window(21, 40, 12, 4)
 
 
 def test_window_gradient_T42L20(gpulib):

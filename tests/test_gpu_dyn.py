@@ -139,19 +139,6 @@ def test_many_levels_steps_match_oracle(gpulib, nlev, precision):
     assert abs(mg - mo) / mo < 1e-13
 
 
-def test_many_levels_adjoint_refused(gpulib):
-    """The adjoint holds one level per lane: above 32 levels it returns
-    AEROS_ERR_UNSUPPORTED instead of running."""
-    from aeros_gb300 import _capi
-    g, o, s = make_pair(21, 40)
-    st = moving_state(o, seed=5)
-    g.set_state(*st)
-    n = g.state_size()
-    with pytest.raises(_capi.AerosError) as ei:
-        g.step_ad(np.zeros(n, np.complex128), np.zeros(n, np.complex128))
-    assert ei.value.code == -7
-
-
 def test_hs_rest_noise_start(gpulib):
     """Rest + 0.1 K noise (the Held-Suarez start): T and ln ps match from the
     first step; vor and D start at round-off size (dzeta/dt is analytically 0
