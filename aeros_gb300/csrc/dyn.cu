@@ -18,6 +18,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include "aeros_internal.h"
 #include "fft.cuh"
@@ -30,6 +31,7 @@ namespace {
 
 constexpr int kMaxLev = 64;    // levels of a handle
 constexpr int kLaneLev = 32;   // levels of the lane-per-level kernels (k_spectral, the adjoint's kernels)
+constexpr int kColLev20 = 20;  // the smallest level bound of the column kernel's instantiations
 constexpr double kNrmD = 0.39894228040143267794;   // 1/sqrt(2 pi)
 constexpr double kRsqrt4Pi = 0.28209479177387814347;   // 1/sqrt(4 pi): field mean per (0,0) coefficient
 
@@ -102,8 +104,10 @@ struct ColArgs {
     const DynConst *__restrict__ dc = cka.dc;                                             \
     const double2 *__restrict__ tspec = cka.tspec;                                        \
     const int nlm = cka.nlm
-// MAXL: the most levels a launch holds (32, or 64 for handles of more than 32 levels, so that
-// the register-resident chunks of the <= 32-level instantiations stay as they are).
+// MAXL: the most levels a launch holds (20, 32 or 64): the per-lane level arrays are sized
+// MAXL / LPC, so a handle of at most 20 levels (the Held-Suarez L16 and L20 configurations)
+// takes the instantiation whose arrays are smallest, and with them its register count, which
+// sets how many warps fit on an SM (at one member the kernel has fewer warps than SMs can hold).
 template <int LPC, bool RAG = false, int MAXL = kLaneLev>
 __global__ void __launch_bounds__(256) k_column(const __grid_constant__ RagPack<ColArgs> rpk) {
     COLUMN_ARGS;
@@ -2018,18 +2022,20 @@ int run_tendency(Dyn &d, int hs_on, bool physics) {
     if (split_column_df(d)) {
         // split form: the column terms in double-float on the FP32/INT32 pipes, a thread per column
         rc = go((const void *)k_column_df<>, (const void *)k_column_df<true>, (unsigned)((ncol + ct - 1) / ct));
-    } else if (d.NL > kLaneLev) {
-        // more than 32 levels: the instantiations whose per-lane chunks hold 64 levels
-        if (lpc == 16) rc = go((const void *)k_column<16, false, kMaxLev>, (const void *)k_column<16, true, kMaxLev>, nb);
-        else if (lpc == 8) rc = go((const void *)k_column<8, false, kMaxLev>, (const void *)k_column<8, true, kMaxLev>, nb);
-        else if (lpc == 4) rc = go((const void *)k_column<4, false, kMaxLev>, (const void *)k_column<4, true, kMaxLev>, nb);
-        else if (lpc == 2) rc = go((const void *)k_column<2, false, kMaxLev>, (const void *)k_column<2, true, kMaxLev>, nb);
-        else rc = go((const void *)k_column<1, false, kMaxLev>, (const void *)k_column<1, true, kMaxLev>, nb);
-    } else if (lpc == 16) rc = go((const void *)k_column<16>, (const void *)k_column<16, true>, nb);
-    else if (lpc == 8) rc = go((const void *)k_column<8>, (const void *)k_column<8, true>, nb);
-    else if (lpc == 4) rc = go((const void *)k_column<4>, (const void *)k_column<4, true>, nb);
-    else if (lpc == 2) rc = go((const void *)k_column<2>, (const void *)k_column<2, true>, nb);
-    else rc = go((const void *)k_column<1>, (const void *)k_column<1, true>, nb);
+    } else {
+        // the instantiation whose per-lane chunks hold the fewest levels >= NL
+        auto col = [&](auto maxl) {
+            constexpr int L = decltype(maxl)::value;
+            if (lpc == 16) return go((const void *)k_column<16, false, L>, (const void *)k_column<16, true, L>, nb);
+            if (lpc == 8) return go((const void *)k_column<8, false, L>, (const void *)k_column<8, true, L>, nb);
+            if (lpc == 4) return go((const void *)k_column<4, false, L>, (const void *)k_column<4, true, L>, nb);
+            if (lpc == 2) return go((const void *)k_column<2, false, L>, (const void *)k_column<2, true, L>, nb);
+            return go((const void *)k_column<1, false, L>, (const void *)k_column<1, true, L>, nb);
+        };
+        rc = d.NL > kLaneLev ? col(std::integral_constant<int, kMaxLev>{})
+             : d.NL > kColLev20 ? col(std::integral_constant<int, kLaneLev>{})
+                                : col(std::integral_constant<int, kColLev20>{});
+    }
     if (rc) return rc;
     ++d.launches;
     AEROS_CUDA(cudaGetLastError());
