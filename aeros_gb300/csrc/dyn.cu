@@ -31,7 +31,7 @@ namespace {
 
 constexpr int kMaxLev = 64;    // levels of a handle
 constexpr int kLaneLev = 32;   // levels of the lane-per-level kernels (k_spectral, the adjoint's kernels)
-constexpr int kColLev20 = 20;  // the smallest level bound of the column kernel's instantiations
+constexpr int kColLev20 = 20;  // the smallest level bound of the column and spectral kernels' instantiations
 constexpr double kNrmD = 0.39894228040143267794;   // 1/sqrt(2 pi)
 constexpr double kRsqrt4Pi = 0.28209479177387814347;   // 1/sqrt(4 pi): field mean per (0,0) coefficient
 
@@ -354,7 +354,9 @@ struct SpecColArgs {
     int exact;   // 1: exact fixed-point level products (k_spectral_xq), 0: FP64 (k_spectral_cols)
 };
 
-template <bool RAG = false>
+// LMAX: the most levels of the launch (20 or 32): the lane's row of M^-1 is a register array of
+// LMAX entries, unrolled, so a handle of at most 20 levels takes the shorter body.
+template <bool RAG = false, int LMAX = kLaneLev>
 __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPack<SpecArgs> rpk) {
     uint3 bid, gdim;
     const SpecArgs &a = rag_part<RAG>(rpk, bid, gdim);
@@ -412,12 +414,12 @@ __global__ void __launch_bounds__(256) k_spectral(const __grid_constant__ RagPac
                                    dold.y + h * rd.y + hl * (gy.y + pc * pz.y) + lam * wx.y);
         if (!act) rhs = z;
         const double *Mi = a.MinvT + (size_t)l * NL * NL;
-        double mrow[kLaneLev];   // this lane's row of the inverse, loaded before the solve
+        double mrow[LMAX];   // this lane's row of the inverse, loaded before the solve
 #pragma unroll
-        for (int j = 0; j < kLaneLev; ++j) mrow[j] = (act && j < NL) ? Mi[j * NL + k] : 0.0;
+        for (int j = 0; j < LMAX; ++j) mrow[j] = (act && j < NL) ? Mi[j * NL + k] : 0.0;
         dnew = z;
 #pragma unroll
-        for (int j = 0; j < kLaneLev; ++j) {
+        for (int j = 0; j < LMAX; ++j) {
             if (j >= NL) break;
             double2 rj = shfl2(rhs, j);
             dnew.x += mrow[j] * rj.x; dnew.y += mrow[j] * rj.y;
@@ -2132,10 +2134,15 @@ int enqueue_step(Dyn &d, bool startup) {
             return rc;
         rc = emit_launch(d.stream, d.rec, (const void *)k_spectral_wide<>, (const void *)k_spectral_wide<true>,
                          dim3((unsigned)((nw + sw - 1) / sw)), dim3(32 * sw), smem, a);
-    } else {
+    } else if (d.NL > kColLev20) {
         long nw = (long)d.g.nlm * d.M;
         rc = emit_launch(d.stream, d.rec, (const void *)k_spectral<>, (const void *)k_spectral<true>, dim3((unsigned)((nw + sw - 1) / sw)),
                          dim3(32 * sw), 0, a);
+    } else {
+        long nw = (long)d.g.nlm * d.M;
+        rc = emit_launch(d.stream, d.rec, (const void *)k_spectral<false, kColLev20>,
+                         (const void *)k_spectral<true, kColLev20>, dim3((unsigned)((nw + sw - 1) / sw)), dim3(32 * sw),
+                         0, a);
     }
     if (rc) return rc;
     ++d.launches;
